@@ -1,0 +1,166 @@
+/* jfem.h — C ABI of libjfem_cuda.so, the sm_103a elasticity hot path.
+ *
+ * Plain C types only: host pointers unless a name says "device".  All calls are
+ * synchronous on return (work runs on a context-owned CUDA stream).  A context is
+ * not thread-safe; use one per host thread.  Status: 0 OK, >0 soft outcome,
+ * <0 error (message in jfem_last_error).
+ *
+ * The entry points replace these reference interfaces (JuliaFEM.jl):
+ *   backend plugin   initialize_backend(::GPU, physics, time)   ext/JuliaFEMCUDAExt.jl:867-869
+ *                    solve_backend!(data, physics; tol, ...)     ext/JuliaFEMCUDAExt.jl:886-916
+ *                    (declared src/backend/abstract.jl:228,241, dispatched :195-200)
+ *   legacy assembly  assemble!(assembly, ::Problem{Elasticity}, elements, time)
+ *                    src/problems_elasticity.jl:65-81 (element kernel :203-451,
+ *                    surface loads :454-502) filling assembly.K / assembly.f
+ *                    (src/assembly/problems.jl:14-40) and the COO→CSC of
+ *                    src/solvers.jl:57-93.
+ */
+#ifndef JFEM_H
+#define JFEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define JFEM_OK                0
+#define JFEM_NOT_CONVERGED     1   /* like the @warn of ext/JuliaFEMCUDAExt.jl:630 */
+#define JFEM_STALL             2   /* learned preconditioner stalled; fell back to Jacobi */
+#define JFEM_ERR_INVALID      -1   /* bad argument / call order (error() in the reference) */
+#define JFEM_ERR_CUDA         -2
+#define JFEM_ERR_OOM          -3
+#define JFEM_ERR_NEG_JACOBIAN -4   /* detJ <= 0 in an element */
+#define JFEM_ERR_NAN          -5   /* NaN/Inf, or J <= 0 in the Neo-Hookean law */
+#define JFEM_ERR_TIMEOUT      -6   /* a bounded device loop ran out of its budget */
+
+/* element, face and material codes */
+#define JFEM_TET4   4
+#define JFEM_TET10 10
+#define JFEM_HEX8   8
+#define JFEM_TRI3   3
+#define JFEM_TRI6   6
+#define JFEM_QUAD4  4
+#define JFEM_LINEAR_ELASTIC 0
+#define JFEM_NEO_HOOKEAN    1
+
+/* solve methods and precisions */
+#define JFEM_PCG_JACOBI   0
+#define JFEM_FCG_LEARNED  1
+#define JFEM_NEWTON       2
+#define JFEM_FP64         0   /* FP64 apply throughout */
+#define JFEM_MIXED        1   /* FP32 apply, FP64 vectors/dots/residual + refinement */
+
+/* jfem_apply flags */
+#define JFEM_APPLY_FP32   1   /* FP32 element arithmetic (default FP64) */
+#define JFEM_APPLY_MASKED 2   /* zero prescribed DOFs of input and output */
+
+typedef struct jfem_ctx jfem_ctx;
+
+/* Keyword arguments of solve!(physics; tol, max_iter, newton_tol, max_newton,
+ * max_cg_per_newton) (src/backend/abstract.jl:181-188) and the Eisenstat–Walker
+ * parameters of ext/JuliaFEMCUDAExt.jl:685-694.  tol is a relative FP64
+ * residual ‖f − K u‖ / ‖f‖ over the free DOFs. */
+typedef struct jfem_solve_opts {
+  int method;             /* JFEM_PCG_JACOBI, JFEM_FCG_LEARNED, JFEM_NEWTON */
+  int precision;          /* JFEM_FP64 or JFEM_MIXED */
+  double tol;
+  int max_iter;
+  double newton_tol;
+  int max_newton;
+  int max_cg_per_newton;
+  int n_load_steps;       /* Newton: prescribed values and loads ramped over steps */
+  double forcing_power;
+  double forcing_max;
+  double time_budget_s;   /* 0 = none; else JFEM_ERR_TIMEOUT when exceeded */
+} jfem_solve_opts;
+
+#define JFEM_HISTORY_MAX 256
+/* Fields of ElasticitySolution (src/backend/abstract.jl:138-151). */
+typedef struct jfem_stats {
+  int status;
+  int newton_iterations;
+  int cg_iterations;
+  int refinements;        /* FP64 true-residual evaluations */
+  int fallbacks;          /* learned FCG → Jacobi-PCG switches */
+  double residual;        /* final relative FP64 residual */
+  double solve_time_s;
+  int history_len;
+  double history[3 * JFEM_HISTORY_MAX];   /* (cg_iters, ‖R‖, η) per Newton iteration */
+} jfem_stats;
+
+/* Fill opts with the reference defaults (tol 1e-6, max_iter 1000, newton_tol 1e-6,
+ * max_newton 20, max_cg_per_newton 50, forcing 0.5 / 0.9). */
+void jfem_default_opts(jfem_solve_opts* opts);
+const char* jfem_version(void);
+
+/* context lifetime (replaces CUDA.jl device/array management of
+ * ext/JuliaFEMCUDAExt.jl:86-217) */
+int jfem_create(jfem_ctx** out, int device_ordinal);
+int jfem_destroy(jfem_ctx* ctx);
+const char* jfem_last_error(const jfem_ctx* ctx);
+
+/* Model definition — the host packing of initialize_gpu_data!
+ * (ext/JuliaFEMCUDAExt.jl:86-217): coordinates, connectivity, materials,
+ * Dirichlet masks and the surface-traction table.
+ *   X     3 × n_nodes column-major (x,y,z of node 1, then node 2, …)
+ *   conn  n_en × n_elem column-major, node numbers starting at index_base
+ * The node→element adjacency and the sparsity pattern are built on the device. */
+int jfem_set_mesh(jfem_ctx* ctx, int elem_type, int64_t n_nodes, const double* X,
+                  int64_t n_elem, const int64_t* conn, int index_base);
+/* E, nu: n_elem values when per_element, else 1 (problems_elasticity.jl:310-311). */
+int jfem_set_material(jfem_ctx* ctx, int model, const double* E, const double* nu,
+                      int per_element);
+/* Elasticity properties finite_strain / geometric_stiffness (problems_elasticity.jl:36-46). */
+int jfem_set_formulation(jfem_ctx* ctx, int finite_strain, int geometric_stiffness);
+/* Prescribed DOFs (global DOF = 3(node-base)+comp+base) and their values
+ * (src/problems_dirichlet.jl:60-89, src/solvers.jl:196-210).  values may be NULL (zero). */
+int jfem_set_dirichlet(jfem_ctx* ctx, int64_t n, const int64_t* dofs, const double* values,
+                       int index_base);
+/* Surface traction: face_conn n_fn × n_faces column-major, t 3 × n_faces
+ * (problems_elasticity.jl:454-502, consistent integration). */
+int jfem_set_traction(jfem_ctx* ctx, int face_type, int64_t n_faces, const int64_t* face_conn,
+                      const double* t, int index_base);
+/* Surface loads: traction t (3 × n_faces, may be NULL) and pressure p (n_faces, may
+ * be NULL; positive towards the surface, f += w·(−p)·n·N with n the normalised
+ * ∂X/∂ξ₁ × ∂X/∂ξ₂ of the face, problems_elasticity.jl:486-493).  Replaces the
+ * previous face table. */
+int jfem_set_surface_load(jfem_ctx* ctx, int face_type, int64_t n_faces, const int64_t* face_conn,
+                          const double* t, const double* p, int index_base);
+/* Current displacement state u (3 n_nodes) for finite-strain assembly / tangent. */
+int jfem_set_state(jfem_ctx* ctx, const double* u);
+
+/* FP64 assembly of the global K (CSC, structural pattern of sparse.jl:121-132 +
+ * sparse(): full 3×3 node blocks, explicit zeros kept) and of f = f_ext − f_int
+ * (problems_elasticity.jl:433).  Call with colptr == NULL to get nnz in *nnz_inout;
+ * then with arrays of n+1, nnz, nnz entries.  f (3 n_nodes) may be NULL. */
+int jfem_assemble_csc(jfem_ctx* ctx, int index_base, int64_t* nnz_inout, int64_t* colptr,
+                      int64_t* rowval, double* nzval, double* f);
+
+/* Matrix-free y = K v (tangent at the current state for finite strain); the
+ * pure operator (does not subtract f_ext, unlike ext/JuliaFEMCUDAExt.jl:442-478). */
+int jfem_apply(jfem_ctx* ctx, const double* v, double* y, int flags);
+/* Same with device pointers (3 n_nodes doubles each). */
+int jfem_apply_device(jfem_ctx* ctx, const double* v_device, double* y_device, int flags);
+
+/* Internal force f_int(u) at the current state (FP64), host or device output. */
+int jfem_internal_force(jfem_ctx* ctx, double* f_int);
+
+/* solve_backend! (ext/JuliaFEMCUDAExt.jl:886-916): load vector, Dirichlet values,
+ * PCG / learned FCG / Newton–Krylov per opts.  u (3 n_nodes) receives the
+ * displacement.  stats may be NULL. */
+int jfem_solve(jfem_ctx* ctx, const jfem_solve_opts* opts, double* u, jfem_stats* stats);
+/* Same with u left in device memory (u_device: 3 n_nodes doubles). */
+int jfem_solve_device(jfem_ctx* ctx, const jfem_solve_opts* opts, double* u_device,
+                      jfem_stats* stats);
+
+/* Device-side counters of the last call: kernels launched by the library. */
+int64_t jfem_kernel_launches(const jfem_ctx* ctx);
+/* Event-timed duration (ms) of the last matrix-free apply launch sequence. */
+double jfem_last_apply_ms(const jfem_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JFEM_H */

@@ -1,0 +1,251 @@
+"""ctypes binding of libjfem_cuda.so (include/jfem.h).
+
+The library is the product: there is no CPU fallback.  Loading fails loudly
+when the shared object has not been built (``build()`` in __graft_entry__ or
+``python juliafem.jl_gb300/build.py``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libjfem_cuda.so"
+
+OK, NOT_CONVERGED, STALL = 0, 1, 2
+ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_NEG_JACOBIAN, ERR_NAN, ERR_TIMEOUT = -1, -2, -3, -4, -5, -6
+TET4, TET10, HEX8 = 4, 10, 8
+TRI3, TRI6, QUAD4 = 3, 6, 4
+LINEAR_ELASTIC, NEO_HOOKEAN = 0, 1
+PCG_JACOBI, FCG_LEARNED, NEWTON = 0, 1, 2
+FP64, MIXED = 0, 1
+APPLY_FP32, APPLY_MASKED = 1, 2
+HISTORY_MAX = 256
+
+NEN = {TET4: 4, TET10: 10, HEX8: 8}
+NFN = {TRI3: 3, TRI6: 6, QUAD4: 4}
+
+_ERRNAMES = {ERR_INVALID: "invalid argument", ERR_CUDA: "CUDA error", ERR_OOM: "out of device memory",
+             ERR_NEG_JACOBIAN: "non-positive Jacobian", ERR_NAN: "NaN / invalid material state",
+             ERR_TIMEOUT: "time budget exceeded"}
+
+
+class JFEMError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_ERRNAMES.get(code, 'error')} ({code}): {msg}")
+        self.code = code
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("method", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int),
+                ("newton_tol", C.c_double), ("max_newton", C.c_int), ("max_cg_per_newton", C.c_int),
+                ("n_load_steps", C.c_int), ("forcing_power", C.c_double), ("forcing_max", C.c_double),
+                ("time_budget_s", C.c_double)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("status", C.c_int), ("newton_iterations", C.c_int), ("cg_iterations", C.c_int),
+                ("refinements", C.c_int), ("fallbacks", C.c_int), ("residual", C.c_double),
+                ("solve_time_s", C.c_double), ("history_len", C.c_int),
+                ("history", C.c_double * (3 * HISTORY_MAX))]
+
+    def history_list(self):
+        return [(int(self.history[3 * i]), float(self.history[3 * i + 1]), float(self.history[3 * i + 2]))
+                for i in range(self.history_len)]
+
+
+# Every symbol include/jfem.h declares, with its ctypes signature.
+_P = C.c_void_p
+_i64 = C.c_int64
+_i64p = C.POINTER(C.c_int64)
+_f64p = C.POINTER(C.c_double)
+SIGNATURES = {
+    "jfem_version": (C.c_char_p, []),
+    "jfem_default_opts": (None, [C.POINTER(SolveOpts)]),
+    "jfem_create": (C.c_int, [C.POINTER(_P), C.c_int]),
+    "jfem_destroy": (C.c_int, [_P]),
+    "jfem_last_error": (C.c_char_p, [_P]),
+    "jfem_set_mesh": (C.c_int, [_P, C.c_int, _i64, _f64p, _i64, _i64p, C.c_int]),
+    "jfem_set_material": (C.c_int, [_P, C.c_int, _f64p, _f64p, C.c_int]),
+    "jfem_set_formulation": (C.c_int, [_P, C.c_int, C.c_int]),
+    "jfem_set_dirichlet": (C.c_int, [_P, _i64, _i64p, _f64p, C.c_int]),
+    "jfem_set_traction": (C.c_int, [_P, C.c_int, _i64, _i64p, _f64p, C.c_int]),
+    "jfem_set_surface_load": (C.c_int, [_P, C.c_int, _i64, _i64p, _f64p, _f64p, C.c_int]),
+    "jfem_set_state": (C.c_int, [_P, _f64p]),
+    "jfem_assemble_csc": (C.c_int, [_P, C.c_int, _i64p, _i64p, _i64p, _f64p, _f64p]),
+    "jfem_apply": (C.c_int, [_P, _f64p, _f64p, C.c_int]),
+    "jfem_apply_device": (C.c_int, [_P, _P, _P, C.c_int]),
+    "jfem_internal_force": (C.c_int, [_P, _f64p]),
+    "jfem_solve": (C.c_int, [_P, C.POINTER(SolveOpts), _f64p, C.POINTER(Stats)]),
+    "jfem_solve_device": (C.c_int, [_P, C.POINTER(SolveOpts), _P, C.POINTER(Stats)]),
+    "jfem_kernel_launches": (_i64, [_P]),
+    "jfem_last_apply_ms": (C.c_double, [_P]),
+}
+
+_lib = None
+
+
+def load(path: Path | str | None = None):
+    """Load the shared library (raises if it is missing — there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p.name} is not built; run __graft_entry__.build() "
+                           "(the CUDA library is required, there is no CPU path)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ptr(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def default_opts(**kw) -> SolveOpts:
+    o = SolveOpts()
+    load().jfem_default_opts(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise TypeError(f"unknown solve option {k}")
+        setattr(o, k, v)
+    return o
+
+
+class Context:
+    """One device context (one mesh on one GPU) behind the C ABI."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        h = C.c_void_p()
+        rc = self._lib.jfem_create(C.byref(h), int(device))
+        if rc != 0:
+            raise JFEMError(rc, "jfem_create failed (no usable CUDA device?)")
+        self._h = h
+        self.n_nodes = 0
+        self.n_elem = 0
+        self.elem_type = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.jfem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int) -> int:
+        if rc < 0:
+            raise JFEMError(rc, self._lib.jfem_last_error(self._h).decode())
+        return rc
+
+    # -- model -----------------------------------------------------------------
+    def set_mesh(self, elem_type: int, X, conn, index_base: int = 0):
+        X = np.ascontiguousarray(X, dtype=np.float64).reshape(-1, 3)
+        conn = np.ascontiguousarray(conn, dtype=np.int64).reshape(-1, NEN[elem_type])
+        self._check(self._lib.jfem_set_mesh(self._h, elem_type, X.shape[0], _ptr(X, _f64p), conn.shape[0],
+                                            _ptr(conn, _i64p), index_base))
+        self.n_nodes, self.n_elem, self.elem_type = X.shape[0], conn.shape[0], elem_type
+
+    def set_material(self, E, nu, model: int = LINEAR_ELASTIC):
+        E = np.atleast_1d(np.asarray(E, dtype=np.float64))
+        nu = np.atleast_1d(np.asarray(nu, dtype=np.float64))
+        per = int(E.size > 1 or nu.size > 1)
+        if per:
+            E = np.ascontiguousarray(np.broadcast_to(E, (self.n_elem,)))
+            nu = np.ascontiguousarray(np.broadcast_to(nu, (self.n_elem,)))
+        self._check(self._lib.jfem_set_material(self._h, model, _ptr(E, _f64p), _ptr(nu, _f64p), per))
+
+    def set_formulation(self, finite_strain: bool, geometric_stiffness: bool):
+        self._check(self._lib.jfem_set_formulation(self._h, int(finite_strain), int(geometric_stiffness)))
+
+    def set_dirichlet(self, dofs, values=None, index_base: int = 0):
+        dofs = np.ascontiguousarray(dofs, dtype=np.int64)
+        vals = None if values is None else np.ascontiguousarray(np.broadcast_to(values, dofs.shape),
+                                                                 dtype=np.float64)
+        self._check(self._lib.jfem_set_dirichlet(self._h, dofs.size, _ptr(dofs, _i64p), _ptr(vals, _f64p),
+                                                 index_base))
+
+    def set_traction(self, face_type: int, face_conn, t, index_base: int = 0):
+        fc = np.ascontiguousarray(face_conn, dtype=np.int64).reshape(-1, NFN[face_type])
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(t, dtype=np.float64), (fc.shape[0], 3)))
+        self._check(self._lib.jfem_set_traction(self._h, face_type, fc.shape[0], _ptr(fc, _i64p),
+                                                _ptr(t, _f64p), index_base))
+
+    def set_surface_load(self, face_type: int, face_conn, t=None, p=None, index_base: int = 0):
+        fc = np.ascontiguousarray(face_conn, dtype=np.int64).reshape(-1, NFN[face_type])
+        nf = fc.shape[0]
+        t = None if t is None else np.ascontiguousarray(np.broadcast_to(np.asarray(t, dtype=np.float64), (nf, 3)))
+        p = None if p is None else np.ascontiguousarray(np.broadcast_to(np.asarray(p, dtype=np.float64), (nf,)))
+        self._check(self._lib.jfem_set_surface_load(self._h, face_type, nf, _ptr(fc, _i64p), _ptr(t, _f64p),
+                                                    _ptr(p, _f64p), index_base))
+
+    def set_state(self, u=None):
+        u = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        self._check(self._lib.jfem_set_state(self._h, _ptr(u, _f64p)))
+
+    # -- operators -------------------------------------------------------------
+    def assemble_csc(self, index_base: int = 0, want_f: bool = True):
+        nnz = C.c_int64(0)
+        self._check(self._lib.jfem_assemble_csc(self._h, index_base, C.byref(nnz), None, None, None, None))
+        n = 3 * self.n_nodes
+        colptr = np.empty(n + 1, np.int64)
+        rowval = np.empty(nnz.value, np.int64)
+        nzval = np.empty(nnz.value, np.float64)
+        f = np.empty(n, np.float64) if want_f else None
+        self._check(self._lib.jfem_assemble_csc(self._h, index_base, C.byref(nnz), _ptr(colptr, _i64p),
+                                                _ptr(rowval, _i64p), _ptr(nzval, _f64p), _ptr(f, _f64p)))
+        return colptr, rowval, nzval, f
+
+    def apply(self, v, fp32: bool = False, masked: bool = False):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        y = np.empty_like(v)
+        flags = (APPLY_FP32 if fp32 else 0) | (APPLY_MASKED if masked else 0)
+        self._check(self._lib.jfem_apply(self._h, _ptr(v, _f64p), _ptr(y, _f64p), flags))
+        return y
+
+    def apply_device(self, v_ptr: int, y_ptr: int, fp32: bool = True, masked: bool = False):
+        flags = (APPLY_FP32 if fp32 else 0) | (APPLY_MASKED if masked else 0)
+        self._check(self._lib.jfem_apply_device(self._h, C.c_void_p(v_ptr), C.c_void_p(y_ptr), flags))
+
+    def internal_force(self):
+        f = np.empty(3 * self.n_nodes)
+        self._check(self._lib.jfem_internal_force(self._h, _ptr(f, _f64p)))
+        return f
+
+    def solve(self, opts: SolveOpts | None = None, **kw):
+        o = opts if opts is not None else default_opts(**kw)
+        u = np.empty(3 * self.n_nodes)
+        st = Stats()
+        rc = self._check(self._lib.jfem_solve(self._h, C.byref(o), _ptr(u, _f64p), C.byref(st)))
+        return u, st, rc
+
+    def solve_device(self, u_ptr: int, opts: SolveOpts | None = None, **kw):
+        o = opts if opts is not None else default_opts(**kw)
+        st = Stats()
+        rc = self._check(self._lib.jfem_solve_device(self._h, C.byref(o), C.c_void_p(u_ptr), C.byref(st)))
+        return st, rc
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self._lib.jfem_kernel_launches(self._h))
+
+    @property
+    def last_apply_ms(self) -> float:
+        return float(self._lib.jfem_last_apply_ms(self._h))

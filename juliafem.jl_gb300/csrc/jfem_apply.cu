@@ -1,0 +1,275 @@
+// jfem_apply.cu — matrix-free K·v / tangent apply and internal force.
+//
+// Reference: the two-phase Tet4 operator of ext/JuliaFEMCUDAExt.jl:222-361,442-478
+// (stress per Gauss point, then an atomic-free node gather) and the nodal matvec
+// of src/nodal_assembly_structures.jl:197-212.  Here the stress never leaves
+// registers: phase 1 is one thread per element computing y_e = K_e v_e for every
+// integration point and writing the element vector (SoA, coalesced); phase 2 is
+// one thread per node summing the element vectors of that node in ascending
+// element order (deterministic, no atomics) and optionally a p·Ap partial sum.
+//
+// Geometry is prepared once per mesh/material in FP64 and stored as FP32 (and
+// FP64 for the residual path): for affine elements (every Tet4, straight-sided
+// Tet10, parallelepiped Hex8) J is constant, so one record per element holds
+// J⁻¹ (9) and λ·detJ, μ·detJ (2); otherwise a record per integration point holds
+// J⁻¹ (9) and detJ, plus λ, μ per element.  Computing J from FP32 coordinates
+// would lose |X|/h·2⁻²⁴ relative accuracy (≈2e-5 on a 20-long beam with h = 0.05).
+//
+// Per integration point with reference derivatives dN (compile-time constants):
+//   Gv[c][a] = Σ_i v_i[c] dN_i[a],  ∇v[c][d] = Σ_a Gv[c][a] J⁻¹[d][a]
+//   flux P (σ, or the tangent δP = F δS + ∇v S),  Q[c][a] = w detJ Σ_d P[c][d] J⁻¹[d][a]
+//   y_i[c] += Σ_a Q[c][a] dN_i[a]
+#include "jfem_common.cuh"
+
+namespace jfem {
+
+void launch_apply_tet4(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop);
+void launch_apply_tet10(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop);
+void launch_apply_hex8(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop);
+
+// ---------------------------------------------------------------------------
+// geometry preparation (FP64)
+// ---------------------------------------------------------------------------
+template <int ET>
+__global__ void k_affine_check(int64_t E, const int* __restrict__ conn, const double* __restrict__ X,
+                               int* __restrict__ nonaffine, int* err) {
+  constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    double J0[3][3];
+    for (int q = 0; q < NQ; ++q) {
+      double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+      for (int i = 0; i < NN; ++i) {
+        const int64_t n = conn[(int64_t)i * E + e];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) J[a][b] += dshape(ET, q, i, a) * X[3 * n + b];
+      }
+      if (!(det3(J) > 0.0)) raise_error(err, JFEM_ERR_NEG_JACOBIAN);
+      if (q == 0) {
+        for (int a = 0; a < 3; ++a)
+          for (int b = 0; b < 3; ++b) J0[a][b] = J[a][b];
+      } else {
+        double sc = 0.0, df = 0.0;
+        for (int a = 0; a < 3; ++a)
+          for (int b = 0; b < 3; ++b) {
+            sc = fmax(sc, fabs(J0[a][b]));
+            df = fmax(df, fabs(J[a][b] - J0[a][b]));
+          }
+        if (df > 1e-12 * sc) atomicExch(nonaffine, 1);
+      }
+    }
+  }
+}
+
+// Records (SoA, stride E):
+//   affine:     k = 0..8 J⁻¹ (row-major [d][a]), 9 λ·detJ, 10 μ·detJ           → 11
+//   non-affine: k = 10q + 0..8 J⁻¹, 10q + 9 detJ; then 10NQ: λ, 10NQ+1: μ      → 10NQ+2
+template <int ET>
+__global__ void k_prepare_geo(int64_t E, const int* __restrict__ conn, const double* __restrict__ X,
+                              const double* __restrict__ lam, const double* __restrict__ mu, int affine,
+                              double* __restrict__ g64, float* __restrict__ g32) {
+  constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    const int nq = affine ? 1 : NQ;
+    for (int q = 0; q < nq; ++q) {
+      double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+      for (int i = 0; i < NN; ++i) {
+        const int64_t n = conn[(int64_t)i * E + e];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) J[a][b] += dshape(ET, q, i, a) * X[3 * n + b];
+      }
+      const double det = det3(J);
+      double A[3][3];
+      adj3(J, A);
+      const double id = 1.0 / det;
+      // J⁻¹[d][a] with ∂N/∂X_d = Σ_a J⁻¹[d][a] ∂N/∂ξ_a
+      double rec[10];
+      for (int d = 0; d < 3; ++d)
+        for (int a = 0; a < 3; ++a) rec[3 * d + a] = A[d][a] * id;
+      if (affine) {
+        for (int k = 0; k < 9; ++k) {
+          g64[(int64_t)k * E + e] = rec[k];
+          g32[(int64_t)k * E + e] = (float)rec[k];
+        }
+        const double ld = lam[e] * det, md = mu[e] * det;
+        g64[(int64_t)9 * E + e] = ld;
+        g64[(int64_t)10 * E + e] = md;
+        g32[(int64_t)9 * E + e] = (float)ld;
+        g32[(int64_t)10 * E + e] = (float)md;
+      } else {
+        rec[9] = det;
+        for (int k = 0; k < 10; ++k) {
+          g64[(int64_t)(10 * q + k) * E + e] = rec[k];
+          g32[(int64_t)(10 * q + k) * E + e] = (float)rec[k];
+        }
+      }
+    }
+    if (!affine) {
+      g64[(int64_t)(10 * NQ) * E + e] = lam[e];
+      g64[(int64_t)(10 * NQ + 1) * E + e] = mu[e];
+      g32[(int64_t)(10 * NQ) * E + e] = (float)lam[e];
+      g32[(int64_t)(10 * NQ + 1) * E + e] = (float)mu[e];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// phase 2: node gather (ascending element order), masking and optional v·y partials
+// ---------------------------------------------------------------------------
+template <typename R, bool DOT>
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_gather(int64_t N, int64_t E, const int* __restrict__ ptr,
+                                                             const unsigned* __restrict__ adj,
+                                                             const R* __restrict__ ye,
+                                                             const uint8_t* __restrict__ mask, int masked,
+                                                             const double* __restrict__ v,
+                                                             double* __restrict__ y, double* __restrict__ part,
+                                                             const int* __restrict__ stop) {
+  __shared__ double sh[32];
+  if (stop && *stop) return;
+  double dot = 0.0;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    const int t1 = __ldg(ptr + j + 1);
+    for (int t = __ldg(ptr + j); t < t1; ++t) {
+      const unsigned pk = __ldg(adj + t);
+      const int64_t e = pk >> 4;
+      const int a = (int)(pk & 15u);
+      s0 += (double)__ldg(ye + (int64_t)(3 * a + 0) * E + e);
+      s1 += (double)__ldg(ye + (int64_t)(3 * a + 1) * E + e);
+      s2 += (double)__ldg(ye + (int64_t)(3 * a + 2) * E + e);
+    }
+    if (masked) {
+      const uint8_t m = __ldg(mask + j);
+      if (m & 1) s0 = 0.0;
+      if (m & 2) s1 = 0.0;
+      if (m & 4) s2 = 0.0;
+    }
+    y[3 * j] = s0;
+    y[3 * j + 1] = s1;
+    y[3 * j + 2] = s2;
+    if (DOT) dot += v[3 * j] * s0 + v[3 * j + 1] * s1 + v[3 * j + 2] * s2;
+  }
+  if (DOT) {
+    const double b = block_sum(dot, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = b;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+int geometry_invalidate(Ctx* c) {
+  if (c->geo64) { dfree(c, c->geo64); c->geo64 = nullptr; }
+  if (c->geo32) { dfree(c, c->geo32); c->geo32 = nullptr; }
+  c->geo_ready = false;
+  return 0;
+}
+
+template <int ET>
+static int prepare_et(Ctx* c) {
+  constexpr int NQ = Elem<ET>::NQ;
+  int* flag = nullptr;
+  if (cudaMalloc(&flag, sizeof(int)) != cudaSuccess) return set_err(c, JFEM_ERR_OOM, "geometry flag");
+  cudaMemsetAsync(flag, 0, sizeof(int), c->stream);
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  k_affine_check<ET><<<grid_for(c->E, 128), 128, 0, c->stream>>>(c->E, c->conn, c->X64, flag, c->d_err);
+  int h_flag = 0, h_err = 0;
+  cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(&h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  int rc = sync_and_check(c, "affine check");
+  cudaFree(flag);
+  c->launches += 1;
+  if (rc) return rc;
+  if (h_err) return set_err(c, JFEM_ERR_NEG_JACOBIAN, "element with non-positive Jacobian determinant");
+  c->geo_affine = (h_flag == 0);
+  const int64_t rec = c->geo_affine ? 11 : (10 * NQ + 2);
+  if ((rc = dalloc(c, &c->geo64, rec * c->E))) return rc;
+  if ((rc = dalloc(c, &c->geo32, rec * c->E))) return rc;
+  k_prepare_geo<ET><<<grid_for(c->E, 128), 128, 0, c->stream>>>(c->E, c->conn, c->X64, c->lam64, c->mu64,
+                                                                c->geo_affine ? 1 : 0, c->geo64, c->geo32);
+  c->launches += 1;
+  rc = sync_and_check(c, "geometry");
+  if (!rc) c->geo_ready = true;
+  return rc;
+}
+
+int geometry_prepare(Ctx* c) {
+  if (c->geo_ready) return 0;
+  if (!c->have_material) return set_err(c, JFEM_ERR_INVALID, "jfem_set_material must come first");
+  switch (c->et) {
+    case JFEM_TET4: return prepare_et<JFEM_TET4>(c);
+    case JFEM_TET10: return prepare_et<JFEM_TET10>(c);
+    default: return prepare_et<JFEM_HEX8>(c);
+  }
+}
+
+static void launch_elements(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop) {
+  switch (c->et) {
+    case JFEM_TET4: launch_apply_tet4(c, fp32, mode, v, mask_in, stop); break;
+    case JFEM_TET10: launch_apply_tet10(c, fp32, mode, v, mask_in, stop); break;
+    default: launch_apply_hex8(c, fp32, mode, v, mask_in, stop); break;
+  }
+}
+
+// Enqueue (no sync): y = K v (masked rows zero when masked), partial v·y sums
+// into part[0..JFEM_RED_BLOCKS) when part != nullptr.
+void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, bool mask_in, double* part,
+                   const int* stop) {
+  launch_elements(c, fp32, 0, v, mask_in, stop);
+  const unsigned gb = part ? JFEM_RED_BLOCKS : grid_for(c->N, JFEM_RED_THREADS);
+  if (fp32) {
+    if (part) k_gather<float, true><<<gb, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->E, c->adj_ptr, c->adj, c->ye32, c->mask, masked, v, y, part, stop);
+    else k_gather<float, false><<<gb, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->E, c->adj_ptr, c->adj, c->ye32, c->mask, masked, v, y, part, stop);
+  } else {
+    if (part) k_gather<double, true><<<gb, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->E, c->adj_ptr, c->adj, c->ye64, c->mask, masked, v, y, part, stop);
+    else k_gather<double, false><<<gb, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->E, c->adj_ptr, c->adj, c->ye64, c->mask, masked, v, y, part, stop);
+  }
+  c->launches += 1;
+}
+
+int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, double* part) {
+  int rc = geometry_prepare(c);
+  if (rc) return rc;
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  cudaEventRecord(c->ev0, c->stream);
+  enqueue_apply(c, v, y, fp32, masked, masked, part, nullptr);
+  cudaEventRecord(c->ev1, c->stream);
+  int h_err = 0;
+  cudaMemcpyAsync(&h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  rc = sync_and_check(c, "apply");
+  if (rc) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->last_apply_ms = ms;
+  if (h_err) return set_err(c, h_err, "invalid material state in apply (det C <= 0 or NaN)");
+  return 0;
+}
+
+// Enqueue f_int(u) (FP64) into f (no sync).  Linear small strain: K u.
+void enqueue_internal_force(Ctx* c, double* f) {
+  if (!c->finite) launch_elements(c, false, 0, c->u_state, false, nullptr);
+  else launch_elements(c, false, 1, nullptr, false, nullptr);
+  k_gather<double, false><<<grid_for(c->N, JFEM_RED_THREADS), JFEM_RED_THREADS, 0, c->stream>>>(
+      c->N, c->E, c->adj_ptr, c->adj, c->ye64, c->mask, 0, nullptr, f, nullptr, nullptr);
+  c->launches += 1;
+}
+
+int internal_force_device(Ctx* c, double* f) {
+  int rc = geometry_prepare(c);
+  if (rc) return rc;
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  enqueue_internal_force(c, f);
+  int h_err = 0;
+  cudaMemcpyAsync(&h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  rc = sync_and_check(c, "internal force");
+  if (rc) return rc;
+  if (h_err) return set_err(c, h_err, "invalid material state (det C <= 0 or NaN)");
+  return 0;
+}
+
+}  // namespace jfem

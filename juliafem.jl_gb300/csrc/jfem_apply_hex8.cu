@@ -1,0 +1,8 @@
+// jfem_apply_hex8.cu — element-kernel instantiations for Hex8.
+#include "jfem_apply_kernels.cuh"
+
+namespace jfem {
+void launch_apply_hex8(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop) {
+  launch_apply_et<JFEM_HEX8>(c, fp32, mode, v, mask_in, stop);
+}
+}  // namespace jfem

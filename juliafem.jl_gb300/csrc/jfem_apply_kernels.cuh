@@ -1,0 +1,316 @@
+// jfem_apply_kernels.cuh — element kernels of the matrix-free apply (see
+// jfem_apply.cu for the design); included by one translation unit per element
+// type so the instantiations compile in parallel.
+#pragma once
+#include "jfem_common.cuh"
+
+namespace jfem {
+
+enum Kin { KIN_SMALL = 0, KIN_SVK = 1, KIN_NH = 2 };
+
+// ---------------------------------------------------------------------------
+// constitutive flux at one integration point
+// ---------------------------------------------------------------------------
+// Linear small strain: P = λ tr(ε) I + 2μ ε with ε = sym(∇v).
+template <typename R>
+__device__ __forceinline__ void flux_small(const R gv[3][3], R lam, R mu, R P[3][3]) {
+  const R tr = gv[0][0] + gv[1][1] + gv[2][2];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) P[c][d] = mu * (gv[c][d] + gv[d][c]) + (c == d ? lam * tr : R(0));
+}
+
+// Finite-strain tangent: δP = F δS + [geom] ∇v S, δE = sym(Fᵀ∇v).
+// SVK: S = λ tr(E) I + 2μ E, δS = λ tr(δE) I + 2μ δE.
+// Neo-Hookean: S = μ(I − C⁻¹) + λ lnJ C⁻¹, δS = λ tr(C⁻¹δE) C⁻¹ + 2(μ − λ lnJ) C⁻¹ δE C⁻¹.
+// Returns false when det C ≤ 0.
+template <typename R, int KIN, bool GEOM>
+__device__ __forceinline__ bool flux_tangent(const R gu[3][3], const R gv[3][3], R lam, R mu, R P[3][3]) {
+  R F[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) F[i][j] = gu[i][j] + (i == j ? R(1) : R(0));
+  // C = FᵀF, δE = sym(Fᵀ ∇v)
+  R C[3][3], dE[3][3], FtG[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      C[i][j] = F[0][i] * F[0][j] + F[1][i] * F[1][j] + F[2][i] * F[2][j];
+      FtG[i][j] = F[0][i] * gv[0][j] + F[1][i] * gv[1][j] + F[2][i] * gv[2][j];
+    }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dE[i][j] = R(0.5) * (FtG[i][j] + FtG[j][i]);
+  R S[3][3], dS[3][3];
+  bool ok = true;
+  if (KIN == KIN_SVK) {
+    const R trE = R(0.5) * (C[0][0] + C[1][1] + C[2][2] - R(3));
+    const R trdE = dE[0][0] + dE[1][1] + dE[2][2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const R Eij = R(0.5) * (C[i][j] - (i == j ? R(1) : R(0)));
+        S[i][j] = R(2) * mu * Eij + (i == j ? lam * trE : R(0));
+        dS[i][j] = R(2) * mu * dE[i][j] + (i == j ? lam * trdE : R(0));
+      }
+  } else {
+    const R detC = det3(C);
+    ok = detC > R(0);
+    R Ci[3][3];
+    adj3(C, Ci);
+    const R id = R(1) / detC;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Ci[i][j] *= id;
+    const R lnJ = R(0.5) * log(detC);
+    const R cc = mu - lam * lnJ;
+    R CidE[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) CidE[i][j] = Ci[i][0] * dE[0][j] + Ci[i][1] * dE[1][j] + Ci[i][2] * dE[2][j];
+    const R tr = CidE[0][0] + CidE[1][1] + CidE[2][2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        S[i][j] = mu * ((i == j ? R(1) : R(0)) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+        const R CdC = CidE[i][0] * Ci[0][j] + CidE[i][1] * Ci[1][j] + CidE[i][2] * Ci[2][j];
+        dS[i][j] = lam * tr * Ci[i][j] + R(2) * cc * CdC;
+      }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      R s = F[i][0] * dS[0][j] + F[i][1] * dS[1][j] + F[i][2] * dS[2][j];
+      if (GEOM) s += gv[i][0] * S[0][j] + gv[i][1] * S[1][j] + gv[i][2] * S[2][j];
+      P[i][j] = s;
+    }
+  return ok;
+}
+
+// First Piola stress P = F S at state u (finite) — internal force flux.
+template <typename R, int KIN>
+__device__ __forceinline__ bool flux_pk1(const R gu[3][3], R lam, R mu, R P[3][3]) {
+  R F[3][3], C[3][3], S[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) F[i][j] = gu[i][j] + (i == j ? R(1) : R(0));
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[i][j] = F[0][i] * F[0][j] + F[1][i] * F[1][j] + F[2][i] * F[2][j];
+  bool ok = true;
+  if (KIN == KIN_SVK) {
+    const R trE = R(0.5) * (C[0][0] + C[1][1] + C[2][2] - R(3));
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) S[i][j] = mu * (C[i][j] - (i == j ? R(1) : R(0))) + (i == j ? lam * trE : R(0));
+  } else {
+    const R detC = det3(C);
+    ok = detC > R(0);
+    R Ci[3][3];
+    adj3(C, Ci);
+    const R id = R(1) / detC;
+    const R lnJ = R(0.5) * log(detC);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) S[i][j] = mu * ((i == j ? R(1) : R(0)) - Ci[i][j] * id) + lam * lnJ * Ci[i][j] * id;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) P[i][j] = F[i][0] * S[0][j] + F[i][1] * S[1][j] + F[i][2] * S[2][j];
+  return ok;
+}
+
+// ---------------------------------------------------------------------------
+// phase 1: element kernel
+//   MODE 0: y = K v (linear) / K_T(u) v (finite, KIN ≠ SMALL)
+//   MODE 1: y = f_int(u) (v ignored; KIN ≠ SMALL)
+// ---------------------------------------------------------------------------
+template <int ET, typename R, bool AFFINE, int KIN, bool GEOM, int MODE>
+__global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __restrict__ conn,
+                                                    const R* __restrict__ geo, const double* __restrict__ v,
+                                                    const double* __restrict__ u,
+                                                    const uint8_t* __restrict__ mask, R* __restrict__ ye,
+                                                    int* err, const int* __restrict__ stop,
+                                                    int mask_in) {
+  constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
+  if (stop && *stop) return;
+  constexpr bool NEED_U = (KIN != KIN_SMALL);
+  constexpr bool NEED_V = (MODE == 0);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    int nodes[NN];
+#pragma unroll
+    for (int i = 0; i < NN; ++i) nodes[i] = __ldg(conn + (int64_t)i * E + e);
+    R ve[NN][3], ue[NN][3];
+#pragma unroll
+    for (int i = 0; i < NN; ++i) {
+      const int64_t n = nodes[i];
+      if (NEED_V) {
+        ve[i][0] = (R)__ldg(v + 3 * n);
+        ve[i][1] = (R)__ldg(v + 3 * n + 1);
+        ve[i][2] = (R)__ldg(v + 3 * n + 2);
+        if (mask_in) {
+          const uint8_t m = __ldg(mask + n);
+          if (m & 1) ve[i][0] = R(0);
+          if (m & 2) ve[i][1] = R(0);
+          if (m & 4) ve[i][2] = R(0);
+        }
+      }
+      if (NEED_U) {
+        ue[i][0] = (R)__ldg(u + 3 * n);
+        ue[i][1] = (R)__ldg(u + 3 * n + 1);
+        ue[i][2] = (R)__ldg(u + 3 * n + 2);
+      }
+    }
+    R y[NN][3];
+#pragma unroll
+    for (int i = 0; i < NN; ++i) y[i][0] = y[i][1] = y[i][2] = R(0);
+    R iJ[9], lam, mu, det = R(1);
+    if (AFFINE) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) iJ[k] = __ldg(geo + (int64_t)k * E + e);
+      lam = __ldg(geo + (int64_t)9 * E + e);
+      mu = __ldg(geo + (int64_t)10 * E + e);
+    } else {
+      lam = __ldg(geo + (int64_t)(10 * NQ) * E + e);
+      mu = __ldg(geo + (int64_t)(10 * NQ + 1) * E + e);
+    }
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      if (!AFFINE) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) iJ[k] = __ldg(geo + (int64_t)(10 * q + k) * E + e);
+        det = __ldg(geo + (int64_t)(10 * q + 9) * E + e);
+      }
+      R gv[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, gu[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+      if (NEED_V) {
+        R G[3][3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            R s = R(0);
+#pragma unroll
+            for (int i = 0; i < NN; ++i) {
+              const R dn = (R)dshape(ET, q, i, a);
+              if (dn != R(0)) s += ve[i][c] * dn;
+            }
+            G[c][a] = s;
+          }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) gv[c][d] = G[c][0] * iJ[3 * d] + G[c][1] * iJ[3 * d + 1] + G[c][2] * iJ[3 * d + 2];
+      }
+      if (NEED_U) {
+        R G[3][3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            R s = R(0);
+#pragma unroll
+            for (int i = 0; i < NN; ++i) {
+              const R dn = (R)dshape(ET, q, i, a);
+              if (dn != R(0)) s += ue[i][c] * dn;
+            }
+            G[c][a] = s;
+          }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) gu[c][d] = G[c][0] * iJ[3 * d] + G[c][1] * iJ[3 * d + 1] + G[c][2] * iJ[3 * d + 2];
+      }
+      R P[3][3];
+      if (MODE == 1) {
+        ok &= flux_pk1<R, KIN>(gu, lam, mu, P);
+      } else if (KIN == KIN_SMALL) {
+        flux_small<R>(gv, lam, mu, P);
+      } else {
+        ok &= flux_tangent<R, KIN, GEOM>(gu, gv, lam, mu, P);
+      }
+      // Q[c][a] = w·detJ Σ_d P[c][d] J⁻¹[d][a]   (affine records carry detJ inside λ, μ)
+      const R wq = (R)qp_weight(ET, q) * det;
+      R Q[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) Q[c][a] = wq * (P[c][0] * iJ[a] + P[c][1] * iJ[3 + a] + P[c][2] * iJ[6 + a]);
+#pragma unroll
+      for (int i = 0; i < NN; ++i)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const R dn = (R)dshape(ET, q, i, a);
+          if (dn != R(0)) {
+            y[i][0] += Q[0][a] * dn;
+            y[i][1] += Q[1][a] * dn;
+            y[i][2] += Q[2][a] * dn;
+          }
+        }
+    }
+    if (!ok) raise_error(err, JFEM_ERR_NAN);
+#pragma unroll
+    for (int i = 0; i < NN; ++i)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) ye[(int64_t)(3 * i + c) * E + e] = y[i][c];
+  }
+}
+
+
+// ---------------------------------------------------------------------------
+// launch helpers, instantiated once per element type (jfem_apply_<type>.cu)
+// ---------------------------------------------------------------------------
+template <int ET, typename R, bool AFFINE, int KIN, bool GEOM, int MODE>
+static void launch_elem(Ctx* c, const R* geo, const double* v, R* ye, const int* stop, bool mask_in) {
+  const unsigned g = grid_for(c->E, 128, 1LL << 30);
+  k_apply_elem<ET, R, AFFINE, KIN, GEOM, MODE><<<g, 128, 0, c->stream>>>(c->E, c->conn, geo, v, c->u_state, c->mask,
+                                                                         ye, c->d_err, stop, mask_in ? 1 : 0);
+  c->launches += 1;
+}
+
+template <int ET, typename R, bool AFFINE, int MODE>
+static void dispatch_kin(Ctx* c, const R* geo, const double* v, R* ye, bool mask_in, const int* stop) {
+  const int kin = (!c->finite && MODE == 0) ? KIN_SMALL : (c->model == JFEM_NEO_HOOKEAN ? KIN_NH : KIN_SVK);
+  if (MODE == 0 && kin == KIN_SMALL) {
+    launch_elem<ET, R, AFFINE, KIN_SMALL, false, 0>(c, geo, v, ye, stop, mask_in);
+  } else if (kin == KIN_SVK) {
+    if (MODE == 1) launch_elem<ET, R, AFFINE, KIN_SVK, false, 1>(c, geo, v, ye, stop, false);
+    else if (c->geom) launch_elem<ET, R, AFFINE, KIN_SVK, true, 0>(c, geo, v, ye, stop, mask_in);
+    else launch_elem<ET, R, AFFINE, KIN_SVK, false, 0>(c, geo, v, ye, stop, mask_in);
+  } else if (kin == KIN_NH) {
+    if (MODE == 1) launch_elem<ET, R, AFFINE, KIN_NH, false, 1>(c, geo, v, ye, stop, false);
+    else if (c->geom) launch_elem<ET, R, AFFINE, KIN_NH, true, 0>(c, geo, v, ye, stop, mask_in);
+    else launch_elem<ET, R, AFFINE, KIN_NH, false, 0>(c, geo, v, ye, stop, mask_in);
+  }
+}
+
+// mode 0: y = K v (tangent for finite strain); mode 1: f_int(u) (finite strain only)
+template <int ET>
+void launch_apply_et(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop) {
+  if (fp32) {
+    if (c->geo_affine) dispatch_kin<ET, float, true, 0>(c, c->geo32, v, c->ye32, mask_in, stop);
+    else dispatch_kin<ET, float, false, 0>(c, c->geo32, v, c->ye32, mask_in, stop);
+  } else if (mode == 0) {
+    if (c->geo_affine) dispatch_kin<ET, double, true, 0>(c, c->geo64, v, c->ye64, mask_in, stop);
+    else dispatch_kin<ET, double, false, 0>(c, c->geo64, v, c->ye64, mask_in, stop);
+  } else {
+    if (c->geo_affine) dispatch_kin<ET, double, true, 1>(c, c->geo64, v, c->ye64, false, stop);
+    else dispatch_kin<ET, double, false, 1>(c, c->geo64, v, c->ye64, false, stop);
+  }
+}
+
+}  // namespace jfem

@@ -1,0 +1,8 @@
+// jfem_apply_tet10.cu — element-kernel instantiations for Tet10.
+#include "jfem_apply_kernels.cuh"
+
+namespace jfem {
+void launch_apply_tet10(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop) {
+  launch_apply_et<JFEM_TET10>(c, fp32, mode, v, mask_in, stop);
+}
+}  // namespace jfem

@@ -1,0 +1,8 @@
+// jfem_apply_tet4.cu — element-kernel instantiations for Tet4.
+#include "jfem_apply_kernels.cuh"
+
+namespace jfem {
+void launch_apply_tet4(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop) {
+  launch_apply_et<JFEM_TET4>(c, fp32, mode, v, mask_in, stop);
+}
+}  // namespace jfem

@@ -1,0 +1,579 @@
+// jfem_assemble.cu — FP64 element integration fused with a deterministic scatter
+// into the global CSC matrix, surface traction, and the Jacobi diagonal.
+//
+// Reference semantics: element kernel src/problems_elasticity.jl:203-451
+// (Km += w BLᵀ D BL, Kg += w BNLᵀ Ŝ BNL, f_int += w BLᵀ σ), COO push + sparse()
+// of src/sparse/sparse.jl:121-132,53 (full 3×3 node blocks, zeros kept,
+// duplicates summed in element order), traction :454-502.
+//
+// Design: kernel 1 evaluates every integration point once (∇N, w·detJ, F, S, 𝔻,
+// P) into a per-point record.  Kernel 2 runs one warp per node J (= one block
+// column of K): it walks the elements of J in ascending element order, forms the
+// 3×3 blocks (b, a) of each element matrix on the fly (lane = (b, row comp)) and
+// adds them into a per-warp shared-memory column.  Every global entry therefore
+// receives its element contributions in ascending element order — the same order
+// sparse() sums the COO duplicates — with no atomics, and element matrices are
+// never written to HBM.
+#include "jfem_common.cuh"
+
+namespace jfem {
+
+// Voigt order 11, 22, 33, 12, 23, 13 (problems_elasticity.jl:189-197)
+__device__ __constant__ int c_VI[6] = {0, 1, 2, 0, 1, 0};
+__device__ __constant__ int c_VJ[6] = {0, 1, 2, 1, 2, 2};
+
+template <int ET>
+struct QD {
+  static constexpr int NN = Elem<ET>::NN;
+  static constexpr int G = 0;                 // ∇N  [NN][3]
+  static constexpr int W = 3 * NN;            // w·detJ
+  static constexpr int FF = W + 1;            // F   [3][3]
+  static constexpr int S = FF + 9;            // S   Voigt [6]
+  static constexpr int D = S + 6;             // 𝔻   [6][6]
+  static constexpr int P = D + 36;            // P = F·S [3][3]
+  static constexpr int SIZE = P + 9;
+};
+
+// Material law at one integration point (FP64).  gu = ∇u.  Returns 0 or an error.
+__device__ int material64(int model, bool finite, double lam, double mu, const double gu[3][3],
+                          double F[3][3], double S6[6], double D[6][6]) {
+  double eps[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      F[i][j] = (i == j ? 1.0 : 0.0) + (finite ? gu[i][j] : 0.0);
+      if (finite) {
+        double gtg = 0.0;
+        for (int k = 0; k < 3; ++k) gtg += gu[k][i] * gu[k][j];
+        eps[i][j] = 0.5 * (gu[i][j] + gu[j][i] + gtg);
+      } else {
+        eps[i][j] = 0.5 * (gu[i][j] + gu[j][i]);
+      }
+    }
+  if (model == JFEM_NEO_HOOKEAN) {
+    // ψ = μ/2(I₁−3) − μ lnJ + λ/2 ln²J (src/materials/neo_hookean.jl:129-143)
+    double C[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) C[i][j] = 2.0 * eps[i][j] + (i == j ? 1.0 : 0.0);
+    const double detC = det3(C);
+    if (!(detC > 0.0)) return JFEM_ERR_NAN;
+    const double lnJ = 0.5 * log(detC);
+    double Ci[3][3];
+    adj3(C, Ci);
+    const double id = 1.0 / detC;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) Ci[i][j] *= id;
+    for (int I = 0; I < 6; ++I) {
+      const int i = c_VI[I], j = c_VJ[I];
+      S6[I] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+    }
+    const double cc = mu - lam * lnJ;
+    for (int I = 0; I < 6; ++I)
+      for (int K = 0; K < 6; ++K) {
+        const int i = c_VI[I], j = c_VJ[I], k = c_VI[K], l = c_VJ[K];
+        D[I][K] = lam * Ci[i][j] * Ci[k][l] + cc * (Ci[i][k] * Ci[j][l] + Ci[i][l] * Ci[j][k]);
+      }
+  } else {
+    // Hooke (problems_elasticity.jl:313-317); finite strain = St-Venant–Kirchhoff
+    for (int I = 0; I < 6; ++I)
+      for (int K = 0; K < 6; ++K) D[I][K] = 0.0;
+    D[0][0] = D[1][1] = D[2][2] = 2.0 * mu + lam;
+    D[3][3] = D[4][4] = D[5][5] = mu;
+    D[0][1] = D[1][0] = D[1][2] = D[2][1] = D[0][2] = D[2][0] = lam;
+    double ev[6];
+    for (int I = 0; I < 6; ++I) ev[I] = (I < 3 ? 1.0 : 2.0) * eps[c_VI[I]][c_VJ[I]];
+    for (int I = 0; I < 6; ++I) {
+      double s = 0.0;
+      for (int K = 0; K < 6; ++K) s += D[I][K] * ev[K];
+      S6[I] = s;
+    }
+  }
+  return 0;
+}
+
+// Kernel 1: one thread per (element, integration point).
+template <int ET>
+__global__ void __launch_bounds__(128) k_qpoint64(int64_t E, const int* __restrict__ conn,
+                                                  const double* __restrict__ X,
+                                                  const double* __restrict__ u, int use_u,
+                                                  const double* __restrict__ lam_e,
+                                                  const double* __restrict__ mu_e, int model, int finite,
+                                                  double* __restrict__ qd, int* err) {
+  constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
+  using L = QD<ET>;
+  const int64_t total = E * NQ;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = t / NQ;
+    const int q = (int)(t - e * NQ);
+    int nodes[NN];
+#pragma unroll
+    for (int i = 0; i < NN; ++i) nodes[i] = conn[(int64_t)i * E + e];
+    double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double dN[NN][3];
+#pragma unroll
+    for (int i = 0; i < NN; ++i) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) dN[i][a] = dshape(ET, q, i, a);
+      const double x0 = X[3 * (int64_t)nodes[i]], x1 = X[3 * (int64_t)nodes[i] + 1],
+                   x2 = X[3 * (int64_t)nodes[i] + 2];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        J[a][0] += dN[i][a] * x0;
+        J[a][1] += dN[i][a] * x1;
+        J[a][2] += dN[i][a] * x2;
+      }
+    }
+    const double det = det3(J);
+    double* out = qd + t * L::SIZE;
+    if (!(det > 0.0)) {
+      raise_error(err, JFEM_ERR_NEG_JACOBIAN);
+      for (int k = 0; k < L::SIZE; ++k) out[k] = 0.0;
+      continue;
+    }
+    double iJ[3][3];
+    adj3(J, iJ);
+    const double id = 1.0 / det;
+    double g[NN][3];
+    double gu[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+    for (int i = 0; i < NN; ++i) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        g[i][a] = (iJ[a][0] * dN[i][0] + iJ[a][1] * dN[i][1] + iJ[a][2] * dN[i][2]) * id;
+      if (use_u) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const double uc = u[3 * (int64_t)nodes[i] + c];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) gu[c][d] += uc * g[i][d];
+        }
+      }
+    }
+    double F[3][3], S6[6], D[6][6];
+    const int rc = material64(model, finite != 0, lam_e[e], mu_e[e], gu, F, S6, D);
+    if (rc) raise_error(err, rc);
+#pragma unroll
+    for (int i = 0; i < NN; ++i)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) out[L::G + 3 * i + a] = g[i][a];
+    out[L::W] = qp_weight(ET, q) * det;
+    for (int k = 0; k < 9; ++k) out[L::FF + k] = F[k / 3][k % 3];
+    for (int k = 0; k < 6; ++k) out[L::S + k] = S6[k];
+    for (int k = 0; k < 36; ++k) out[L::D + k] = D[k / 6][k % 6];
+    double S[3][3];
+    for (int I = 0; I < 6; ++I) {
+      S[c_VI[I]][c_VJ[I]] = S6[I];
+      S[c_VJ[I]][c_VI[I]] = S6[I];
+    }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) out[L::P + 3 * i + j] = F[i][0] * S[0][j] + F[i][1] * S[1][j] + F[i][2] * S[2][j];
+  }
+}
+
+// BL column for component k of a node with gradient g (problems_elasticity.jl:269-302).
+__device__ __forceinline__ void bl_column(const double F[9], const double g[3], int k, double c[6]) {
+  const double f0 = F[3 * k + 0], f1 = F[3 * k + 1], f2 = F[3 * k + 2];
+  c[0] = f0 * g[0];
+  c[1] = f1 * g[1];
+  c[2] = f2 * g[2];
+  c[3] = f0 * g[1] + f1 * g[0];
+  c[4] = f1 * g[2] + f2 * g[1];
+  c[5] = f2 * g[0] + f0 * g[2];
+}
+
+// Kernel 2: warp per node column; shared accumulator per warp laid out exactly as
+// the node's three CSC columns: acc[k][slot][i] ↔ nzval[9 bp + 3 d k + 3 slot + i].
+template <int ET>
+__global__ void k_scatter64(int64_t N, int64_t E, const int* __restrict__ conn,
+                            const int* __restrict__ adj_ptr, const unsigned* __restrict__ adj,
+                            const int* __restrict__ nb_ptr, const uint16_t* __restrict__ slot,
+                            const double* __restrict__ qd, int geom, int dmax,
+                            double* __restrict__ nzval, double* __restrict__ fint) {
+  constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
+  using L = QD<ET>;
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  double* acc = smem + (size_t)wib * 9 * dmax;
+  const int b = lane / 3, i = lane - 3 * (lane / 3);
+  const bool active = lane < 3 * NN;
+  for (int64_t J = (int64_t)blockIdx.x * wpb + wib; J < N; J += (int64_t)gridDim.x * wpb) {
+    const int d = nb_ptr[J + 1] - nb_ptr[J];
+    for (int k = lane; k < 9 * d; k += 32) acc[k] = 0.0;
+    __syncwarp();
+    double fa = 0.0;
+    for (int t = adj_ptr[J]; t < adj_ptr[J + 1]; ++t) {
+      const unsigned pk = adj[t];
+      const int64_t e = pk >> 4;
+      const int a = (int)(pk & 15u);
+      double K0 = 0.0, K1 = 0.0, K2 = 0.0;
+      for (int q = 0; q < NQ; ++q) {
+        const double* rec = qd + (e * NQ + q) * L::SIZE;
+        const double w = rec[L::W];
+        const double ga[3] = {rec[L::G + 3 * a], rec[L::G + 3 * a + 1], rec[L::G + 3 * a + 2]};
+        if (active) {
+          const double gb[3] = {rec[L::G + 3 * b], rec[L::G + 3 * b + 1], rec[L::G + 3 * b + 2]};
+          double Fm[9];
+#pragma unroll
+          for (int k = 0; k < 9; ++k) Fm[k] = rec[L::FF + k];
+          double cb[6];
+          bl_column(Fm, gb, i, cb);
+          double tj[6];
+#pragma unroll
+          for (int Jv = 0; Jv < 6; ++Jv) {
+            double s = 0.0;
+#pragma unroll
+            for (int Iv = 0; Iv < 6; ++Iv) s += cb[Iv] * rec[L::D + 6 * Iv + Jv];
+            tj[Jv] = s;
+          }
+          double kk[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            double ca[6];
+            bl_column(Fm, ga, k, ca);
+            double s = 0.0;
+#pragma unroll
+            for (int Jv = 0; Jv < 6; ++Jv) s += tj[Jv] * ca[Jv];
+            kk[k] = s;
+          }
+          if (geom) {
+            // BNLᵀ Ŝ BNL block: δ_ik ∇N_b·S·∇N_a (problems_elasticity.jl:378-404)
+            const double* S6 = rec + L::S;
+            const double Sg0 = S6[0] * ga[0] + S6[3] * ga[1] + S6[5] * ga[2];
+            const double Sg1 = S6[3] * ga[0] + S6[1] * ga[1] + S6[4] * ga[2];
+            const double Sg2 = S6[5] * ga[0] + S6[4] * ga[1] + S6[2] * ga[2];
+            kk[i] += gb[0] * Sg0 + gb[1] * Sg1 + gb[2] * Sg2;
+          }
+          K0 += w * kk[0];
+          K1 += w * kk[1];
+          K2 += w * kk[2];
+        }
+        if (lane < 3) {
+          const double* P = rec + L::P;
+          fa += w * (P[3 * lane] * ga[0] + P[3 * lane + 1] * ga[1] + P[3 * lane + 2] * ga[2]);
+        }
+      }
+      if (active) {
+        const int s = slot[(int64_t)t * NN + b];
+        acc[0 * 3 * d + 3 * s + i] += K0;
+        acc[1 * 3 * d + 3 * s + i] += K1;
+        acc[2 * 3 * d + 3 * s + i] += K2;
+      }
+      __syncwarp();
+    }
+    if (nzval) {
+      double* out = nzval + 9 * (int64_t)nb_ptr[J];
+      for (int k = lane; k < 9 * d; k += 32) out[k] = acc[k];
+    }
+    if (fint && lane < 3) fint[3 * J + lane] = fa;
+    __syncwarp();
+  }
+}
+
+__global__ void k_csc_index(int64_t N, const int* __restrict__ nb_ptr, const int* __restrict__ nbr, int base,
+                            int64_t* __restrict__ colptr, int64_t* __restrict__ rowval) {
+  for (int64_t J = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; J < N; J += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p0 = nb_ptr[J];
+    const int d = nb_ptr[J + 1] - nb_ptr[J];
+    for (int k = 0; k < 3; ++k) {
+      colptr[3 * J + k] = 9 * p0 + (int64_t)3 * d * k + base;
+      if (rowval) {
+        int64_t* out = rowval + 9 * p0 + (int64_t)3 * d * k;
+        for (int s = 0; s < d; ++s) {
+          const int64_t r = 3 * (int64_t)nbr[p0 + s];
+          out[3 * s + 0] = r + base;
+          out[3 * s + 1] = r + 1 + base;
+          out[3 * s + 2] = r + 2 + base;
+        }
+      }
+    }
+    if (J == N - 1) colptr[3 * N] = 9 * (int64_t)nb_ptr[N] + base;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// surface traction: per face consistent load (FP64) then node gather in
+// ascending face order (deterministic; the reference GPU kernel uses atomics,
+// ext/JuliaFEMCUDAExt.jl:368-416).
+// ---------------------------------------------------------------------------
+__device__ void face_basis(int ft, int q, double N[6], double dN[6][2]) {
+  double u, v;
+  if (ft == JFEM_TRI3) {
+    u = v = 1.0 / 3.0;
+    N[0] = 1 - u - v; N[1] = u; N[2] = v;
+    dN[0][0] = -1; dN[0][1] = -1; dN[1][0] = 1; dN[1][1] = 0; dN[2][0] = 0; dN[2][1] = 1;
+    return;
+  }
+  if (ft == JFEM_TRI6) {
+    const double pu[3] = {2.0 / 3.0, 1.0 / 6.0, 1.0 / 6.0}, pv[3] = {1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0};
+    u = pu[q]; v = pv[q];
+    N[0] = 1 - 3 * u - 3 * v + 2 * u * u + 4 * u * v + 2 * v * v;
+    N[1] = -u + 2 * u * u;
+    N[2] = -v + 2 * v * v;
+    N[3] = 4 * u - 4 * u * u - 4 * u * v;
+    N[4] = 4 * u * v;
+    N[5] = 4 * v - 4 * u * v - 4 * v * v;
+    dN[0][0] = -3 + 4 * u + 4 * v; dN[0][1] = -3 + 4 * u + 4 * v;
+    dN[1][0] = -1 + 4 * u; dN[1][1] = 0;
+    dN[2][0] = 0; dN[2][1] = -1 + 4 * v;
+    dN[3][0] = 4 - 8 * u - 4 * v; dN[3][1] = -4 * u;
+    dN[4][0] = 4 * v; dN[4][1] = 4 * u;
+    dN[5][0] = -4 * v; dN[5][1] = 4 - 4 * u - 8 * v;
+    return;
+  }
+  const double s[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+  u = ((q & 1) ? JFEM_GL2 : -JFEM_GL2);
+  v = ((q & 2) ? JFEM_GL2 : -JFEM_GL2);
+  for (int i = 0; i < 4; ++i) {
+    N[i] = 0.25 * (1 + s[i][0] * u) * (1 + s[i][1] * v);
+    dN[i][0] = 0.25 * s[i][0] * (1 + s[i][1] * v);
+    dN[i][1] = 0.25 * (1 + s[i][0] * u) * s[i][1];
+  }
+}
+
+__global__ void k_face_load(int64_t F, int ft, int nfn, const int* __restrict__ fconn,
+                            const double* __restrict__ X, const double* __restrict__ trac,
+                            double* __restrict__ fe /* [nfn*3][F] */) {
+  const int nq = face_nq(ft);
+  const double wq = ft == JFEM_TRI3 ? 0.5 : ft == JFEM_TRI6 ? 1.0 / 6.0 : 1.0;
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < F; f += (int64_t)gridDim.x * blockDim.x) {
+    double acc[6][3];
+    for (int i = 0; i < nfn; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.0;
+    const double t0 = trac[4 * f], t1 = trac[4 * f + 1], t2 = trac[4 * f + 2], pr = trac[4 * f + 3];
+    for (int q = 0; q < nq; ++q) {
+      double N[6], dN[6][2];
+      face_basis(ft, q, N, dN);
+      double T[2][3] = {{0, 0, 0}, {0, 0, 0}};
+      for (int i = 0; i < nfn; ++i) {
+        const int64_t n = fconn[(int64_t)i * F + f];
+        for (int b = 0; b < 3; ++b) {
+          T[0][b] += dN[i][0] * X[3 * n + b];
+          T[1][b] += dN[i][1] * X[3 * n + b];
+        }
+      }
+      const double cx = T[0][1] * T[1][2] - T[0][2] * T[1][1];
+      const double cy = T[0][2] * T[1][0] - T[0][0] * T[1][2];
+      const double cz = T[0][0] * T[1][1] - T[0][1] * T[1][0];
+      const double w = wq * sqrt(cx * cx + cy * cy + cz * cz);
+      // pressure: f += w·(−p)·n·N with n = (∂X/∂ξ₁ × ∂X/∂ξ₂)/‖·‖ (problems_elasticity.jl:486-493)
+      for (int i = 0; i < nfn; ++i) {
+        acc[i][0] += (w * t0 - wq * pr * cx) * N[i];
+        acc[i][1] += (w * t1 - wq * pr * cy) * N[i];
+        acc[i][2] += (w * t2 - wq * pr * cz) * N[i];
+      }
+    }
+    for (int i = 0; i < nfn; ++i)
+      for (int c = 0; c < 3; ++c) fe[(int64_t)(3 * i + c) * F + f] = acc[i][c];
+  }
+}
+
+// Node gather of per-item contributions stored SoA [(local*3 + c)][M].
+template <typename Tin>
+__global__ void k_node_gather(int64_t N, int64_t M, const int* __restrict__ ptr, const unsigned* __restrict__ adj,
+                              const Tin* __restrict__ ye, double* __restrict__ y, int accumulate) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int t = ptr[j]; t < ptr[j + 1]; ++t) {
+      const unsigned pk = adj[t];
+      const int64_t e = pk >> 4;
+      const int a = (int)(pk & 15u);
+      s0 += (double)ye[(int64_t)(3 * a + 0) * M + e];
+      s1 += (double)ye[(int64_t)(3 * a + 1) * M + e];
+      s2 += (double)ye[(int64_t)(3 * a + 2) * M + e];
+    }
+    if (accumulate) {
+      y[3 * j] += s0; y[3 * j + 1] += s1; y[3 * j + 2] += s2;
+    } else {
+      y[3 * j] = s0; y[3 * j + 1] = s1; y[3 * j + 2] = s2;
+    }
+  }
+}
+template __global__ void k_node_gather<float>(int64_t, int64_t, const int*, const unsigned*, const float*, double*, int);
+template __global__ void k_node_gather<double>(int64_t, int64_t, const int*, const unsigned*, const double*, double*, int);
+
+int traction_device(Ctx* c, double* f_d) {
+  cudaMemsetAsync(f_d, 0, 3 * c->N * sizeof(double), c->stream);
+  if (c->F == 0) return 0;
+  double* fe = nullptr;
+  if (cudaMalloc(&fe, (size_t)c->F * c->nfn * 3 * sizeof(double)) != cudaSuccess)
+    return set_err(c, JFEM_ERR_OOM, "traction scratch");
+  k_face_load<<<grid_for(c->F, 128), 128, 0, c->stream>>>(c->F, c->ft, c->nfn, c->fconn, c->X64, c->ftrac, fe);
+  k_node_gather<double><<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->F, c->fadj_ptr, c->fadj, fe, f_d, 0);
+  c->launches += 2;
+  const int rc = sync_and_check(c, "traction");
+  cudaFree(fe);
+  return rc;
+}
+
+template <int ET>
+static int assemble_et(Ctx* c, int base, int64_t* colptr_d, int64_t* rowval_d, double* nzval_d, double* fint_d) {
+  using L = QD<ET>;
+  constexpr int NQ = Elem<ET>::NQ;
+  double* qd = nullptr;
+  const size_t bytes = (size_t)c->E * NQ * L::SIZE * sizeof(double);
+  if (cudaMalloc(&qd, bytes) != cudaSuccess) return set_err(c, JFEM_ERR_OOM, "assembly integration-point buffer");
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  k_qpoint64<ET><<<grid_for(c->E * NQ, 128), 128, 0, c->stream>>>(
+      c->E, c->conn, c->X64, c->u_state, c->have_state ? 1 : 0, c->lam64, c->mu64, c->model, c->finite, qd, c->d_err);
+  int wpb = 4;
+  while (wpb > 1 && (size_t)wpb * 9 * c->dmax * sizeof(double) > 96 * 1024) wpb >>= 1;
+  const size_t sm = (size_t)wpb * 9 * c->dmax * sizeof(double);
+  if (sm > 200 * 1024) { cudaFree(qd); return set_err(c, JFEM_ERR_INVALID, "node degree too large for assembly"); }
+  cudaFuncSetAttribute(k_scatter64<ET>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int64_t blocks = (c->N + wpb - 1) / wpb;
+  if (blocks > 152 * 64) blocks = 152 * 64;
+  k_scatter64<ET><<<(unsigned)blocks, 32 * wpb, sm, c->stream>>>(c->N, c->E, c->conn, c->adj_ptr, c->adj, c->nb_ptr,
+                                                                  c->slot, qd, c->geom, c->dmax, nzval_d, fint_d);
+  c->launches += 2;
+  if (colptr_d) {
+    k_csc_index<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, base, colptr_d, rowval_d);
+    c->launches += 1;
+  }
+  int h_err = 0;
+  cudaMemcpyAsync(&h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  int rc = sync_and_check(c, "assembly");
+  cudaFree(qd);
+  if (rc) return rc;
+  if (h_err == JFEM_ERR_NEG_JACOBIAN) return set_err(c, h_err, "element with non-positive Jacobian determinant");
+  if (h_err) return set_err(c, h_err, "invalid material state (J <= 0 or NaN)");
+  return 0;
+}
+
+int assemble_csc_device(Ctx* c, int base, int64_t* colptr_d, int64_t* rowval_d, double* nzval_d, double* fint_d) {
+  switch (c->et) {
+    case JFEM_TET4: return assemble_et<JFEM_TET4>(c, base, colptr_d, rowval_d, nzval_d, fint_d);
+    case JFEM_TET10: return assemble_et<JFEM_TET10>(c, base, colptr_d, rowval_d, nzval_d, fint_d);
+    default: return assemble_et<JFEM_HEX8>(c, base, colptr_d, rowval_d, nzval_d, fint_d);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi diagonal of K (or of the tangent at the current state), FP64, then
+// dinv = 1/diag on free DOFs, 0 on prescribed ones.
+// ---------------------------------------------------------------------------
+template <int ET>
+__global__ void __launch_bounds__(128) k_diag64(int64_t E, const int* __restrict__ conn,
+                                                const double* __restrict__ X, const double* __restrict__ u,
+                                                int use_u, const double* __restrict__ lam_e,
+                                                const double* __restrict__ mu_e, int model, int finite, int geom,
+                                                double* __restrict__ de, int* err) {
+  constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    int nodes[NN];
+#pragma unroll
+    for (int i = 0; i < NN; ++i) nodes[i] = conn[(int64_t)i * E + e];
+    double acc[NN][3];
+#pragma unroll
+    for (int i = 0; i < NN; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.0;
+    for (int q = 0; q < NQ; ++q) {
+      double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+      for (int i = 0; i < NN; ++i)
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int bb = 0; bb < 3; ++bb) J[a][bb] += dshape(ET, q, i, a) * X[3 * (int64_t)nodes[i] + bb];
+      const double det = det3(J);
+      if (!(det > 0.0)) { raise_error(err, JFEM_ERR_NEG_JACOBIAN); break; }
+      double iJ[3][3];
+      adj3(J, iJ);
+      const double id = 1.0 / det;
+      double gu[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+      if (use_u) {
+#pragma unroll
+        for (int i = 0; i < NN; ++i) {
+          double g[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+            g[a] = (iJ[a][0] * dshape(ET, q, i, 0) + iJ[a][1] * dshape(ET, q, i, 1) + iJ[a][2] * dshape(ET, q, i, 2)) * id;
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) {
+            const double uc = u[3 * (int64_t)nodes[i] + cc];
+            gu[cc][0] += uc * g[0]; gu[cc][1] += uc * g[1]; gu[cc][2] += uc * g[2];
+          }
+        }
+      }
+      double F[3][3], S6[6], D[6][6];
+      const int rc = material64(model, finite != 0, lam_e[e], mu_e[e], gu, F, S6, D);
+      if (rc) raise_error(err, rc);
+      const double w = qp_weight(ET, q) * det;
+      const double Fm[9] = {F[0][0], F[0][1], F[0][2], F[1][0], F[1][1], F[1][2], F[2][0], F[2][1], F[2][2]};
+#pragma unroll
+      for (int i = 0; i < NN; ++i) {
+        double g[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+          g[a] = (iJ[a][0] * dshape(ET, q, i, 0) + iJ[a][1] * dshape(ET, q, i, 1) + iJ[a][2] * dshape(ET, q, i, 2)) * id;
+        double gsg = 0.0;
+        if (geom) {
+          gsg = g[0] * (S6[0] * g[0] + S6[3] * g[1] + S6[5] * g[2]) + g[1] * (S6[3] * g[0] + S6[1] * g[1] + S6[4] * g[2]) +
+                g[2] * (S6[5] * g[0] + S6[4] * g[1] + S6[2] * g[2]);
+        }
+        for (int k = 0; k < 3; ++k) {
+          double cb[6];
+          bl_column(Fm, g, k, cb);
+          double s = 0.0;
+          for (int I = 0; I < 6; ++I) {
+            double t = 0.0;
+            for (int K = 0; K < 6; ++K) t += D[I][K] * cb[K];
+            s += cb[I] * t;
+          }
+          acc[i][k] += w * (s + gsg);
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < NN; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) de[(int64_t)(3 * i + k) * E + e] = acc[i][k];
+  }
+}
+
+__global__ void k_invert_diag(int64_t N, const uint8_t* __restrict__ mask, double* __restrict__ d, int* err) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t m = mask[j];
+    for (int c = 0; c < 3; ++c) {
+      const double v = d[3 * j + c];
+      if ((m >> c) & 1) {
+        d[3 * j + c] = 0.0;
+      } else if (!(v > 0.0) || !isfinite(v)) {
+        raise_error(err, JFEM_ERR_NAN);
+        d[3 * j + c] = 0.0;
+      } else {
+        d[3 * j + c] = 1.0 / v;
+      }
+    }
+  }
+}
+
+int jacobi_diag_device(Ctx* c, double* dinv_d) {
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  const int use_u = c->have_state ? 1 : 0;
+  const unsigned g = grid_for(c->E, 128);
+  switch (c->et) {
+    case JFEM_TET4:
+      k_diag64<JFEM_TET4><<<g, 128, 0, c->stream>>>(c->E, c->conn, c->X64, c->u_state, use_u, c->lam64, c->mu64,
+                                                    c->model, c->finite, c->geom, c->ye64, c->d_err);
+      break;
+    case JFEM_TET10:
+      k_diag64<JFEM_TET10><<<g, 128, 0, c->stream>>>(c->E, c->conn, c->X64, c->u_state, use_u, c->lam64, c->mu64,
+                                                      c->model, c->finite, c->geom, c->ye64, c->d_err);
+      break;
+    default:
+      k_diag64<JFEM_HEX8><<<g, 128, 0, c->stream>>>(c->E, c->conn, c->X64, c->u_state, use_u, c->lam64, c->mu64,
+                                                    c->model, c->finite, c->geom, c->ye64, c->d_err);
+  }
+  k_node_gather<double><<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->E, c->adj_ptr, c->adj, c->ye64, dinv_d, 0);
+  k_invert_diag<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->mask, dinv_d, c->d_err);
+  c->launches += 3;
+  int h_err = 0;
+  cudaMemcpyAsync(&h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  int rc = sync_and_check(c, "jacobi diagonal");
+  if (rc) return rc;
+  if (h_err == JFEM_ERR_NEG_JACOBIAN) return set_err(c, h_err, "element with non-positive Jacobian determinant");
+  if (h_err) return set_err(c, h_err, "non-positive or non-finite diagonal entry (unconstrained or degenerate DOF)");
+  return 0;
+}
+
+}  // namespace jfem

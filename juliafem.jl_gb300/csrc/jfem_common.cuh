@@ -1,0 +1,300 @@
+// jfem_common.cuh — shared declarations of libjfem_cuda.so (sm_103a).
+//
+// Device data layout (one context = one mesh on one GPU):
+//   X64   [N][3]  f64    node coordinates (FP64 parity path)
+//   X32   [N]     float4 node coordinates (FP32 apply; .w unused)
+//   conn  [n_en][E] i32  structure-of-arrays connectivity (coalesced per local node)
+//   adj_ptr[N+1], adj[E*n_en]  node → (element<<4 | local) lists, ascending element
+//   nb_ptr[N+1],  nbr[nb]      node → sorted neighbour nodes (3×3 block pattern)
+//   slot[E*n_en*n_en] u16      for adjacency entry t of node J and local node b of
+//                              that element: position of conn[b] in nbr(J)
+//   lam/mu [E] f64 + f32       per-element Lamé constants
+//   mask  [N] u8               bit c set: DOF 3n+c prescribed
+//   ye32/ye64 [n_en*3][E]      per-element apply results (SoA), gathered per node
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/jfem.h"
+
+#define JFEM_MAX_NEIGHBOURS 512   // unique neighbour nodes per node (pattern build)
+#define JFEM_RED_BLOCKS 1216      // fixed reduction grid: 152 SMs x 8 → deterministic sums
+#define JFEM_RED_THREADS 256
+
+namespace jfem {
+
+// ---------------------------------------------------------------------------
+// Element traits.  Shape-function derivatives at the integration points are
+// constexpr so that, in fully unrolled loops, the compiler folds the table into
+// immediates (zero entries vanish).  Rules: Tet4 GLTET1, Tet10 GLTET4, Hex8
+// GLHEX8 (src/elements/integrate.jl:19,27-28; src/quadrature/gltet.jl:7-25,
+// src/quadrature/glquad.jl:6-40); derivatives from
+// src/basis/lagrange_generated.jl:229-311.
+// ---------------------------------------------------------------------------
+template <int ET> struct Elem;
+template <> struct Elem<JFEM_TET4> { static constexpr int NN = 4, NQ = 1; };
+template <> struct Elem<JFEM_TET10> { static constexpr int NN = 10, NQ = 4; };
+template <> struct Elem<JFEM_HEX8> { static constexpr int NN = 8, NQ = 8; };
+
+// (5 ± 3√5)/20 and (5 − √5)/20, the GLTET4 abscissae; 1/√3 for Gauss–Legendre 2.
+#define JFEM_TET4A 0.58541019662496845446
+#define JFEM_TET4B 0.13819660112501051518
+#define JFEM_GL2 0.5773502691896258
+
+__host__ __device__ constexpr double qp_coord(int et, int q, int d) {
+  if (et == JFEM_TET4) return 0.25;
+  if (et == JFEM_TET10) return (q == d) ? JFEM_TET4A : JFEM_TET4B;   // (a,b,b),(b,a,b),(b,b,a),(b,b,b)
+  // Hex8: q = i + 2j + 4k, first coordinate fastest
+  return ((q >> d) & 1) ? JFEM_GL2 : -JFEM_GL2;
+}
+
+__host__ __device__ constexpr double qp_weight(int et, int q) {
+  return et == JFEM_TET4 ? 1.0 / 6.0 : et == JFEM_TET10 ? 1.0 / 24.0 : 1.0;
+}
+
+__host__ __device__ constexpr double hex_sign(int i, int d) {
+  // node order (-1,-1,-1),(1,-1,-1),(1,1,-1),(-1,1,-1),(-1,-1,1),(1,-1,1),(1,1,1),(-1,1,1)
+  return d == 0 ? ((i == 1 || i == 2 || i == 5 || i == 6) ? 1.0 : -1.0)
+       : d == 1 ? ((i == 2 || i == 3 || i == 6 || i == 7) ? 1.0 : -1.0)
+                : (i >= 4 ? 1.0 : -1.0);
+}
+
+// ∂N_i/∂ξ_d at integration point q.
+__host__ __device__ constexpr double dshape(int et, int q, int i, int d) {
+  if (et == JFEM_TET4) {
+    return i == 0 ? -1.0 : (i - 1 == d ? 1.0 : 0.0);
+  }
+  if (et == JFEM_TET10) {
+    const double u = qp_coord(et, q, 0), v = qp_coord(et, q, 1), w = qp_coord(et, q, 2);
+    switch (i) {
+      case 0: return -3.0 + 4.0 * u + 4.0 * v + 4.0 * w;
+      case 1: return d == 0 ? -1.0 + 4.0 * u : 0.0;
+      case 2: return d == 1 ? -1.0 + 4.0 * v : 0.0;
+      case 3: return d == 2 ? -1.0 + 4.0 * w : 0.0;
+      case 4: return d == 0 ? 4.0 - 8.0 * u - 4.0 * v - 4.0 * w : -4.0 * u;
+      case 5: return d == 0 ? 4.0 * v : d == 1 ? 4.0 * u : 0.0;
+      case 6: return d == 1 ? 4.0 - 8.0 * v - 4.0 * u - 4.0 * w : -4.0 * v;
+      case 7: return d == 2 ? 4.0 - 8.0 * w - 4.0 * u - 4.0 * v : -4.0 * w;
+      case 8: return d == 0 ? 4.0 * w : d == 1 ? 0.0 : 4.0 * u;
+      default: return d == 0 ? 0.0 : d == 1 ? 4.0 * w : 4.0 * v;
+    }
+  }
+  // Hex8 trilinear
+  const double x0 = qp_coord(et, q, 0), x1 = qp_coord(et, q, 1), x2 = qp_coord(et, q, 2);
+  const double f0 = 1.0 + hex_sign(i, 0) * x0, f1 = 1.0 + hex_sign(i, 1) * x1,
+               f2 = 1.0 + hex_sign(i, 2) * x2;
+  return d == 0 ? 0.125 * hex_sign(i, 0) * f1 * f2
+       : d == 1 ? 0.125 * f0 * hex_sign(i, 1) * f2
+                : 0.125 * f0 * f1 * hex_sign(i, 2);
+}
+
+// Surface rules: Tri3 GLTRI1, Tri6 GLTRI3, Quad4 GLQUAD4 (integrate.jl:15,23-24).
+__host__ __device__ inline int face_nodes(int ft) { return ft == JFEM_TRI3 ? 3 : ft == JFEM_TRI6 ? 6 : 4; }
+__host__ __device__ inline int face_nq(int ft) { return ft == JFEM_TRI3 ? 1 : ft == JFEM_TRI6 ? 3 : 4; }
+
+// ---------------------------------------------------------------------------
+// small dense helpers (Real = float or double)
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ R det3(const R J[3][3]) {
+  return J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+         J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+         J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+}
+
+// adjugate: adj = det · J⁻¹
+template <typename R>
+__device__ __forceinline__ void adj3(const R J[3][3], R A[3][3]) {
+  A[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  A[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+  A[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+  A[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  A[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+  A[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+  A[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  A[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+  A[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+}
+
+// Block-wide deterministic sum (fixed tree order).  blockDim.x ≤ 1024, multiple of 32.
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T* sh /* ≥ 32 entries */) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  T r = (threadIdx.x < nw) ? sh[threadIdx.x] : T(0);
+  if (w == 0)
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  __syncthreads();
+  if (threadIdx.x == 0) sh[0] = r;
+  __syncthreads();
+  r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// Sum of n partials in a fixed order (every thread returns the same value).
+__device__ __forceinline__ double reduce_partials(const double* __restrict__ part, int n, double* sh) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+  return block_sum(s, sh);
+}
+
+// Device error flag: first error wins.
+__device__ __forceinline__ void raise_error(int* flag, int code) { atomicCAS(flag, 0, code); }
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct SolverScalars {
+  double rz[2];      // r·z by iteration parity
+  double rr[2];      // r·r by iteration parity
+  double bb;         // ‖b_free‖²
+  double tol2;       // tol² · bb — stop threshold on r·r
+  int done[2];       // stop flag by iteration parity
+  int iters;
+  int max_iters;
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int64_t launches = 0;
+  double last_apply_ms = 0.0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  // mesh
+  int et = 0, nn = 0;
+  int64_t N = 0, E = 0;
+  double* X64 = nullptr;
+  float4* X32 = nullptr;
+  int* conn = nullptr;
+  int* adj_ptr = nullptr;
+  unsigned* adj = nullptr;
+  int* nb_ptr = nullptr;
+  int* nbr = nullptr;
+  uint16_t* slot = nullptr;
+  int64_t n_blocks = 0;   // 3×3 blocks in the pattern
+  int dmax = 0;           // max neighbours of a node
+  int amax = 0;           // max elements of a node
+
+  // material / formulation
+  int model = JFEM_LINEAR_ELASTIC;
+  int finite = 0, geom = 0;
+  double* lam64 = nullptr;
+  double* mu64 = nullptr;
+  float* lam32 = nullptr;
+  float* mu32 = nullptr;
+  bool have_material = false;
+
+  // Dirichlet
+  uint8_t* mask = nullptr;
+  double* gvals = nullptr;   // prescribed values (3N, zero on free DOFs)
+  int64_t n_fixed = 0;
+  int64_t n_fixed_nonzero = 0;
+
+  // traction
+  int ft = 0, nfn = 0;
+  int64_t F = 0;
+  int* fconn = nullptr;
+  double* ftrac = nullptr;    // [F][4]: traction (3) and pressure
+  int* fadj_ptr = nullptr;
+  unsigned* fadj = nullptr;
+  double* f_ext = nullptr;
+  bool f_ext_dirty = true;
+
+  // state (finite strain)
+  double* u_state = nullptr;
+  bool have_state = false;
+
+  // operator geometry (FP64-prepared; see jfem_apply.cu)
+  bool geo_ready = false;
+  bool geo_affine = true;
+  double* geo64 = nullptr;
+  float* geo32 = nullptr;
+
+  // scratch
+  float* ye32 = nullptr;
+  double* ye64 = nullptr;
+  double* qd = nullptr;       // FP64 per-integration-point data for assembly
+  size_t qd_bytes = 0;
+  int* d_err = nullptr;
+
+  // solver
+  double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *Ap = nullptr,
+         *dinv = nullptr, *b = nullptr, *tmp = nullptr, *tmp2 = nullptr;
+  double* part = nullptr;     // reduction partials (4 × JFEM_RED_BLOCKS)
+  SolverScalars* sc = nullptr;
+  SolverScalars* sc_host = nullptr;   // pinned mirror
+  double* norms = nullptr;            // 2 doubles
+  double* norms_host = nullptr;       // pinned mirror
+  cudaGraphExec_t pcg_graph = nullptr;
+  int pcg_graph_key = -1;
+  int64_t chunk_launches = 0;
+
+  std::vector<void*> owned;   // everything cudaMalloc'ed for this mesh
+};
+
+// error helpers (host)
+int set_err(Ctx* c, int code, const std::string& msg);
+int cuda_check(Ctx* c, cudaError_t e, const char* what);
+int sync_and_check(Ctx* c, const char* what);
+template <typename T>
+int dalloc(Ctx* c, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return set_err(c, JFEM_ERR_OOM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  }
+  c->owned.push_back((void*)*p);
+  return 0;
+}
+void dfree(Ctx* c, void* p);
+void free_mesh(Ctx* c);
+
+inline int grid_for(int64_t n, int threads, int64_t cap = 152LL * 64) {
+  int64_t g = (n + threads - 1) / threads;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (int)g;
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers (one TU each)
+// ---------------------------------------------------------------------------
+// jfem_mesh.cu
+int mesh_setup(Ctx* c, int et, int64_t N, const double* X, int64_t E, const int64_t* conn, int base);
+int faces_setup(Ctx* c, int ft, int64_t F, const int64_t* fconn, const double* t, const double* p, int base);
+int exclusive_scan_i32(Ctx* c, const int* in, int* out, int64_t n, int64_t* total);
+// jfem_assemble.cu
+int assemble_csc_device(Ctx* c, int base, int64_t* colptr_d, int64_t* rowval_d, double* nzval_d,
+                        double* f_d);
+int traction_device(Ctx* c, double* f_d);
+int jacobi_diag_device(Ctx* c, double* dinv_d);
+// jfem_apply.cu
+int geometry_prepare(Ctx* c);
+int geometry_invalidate(Ctx* c);
+void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, bool mask_in, double* part,
+                   const int* stop);
+void enqueue_internal_force(Ctx* c, double* f);
+int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, double* partial_pAp);
+int internal_force_device(Ctx* c, double* f_d);
+// jfem_solver.cu
+void enqueue_axpy(Ctx* c, int64_t n, double a, const double* x, double* y);
+int solve_device(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stats* st);
+
+}  // namespace jfem
+
+struct jfem_ctx {
+  jfem::Ctx c;
+};

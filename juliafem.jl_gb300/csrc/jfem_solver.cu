@@ -1,0 +1,486 @@
+// jfem_solver.cu — Jacobi-PCG (FP64 vectors and dots, FP32 or FP64 apply, FP64
+// true-residual "reliable updates" = iterative refinement) and inexact
+// Newton–Krylov with load stepping for finite strain.
+//
+// Reference loops: CG of src/backend/cpu.jl:221-254 and
+// ext/JuliaFEMCUDAExt.jl:531-577 (there with a device→host sync per dot and an
+// allocation per operator call); Newton–Krylov with Eisenstat–Walker forcing
+// ext/JuliaFEMCUDAExt.jl:685-854 (η = min(forcing_max, ‖R‖^forcing_power),
+// :723-724,819-820); legacy Newton src/solvers.jl:575-620.
+//
+// Device loop: one PCG iteration is four launches — element apply, node gather
+// (+ p·Ap partials), update 1 (x, r, z, r·z and r·r partials), update 2 (p and
+// the scalars).  Reductions are fixed-shape block partials summed in a fixed
+// order, so every run gives bit-identical iterates.  Scalars and the stop flag
+// live in two slots selected by iteration parity: iteration k reads slot s and
+// only block 0 of its last launch writes slot 1−s, so no launch reads what it
+// writes.  Chunks of PCG_CHUNK (even) iterations are captured once into a CUDA
+// graph; the host reads the scalars between chunks only.  After convergence
+// every launch returns at entry, so overshoot inside a chunk costs nothing.
+#include <chrono>
+#include <cmath>
+
+#include "jfem_common.cuh"
+
+namespace jfem {
+
+#define PCG_CHUNK 16
+#define G_ JFEM_RED_BLOCKS
+// part layout: [0,G) p·Ap, [G,2G) r·z, [2G,3G) r·r, [3G,4G) residual norms
+
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_pcg_update1(int64_t n, const SolverScalars* __restrict__ sc,
+                                                                  int slot, double* __restrict__ x,
+                                                                  double* __restrict__ r, double* __restrict__ z,
+                                                                  const double* __restrict__ p,
+                                                                  const double* __restrict__ Ap,
+                                                                  const double* __restrict__ dinv,
+                                                                  double* __restrict__ part) {
+  __shared__ double sh[32];
+  if (sc->done[slot]) return;
+  const double pAp = reduce_partials(part, G_, sh);
+  const double alpha = sc->rz[slot] / pAp;
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    const double ri = r[i] - alpha * Ap[i];
+    r[i] = ri;
+    const double zi = dinv[i] * ri;
+    z[i] = zi;
+    rz += ri * zi;
+    rr += ri * ri;
+  }
+  rz = block_sum(rz, sh);
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    part[G_ + blockIdx.x] = rz;
+    part[2 * G_ + blockIdx.x] = rr;
+  }
+}
+
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_pcg_update2(int64_t n, SolverScalars* __restrict__ sc, int slot,
+                                                                  double* __restrict__ p, const double* __restrict__ z,
+                                                                  const double* __restrict__ part) {
+  __shared__ double sh[32];
+  const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+  if (sc->done[slot]) {
+    if (lead) {   // carry the final state into the other slot
+      sc->done[1 - slot] = 1;
+      sc->rz[1 - slot] = sc->rz[slot];
+      sc->rr[1 - slot] = sc->rr[slot];
+    }
+    return;
+  }
+  const double rz_new = reduce_partials(part + G_, G_, sh);
+  const double rr_new = reduce_partials(part + 2 * G_, G_, sh);
+  const double beta = rz_new / sc->rz[slot];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + beta * p[i];
+  if (lead) {
+    const int it = sc->iters + 1;
+    sc->iters = it;
+    sc->rz[1 - slot] = rz_new;
+    sc->rr[1 - slot] = rr_new;
+    sc->done[1 - slot] = (rr_new <= sc->tol2 || it >= sc->max_iters || !(rr_new == rr_new)) ? 1 : 0;
+  }
+}
+
+// r = (f − y) on free DOFs, 0 on prescribed (y may be null = 0); ‖r‖² partials
+// → part[3G..4G); when fn2 is set also ‖y‖² over all DOFs → part[0..G).
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_residual(int64_t N, const double* __restrict__ f, double fs,
+                                                               const double* __restrict__ y,
+                                                               const uint8_t* __restrict__ mask,
+                                                               double* __restrict__ r, int fn2,
+                                                               double* __restrict__ part) {
+  __shared__ double sh[32];
+  double rr = 0.0, yy = 0.0;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t m = mask[j];
+    for (int c = 0; c < 3; ++c) {
+      const double yv = y ? y[3 * j + c] : 0.0;
+      const double v = ((m >> c) & 1) ? 0.0 : fs * f[3 * j + c] - yv;
+      r[3 * j + c] = v;
+      rr += v * v;
+      yy += yv * yv;
+    }
+  }
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) part[3 * G_ + blockIdx.x] = rr;
+  if (fn2) {
+    yy = block_sum(yy, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = yy;
+  }
+}
+
+// z = dinv r (and p = z on restart); r·z → part[G..2G), r·r → part[2G..3G)
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_precond(int64_t n, const double* __restrict__ r,
+                                                              const double* __restrict__ dinv, double* __restrict__ z,
+                                                              double* __restrict__ p, int restart,
+                                                              double* __restrict__ part) {
+  __shared__ double sh[32];
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double ri = r[i];
+    const double zi = dinv[i] * ri;
+    z[i] = zi;
+    if (restart) p[i] = zi;
+    rz += ri * zi;
+    rr += ri * ri;
+  }
+  rz = block_sum(rz, sh);
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    part[G_ + blockIdx.x] = rz;
+    part[2 * G_ + blockIdx.x] = rr;
+  }
+}
+
+// slot 0 ← (r·z, r·r) of k_precond; optionally bb ← r·r and tol2 = tol² bb
+__global__ void k_scalars_reset(SolverScalars* __restrict__ sc, const double* __restrict__ part, int set_bb,
+                                double tol, int max_iters, int reset_iters) {
+  __shared__ double sh[32];
+  const double rz = reduce_partials(part + G_, G_, sh);
+  const double rr = reduce_partials(part + 2 * G_, G_, sh);
+  if (threadIdx.x == 0) {
+    sc->rz[0] = rz;
+    sc->rr[0] = rr;
+    if (set_bb) {
+      sc->bb = rr;
+      sc->tol2 = tol * tol * rr;
+    }
+    if (reset_iters) sc->iters = 0;
+    sc->max_iters = max_iters;
+    sc->done[0] = (rr <= sc->tol2 || sc->iters >= max_iters) ? 1 : 0;
+    sc->done[1] = 0;
+  }
+}
+
+// out[0] = Σ part[3G..4G), out[1] = Σ part[0..G)
+__global__ void k_sum_norms(const double* __restrict__ part, double* __restrict__ out) {
+  __shared__ double sh[32];
+  const double a = reduce_partials(part + 3 * G_, G_, sh);
+  const double b = reduce_partials(part, G_, sh);
+  if (threadIdx.x == 0) {
+    out[0] = a;
+    out[1] = b;
+  }
+}
+
+// u += du on free DOFs, u += dg on prescribed DOFs
+__global__ void k_update_state(int64_t N, double* __restrict__ u, const double* __restrict__ du,
+                               const double* __restrict__ dg, const uint8_t* __restrict__ mask) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t m = mask[j];
+    for (int c = 0; c < 3; ++c) u[3 * j + c] += ((m >> c) & 1) ? dg[3 * j + c] : du[3 * j + c];
+  }
+}
+
+// dg = frac·g − u on prescribed DOFs (the incremental Dirichlet value of
+// src/problems_dirichlet.jl:60-89), 0 elsewhere; ‖dg‖² → part[3G..4G)
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_bc_increment(int64_t N, const double* __restrict__ gvals,
+                                                                   double frac, const double* __restrict__ u,
+                                                                   const uint8_t* __restrict__ mask,
+                                                                   double* __restrict__ dg, double* __restrict__ part) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t m = mask[j];
+    for (int c = 0; c < 3; ++c) {
+      const double v = ((m >> c) & 1) ? frac * gvals[3 * j + c] - u[3 * j + c] : 0.0;
+      dg[3 * j + c] = v;
+      s += v * v;
+    }
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) part[3 * G_ + blockIdx.x] = s;
+}
+
+__global__ void k_sub_free(int64_t n, double* __restrict__ a, const double* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    a[i] -= b[i];   // b is masked (zero on prescribed rows)
+}
+
+__global__ void k_axpy(int64_t n, double a, const double* __restrict__ x, double* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] += a * x[i];
+}
+
+void enqueue_axpy(Ctx* c, int64_t n, double a, const double* x, double* y) {
+  k_axpy<<<grid_for(n, 256), 256, 0, c->stream>>>(n, a, x, y);
+  c->launches += 1;
+}
+
+// ---------------------------------------------------------------------------
+// host orchestration
+// ---------------------------------------------------------------------------
+static double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+static int read_scalars(Ctx* c) {
+  cudaMemcpyAsync(c->sc_host, c->sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, c->stream);
+  return sync_and_check(c, "solver scalars");
+}
+
+static int read_norms(Ctx* c, double* a, double* b) {
+  k_sum_norms<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->part, c->norms);
+  c->launches += 1;
+  cudaMemcpyAsync(c->norms_host, c->norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  int rc = sync_and_check(c, "norms");
+  if (rc) return rc;
+  *a = c->norms_host[0];
+  if (b) *b = c->norms_host[1];
+  return 0;
+}
+
+// r ← f − K x (FP64 apply, prescribed rows zero); returns ‖r‖²
+static int true_residual(Ctx* c, const double* f, const double* xv, double* r, double* rr_out) {
+  enqueue_apply(c, xv, c->tmp, false, true, false, nullptr, nullptr);
+  k_residual<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, f, 1.0, c->tmp, c->mask, r, 0, c->part);
+  c->launches += 1;
+  return read_norms(c, rr_out, nullptr);
+}
+
+static void enqueue_iteration(Ctx* c, bool fp32, int slot) {
+  enqueue_apply(c, c->p, c->Ap, fp32, true, false, c->part, &c->sc->done[slot]);
+  k_pcg_update1<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->sc, slot, c->x, c->r, c->z, c->p, c->Ap,
+                                                       c->dinv, c->part);
+  k_pcg_update2<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->sc, slot, c->p, c->z, c->part);
+  c->launches += 2;
+}
+
+static int graph_key(Ctx* c, bool fp32) {
+  return (fp32 ? 1 : 0) | (c->finite << 1) | (c->model << 2) | (c->geom << 3) | ((c->geo_affine ? 1 : 0) << 4) |
+         (c->et << 5);
+}
+
+static int build_graph(Ctx* c, bool fp32) {
+  const int key = graph_key(c, fp32);
+  if (c->pcg_graph && c->pcg_graph_key == key) return 0;
+  if (c->pcg_graph) {
+    cudaGraphExecDestroy(c->pcg_graph);
+    c->pcg_graph = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  const int64_t l0 = c->launches;
+  cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_check(c, e, "begin capture");
+  for (int k = 0; k < PCG_CHUNK; ++k) enqueue_iteration(c, fp32, k & 1);
+  e = cudaStreamEndCapture(c->stream, &g);
+  if (e != cudaSuccess) return cuda_check(c, e, "end capture");
+  e = cudaGraphInstantiate(&c->pcg_graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_check(c, e, "graph instantiate");
+  c->pcg_graph_key = key;
+  c->chunk_launches = c->launches - l0;
+  c->launches = l0;   // counted when the graph runs
+  return 0;
+}
+
+struct PcgResult {
+  int iters = 0;
+  int refinements = 0;
+  double relres = 0.0;
+  int status = 0;
+};
+
+// PCG on the masked operator for K x = f over the free DOFs; x holds the
+// initial guess (prescribed entries fixed).  tol is relative to ‖f_free − K x₀‖
+// when x_zero_free (the usual case), so the ratio is the relative residual.
+// reliable: recompute the residual in FP64 whenever the recursive one has
+// dropped by 100× since the last true one, and at recursive convergence.
+static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, double time_budget, double t_start,
+               bool reliable, bool x_zero, PcgResult* res) {
+  int rc = 0;
+  double rr0 = 0.0;
+  if (x_zero) {
+    k_residual<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, f, 1.0, nullptr, c->mask, c->r, 0, c->part);
+    c->launches += 1;
+    if ((rc = read_norms(c, &rr0, nullptr))) return rc;
+  } else if ((rc = true_residual(c, f, c->x, c->r, &rr0))) {
+    return rc;
+  }
+  k_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->r, c->dinv, c->z, c->p, 1, c->part);
+  k_scalars_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 1, tol, max_iter, 1);
+  c->launches += 2;
+  if ((rc = read_scalars(c))) return rc;
+  const double bb = c->sc_host->bb;
+  if (!(bb > 0.0)) {
+    res->iters = 0;
+    res->relres = 0.0;
+    res->status = 0;
+    return 0;
+  }
+  if ((rc = build_graph(c, fp32))) return rc;
+  double rr_true_last = rr0;
+  int refinements = 0;
+  for (;;) {
+    if (!c->sc_host->done[0]) {
+      cudaError_t e = cudaGraphLaunch(c->pcg_graph, c->stream);
+      if (e != cudaSuccess) return cuda_check(c, e, "graph launch");
+      c->launches += c->chunk_launches;
+      if ((rc = read_scalars(c))) return rc;
+    }
+    const SolverScalars& s = *c->sc_host;
+    const double rr = s.rr[0];
+    if (!(rr == rr)) return set_err(c, JFEM_ERR_NAN, "NaN in the CG recurrence");
+    const bool at_cap = s.iters >= max_iter;
+    const bool check = s.done[0] || (reliable && rr < 1e-4 * rr_true_last);
+    if (check) {
+      double rr_t = rr;
+      if (reliable) {
+        if ((rc = true_residual(c, f, c->x, c->r, &rr_t))) return rc;
+        ++refinements;
+      }
+      if (!(rr_t == rr_t)) return set_err(c, JFEM_ERR_NAN, "NaN in the true residual");
+      if (rr_t <= tol * tol * bb || at_cap || !reliable) {
+        res->iters = s.iters;
+        res->refinements = refinements;
+        res->relres = std::sqrt(rr_t / bb);
+        res->status = (rr_t <= tol * tol * bb * 1.0000001) ? 0 : JFEM_NOT_CONVERGED;
+        return 0;
+      }
+      // reliable update: r ← true residual, keep the search direction
+      rr_true_last = rr_t;
+      k_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->r, c->dinv, c->z, c->p, 0, c->part);
+      k_scalars_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 0, tol, max_iter, 0);
+      c->launches += 2;
+      if ((rc = read_scalars(c))) return rc;
+    }
+    if (time_budget > 0.0 && now_s() - t_start > time_budget)
+      return set_err(c, JFEM_ERR_TIMEOUT, "solve exceeded its time budget");
+  }
+}
+
+static int prepare_rhs(Ctx* c) {
+  if (c->f_ext_dirty) {
+    int rc = traction_device(c, c->f_ext);
+    if (rc) return rc;
+    c->f_ext_dirty = false;
+  }
+  return 0;
+}
+
+static void fill_stats(jfem_stats* st, int status, int newton, int cg, int refin, double res, double t) {
+  if (!st) return;
+  st->status = status;
+  st->newton_iterations = newton;
+  st->cg_iterations = cg;
+  st->refinements = refin;
+  st->residual = res;
+  st->solve_time_s = t;
+}
+
+// Linear solve K u = f_ext with prescribed values eliminated (solvers.jl:192-216).
+static int solve_linear(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stats* st) {
+  const double t0 = now_s();
+  int rc = 0;
+  if ((rc = geometry_prepare(c))) return rc;
+  if ((rc = prepare_rhs(c))) return rc;
+  if ((rc = jacobi_diag_device(c, c->dinv))) return rc;
+  cudaMemcpyAsync(c->x, c->gvals, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  const bool fp32 = o->precision == JFEM_MIXED;
+  PcgResult pr;
+  rc = pcg(c, c->f_ext, fp32, o->tol, o->max_iter, o->time_budget_s, t0, true, c->n_fixed_nonzero == 0, &pr);
+  if (rc) return rc;
+  cudaMemcpyAsync(u_d, c->x, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  if ((rc = sync_and_check(c, "solution copy"))) return rc;
+  fill_stats(st, pr.status, 1, pr.iters, pr.refinements, pr.relres, now_s() - t0);
+  if (st) st->history_len = 0;
+  return pr.status;
+}
+
+// Inexact Newton–Krylov with load stepping.  Step s of S applies s/S of the
+// traction and of the prescribed values; the first iteration of a step carries
+// the increment of the prescribed DOFs.  Converged when ‖R_free‖ ≤
+// newton_tol·‖f_int‖ (FP64; f_int over all DOFs, reactions included).
+static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stats* st) {
+  const double t0 = now_s();
+  int rc = 0;
+  if ((rc = geometry_prepare(c))) return rc;
+  if ((rc = prepare_rhs(c))) return rc;
+  const int64_t n = 3 * c->N;
+  if (!c->have_state) {
+    cudaMemsetAsync(c->u_state, 0, n * sizeof(double), c->stream);
+    c->have_state = true;
+  }
+  const int steps = o->n_load_steps > 0 ? o->n_load_steps : 1;
+  const bool fp32 = o->precision == JFEM_MIXED;
+  int total_cg = 0, total_newton = 0, refin = 0, hist = 0, status = 0;
+  double last_rel = 0.0;
+  double* dg = c->tmp2;
+  if (st) st->history_len = 0;
+  for (int s = 1; s <= steps; ++s) {
+    const double frac = (double)s / steps;
+    bool converged = false;
+    for (int k = 1; k <= o->max_newton + 1; ++k) {
+      // R = frac f_ext − f_int(u) on free DOFs
+      enqueue_internal_force(c, c->Ap);
+      k_residual<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->f_ext, frac, c->Ap, c->mask, c->b, 1, c->part);
+      c->launches += 1;
+      double rr = 0.0, ff = 0.0;
+      if ((rc = read_norms(c, &rr, &ff))) return rc;
+      const double rn = std::sqrt(rr);
+      double scale = std::sqrt(ff);
+      if (!(scale > 0.0)) scale = 1.0;
+      if (!(rn == rn)) return set_err(c, JFEM_ERR_NAN, "NaN in the Newton residual");
+      last_rel = rn / scale;
+      // prescribed-value increment of this step
+      k_bc_increment<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->gvals, frac, c->u_state, c->mask, dg, c->part);
+      c->launches += 1;
+      double dgg = 0.0;
+      if ((rc = read_norms(c, &dgg, nullptr))) return rc;
+      if (dgg == 0.0 && rn <= o->newton_tol * scale) {
+        converged = true;
+        break;
+      }
+      if (k > o->max_newton) break;
+      // tangent Jacobi diagonal at u, rhs b = R − K_T dg
+      if ((rc = jacobi_diag_device(c, c->dinv))) return rc;
+      if (dgg > 0.0) {
+        enqueue_apply(c, dg, c->tmp, fp32, true, false, nullptr, nullptr);
+        k_sub_free<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->b, c->tmp);
+        c->launches += 1;
+      }
+      double eta = std::pow(last_rel, o->forcing_power);
+      if (eta > o->forcing_max) eta = o->forcing_max;
+      if (eta < 1e-12) eta = 1e-12;
+      cudaMemsetAsync(c->x, 0, n * sizeof(double), c->stream);
+      PcgResult pr;
+      if ((rc = pcg(c, c->b, fp32, eta, o->max_cg_per_newton, o->time_budget_s, t0, false, true, &pr))) return rc;
+      total_cg += pr.iters;
+      refin += pr.refinements;
+      ++total_newton;
+      k_update_state<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->u_state, c->x, dg, c->mask);
+      c->launches += 1;
+      if (st && hist < JFEM_HISTORY_MAX) {
+        st->history[3 * hist] = pr.iters;
+        st->history[3 * hist + 1] = rn;
+        st->history[3 * hist + 2] = eta;
+        st->history_len = ++hist;
+      }
+      if (o->time_budget_s > 0.0 && now_s() - t0 > o->time_budget_s)
+        return set_err(c, JFEM_ERR_TIMEOUT, "solve exceeded its time budget");
+    }
+    if (!converged) status = JFEM_NOT_CONVERGED;
+  }
+  cudaMemcpyAsync(u_d, c->u_state, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  if ((rc = sync_and_check(c, "solution copy"))) return rc;
+  fill_stats(st, status, total_newton, total_cg, refin, last_rel, now_s() - t0);
+  return status;
+}
+
+int solve_device(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stats* st) {
+  if (c->N == 0) return set_err(c, JFEM_ERR_INVALID, "jfem_set_mesh must come first");
+  if (!c->have_material) return set_err(c, JFEM_ERR_INVALID, "jfem_set_material must come first");
+  if (!o) return set_err(c, JFEM_ERR_INVALID, "opts is NULL");
+  if (!(o->tol > 0.0) || o->max_iter <= 0) return set_err(c, JFEM_ERR_INVALID, "tol must be > 0 and max_iter > 0");
+  if (o->method == JFEM_NEWTON && (o->max_newton <= 0 || o->max_cg_per_newton <= 0 || !(o->newton_tol > 0.0)))
+    return set_err(c, JFEM_ERR_INVALID, "Newton options must be positive");
+  switch (o->method) {
+    case JFEM_PCG_JACOBI: return solve_linear(c, o, u_d, st);
+    case JFEM_NEWTON: return solve_newton(c, o, u_d, st);
+    default: return set_err(c, JFEM_ERR_INVALID, "unknown solve method");
+  }
+}
+
+}  // namespace jfem
