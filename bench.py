@@ -1,0 +1,336 @@
+#!/usr/bin/env python
+"""Benchmark: time to FP64 relative residual 1e-8 on the 2M-DOF Tet10 cantilever.
+
+Workload: [0,20]×[0,2]² box, 200×20×20 cubes × 6 Tet10 (480,000 elements,
+674,081 nodes, 2,022,243 DOFs), GLTET4 quadrature, E = 210e3, ν = 0.3, x = 0
+face clamped, traction (0,0,−1) on the x = 20 face (800 Tri6).  A step is one
+Jacobi-PCG solve from u = 0 to ‖f − K u‖/‖f‖ ≤ 1e-8 over the free DOFs (FP32
+matrix-free apply, FP64 vectors, dots and true-residual refinement), with the
+mesh, material and loads resident in HBM.  Also reported: matrix-free K·u
+throughput (GDOF/s), its roofline fraction, the end-to-end time through the C
+ABI from host buffers, and the CPU baseline (oracle port on the host cores).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--size NX NY NZ]
+
+N > 1: one process per GPU (torchrun), each rank solves its own replica (the
+path does not exchange data between instances); the time is the max over
+ranks, scaling "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "time-to-1e-8 residual, 2M-DOF Tet10 cantilever (Jacobi-PCG, FP32 apply + FP64 refinement)"
+UNIT = "s"
+TOL = 1e-8
+# Jacobi-PCG iterations the 200×20×20 Tet10 cantilever needs to reach 1e-8 (FP64
+# arithmetic, measured by the GPU arm of this benchmark); the CPU arm times a
+# bounded sample of iterations and scales to this count.
+FULL_PCG_ITERS = 6000
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--size", type=int, nargs=3, default=[200, 20, 20])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample-div", type=int, default=4, help="CPU sample = 1/div of the cubes along x")
+    p.add_argument("--cpu-sample-iters", type=int, default=200)
+    return p.parse_args()
+
+
+def dist_setup(backend):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, v, device=None):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle sample (cpu_baseline and --impl reference)
+# ---------------------------------------------------------------------------
+def cpu_sample(jfem, size, div, iters):
+    """Oracle (C++ FP64, OpenMP on all host cores): assemble a 1/div slab of the
+    workload into CSC and run `iters` Jacobi-PCG iterations on it; scale to the
+    full workload (work is linear in elements / DOFs) and to FULL_PCG_ITERS."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    nx, ny, nz = size
+    sx = max(1, nx // div)
+    w = jfem.workloads.cantilever(10, sx, ny, nz, 20.0 * sx / 200, 2.0 * ny / 20, 2.0 * nz / 20)
+    m = w.mesh
+    t0 = time.perf_counter()
+    cp, rv = oracle.pattern(10, m.n_nodes, m.conn)
+    nz_, _ = oracle.assemble_pattern(10, m.X, m.conn, w.E, w.nu, cp, rv)
+    f = oracle.traction(w.face_type, w.faces, m.X, w.traction)
+    t1 = time.perf_counter()
+    _, it, rr, st = oracle.pcg(cp, rv, nz_, f, w.fixed_mask(), tol=1e-30, maxit=iters)
+    t2 = time.perf_counter()
+    scale = nx / sx
+    t_asm = (t1 - t0) * scale
+    t_iter = (t2 - t1) / max(it, 1) * scale
+    value = t_asm + t_iter * FULL_PCG_ITERS
+    sample = (f"Tet10 {sx}x{ny}x{nz} slab ({m.n_elem} elements, {m.n_dofs} DOFs): CSC assembly + {it} "
+              f"Jacobi-PCG iterations, scaled x{scale:g} in size and to {FULL_PCG_ITERS} iterations")
+    return dict(value=value, unit=UNIT, cores=oracle.get_threads(), kind="port", sample=sample,
+                assembly_s=t_asm, s_per_iter=t_iter)
+
+
+def run_reference(args):
+    ws, rank, local = dist_setup("gloo")
+    if rank != 0:
+        return 0
+    import jfem_loader
+    jfem = jfem_loader.load_package()
+    times = []
+    last = None
+    for k in range(args.warmup + args.steps):
+        r = cpu_sample(jfem, args.size, args.cpu_sample_div, args.cpu_sample_iters)
+        if k >= args.warmup:
+            times.append(r["value"])
+        last = r
+    v = statistics.mean(times)
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": workload_config(args.size),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": "port",
+                             "sample": last["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(size):
+    nx, ny, nz = size
+    return {"workload": f"tet10_cantilever_{nx}x{ny}x{nz}", "elements": 6 * nx * ny * nz,
+            "dofs": 3 * (2 * nx + 1) * (2 * ny + 1) * (2 * nz + 1), "solver": "Jacobi-PCG",
+            "tol": TOL, "apply": "matrix-free FP32, FP64 vectors/dots/residual",
+            "l2": "flushed before every step (256 MiB write)"}
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def setup_ctx(jfem, w, device, pinned=None):
+    ctx = jfem.Context(device)
+    m = w.mesh
+    X, conn = (m.X, m.conn) if pinned is None else pinned
+    ctx.set_mesh(m.elem_type, X, conn)
+    ctx.set_material(w.E, w.nu)
+    ctx.set_dirichlet(w.fixed_dofs, w.fixed_values)
+    ctx.set_traction(w.face_type, w.faces, w.traction)
+    return ctx
+
+
+def run_gpu(args):
+    ws, rank, local = dist_setup("nccl")
+    import torch
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import jfem_loader
+    jfem = jfem_loader.load_package()
+    from jfem_gb300 import build as _b
+    _b.build()
+    nx, ny, nz = args.size
+    w = jfem.workloads.cfg_tet10_cantilever(nx, ny, nz)
+    m = w.mesh
+    n = m.n_dofs
+    t_setup0 = time.perf_counter()
+    ctx = setup_ctx(jfem, w, local)
+    t_setup = time.perf_counter() - t_setup0
+    opts = jfem.default_opts(method=jfem._abi.PCG_JACOBI, precision=jfem._abi.MIXED, tol=TOL, max_iter=500000)
+    u = torch.empty(n, dtype=torch.float64, device=dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    for _ in range(args.warmup):
+        st, rc = ctx.solve_device(u.data_ptr(), opts)
+    torch.cuda.synchronize()
+    barrier(ws)
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.kernel_launches
+    times, iters, refin, res = [], [], [], []
+    torch.cuda.synchronize()
+    barrier(ws)
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st, rc = ctx.solve_device(u.data_ptr(), opts)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        iters.append(st.cg_iterations)
+        refin.append(st.refinements)
+        res.append(st.residual)
+        if rc != 0:
+            raise RuntimeError(f"solve did not converge: status {rc}, residual {st.residual}")
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches = ctx.kernel_launches - launches0
+    clk = clocks.stop()
+    t_step = statistics.mean(times)
+    t_step = max_over_ranks(ws, t_step, dev)
+
+    # matrix-free apply: per-kernel CUDA-event timing on the context stream
+    ms_el, ms_ga = ctx.time_apply(reps=50, fp32=True, masked=True)
+    t_apply = (ms_el + ms_ga) / 1e3
+    nn = 10
+    alg_bytes = m.n_elem * (4 * nn + 44) + 16 * n      # conn + geometry records + v read + y write
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / t_apply / 1e9
+    # FP64 apply for the residual path, for reference
+    ms_el64, ms_ga64 = ctx.time_apply(reps=10, fp32=False, masked=True)
+
+    # end to end through the C ABI from pinned host buffers
+    Xp = torch.from_numpy(np.ascontiguousarray(m.X)).pin_memory()
+    Cp = torch.from_numpy(np.ascontiguousarray(m.conn)).pin_memory()
+    e2e_times = []
+    e2e_steps = max(1, min(args.steps, 3))
+    ctx.close()
+    for k in range(e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c2 = setup_ctx(jfem, w, local, pinned=(Xp.numpy(), Cp.numpy()))
+        uh, st2, rc2 = c2.solve(opts)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        c2.close()
+        if k > 0:                      # first round is a warm-up
+            e2e_times.append(t1 - t0)
+    h2d = m.X.nbytes + m.conn.nbytes + 16 + w.fixed_dofs.nbytes + w.fixed_values.nbytes + \
+        w.faces.nbytes + w.traction.nbytes
+    d2h = 8 * n
+    e2e = max_over_ranks(ws, statistics.mean(e2e_times), dev)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": t_step, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32-apply/f64-residual", "data": "synthetic",
+                "config": workload_config(args.size),
+                "pcg_iterations": int(statistics.median(iters)), "refinements": int(statistics.median(refin)),
+                "final_relative_residual": max(res),
+                "kxu_gdofs": n / t_apply / 1e9,
+                "apply_ms": {"element": ms_el, "gather": ms_ga, "fp64_element": ms_el64, "fp64_gather": ms_ga64},
+                "setup_s": t_setup,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": None,
+                             "kernel": "matrix-free FP32 apply (element + node-gather launches)",
+                             "algorithmic_bytes": alg_bytes, "peak_kind": peak_kind},
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                "gpu_launches": int(launches),
+                "clocks": clk}
+        if ws == 1 and not args.no_cpu_baseline:
+            cb = cpu_sample(jfem, args.size, args.cpu_sample_div, args.cpu_sample_iters)
+            line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

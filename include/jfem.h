@@ -155,10 +155,17 @@ int jfem_solve(jfem_ctx* ctx, const jfem_solve_opts* opts, double* u, jfem_stats
 int jfem_solve_device(jfem_ctx* ctx, const jfem_solve_opts* opts, double* u_device,
                       jfem_stats* stats);
 
-/* Device-side counters of the last call: kernels launched by the library. */
+/* Kernels launched by the library on this context since its creation. */
 int64_t jfem_kernel_launches(const jfem_ctx* ctx);
 /* Event-timed duration (ms) of the last matrix-free apply launch sequence. */
 double jfem_last_apply_ms(const jfem_ctx* ctx);
+/* The context's CUDA stream (cudaStream_t), for event timing and interop. */
+void* jfem_stream(const jfem_ctx* ctx);
+/* Runs the apply (flags as jfem_apply) reps times on device-resident vectors
+ * and returns the mean CUDA-event duration of the element kernel and of the node
+ * gather kernel (ms), each measured on the context stream.  No counterpart in the
+ * reference (measurement hook). */
+int jfem_time_apply(jfem_ctx* ctx, int flags, int reps, double* ms_element, double* ms_gather);
 
 #ifdef __cplusplus
 }

@@ -82,6 +82,8 @@ SIGNATURES = {
     "jfem_solve_device": (C.c_int, [_P, C.POINTER(SolveOpts), _P, C.POINTER(Stats)]),
     "jfem_kernel_launches": (_i64, [_P]),
     "jfem_last_apply_ms": (C.c_double, [_P]),
+    "jfem_stream": (C.c_void_p, [_P]),
+    "jfem_time_apply": (C.c_int, [_P, C.c_int, C.c_int, _f64p, _f64p]),
 }
 
 _lib = None
@@ -249,3 +251,14 @@ class Context:
     @property
     def last_apply_ms(self) -> float:
         return float(self._lib.jfem_last_apply_ms(self._h))
+
+    @property
+    def stream(self) -> int:
+        return int(self._lib.jfem_stream(self._h) or 0)
+
+    def time_apply(self, reps: int = 20, fp32: bool = True, masked: bool = True):
+        """Mean CUDA-event ms of (element kernel, gather kernel) of one apply."""
+        a, b = C.c_double(0), C.c_double(0)
+        flags = (APPLY_FP32 if fp32 else 0) | (APPLY_MASKED if masked else 0)
+        self._check(self._lib.jfem_time_apply(self._h, flags, int(reps), C.byref(a), C.byref(b)))
+        return a.value, b.value

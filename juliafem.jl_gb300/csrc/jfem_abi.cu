@@ -138,6 +138,17 @@ int64_t jfem_kernel_launches(const jfem_ctx* h) { return h ? h->c.launches : 0; 
 
 double jfem_last_apply_ms(const jfem_ctx* h) { return h ? h->c.last_apply_ms : 0.0; }
 
+void* jfem_stream(const jfem_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
+
+int jfem_time_apply(jfem_ctx* h, int flags, int reps, double* ms_element, double* ms_gather) {
+  ENTER(h);
+  Ctx* c = &h->c;
+  if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
+  if (!ms_element || !ms_gather) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL output");
+  return jfem::time_apply(c, (flags & JFEM_APPLY_FP32) != 0, (flags & JFEM_APPLY_MASKED) != 0, reps, ms_element,
+                          ms_gather);
+}
+
 int jfem_set_mesh(jfem_ctx* h, int elem_type, int64_t n_nodes, const double* X, int64_t n_elem, const int64_t* conn,
                   int index_base) {
   ENTER(h);

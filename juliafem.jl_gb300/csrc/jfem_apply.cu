@@ -273,3 +273,52 @@ int internal_force_device(Ctx* c, double* f) {
 }
 
 }  // namespace jfem
+
+namespace jfem {
+
+__global__ void k_fill_pattern(int64_t n, double* __restrict__ v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] = 1.0 + 1e-3 * (double)(i % 97);
+}
+
+// Event-timed element and gather kernels of the apply, reps times on ctx vectors.
+int time_apply(Ctx* c, bool fp32, bool masked, int reps, double* ms_elem, double* ms_gather) {
+  int rc = geometry_prepare(c);
+  if (rc) return rc;
+  if (reps <= 0) return set_err(c, JFEM_ERR_INVALID, "reps must be positive");
+  k_fill_pattern<<<grid_for(3 * c->N, 256), 256, 0, c->stream>>>(3 * c->N, c->tmp);
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  double se = 0.0, sg = 0.0;
+  for (int r = 0; r < reps; ++r) {
+    cudaEventRecord(e0, c->stream);
+    launch_elements(c, fp32, 0, c->tmp, masked, nullptr);
+    cudaEventRecord(e1, c->stream);
+    if (fp32)
+      k_gather<float, true><<<JFEM_RED_BLOCKS, JFEM_RED_THREADS, 0, c->stream>>>(
+          c->N, c->E, c->adj_ptr, c->adj, c->ye32, c->mask, masked, c->tmp, c->tmp2, c->part, nullptr);
+    else
+      k_gather<double, true><<<JFEM_RED_BLOCKS, JFEM_RED_THREADS, 0, c->stream>>>(
+          c->N, c->E, c->adj_ptr, c->adj, c->ye64, c->mask, masked, c->tmp, c->tmp2, c->part, nullptr);
+    c->launches += 1;
+    cudaEventRecord(e2, c->stream);
+    cudaEventSynchronize(e2);
+    float a = 0.f, b = 0.f;
+    cudaEventElapsedTime(&a, e0, e1);
+    cudaEventElapsedTime(&b, e1, e2);
+    se += a;
+    sg += b;
+  }
+  rc = sync_and_check(c, "timed apply");
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  if (rc) return rc;
+  *ms_elem = se / reps;
+  *ms_gather = sg / reps;
+  return 0;
+}
+
+}  // namespace jfem

@@ -230,7 +230,7 @@ struct Ctx {
 
   // solver
   double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *Ap = nullptr,
-         *dinv = nullptr, *b = nullptr, *tmp = nullptr, *tmp2 = nullptr;
+         *dinv = nullptr, *b = nullptr, *tmp = nullptr, *tmp2 = nullptr, *xbest = nullptr;
   double* part = nullptr;     // reduction partials (4 × JFEM_RED_BLOCKS)
   SolverScalars* sc = nullptr;
   SolverScalars* sc_host = nullptr;   // pinned mirror
@@ -289,6 +289,7 @@ void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, b
 void enqueue_internal_force(Ctx* c, double* f);
 int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, double* partial_pAp);
 int internal_force_device(Ctx* c, double* f_d);
+int time_apply(Ctx* c, bool fp32, bool masked, int reps, double* ms_elem, double* ms_gather);
 // jfem_solver.cu
 void enqueue_axpy(Ctx* c, int64_t n, double a, const double* x, double* y);
 int solve_device(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stats* st);

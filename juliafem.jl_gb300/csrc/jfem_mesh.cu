@@ -374,7 +374,7 @@ int mesh_setup(Ctx* c, int et, int64_t N, const double* X, int64_t E, const int6
   if ((rc = dalloc(c, &c->gvals, n))) return rc;
   if ((rc = dalloc(c, &c->f_ext, n))) return rc;
   if ((rc = dalloc(c, &c->u_state, n))) return rc;
-  double** vecs[] = {&c->x, &c->r, &c->z, &c->p, &c->Ap, &c->dinv, &c->b, &c->tmp, &c->tmp2};
+  double** vecs[] = {&c->x, &c->r, &c->z, &c->p, &c->Ap, &c->dinv, &c->b, &c->tmp, &c->tmp2, &c->xbest};
   for (double** v : vecs)
     if ((rc = dalloc(c, v, n))) return rc;
   if ((rc = dalloc(c, &c->part, 4 * JFEM_RED_BLOCKS))) return rc;

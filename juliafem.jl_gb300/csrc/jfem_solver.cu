@@ -285,9 +285,18 @@ struct PcgResult {
 
 // PCG on the masked operator for K x = f over the free DOFs; x holds the
 // initial guess (prescribed entries fixed).  tol is relative to ‖f_free − K x₀‖
-// when x_zero_free (the usual case), so the ratio is the relative residual.
-// reliable: recompute the residual in FP64 whenever the recursive one has
-// dropped by 100× since the last true one, and at recursive convergence.
+// (the relative residual when the free part of x₀ is zero).
+//
+// The stopping test always uses the true FP64 residual f − K x.  A "refinement"
+// replaces the recursive residual by the true one and restarts the direction
+// (p = z): with an FP32 operator the recursion drifts from the FP64 residual by
+// about ε₃₂·‖K‖‖x‖, and keeping the old direction after the replacement
+// diverges, while restarting converges (defect correction with CG inner
+// solves).  Refinements happen at recursive convergence and, when `reliable`,
+// each time the recursive residual has dropped by `ru` (in r·r) since the last
+// true residual.  When two refinements in a row gain less than 2× the solve has
+// reached the attainable accuracy of the arithmetic: the best iterate is kept
+// and JFEM_NOT_CONVERGED returned.
 static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, double time_budget, double t_start,
                bool reliable, bool x_zero, PcgResult* res) {
   int rc = 0;
@@ -304,15 +313,17 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
   c->launches += 2;
   if ((rc = read_scalars(c))) return rc;
   const double bb = c->sc_host->bb;
-  if (!(bb > 0.0)) {
-    res->iters = 0;
-    res->relres = 0.0;
-    res->status = 0;
-    return 0;
-  }
+  res->iters = 0;
+  res->refinements = 0;
+  res->relres = 0.0;
+  res->status = 0;
+  if (!(bb > 0.0)) return 0;
   if ((rc = build_graph(c, fp32))) return rc;
-  double rr_true_last = rr0;
-  int refinements = 0;
+  const double ru = fp32 ? 1e-4 : 0.0;
+  const double goal = tol * tol * bb;
+  double rr_true_last = rr0, rr_best = rr0;
+  cudaMemcpyAsync(c->xbest, c->x, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  int refinements = 0, stalls = 0;
   for (;;) {
     if (!c->sc_host->done[0]) {
       cudaError_t e = cudaGraphLaunch(c->pcg_graph, c->stream);
@@ -322,26 +333,40 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
     }
     const SolverScalars& s = *c->sc_host;
     const double rr = s.rr[0];
-    if (!(rr == rr)) return set_err(c, JFEM_ERR_NAN, "NaN in the CG recurrence");
-    const bool at_cap = s.iters >= max_iter;
-    const bool check = s.done[0] || (reliable && rr < 1e-4 * rr_true_last);
+    const int iters = s.iters;
+    const bool at_cap = iters >= max_iter;
+    const bool bad = !(rr == rr) || !(s.rz[0] > 0.0) || rr > 1e30 * bb;
+    const bool check = s.done[0] || bad || (reliable && rr < ru * rr_true_last);
     if (check) {
-      double rr_t = rr;
-      if (reliable) {
-        if ((rc = true_residual(c, f, c->x, c->r, &rr_t))) return rc;
-        ++refinements;
+      double rr_t = 0.0;
+      if ((rc = true_residual(c, f, c->x, c->r, &rr_t))) return rc;
+      ++refinements;
+      const bool finite = rr_t == rr_t && rr_t < 1e300;
+      if (finite && rr_t < rr_best) {
+        rr_best = rr_t;
+        cudaMemcpyAsync(c->xbest, c->x, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
       }
-      if (!(rr_t == rr_t)) return set_err(c, JFEM_ERR_NAN, "NaN in the true residual");
-      if (rr_t <= tol * tol * bb || at_cap || !reliable) {
-        res->iters = s.iters;
+      stalls = (finite && rr_t < 0.25 * rr_true_last) ? 0 : stalls + 1;
+      const bool converged = finite && rr_t <= goal;
+      if (converged || at_cap || stalls >= 2 || !finite) {
+        if (!converged) {   // return the best iterate found
+          cudaMemcpyAsync(c->x, c->xbest, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+          if ((rc = sync_and_check(c, "best iterate"))) return rc;
+        }
+        res->iters = iters;
         res->refinements = refinements;
-        res->relres = std::sqrt(rr_t / bb);
-        res->status = (rr_t <= tol * tol * bb * 1.0000001) ? 0 : JFEM_NOT_CONVERGED;
+        res->relres = std::sqrt((converged ? rr_t : rr_best) / bb);
+        res->status = converged ? 0 : JFEM_NOT_CONVERGED;
         return 0;
       }
-      // reliable update: r ← true residual, keep the search direction
       rr_true_last = rr_t;
-      k_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->r, c->dinv, c->z, c->p, 0, c->part);
+      if (!finite) {   // restart from the best iterate
+        cudaMemcpyAsync(c->x, c->xbest, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+        if ((rc = true_residual(c, f, c->x, c->r, &rr_t))) return rc;
+        rr_true_last = rr_t;
+      }
+      // refinement: r ← true residual, restart p = z
+      k_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->r, c->dinv, c->z, c->p, 1, c->part);
       k_scalars_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 0, tol, max_iter, 0);
       c->launches += 2;
       if ((rc = read_scalars(c))) return rc;

@@ -12,8 +12,8 @@ def test_pcg_tet4_cantilever(jfem, gpu_ctx_factory, precision):
     w = jfem.workloads.cfg_tet4_cantilever()
     d = np.load(GOLDEN / "tet4_cantilever.npz")
     with gpu_ctx_factory(w) as ctx:
-        u, st, rc = ctx.solve(method=0, precision=precision, tol=1e-12, max_iter=100000)
-    assert rc == 0 and st.residual <= 1e-12
+        u, st, rc = ctx.solve(method=0, precision=precision, tol=1e-10, max_iter=100000)
+    assert rc == 0 and st.residual <= 1e-10
     assert rel_err(u, d["u"]) <= 1e-8
     assert np.all(u[w.fixed_dofs] == 0.0)
 
@@ -22,8 +22,8 @@ def test_pcg_tet10_small_cantilever_mixed(jfem, gpu_ctx_factory):
     w = jfem.workloads.cantilever(10, 40, 4, 4, 4.0, 0.4, 0.4)
     d = np.load(GOLDEN / "tet10_cantilever_small.npz")
     with gpu_ctx_factory(w) as ctx:
-        u, st, rc = ctx.solve(method=0, precision=1, tol=1e-12, max_iter=200000)
-        u2, st2, _ = ctx.solve(method=0, precision=1, tol=1e-12, max_iter=200000)
+        u, st, rc = ctx.solve(method=0, precision=1, tol=1e-10, max_iter=200000)
+        u2, st2, _ = ctx.solve(method=0, precision=1, tol=1e-10, max_iter=200000)
     assert rc == 0 and rel_err(u, d["u"]) <= 1e-8
     assert st.refinements >= 1
     assert np.array_equal(u, u2) and st.cg_iterations == st2.cg_iterations    # bit-reproducible
@@ -36,7 +36,7 @@ def test_patch_test_reference_fixture_gpu(jfem, gpu_ctx_factory):
         ctx.set_material(float(d["E"]), float(d["nu"]))
         ctx.set_dirichlet(d["dofs"], d["vals"])
         ctx.set_surface_load(3, d["faces"], p=d["p"])
-        u, st, rc = ctx.solve(method=0, precision=0, tol=1e-14, max_iter=1000)
+        u, st, rc = ctx.solve(method=0, precision=0, tol=1e-12, max_iter=1000)
     assert np.abs(u - d["u_exact"]).max() <= 1e-10 * np.abs(d["u_exact"]).max()
 
 
@@ -56,7 +56,7 @@ def test_prescribed_nonzero_displacement(jfem, orc, gpu_ctx_factory):
         ctx.set_mesh(4, m.X, m.conn)
         ctx.set_material(210e3, 0.3)
         ctx.set_dirichlet(dofs, vals)
-        u, st, rc = ctx.solve(method=0, precision=1, tol=1e-12, max_iter=100000)
+        u, st, rc = ctx.solve(method=0, precision=1, tol=1e-10, max_iter=100000)
     assert rc == 0 and rel_err(u, uo) <= 1e-8
 
 
@@ -78,9 +78,9 @@ def test_solve_api_physics(jfem):
     ph = jfem.Physics(jfem.Tet4, w.mesh.X, w.mesh.conn, E=210e3, nu=0.3)
     jfem.add_dirichlet_(ph, w.mesh.nodes_where(0, 0.0))
     jfem.add_neumann_(ph, jfem.Tri3, w.faces, (0.0, 0.0, -1.0))
-    sol = jfem.solve_(ph, backend=jfem.GPU(), tol=1e-12, max_iter=100000)
+    sol = jfem.solve_(ph, backend=jfem.GPU(), tol=1e-10, max_iter=100000)
     assert isinstance(sol, jfem.ElasticitySolution)
-    assert sol.newton_iterations == 1 and sol.cg_iterations > 0 and sol.residual <= 1e-12
+    assert sol.newton_iterations == 1 and sol.cg_iterations > 0 and sol.residual <= 1e-10
     assert rel_err(sol.u, d["u"]) <= 1e-8
 
 
@@ -109,7 +109,7 @@ def test_legacy_problem_assemble_and_run(jfem, orc):
         bc.elements.append(el)
     an = jfem.Analysis(jfem.Linear)
     jfem.add_problems_(an, [body, bc])
-    an.properties["tol"] = 1e-14
+    an.properties["tol"] = 1e-12
     u = jfem.run_(an)
     uu = np.concatenate([u[int(n)] for n in ids])
     assert np.abs(uu - d["u_exact"]).max() <= 1e-10 * np.abs(d["u_exact"]).max()
