@@ -74,6 +74,7 @@ typedef struct jfem_solve_opts {
   double forcing_power;
   double forcing_max;
   double time_budget_s;   /* 0 = none; else JFEM_ERR_TIMEOUT when exceeded */
+  double refine_drop;     /* JFEM_MIXED: FP64 residual each time ‖r‖ drops by this factor (0 → 0.3) */
 } jfem_solve_opts;
 
 #define JFEM_HISTORY_MAX 256

@@ -23,9 +23,9 @@
 
 namespace jfem {
 
-void launch_apply_tet4(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop);
-void launch_apply_tet10(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop);
-void launch_apply_hex8(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop);
+void launch_apply_tet4(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in, const int* stop);
+void launch_apply_tet10(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in, const int* stop);
+void launch_apply_hex8(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in, const int* stop);
 
 // ---------------------------------------------------------------------------
 // geometry preparation (FP64)
@@ -119,8 +119,11 @@ __global__ void k_prepare_geo(int64_t E, const int* __restrict__ conn, const dou
 }
 
 // ---------------------------------------------------------------------------
-// phase 2: node gather (ascending element order), masking and optional v·y partials
+// phase 2: node gather (ascending element order), masking and optional v·y partials.
+// One thread per node (GATHER_GL = 1; with GL > 1 lanes split a node's entries
+// and combine in a fixed butterfly — measured slower on the Tet10 beam).
 // ---------------------------------------------------------------------------
+#define GATHER_GL 1
 template <typename R, bool DOT>
 __global__ void __launch_bounds__(JFEM_RED_THREADS) k_gather(int64_t N, int64_t E, const int* __restrict__ ptr,
                                                              const unsigned* __restrict__ adj,
@@ -129,35 +132,67 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_gather(int64_t N, int64_t 
                                                              const double* __restrict__ v,
                                                              double* __restrict__ y, double* __restrict__ part,
                                                              const int* __restrict__ stop) {
+  constexpr int GL = GATHER_GL, NPW = 32 / GL;
   __shared__ double sh[32];
   if (stop && *stop) return;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane & (GL - 1);
+  const int grp = lane / GL;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   double dot = 0.0;
-  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t jb = warp * NPW; jb < N; jb += nwarps * NPW) {   // warp-uniform trip count
+    const int64_t j = jb + grp;
+    const bool act = j < N;
     double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-    const int t1 = __ldg(ptr + j + 1);
-    for (int t = __ldg(ptr + j); t < t1; ++t) {
-      const unsigned pk = __ldg(adj + t);
-      const int64_t e = pk >> 4;
-      const int a = (int)(pk & 15u);
-      s0 += (double)__ldg(ye + (int64_t)(3 * a + 0) * E + e);
-      s1 += (double)__ldg(ye + (int64_t)(3 * a + 1) * E + e);
-      s2 += (double)__ldg(ye + (int64_t)(3 * a + 2) * E + e);
+    if (act) {
+      const int t1 = __ldg(ptr + j + 1);
+      for (int t = __ldg(ptr + j) + sub; t < t1; t += GL) {
+        const unsigned pk = __ldg(adj + t);
+        const int64_t e = pk >> 4;
+        const int a = (int)(pk & 15u);
+        s0 += (double)__ldg(ye + (int64_t)(3 * a + 0) * E + e);
+        s1 += (double)__ldg(ye + (int64_t)(3 * a + 1) * E + e);
+        s2 += (double)__ldg(ye + (int64_t)(3 * a + 2) * E + e);
+      }
     }
-    if (masked) {
-      const uint8_t m = __ldg(mask + j);
-      if (m & 1) s0 = 0.0;
-      if (m & 2) s1 = 0.0;
-      if (m & 4) s2 = 0.0;
+#pragma unroll
+    for (int o = GL / 2; o > 0; o >>= 1) {
+      s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
     }
-    y[3 * j] = s0;
-    y[3 * j + 1] = s1;
-    y[3 * j + 2] = s2;
-    if (DOT) dot += v[3 * j] * s0 + v[3 * j + 1] * s1 + v[3 * j + 2] * s2;
+    if (act && sub == 0) {
+      if (masked) {
+        const uint8_t m = __ldg(mask + j);
+        if (m & 1) s0 = 0.0;
+        if (m & 2) s1 = 0.0;
+        if (m & 4) s2 = 0.0;
+      }
+      y[3 * j] = s0;
+      y[3 * j + 1] = s1;
+      y[3 * j + 2] = s2;
+      if (DOT) dot += v[3 * j] * s0 + v[3 * j + 1] * s1 + v[3 * j + 2] * s2;
+    }
   }
   if (DOT) {
     const double b = block_sum(dot, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = b;
   }
+}
+
+// Split v into FP32 (hi, lo) pairs: hi = fl32(v), lo = fl32(v − hi).
+__global__ void k_split(int64_t n, const double* __restrict__ v, float2* __restrict__ v2) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = v[i];
+    const float hi = (float)x;
+    v2[i] = make_float2(hi, (float)(x - (double)hi));
+  }
+}
+
+void enqueue_split(Ctx* c, const double* v, float2* v2) {
+  k_split<<<grid_for(3 * c->N, 256), 256, 0, c->stream>>>(3 * c->N, v, v2);
+  c->launches += 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -208,20 +243,17 @@ int geometry_prepare(Ctx* c) {
   }
 }
 
-static void launch_elements(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop) {
+static void launch_elements(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in,
+                            const int* stop) {
   switch (c->et) {
-    case JFEM_TET4: launch_apply_tet4(c, fp32, mode, v, mask_in, stop); break;
-    case JFEM_TET10: launch_apply_tet10(c, fp32, mode, v, mask_in, stop); break;
-    default: launch_apply_hex8(c, fp32, mode, v, mask_in, stop); break;
+    case JFEM_TET4: launch_apply_tet4(c, fp32, mode, v, v2, mask_in, stop); break;
+    case JFEM_TET10: launch_apply_tet10(c, fp32, mode, v, v2, mask_in, stop); break;
+    default: launch_apply_hex8(c, fp32, mode, v, v2, mask_in, stop); break;
   }
 }
 
-// Enqueue (no sync): y = K v (masked rows zero when masked), partial v·y sums
-// into part[0..JFEM_RED_BLOCKS) when part != nullptr.
-void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, bool mask_in, double* part,
-                   const int* stop) {
-  launch_elements(c, fp32, 0, v, mask_in, stop);
-  const unsigned gb = part ? JFEM_RED_BLOCKS : grid_for(c->N, JFEM_RED_THREADS);
+static void launch_gather(Ctx* c, bool fp32, bool masked, const double* v, double* y, double* part, const int* stop) {
+  const unsigned gb = part ? JFEM_RED_BLOCKS : grid_for(c->N * GATHER_GL, JFEM_RED_THREADS);
   if (fp32) {
     if (part) k_gather<float, true><<<gb, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->E, c->adj_ptr, c->adj, c->ye32, c->mask, masked, v, y, part, stop);
     else k_gather<float, false><<<gb, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->E, c->adj_ptr, c->adj, c->ye32, c->mask, masked, v, y, part, stop);
@@ -232,12 +264,20 @@ void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, b
   c->launches += 1;
 }
 
+// Enqueue (no sync): y = K v (masked rows zero when masked), partial v·y sums
+// into part[0..JFEM_RED_BLOCKS) when part != nullptr.
+void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, bool mask_in, double* part,
+                   const int* stop, const float2* v2) {
+  launch_elements(c, fp32, 0, v, fp32 ? v2 : nullptr, mask_in, stop);
+  launch_gather(c, fp32, masked, v, y, part, stop);
+}
+
 int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, double* part) {
   int rc = geometry_prepare(c);
   if (rc) return rc;
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
   cudaEventRecord(c->ev0, c->stream);
-  enqueue_apply(c, v, y, fp32, masked, masked, part, nullptr);
+  enqueue_apply(c, v, y, fp32, masked, masked, part, nullptr, nullptr);
   cudaEventRecord(c->ev1, c->stream);
   int h_err = 0;
   cudaMemcpyAsync(&h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
@@ -252,11 +292,9 @@ int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, dou
 
 // Enqueue f_int(u) (FP64) into f (no sync).  Linear small strain: K u.
 void enqueue_internal_force(Ctx* c, double* f) {
-  if (!c->finite) launch_elements(c, false, 0, c->u_state, false, nullptr);
-  else launch_elements(c, false, 1, nullptr, false, nullptr);
-  k_gather<double, false><<<grid_for(c->N, JFEM_RED_THREADS), JFEM_RED_THREADS, 0, c->stream>>>(
-      c->N, c->E, c->adj_ptr, c->adj, c->ye64, c->mask, 0, nullptr, f, nullptr, nullptr);
-  c->launches += 1;
+  if (!c->finite) launch_elements(c, false, 0, c->u_state, nullptr, false, nullptr);
+  else launch_elements(c, false, 1, nullptr, nullptr, false, nullptr);
+  launch_gather(c, false, false, nullptr, f, nullptr, nullptr);
 }
 
 int internal_force_device(Ctx* c, double* f) {
@@ -287,6 +325,7 @@ int time_apply(Ctx* c, bool fp32, bool masked, int reps, double* ms_elem, double
   if (rc) return rc;
   if (reps <= 0) return set_err(c, JFEM_ERR_INVALID, "reps must be positive");
   k_fill_pattern<<<grid_for(3 * c->N, 256), 256, 0, c->stream>>>(3 * c->N, c->tmp);
+  if (fp32) enqueue_split(c, c->tmp, c->p2);
   cudaEvent_t e0, e1, e2;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -294,15 +333,9 @@ int time_apply(Ctx* c, bool fp32, bool masked, int reps, double* ms_elem, double
   double se = 0.0, sg = 0.0;
   for (int r = 0; r < reps; ++r) {
     cudaEventRecord(e0, c->stream);
-    launch_elements(c, fp32, 0, c->tmp, masked, nullptr);
+    launch_elements(c, fp32, 0, c->tmp, fp32 ? c->p2 : nullptr, masked, nullptr);
     cudaEventRecord(e1, c->stream);
-    if (fp32)
-      k_gather<float, true><<<JFEM_RED_BLOCKS, JFEM_RED_THREADS, 0, c->stream>>>(
-          c->N, c->E, c->adj_ptr, c->adj, c->ye32, c->mask, masked, c->tmp, c->tmp2, c->part, nullptr);
-    else
-      k_gather<double, true><<<JFEM_RED_BLOCKS, JFEM_RED_THREADS, 0, c->stream>>>(
-          c->N, c->E, c->adj_ptr, c->adj, c->ye64, c->mask, masked, c->tmp, c->tmp2, c->part, nullptr);
-    c->launches += 1;
+    launch_gather(c, fp32, masked, c->tmp, c->tmp2, c->part, nullptr);
     cudaEventRecord(e2, c->stream);
     cudaEventSynchronize(e2);
     float a = 0.f, b = 0.f;

@@ -135,13 +135,34 @@ __device__ __forceinline__ bool flux_pk1(const R gu[3][3], R lam, R mu, R P[3][3
 }
 
 // ---------------------------------------------------------------------------
+// reference derivatives used by the apply: for i ≥ 1 the constexpr table
+// rounded to R; node 0 gets −Σ_{i≥1}, so the discrete gradient of a constant
+// field is exactly zero in R arithmetic and the operator stays symmetric.
+// ---------------------------------------------------------------------------
+template <typename R>
+__host__ __device__ constexpr R dnr(int et, int q, int i, int a) {
+  if (i > 0) return (R)dshape(et, q, i, a);
+  R s = R(0);
+  const int nn = et == JFEM_TET4 ? 4 : et == JFEM_TET10 ? 10 : 8;
+  for (int j = 1; j < nn; ++j) s += (R)dshape(et, q, j, a);
+  return -s;
+}
+
+// ---------------------------------------------------------------------------
 // phase 1: element kernel
 //   MODE 0: y = K v (linear) / K_T(u) v (finite, KIN ≠ SMALL)
 //   MODE 1: y = f_int(u) (v ignored; KIN ≠ SMALL)
+//   SPLIT:  v given as FP32 (hi, lo) pairs per DOF (v ≈ hi + lo).  Gradients
+//           use element-local differences v_i − v_0 = (hi_i − hi_0) + (lo_i − lo_0):
+//           for a smooth field the hi difference is exact (Sterbenz), so ∇v
+//           keeps FP32 accuracy relative to ∇v itself instead of losing
+//           |v|/(h|∇v|) — the cancellation that otherwise limits how far an
+//           FP32 operator can drive the FP64 residual.
 // ---------------------------------------------------------------------------
-template <int ET, typename R, bool AFFINE, int KIN, bool GEOM, int MODE>
+template <int ET, typename R, bool AFFINE, int KIN, bool GEOM, int MODE, bool SPLIT>
 __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __restrict__ conn,
                                                     const R* __restrict__ geo, const double* __restrict__ v,
+                                                    const float2* __restrict__ v2,
                                                     const double* __restrict__ u,
                                                     const uint8_t* __restrict__ mask, R* __restrict__ ye,
                                                     int* err, const int* __restrict__ stop,
@@ -154,25 +175,34 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
     int nodes[NN];
 #pragma unroll
     for (int i = 0; i < NN; ++i) nodes[i] = __ldg(conn + (int64_t)i * E + e);
-    R ve[NN][3], ue[NN][3];
+    // element-local differences (index 0 unused)
+    R dv[NN][3], du[NN][3];
+    R h0[3] = {0, 0, 0}, l0[3] = {0, 0, 0}, u0[3] = {0, 0, 0};
 #pragma unroll
     for (int i = 0; i < NN; ++i) {
       const int64_t n = nodes[i];
-      if (NEED_V) {
-        ve[i][0] = (R)__ldg(v + 3 * n);
-        ve[i][1] = (R)__ldg(v + 3 * n + 1);
-        ve[i][2] = (R)__ldg(v + 3 * n + 2);
-        if (mask_in) {
-          const uint8_t m = __ldg(mask + n);
-          if (m & 1) ve[i][0] = R(0);
-          if (m & 2) ve[i][1] = R(0);
-          if (m & 4) ve[i][2] = R(0);
+      uint8_t m = 0;
+      if (NEED_V && mask_in) m = __ldg(mask + n);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (NEED_V) {
+          R hi, lo = R(0);
+          if (SPLIT) {
+            const float2 t = __ldg(v2 + 3 * n + c);
+            hi = t.x;
+            lo = t.y;
+          } else {
+            hi = (R)__ldg(v + 3 * n + c);
+          }
+          if ((m >> c) & 1) { hi = R(0); lo = R(0); }
+          if (i == 0) { h0[c] = hi; l0[c] = lo; }
+          else dv[i][c] = SPLIT ? (hi - h0[c]) + (lo - l0[c]) : hi - h0[c];
         }
-      }
-      if (NEED_U) {
-        ue[i][0] = (R)__ldg(u + 3 * n);
-        ue[i][1] = (R)__ldg(u + 3 * n + 1);
-        ue[i][2] = (R)__ldg(u + 3 * n + 2);
+        if (NEED_U) {
+          const R uv = (R)__ldg(u + 3 * n + c);
+          if (i == 0) u0[c] = uv;
+          else du[i][c] = uv - u0[c];
+        }
       }
     }
     R y[NN][3];
@@ -205,9 +235,9 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
           for (int a = 0; a < 3; ++a) {
             R s = R(0);
 #pragma unroll
-            for (int i = 0; i < NN; ++i) {
-              const R dn = (R)dshape(ET, q, i, a);
-              if (dn != R(0)) s += ve[i][c] * dn;
+            for (int i = 1; i < NN; ++i) {
+              const R dn = dnr<R>(ET, q, i, a);
+              if (dn != R(0)) s += dv[i][c] * dn;
             }
             G[c][a] = s;
           }
@@ -224,9 +254,9 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
           for (int a = 0; a < 3; ++a) {
             R s = R(0);
 #pragma unroll
-            for (int i = 0; i < NN; ++i) {
-              const R dn = (R)dshape(ET, q, i, a);
-              if (dn != R(0)) s += ue[i][c] * dn;
+            for (int i = 1; i < NN; ++i) {
+              const R dn = dnr<R>(ET, q, i, a);
+              if (dn != R(0)) s += du[i][c] * dn;
             }
             G[c][a] = s;
           }
@@ -254,7 +284,7 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
       for (int i = 0; i < NN; ++i)
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-          const R dn = (R)dshape(ET, q, i, a);
+          const R dn = dnr<R>(ET, q, i, a);
           if (dn != R(0)) {
             y[i][0] += Q[0][a] * dn;
             y[i][1] += Q[1][a] * dn;
@@ -275,41 +305,49 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
 // launch helpers, instantiated once per element type (jfem_apply_<type>.cu)
 // ---------------------------------------------------------------------------
 template <int ET, typename R, bool AFFINE, int KIN, bool GEOM, int MODE>
-static void launch_elem(Ctx* c, const R* geo, const double* v, R* ye, const int* stop, bool mask_in) {
+static void launch_elem(Ctx* c, const R* geo, const double* v, const float2* v2, R* ye, const int* stop,
+                        bool mask_in) {
   const unsigned g = grid_for(c->E, 128, 1LL << 30);
-  k_apply_elem<ET, R, AFFINE, KIN, GEOM, MODE><<<g, 128, 0, c->stream>>>(c->E, c->conn, geo, v, c->u_state, c->mask,
-                                                                         ye, c->d_err, stop, mask_in ? 1 : 0);
+  if (v2 && MODE == 0)
+    k_apply_elem<ET, R, AFFINE, KIN, GEOM, MODE, true><<<g, 128, 0, c->stream>>>(
+        c->E, c->conn, geo, v, v2, c->u_state, c->mask, ye, c->d_err, stop, mask_in ? 1 : 0);
+  else
+    k_apply_elem<ET, R, AFFINE, KIN, GEOM, MODE, false><<<g, 128, 0, c->stream>>>(
+        c->E, c->conn, geo, v, nullptr, c->u_state, c->mask, ye, c->d_err, stop, mask_in ? 1 : 0);
   c->launches += 1;
 }
 
 template <int ET, typename R, bool AFFINE, int MODE>
-static void dispatch_kin(Ctx* c, const R* geo, const double* v, R* ye, bool mask_in, const int* stop) {
+static void dispatch_kin(Ctx* c, const R* geo, const double* v, const float2* v2, R* ye, bool mask_in,
+                         const int* stop) {
   const int kin = (!c->finite && MODE == 0) ? KIN_SMALL : (c->model == JFEM_NEO_HOOKEAN ? KIN_NH : KIN_SVK);
   if (MODE == 0 && kin == KIN_SMALL) {
-    launch_elem<ET, R, AFFINE, KIN_SMALL, false, 0>(c, geo, v, ye, stop, mask_in);
+    launch_elem<ET, R, AFFINE, KIN_SMALL, false, 0>(c, geo, v, v2, ye, stop, mask_in);
   } else if (kin == KIN_SVK) {
-    if (MODE == 1) launch_elem<ET, R, AFFINE, KIN_SVK, false, 1>(c, geo, v, ye, stop, false);
-    else if (c->geom) launch_elem<ET, R, AFFINE, KIN_SVK, true, 0>(c, geo, v, ye, stop, mask_in);
-    else launch_elem<ET, R, AFFINE, KIN_SVK, false, 0>(c, geo, v, ye, stop, mask_in);
+    if (MODE == 1) launch_elem<ET, R, AFFINE, KIN_SVK, false, 1>(c, geo, v, nullptr, ye, stop, false);
+    else if (c->geom) launch_elem<ET, R, AFFINE, KIN_SVK, true, 0>(c, geo, v, v2, ye, stop, mask_in);
+    else launch_elem<ET, R, AFFINE, KIN_SVK, false, 0>(c, geo, v, v2, ye, stop, mask_in);
   } else if (kin == KIN_NH) {
-    if (MODE == 1) launch_elem<ET, R, AFFINE, KIN_NH, false, 1>(c, geo, v, ye, stop, false);
-    else if (c->geom) launch_elem<ET, R, AFFINE, KIN_NH, true, 0>(c, geo, v, ye, stop, mask_in);
-    else launch_elem<ET, R, AFFINE, KIN_NH, false, 0>(c, geo, v, ye, stop, mask_in);
+    if (MODE == 1) launch_elem<ET, R, AFFINE, KIN_NH, false, 1>(c, geo, v, nullptr, ye, stop, false);
+    else if (c->geom) launch_elem<ET, R, AFFINE, KIN_NH, true, 0>(c, geo, v, v2, ye, stop, mask_in);
+    else launch_elem<ET, R, AFFINE, KIN_NH, false, 0>(c, geo, v, v2, ye, stop, mask_in);
   }
 }
 
-// mode 0: y = K v (tangent for finite strain); mode 1: f_int(u) (finite strain only)
+// mode 0: y = K v (tangent for finite strain); mode 1: f_int(u) (finite strain only).
+// v2 (FP32 only): split copy of v, see k_apply_elem.
 template <int ET>
-void launch_apply_et(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop) {
+void launch_apply_et(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in,
+                     const int* stop) {
   if (fp32) {
-    if (c->geo_affine) dispatch_kin<ET, float, true, 0>(c, c->geo32, v, c->ye32, mask_in, stop);
-    else dispatch_kin<ET, float, false, 0>(c, c->geo32, v, c->ye32, mask_in, stop);
+    if (c->geo_affine) dispatch_kin<ET, float, true, 0>(c, c->geo32, v, v2, c->ye32, mask_in, stop);
+    else dispatch_kin<ET, float, false, 0>(c, c->geo32, v, v2, c->ye32, mask_in, stop);
   } else if (mode == 0) {
-    if (c->geo_affine) dispatch_kin<ET, double, true, 0>(c, c->geo64, v, c->ye64, mask_in, stop);
-    else dispatch_kin<ET, double, false, 0>(c, c->geo64, v, c->ye64, mask_in, stop);
+    if (c->geo_affine) dispatch_kin<ET, double, true, 0>(c, c->geo64, v, nullptr, c->ye64, mask_in, stop);
+    else dispatch_kin<ET, double, false, 0>(c, c->geo64, v, nullptr, c->ye64, mask_in, stop);
   } else {
-    if (c->geo_affine) dispatch_kin<ET, double, true, 1>(c, c->geo64, v, c->ye64, false, stop);
-    else dispatch_kin<ET, double, false, 1>(c, c->geo64, v, c->ye64, false, stop);
+    if (c->geo_affine) dispatch_kin<ET, double, true, 1>(c, c->geo64, v, nullptr, c->ye64, false, stop);
+    else dispatch_kin<ET, double, false, 1>(c, c->geo64, v, nullptr, c->ye64, false, stop);
   }
 }
 

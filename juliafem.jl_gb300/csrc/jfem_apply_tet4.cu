@@ -2,7 +2,8 @@
 #include "jfem_apply_kernels.cuh"
 
 namespace jfem {
-void launch_apply_tet4(Ctx* c, bool fp32, int mode, const double* v, bool mask_in, const int* stop) {
-  launch_apply_et<JFEM_TET4>(c, fp32, mode, v, mask_in, stop);
+void launch_apply_tet4(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in,
+                        const int* stop) {
+  launch_apply_et<JFEM_TET4>(c, fp32, mode, v, v2, mask_in, stop);
 }
 }  // namespace jfem

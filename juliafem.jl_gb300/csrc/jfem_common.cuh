@@ -231,6 +231,7 @@ struct Ctx {
   // solver
   double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *Ap = nullptr,
          *dinv = nullptr, *b = nullptr, *tmp = nullptr, *tmp2 = nullptr, *xbest = nullptr;
+  float2* p2 = nullptr;       // FP32 (hi, lo) split of p for the FP32 apply
   double* part = nullptr;     // reduction partials (4 × JFEM_RED_BLOCKS)
   SolverScalars* sc = nullptr;
   SolverScalars* sc_host = nullptr;   // pinned mirror
@@ -285,7 +286,8 @@ int jacobi_diag_device(Ctx* c, double* dinv_d);
 int geometry_prepare(Ctx* c);
 int geometry_invalidate(Ctx* c);
 void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, bool mask_in, double* part,
-                   const int* stop);
+                   const int* stop, const float2* v2);
+void enqueue_split(Ctx* c, const double* v, float2* v2);
 void enqueue_internal_force(Ctx* c, double* f);
 int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, double* partial_pAp);
 int internal_force_device(Ctx* c, double* f_d);

@@ -377,6 +377,7 @@ int mesh_setup(Ctx* c, int et, int64_t N, const double* X, int64_t E, const int6
   double** vecs[] = {&c->x, &c->r, &c->z, &c->p, &c->Ap, &c->dinv, &c->b, &c->tmp, &c->tmp2, &c->xbest};
   for (double** v : vecs)
     if ((rc = dalloc(c, v, n))) return rc;
+  if ((rc = dalloc(c, &c->p2, n))) return rc;
   if ((rc = dalloc(c, &c->part, 4 * JFEM_RED_BLOCKS))) return rc;
   if ((rc = dalloc(c, &c->sc, 1))) return rc;
   if ((rc = dalloc(c, &c->norms, 2))) return rc;

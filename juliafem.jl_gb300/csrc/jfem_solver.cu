@@ -59,7 +59,8 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_pcg_update1(int64_t n, con
 
 __global__ void __launch_bounds__(JFEM_RED_THREADS) k_pcg_update2(int64_t n, SolverScalars* __restrict__ sc, int slot,
                                                                   double* __restrict__ p, const double* __restrict__ z,
-                                                                  const double* __restrict__ part) {
+                                                                  const double* __restrict__ part,
+                                                                  float2* __restrict__ p2) {
   __shared__ double sh[32];
   const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
   if (sc->done[slot]) {
@@ -73,8 +74,14 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_pcg_update2(int64_t n, Sol
   const double rz_new = reduce_partials(part + G_, G_, sh);
   const double rr_new = reduce_partials(part + 2 * G_, G_, sh);
   const double beta = rz_new / sc->rz[slot];
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = z[i] + beta * p[i];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double pi = z[i] + beta * p[i];
+    p[i] = pi;
+    if (p2) {   // FP32 (hi, lo) split for the FP32 apply
+      const float hi = (float)pi;
+      p2[i] = make_float2(hi, (float)(pi - (double)hi));
+    }
+  }
   if (lead) {
     const int it = sc->iters + 1;
     sc->iters = it;
@@ -86,6 +93,8 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_pcg_update2(int64_t n, Sol
 
 // r = (f − y) on free DOFs, 0 on prescribed (y may be null = 0); ‖r‖² partials
 // → part[3G..4G); when fn2 is set also ‖y‖² over all DOFs → part[0..G).
+// fn2 = 1: also ‖y‖² over all DOFs → part[0..G); fn2 = 2: also ‖r_new − r_old‖²
+// (drift of the recursive residual) → part[0..G).
 __global__ void __launch_bounds__(JFEM_RED_THREADS) k_residual(int64_t N, const double* __restrict__ f, double fs,
                                                                const double* __restrict__ y,
                                                                const uint8_t* __restrict__ mask,
@@ -98,9 +107,14 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_residual(int64_t N, const 
     for (int c = 0; c < 3; ++c) {
       const double yv = y ? y[3 * j + c] : 0.0;
       const double v = ((m >> c) & 1) ? 0.0 : fs * f[3 * j + c] - yv;
+      if (fn2 == 2) {
+        const double d = v - r[3 * j + c];
+        yy += d * d;
+      } else {
+        yy += yv * yv;
+      }
       r[3 * j + c] = v;
       rr += v * v;
-      yy += yv * yv;
     }
   }
   rr = block_sum(rr, sh);
@@ -115,14 +129,20 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_residual(int64_t N, const 
 __global__ void __launch_bounds__(JFEM_RED_THREADS) k_precond(int64_t n, const double* __restrict__ r,
                                                               const double* __restrict__ dinv, double* __restrict__ z,
                                                               double* __restrict__ p, int restart,
-                                                              double* __restrict__ part) {
+                                                              double* __restrict__ part, float2* __restrict__ p2) {
   __shared__ double sh[32];
   double rz = 0.0, rr = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double ri = r[i];
     const double zi = dinv[i] * ri;
     z[i] = zi;
-    if (restart) p[i] = zi;
+    if (restart) {
+      p[i] = zi;
+      if (p2) {
+        const float hi = (float)zi;
+        p2[i] = make_float2(hi, (float)(zi - (double)hi));
+      }
+    }
     rz += ri * zi;
     rr += ri * ri;
   }
@@ -165,12 +185,19 @@ __global__ void k_sum_norms(const double* __restrict__ part, double* __restrict_
   }
 }
 
-// u += du on free DOFs, u += dg on prescribed DOFs
+// u += du on free DOFs; prescribed DOFs set to frac·g when assign_fixed
 __global__ void k_update_state(int64_t N, double* __restrict__ u, const double* __restrict__ du,
-                               const double* __restrict__ dg, const uint8_t* __restrict__ mask) {
+                               const double* __restrict__ gvals, double frac, int assign_fixed,
+                               const uint8_t* __restrict__ mask) {
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x) {
     const uint8_t m = mask[j];
-    for (int c = 0; c < 3; ++c) u[3 * j + c] += ((m >> c) & 1) ? dg[3 * j + c] : du[3 * j + c];
+    for (int c = 0; c < 3; ++c) {
+      if ((m >> c) & 1) {
+        if (assign_fixed) u[3 * j + c] = frac * gvals[3 * j + c];
+      } else {
+        u[3 * j + c] += du[3 * j + c];
+      }
+    }
   }
 }
 
@@ -232,19 +259,22 @@ static int read_norms(Ctx* c, double* a, double* b) {
   return 0;
 }
 
-// r ← f − K x (FP64 apply, prescribed rows zero); returns ‖r‖²
-static int true_residual(Ctx* c, const double* f, const double* xv, double* r, double* rr_out) {
-  enqueue_apply(c, xv, c->tmp, false, true, false, nullptr, nullptr);
-  k_residual<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, f, 1.0, c->tmp, c->mask, r, 0, c->part);
+// r ← f − K x (FP64 apply, prescribed rows zero); returns ‖r‖² and, when
+// drift2 is given, ‖r_new − r_old‖² (distance from the recursive residual).
+static int true_residual(Ctx* c, const double* f, const double* xv, double* r, double* rr_out,
+                         double* drift2 = nullptr) {
+  enqueue_apply(c, xv, c->tmp, false, true, false, nullptr, nullptr, nullptr);
+  k_residual<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, f, 1.0, c->tmp, c->mask, r, drift2 ? 2 : 0, c->part);
   c->launches += 1;
-  return read_norms(c, rr_out, nullptr);
+  return read_norms(c, rr_out, drift2);
 }
 
 static void enqueue_iteration(Ctx* c, bool fp32, int slot) {
-  enqueue_apply(c, c->p, c->Ap, fp32, true, false, c->part, &c->sc->done[slot]);
+  enqueue_apply(c, c->p, c->Ap, fp32, true, false, c->part, &c->sc->done[slot], fp32 ? c->p2 : nullptr);
   k_pcg_update1<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->sc, slot, c->x, c->r, c->z, c->p, c->Ap,
                                                        c->dinv, c->part);
-  k_pcg_update2<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->sc, slot, c->p, c->z, c->part);
+  k_pcg_update2<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->sc, slot, c->p, c->z, c->part,
+                                                       fp32 ? c->p2 : nullptr);
   c->launches += 2;
 }
 
@@ -288,17 +318,18 @@ struct PcgResult {
 // (the relative residual when the free part of x₀ is zero).
 //
 // The stopping test always uses the true FP64 residual f − K x.  A "refinement"
-// replaces the recursive residual by the true one and restarts the direction
-// (p = z): with an FP32 operator the recursion drifts from the FP64 residual by
-// about ε₃₂·‖K‖‖x‖, and keeping the old direction after the replacement
-// diverges, while restarting converges (defect correction with CG inner
-// solves).  Refinements happen at recursive convergence and, when `reliable`,
-// each time the recursive residual has dropped by `ru` (in r·r) since the last
-// true residual.  When two refinements in a row gain less than 2× the solve has
+// replaces the recursive residual by the true one.  When the two differ by less
+// than 10 % the search direction is kept (a reliable update: CG keeps its
+// convergence speed); otherwise the direction restarts (p = z), because with an
+// FP32 operator the recursion can drift from the FP64 residual by about
+// ε₃₂·‖K‖‖x‖ and continuing an old direction after a large replacement
+// diverges, while restarting is defect correction with CG inner solves.
+// Refinements happen at recursive convergence and, when `reliable`, each time
+// the recursive residual norm has dropped by `drop` since the last true one.  When two refinements in a row gain less than 2× the solve has
 // reached the attainable accuracy of the arithmetic: the best iterate is kept
 // and JFEM_NOT_CONVERGED returned.
 static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, double time_budget, double t_start,
-               bool reliable, bool x_zero, PcgResult* res) {
+               bool reliable, bool x_zero, PcgResult* res, double drop = 1e-2) {
   int rc = 0;
   double rr0 = 0.0;
   if (x_zero) {
@@ -308,7 +339,8 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
   } else if ((rc = true_residual(c, f, c->x, c->r, &rr0))) {
     return rc;
   }
-  k_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->r, c->dinv, c->z, c->p, 1, c->part);
+  k_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->r, c->dinv, c->z, c->p, 1, c->part,
+                                                   fp32 ? c->p2 : nullptr);
   k_scalars_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 1, tol, max_iter, 1);
   c->launches += 2;
   if ((rc = read_scalars(c))) return rc;
@@ -319,7 +351,7 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
   res->status = 0;
   if (!(bb > 0.0)) return 0;
   if ((rc = build_graph(c, fp32))) return rc;
-  const double ru = fp32 ? 1e-4 : 0.0;
+  const double ru = fp32 ? drop * drop : 0.0;
   const double goal = tol * tol * bb;
   double rr_true_last = rr0, rr_best = rr0;
   cudaMemcpyAsync(c->xbest, c->x, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
@@ -338,8 +370,8 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
     const bool bad = !(rr == rr) || !(s.rz[0] > 0.0) || rr > 1e30 * bb;
     const bool check = s.done[0] || bad || (reliable && rr < ru * rr_true_last);
     if (check) {
-      double rr_t = 0.0;
-      if ((rc = true_residual(c, f, c->x, c->r, &rr_t))) return rc;
+      double rr_t = 0.0, drift2 = 0.0;
+      if ((rc = true_residual(c, f, c->x, c->r, &rr_t, &drift2))) return rc;
       ++refinements;
       const bool finite = rr_t == rr_t && rr_t < 1e300;
       if (finite && rr_t < rr_best) {
@@ -365,8 +397,10 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
         if ((rc = true_residual(c, f, c->x, c->r, &rr_t))) return rc;
         rr_true_last = rr_t;
       }
-      // refinement: r ← true residual, restart p = z
-      k_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->r, c->dinv, c->z, c->p, 1, c->part);
+      // refinement: r ← true residual; keep p when the drift is small, else restart
+      const int restart = (finite && drift2 < 0.01 * rr_t) ? 0 : 1;
+      k_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->r, c->dinv, c->z, c->p, restart, c->part,
+                                                   fp32 ? c->p2 : nullptr);
       k_scalars_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 0, tol, max_iter, 0);
       c->launches += 2;
       if ((rc = read_scalars(c))) return rc;
@@ -405,7 +439,8 @@ static int solve_linear(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
   cudaMemcpyAsync(c->x, c->gvals, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   const bool fp32 = o->precision == JFEM_MIXED;
   PcgResult pr;
-  rc = pcg(c, c->f_ext, fp32, o->tol, o->max_iter, o->time_budget_s, t0, true, c->n_fixed_nonzero == 0, &pr);
+  rc = pcg(c, c->f_ext, fp32, o->tol, o->max_iter, o->time_budget_s, t0, true, c->n_fixed_nonzero == 0, &pr,
+           o->refine_drop > 0.0 ? o->refine_drop : 0.3);
   if (rc) return rc;
   cudaMemcpyAsync(u_d, c->x, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   if ((rc = sync_and_check(c, "solution copy"))) return rc;
@@ -438,6 +473,7 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
     const double frac = (double)s / steps;
     bool converged = false;
     for (int k = 1; k <= o->max_newton + 1; ++k) {
+      const bool first = (k == 1);
       // R = frac f_ext − f_int(u) on free DOFs
       enqueue_internal_force(c, c->Ap);
       k_residual<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->f_ext, frac, c->Ap, c->mask, c->b, 1, c->part);
@@ -449,12 +485,14 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
       if (!(scale > 0.0)) scale = 1.0;
       if (!(rn == rn)) return set_err(c, JFEM_ERR_NAN, "NaN in the Newton residual");
       last_rel = rn / scale;
-      // prescribed-value increment of this step
-      k_bc_increment<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->gvals, frac, c->u_state, c->mask, dg, c->part);
-      c->launches += 1;
+      // increment of the prescribed values: carried by the first iteration of the step
       double dgg = 0.0;
-      if ((rc = read_norms(c, &dgg, nullptr))) return rc;
-      if (dgg == 0.0 && rn <= o->newton_tol * scale) {
+      if (first) {
+        k_bc_increment<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->gvals, frac, c->u_state, c->mask, dg, c->part);
+        c->launches += 1;
+        if ((rc = read_norms(c, &dgg, nullptr))) return rc;
+      }
+      if ((!first || dgg == 0.0) && rn <= o->newton_tol * scale) {
         converged = true;
         break;
       }
@@ -462,7 +500,7 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
       // tangent Jacobi diagonal at u, rhs b = R − K_T dg
       if ((rc = jacobi_diag_device(c, c->dinv))) return rc;
       if (dgg > 0.0) {
-        enqueue_apply(c, dg, c->tmp, fp32, true, false, nullptr, nullptr);
+        enqueue_apply(c, dg, c->tmp, fp32, true, false, nullptr, nullptr, nullptr);
         k_sub_free<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->b, c->tmp);
         c->launches += 1;
       }
@@ -475,7 +513,8 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
       total_cg += pr.iters;
       refin += pr.refinements;
       ++total_newton;
-      k_update_state<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->u_state, c->x, dg, c->mask);
+      k_update_state<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->u_state, c->x, c->gvals, frac, first ? 1 : 0,
+                                                            c->mask);
       c->launches += 1;
       if (st && hist < JFEM_HISTORY_MAX) {
         st->history[3 * hist] = pr.iters;

@@ -414,17 +414,21 @@ def run_(analysis: Analysis, time: float = 0.0):
     node_map, ids = prob._node_map
     dofs, vals = {}, {}
     for bc in bcs:
+        # within one Dirichlet problem later values overwrite earlier ones
+        # (field_vals dict of src/problems_dirichlet.jl:60-89); a DOF constrained by
+        # two problems is an error (check_for_overconstrained_dofs, src/solvers.jl:96-130)
+        mine = {}
         for el in bc.elements:
             for i in range(3):
                 key = f"{bc.parent_field_name or 'displacement'} {i + 1}"
                 if key not in el.fields:
                     continue
                 for n in el.connectivity:
-                    d = 3 * node_map[n] + i
-                    if d in dofs:
-                        raise RuntimeError("problem is overconstrained, not continuing to solution.")
-                    dofs[d] = True
-                    vals[d] = float(el.fields[key])
+                    mine[3 * node_map[n] + i] = float(el.fields[key])
+        if set(mine) & set(dofs):
+            raise RuntimeError("problem is overconstrained, not continuing to solution.")
+        dofs.update({d: True for d in mine})
+        vals.update(mine)
     d = np.array(sorted(dofs), dtype=np.int64)
     ctx.set_dirichlet(d, np.array([vals[k] for k in d]) if d.size else None)
     u, st, rc = ctx.solve(method=_abi.PCG_JACOBI, precision=_abi.FP64, tol=analysis.properties["tol"],
