@@ -34,6 +34,11 @@ extern "C" {
 #define JFEM_ERR_NEG_JACOBIAN -4   /* detJ <= 0 in an element */
 #define JFEM_ERR_NAN          -5   /* NaN/Inf, or J <= 0 in the Neo-Hookean law */
 #define JFEM_ERR_TIMEOUT      -6   /* a bounded device loop ran out of its budget */
+#define JFEM_ERR_TOO_LARGE    -7   /* jfem_apply_noalloc: mesh needs more than its fixed scratch */
+
+/* Size of the fixed device array jfem_apply_noalloc works in (every GPU that
+ * loads the library holds it until the process exits). */
+#define JFEM_NOALLOC_SCRATCH_BYTES (64u << 20)
 
 /* element, face and material codes */
 #define JFEM_TET4   4
@@ -155,6 +160,27 @@ int jfem_solve(jfem_ctx* ctx, const jfem_solve_opts* opts, double* u, jfem_stats
 /* Same with u left in device memory (u_device: 3 n_nodes doubles). */
 int jfem_solve_device(jfem_ctx* ctx, const jfem_solve_opts* opts, double* u_device,
                       jfem_stats* stats);
+
+/* Matrix-free FP64 y = K v for a linear-elastic mesh held entirely in device
+ * memory, without allocating any device memory.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc — a host
+ * application that owns the device memory through its own arena or pool (an
+ * embedding simulation, a Julia CUDA memory pool), or a latency-critical loop
+ * where an allocation could stall the device.  Inputs and outputs are the
+ * caller's device buffers: X (3 × n_nodes), conn (n_en × n_elem column-major,
+ * numbers from index_base), E and nu (one per element), v and y (3 n_nodes).
+ * Working storage is one fixed array of JFEM_NOALLOC_SCRATCH_BYTES per device;
+ * meshes that need more return JFEM_ERR_TOO_LARGE (roughly 200k Tet10,
+ * 280k Hex8 or 500k Tet4 elements).  All calls share that array, so calls that
+ * overlap on the GPU race and must be serialised by the caller.  The first call
+ * on a device resolves the array's address for that device; make it before any
+ * stream capture.  Runs on `stream` (a cudaStream_t, NULL = legacy default) and
+ * returns after the stream has finished the work.  Status as elsewhere
+ * (JFEM_ERR_INVALID for out-of-range connectivity, JFEM_ERR_NEG_JACOBIAN). */
+int jfem_apply_noalloc(int elem_type, int64_t n_nodes, const double* X_device, int64_t n_elem,
+                       const int64_t* conn_device, int index_base, const double* E_device,
+                       const double* nu_device, const double* v_device, double* y_device,
+                       void* stream);
 
 /* Kernels launched by the library on this context since its creation. */
 int64_t jfem_kernel_launches(const jfem_ctx* ctx);

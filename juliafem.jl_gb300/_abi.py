@@ -15,7 +15,8 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libjfem_cuda.so"
 
 OK, NOT_CONVERGED, STALL = 0, 1, 2
-ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_NEG_JACOBIAN, ERR_NAN, ERR_TIMEOUT = -1, -2, -3, -4, -5, -6
+ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_NEG_JACOBIAN, ERR_NAN, ERR_TIMEOUT, ERR_TOO_LARGE = -1, -2, -3, -4, -5, -6, -7
+NOALLOC_SCRATCH_BYTES = 64 << 20
 TET4, TET10, HEX8 = 4, 10, 8
 TRI3, TRI6, QUAD4 = 3, 6, 4
 LINEAR_ELASTIC, NEO_HOOKEAN = 0, 1
@@ -84,6 +85,7 @@ SIGNATURES = {
     "jfem_last_apply_ms": (C.c_double, [_P]),
     "jfem_stream": (C.c_void_p, [_P]),
     "jfem_time_apply": (C.c_int, [_P, C.c_int, C.c_int, _f64p, _f64p]),
+    "jfem_apply_noalloc": (C.c_int, [C.c_int, _i64, _P, _i64, _P, C.c_int, _P, _P, _P, _P, _P]),
 }
 
 _lib = None
