@@ -26,6 +26,9 @@ namespace jfem {
 void launch_apply_tet4(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in, const int* stop);
 void launch_apply_tet10(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in, const int* stop);
 void launch_apply_hex8(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in, const int* stop);
+void launch_tile_tet4(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part, const int* stop);
+void launch_tile_tet10(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part, const int* stop);
+void launch_tile_hex8(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part, const int* stop);
 
 // ---------------------------------------------------------------------------
 // geometry preparation (FP64)
@@ -190,6 +193,58 @@ __global__ void k_split(int64_t n, const double* __restrict__ v, float2* __restr
   }
 }
 
+// Boundary nodes of the tiled apply: sum the tile partials in ascending tile
+// order; optional v·y partials into part[blockIdx.x].
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_tile_boundary(int64_t nb, const int* __restrict__ bnodes,
+                                                                    const int* __restrict__ bptr,
+                                                                    const int* __restrict__ bslots,
+                                                                    const float* __restrict__ bpart,
+                                                                    const uint8_t* __restrict__ mask, int masked,
+                                                                    const double* __restrict__ vdot,
+                                                                    double* __restrict__ y, double* __restrict__ part,
+                                                                    const int* __restrict__ stop) {
+  __shared__ double sh[32];
+  if (stop && *stop) return;
+  double dot = 0.0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nb; k += (int64_t)gridDim.x * blockDim.x) {
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    const int i1 = __ldg(bptr + k + 1);
+    for (int i = __ldg(bptr + k); i < i1; ++i) {
+      const int64_t sl = __ldg(bslots + i);
+      s0 += __ldg(bpart + 3 * sl);
+      s1 += __ldg(bpart + 3 * sl + 1);
+      s2 += __ldg(bpart + 3 * sl + 2);
+    }
+    const int64_t g = __ldg(bnodes + k);
+    if (masked) {
+      const uint8_t m = __ldg(mask + g);
+      if (m & 1) s0 = 0.f;
+      if (m & 2) s1 = 0.f;
+      if (m & 4) s2 = 0.f;
+    }
+    y[3 * g] = s0;
+    y[3 * g + 1] = s1;
+    y[3 * g + 2] = s2;
+    if (part) dot += vdot[3 * g] * (double)s0 + vdot[3 * g + 1] * (double)s1 + vdot[3 * g + 2] * (double)s2;
+  }
+  if (part) {
+    const double b = block_sum(dot, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = b;
+  }
+}
+
+// geometry records to tile order (padding zero)
+__global__ void k_permute_records(int rec, int64_t E, int64_t Epad, const int* __restrict__ perm,
+                                  const float* __restrict__ src, float* __restrict__ dst) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)rec * Epad;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i / Epad);
+    const int64_t p = i - (int64_t)k * Epad;
+    const int e = perm[p];
+    dst[i] = e >= 0 ? src[(int64_t)k * E + e] : 0.f;
+  }
+}
+
 void enqueue_split(Ctx* c, const double* v, float2* v2) {
   k_split<<<grid_for(3 * c->N, 256), 256, 0, c->stream>>>(3 * c->N, v, v2);
   c->launches += 1;
@@ -199,8 +254,14 @@ void enqueue_split(Ctx* c, const double* v, float2* v2) {
 // host side
 // ---------------------------------------------------------------------------
 int geometry_invalidate(Ctx* c) {
+  if (c->pcg_graph) {   // captured launches hold the geometry pointers
+    cudaGraphExecDestroy(c->pcg_graph);
+    c->pcg_graph = nullptr;
+    c->pcg_graph_key = -1;
+  }
   if (c->geo64) { dfree(c, c->geo64); c->geo64 = nullptr; }
   if (c->geo32) { dfree(c, c->geo32); c->geo32 = nullptr; }
+  if (c->geoT32) { dfree(c, c->geoT32); c->geoT32 = nullptr; }
   c->geo_ready = false;
   return 0;
 }
@@ -228,6 +289,12 @@ static int prepare_et(Ctx* c) {
   k_prepare_geo<ET><<<grid_for(c->E, 128), 128, 0, c->stream>>>(c->E, c->conn, c->X64, c->lam64, c->mu64,
                                                                 c->geo_affine ? 1 : 0, c->geo64, c->geo32);
   c->launches += 1;
+  if (c->ntiles > 0) {
+    if ((rc = dalloc(c, &c->geoT32, rec * c->Epad))) return rc;
+    k_permute_records<<<grid_for(rec * c->Epad, 256), 256, 0, c->stream>>>((int)rec, c->E, c->Epad, c->tperm,
+                                                                          c->geo32, c->geoT32);
+    c->launches += 1;
+  }
   rc = sync_and_check(c, "geometry");
   if (!rc) c->geo_ready = true;
   return rc;
@@ -266,8 +333,34 @@ static void launch_gather(Ctx* c, bool fp32, bool masked, const double* v, doubl
 
 // Enqueue (no sync): y = K v (masked rows zero when masked), partial v·y sums
 // into part[0..JFEM_RED_BLOCKS) when part != nullptr.
+// FP32 with a split input and a built tiling → the tiled apply (interior
+// partials in part[0..G), boundary partials in part[3G..4G)); otherwise the
+// two-phase apply (partials in part[0..G)).
+bool apply_is_tiled(const Ctx* c, bool fp32, const float2* v2) { return fp32 && v2 && c->geoT32 && c->ntiles > 0; }
+
+static void launch_tiles(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part,
+                         const int* stop) {
+  switch (c->et) {
+    case JFEM_TET4: launch_tile_tet4(c, v2, vdot, y, masked, part, stop); break;
+    case JFEM_TET10: launch_tile_tet10(c, v2, vdot, y, masked, part, stop); break;
+    default: launch_tile_hex8(c, v2, vdot, y, masked, part, stop); break;
+  }
+}
+
+static void launch_tile_boundary(Ctx* c, const double* vdot, double* y, bool masked, double* part, const int* stop) {
+  k_tile_boundary<<<JFEM_RED_BLOCKS, JFEM_RED_THREADS, 0, c->stream>>>(
+      c->n_bnodes, c->bnodes, c->bptr, c->bslots, c->bpart, c->mask, masked ? 1 : 0, vdot, y,
+      part ? part + 3 * JFEM_RED_BLOCKS : nullptr, stop);
+  c->launches += 1;
+}
+
 void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, bool mask_in, double* part,
                    const int* stop, const float2* v2) {
+  if (apply_is_tiled(c, fp32, v2)) {
+    launch_tiles(c, v2, v, y, masked || mask_in, part, stop);
+    launch_tile_boundary(c, v, y, masked || mask_in, part, stop);
+    return;
+  }
   launch_elements(c, fp32, 0, v, fp32 ? v2 : nullptr, mask_in, stop);
   launch_gather(c, fp32, masked, v, y, part, stop);
 }
@@ -277,7 +370,8 @@ int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, dou
   if (rc) return rc;
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
   cudaEventRecord(c->ev0, c->stream);
-  enqueue_apply(c, v, y, fp32, masked, masked, part, nullptr, nullptr);
+  if (fp32) enqueue_split(c, v, c->p2);
+  enqueue_apply(c, v, y, fp32, masked, masked, part, nullptr, fp32 ? c->p2 : nullptr);
   cudaEventRecord(c->ev1, c->stream);
   int h_err = 0;
   cudaMemcpyAsync(&h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
@@ -333,9 +427,15 @@ int time_apply(Ctx* c, bool fp32, bool masked, int reps, double* ms_elem, double
   double se = 0.0, sg = 0.0;
   for (int r = 0; r < reps; ++r) {
     cudaEventRecord(e0, c->stream);
-    launch_elements(c, fp32, 0, c->tmp, fp32 ? c->p2 : nullptr, masked, nullptr);
-    cudaEventRecord(e1, c->stream);
-    launch_gather(c, fp32, masked, c->tmp, c->tmp2, c->part, nullptr);
+    if (apply_is_tiled(c, fp32, c->p2)) {
+      launch_tiles(c, c->p2, c->tmp, c->tmp2, masked, c->part, nullptr);
+      cudaEventRecord(e1, c->stream);
+      launch_tile_boundary(c, c->tmp, c->tmp2, masked, c->part, nullptr);
+    } else {
+      launch_elements(c, fp32, 0, c->tmp, fp32 ? c->p2 : nullptr, masked, nullptr);
+      cudaEventRecord(e1, c->stream);
+      launch_gather(c, fp32, masked, c->tmp, c->tmp2, c->part, nullptr);
+    }
     cudaEventRecord(e2, c->stream);
     cudaEventSynchronize(e2);
     float a = 0.f, b = 0.f;

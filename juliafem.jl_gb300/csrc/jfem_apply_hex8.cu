@@ -6,4 +6,8 @@ void launch_apply_hex8(Ctx* c, bool fp32, int mode, const double* v, const float
                         const int* stop) {
   launch_apply_et<JFEM_HEX8>(c, fp32, mode, v, v2, mask_in, stop);
 }
+void launch_tile_hex8(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part,
+                      const int* stop) {
+  launch_tile_et<JFEM_HEX8>(c, v2, vdot, y, masked, part, stop);
+}
 }  // namespace jfem

@@ -149,9 +149,110 @@ __host__ __device__ constexpr R dnr(int et, int q, int i, int a) {
 }
 
 // ---------------------------------------------------------------------------
-// phase 1: element kernel
-//   MODE 0: y = K v (linear) / K_T(u) v (finite, KIN ≠ SMALL)
-//   MODE 1: y = f_int(u) (v ignored; KIN ≠ SMALL)
+// Element operator from element-local differences.
+//   dv[i] = v_i − v_0, du[i] = u_i − u_0 (i ≥ 1; index 0 unused).
+//   geo: record base pointer, records strided by `stride` (SoA).
+//   MODE 0: y = K v (linear) / K_T(u) v (finite); MODE 1: y = f_int(u).
+// Returns false when the material state is invalid (det C ≤ 0).
+// ---------------------------------------------------------------------------
+template <int ET, typename R, bool AFFINE, int KIN, bool GEOM, int MODE>
+__device__ __forceinline__ bool element_op(const R (&dv)[Elem<ET>::NN][3], const R (&du)[Elem<ET>::NN][3],
+                                           const R* __restrict__ geo, int64_t stride,
+                                           R (&y)[Elem<ET>::NN][3]) {
+  constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
+  constexpr bool NEED_U = (KIN != KIN_SMALL);
+  constexpr bool NEED_V = (MODE == 0);
+#pragma unroll
+  for (int i = 0; i < NN; ++i) y[i][0] = y[i][1] = y[i][2] = R(0);
+  R iJ[9], lam, mu, det = R(1);
+  if (AFFINE) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) iJ[k] = __ldg(geo + (int64_t)k * stride);
+    lam = __ldg(geo + (int64_t)9 * stride);
+    mu = __ldg(geo + (int64_t)10 * stride);
+  } else {
+    lam = __ldg(geo + (int64_t)(10 * NQ) * stride);
+    mu = __ldg(geo + (int64_t)(10 * NQ + 1) * stride);
+  }
+  bool ok = true;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    if (!AFFINE) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) iJ[k] = __ldg(geo + (int64_t)(10 * q + k) * stride);
+      det = __ldg(geo + (int64_t)(10 * q + 9) * stride);
+    }
+    R gv[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, gu[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    if (NEED_V) {
+      R G[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          R s = R(0);
+#pragma unroll
+          for (int i = 1; i < NN; ++i) {
+            const R dn = dnr<R>(ET, q, i, a);
+            if (dn != R(0)) s += dv[i][c] * dn;
+          }
+          G[c][a] = s;
+        }
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) gv[c][d] = G[c][0] * iJ[3 * d] + G[c][1] * iJ[3 * d + 1] + G[c][2] * iJ[3 * d + 2];
+    }
+    if (NEED_U) {
+      R G[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          R s = R(0);
+#pragma unroll
+          for (int i = 1; i < NN; ++i) {
+            const R dn = dnr<R>(ET, q, i, a);
+            if (dn != R(0)) s += du[i][c] * dn;
+          }
+          G[c][a] = s;
+        }
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) gu[c][d] = G[c][0] * iJ[3 * d] + G[c][1] * iJ[3 * d + 1] + G[c][2] * iJ[3 * d + 2];
+    }
+    R P[3][3];
+    if (MODE == 1) {
+      ok &= flux_pk1<R, KIN>(gu, lam, mu, P);
+    } else if (KIN == KIN_SMALL) {
+      flux_small<R>(gv, lam, mu, P);
+    } else {
+      ok &= flux_tangent<R, KIN, GEOM>(gu, gv, lam, mu, P);
+    }
+    // Q[c][a] = w·detJ Σ_d P[c][d] J⁻¹[d][a]   (affine records carry detJ inside λ, μ)
+    const R wq = (R)qp_weight(ET, q) * det;
+    R Q[3][3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) Q[c][a] = wq * (P[c][0] * iJ[a] + P[c][1] * iJ[3 + a] + P[c][2] * iJ[6 + a]);
+#pragma unroll
+    for (int i = 0; i < NN; ++i)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const R dn = dnr<R>(ET, q, i, a);
+        if (dn != R(0)) {
+          y[i][0] += Q[0][a] * dn;
+          y[i][1] += Q[1][a] * dn;
+          y[i][2] += Q[2][a] * dn;
+        }
+      }
+  }
+  return ok;
+}
+
+// ---------------------------------------------------------------------------
+// two-phase apply, phase 1: one thread per element, element vectors to HBM
 //   SPLIT:  v given as FP32 (hi, lo) pairs per DOF (v ≈ hi + lo).  Gradients
 //           use element-local differences v_i − v_0 = (hi_i − hi_0) + (lo_i − lo_0):
 //           for a smooth field the hi difference is exact (Sterbenz), so ∇v
@@ -167,7 +268,7 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
                                                     const uint8_t* __restrict__ mask, R* __restrict__ ye,
                                                     int* err, const int* __restrict__ stop,
                                                     int mask_in) {
-  constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
+  constexpr int NN = Elem<ET>::NN;
   if (stop && *stop) return;
   constexpr bool NEED_U = (KIN != KIN_SMALL);
   constexpr bool NEED_V = (MODE == 0);
@@ -175,7 +276,6 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
     int nodes[NN];
 #pragma unroll
     for (int i = 0; i < NN; ++i) nodes[i] = __ldg(conn + (int64_t)i * E + e);
-    // element-local differences (index 0 unused)
     R dv[NN][3], du[NN][3];
     R h0[3] = {0, 0, 0}, l0[3] = {0, 0, 0}, u0[3] = {0, 0, 0};
 #pragma unroll
@@ -206,92 +306,7 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
       }
     }
     R y[NN][3];
-#pragma unroll
-    for (int i = 0; i < NN; ++i) y[i][0] = y[i][1] = y[i][2] = R(0);
-    R iJ[9], lam, mu, det = R(1);
-    if (AFFINE) {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) iJ[k] = __ldg(geo + (int64_t)k * E + e);
-      lam = __ldg(geo + (int64_t)9 * E + e);
-      mu = __ldg(geo + (int64_t)10 * E + e);
-    } else {
-      lam = __ldg(geo + (int64_t)(10 * NQ) * E + e);
-      mu = __ldg(geo + (int64_t)(10 * NQ + 1) * E + e);
-    }
-    bool ok = true;
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      if (!AFFINE) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) iJ[k] = __ldg(geo + (int64_t)(10 * q + k) * E + e);
-        det = __ldg(geo + (int64_t)(10 * q + 9) * E + e);
-      }
-      R gv[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, gu[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-      if (NEED_V) {
-        R G[3][3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            R s = R(0);
-#pragma unroll
-            for (int i = 1; i < NN; ++i) {
-              const R dn = dnr<R>(ET, q, i, a);
-              if (dn != R(0)) s += dv[i][c] * dn;
-            }
-            G[c][a] = s;
-          }
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-          for (int d = 0; d < 3; ++d) gv[c][d] = G[c][0] * iJ[3 * d] + G[c][1] * iJ[3 * d + 1] + G[c][2] * iJ[3 * d + 2];
-      }
-      if (NEED_U) {
-        R G[3][3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            R s = R(0);
-#pragma unroll
-            for (int i = 1; i < NN; ++i) {
-              const R dn = dnr<R>(ET, q, i, a);
-              if (dn != R(0)) s += du[i][c] * dn;
-            }
-            G[c][a] = s;
-          }
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-          for (int d = 0; d < 3; ++d) gu[c][d] = G[c][0] * iJ[3 * d] + G[c][1] * iJ[3 * d + 1] + G[c][2] * iJ[3 * d + 2];
-      }
-      R P[3][3];
-      if (MODE == 1) {
-        ok &= flux_pk1<R, KIN>(gu, lam, mu, P);
-      } else if (KIN == KIN_SMALL) {
-        flux_small<R>(gv, lam, mu, P);
-      } else {
-        ok &= flux_tangent<R, KIN, GEOM>(gu, gv, lam, mu, P);
-      }
-      // Q[c][a] = w·detJ Σ_d P[c][d] J⁻¹[d][a]   (affine records carry detJ inside λ, μ)
-      const R wq = (R)qp_weight(ET, q) * det;
-      R Q[3][3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int a = 0; a < 3; ++a) Q[c][a] = wq * (P[c][0] * iJ[a] + P[c][1] * iJ[3 + a] + P[c][2] * iJ[6 + a]);
-#pragma unroll
-      for (int i = 0; i < NN; ++i)
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          const R dn = dnr<R>(ET, q, i, a);
-          if (dn != R(0)) {
-            y[i][0] += Q[0][a] * dn;
-            y[i][1] += Q[1][a] * dn;
-            y[i][2] += Q[2][a] * dn;
-          }
-        }
-    }
+    const bool ok = element_op<ET, R, AFFINE, KIN, GEOM, MODE>(dv, du, geo + e, E, y);
     if (!ok) raise_error(err, JFEM_ERR_NAN);
 #pragma unroll
     for (int i = 0; i < NN; ++i)
@@ -300,6 +315,111 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
   }
 }
 
+// ---------------------------------------------------------------------------
+// tiled FP32 apply (see jfem_tiles.cu).  One CTA of JFEM_TILE threads per tile
+// (persistent over tiles); dynamic shared memory:
+//   ye  [3·NN][T] f32   element vectors of the tile
+//   vs  [3·Lmax]  float2 (hi, lo) of the tile's nodes (masked DOFs zero)
+//   us  [3·Lmax]  f32   state u of the tile's nodes (finite strain only)
+// Interior nodes → y (FP64) directly, boundary nodes → bpart[slot] (f32 × 3);
+// optional v·y partial over interior nodes into part[blockIdx.x].
+// ---------------------------------------------------------------------------
+template <int ET, bool AFFINE, int KIN, bool GEOM>
+__global__ void __launch_bounds__(JFEM_TILE) k_tile_apply(
+    int64_t ntiles, int64_t Epad, const int* __restrict__ tnode_ptr, const int* __restrict__ tnodes,
+    const uint16_t* __restrict__ tconn, const float* __restrict__ geo, const uint16_t* __restrict__ tadj_ptr,
+    const uint16_t* __restrict__ tadj, const int* __restrict__ tbslot, const int* __restrict__ tperm,
+    const float2* __restrict__ v2, const double* __restrict__ vdot, const double* __restrict__ u,
+    const uint8_t* __restrict__ mask, int masked, int Lmax, double* __restrict__ y, float* __restrict__ bpart,
+    double* __restrict__ part, int* err, const int* __restrict__ stop) {
+  constexpr int NN = Elem<ET>::NN;
+  constexpr int T = JFEM_TILE;
+  constexpr bool NEED_U = (KIN != KIN_SMALL);
+  extern __shared__ float4 smem_f4[];
+  float* ye = reinterpret_cast<float*>(smem_f4);
+  float2* vs = reinterpret_cast<float2*>(ye + 3 * NN * T);
+  float* us = reinterpret_cast<float*>(vs + 3 * Lmax);
+  __shared__ double sh[32];
+  if (stop && *stop) return;
+  const int tid = threadIdx.x;
+  double dot = 0.0;
+  bool ok = true;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int n0 = __ldg(tnode_ptr + t);
+    const int L = __ldg(tnode_ptr + t + 1) - n0;
+    for (int j = tid; j < 3 * L; j += T) {
+      const int ln = j / 3, c = j - 3 * (j / 3);
+      const int64_t g = __ldg(tnodes + n0 + ln);
+      float2 h = __ldg(v2 + 3 * g + c);
+      if (masked && ((__ldg(mask + g) >> c) & 1)) h = make_float2(0.f, 0.f);
+      vs[j] = h;
+      if (NEED_U) us[j] = (float)__ldg(u + 3 * g + c);
+    }
+    __syncthreads();
+    const int64_t e = t * T + tid;
+    if (__ldg(tperm + e) >= 0) {
+      int li[NN];
+#pragma unroll
+      for (int a = 0; a < NN; ++a) li[a] = __ldg(tconn + (int64_t)a * Epad + e);
+      float dv[NN][3], du[NN][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float2 h0 = vs[3 * li[0] + c];
+        const float u0 = NEED_U ? us[3 * li[0] + c] : 0.f;
+#pragma unroll
+        for (int i = 1; i < NN; ++i) {
+          const float2 h = vs[3 * li[i] + c];
+          dv[i][c] = (h.x - h0.x) + (h.y - h0.y);
+          if (NEED_U) du[i][c] = us[3 * li[i] + c] - u0;
+        }
+      }
+      float yl[NN][3];
+      ok &= element_op<ET, float, AFFINE, KIN, GEOM, 0>(dv, du, geo + e, Epad, yl);
+#pragma unroll
+      for (int a = 0; a < NN; ++a)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ye[(3 * a + c) * T + tid] = yl[a][c];
+    }
+    __syncthreads();
+    const uint16_t* lp = tadj_ptr + n0 + t;
+    const uint16_t* la = tadj + t * (int64_t)T * NN;
+    for (int j = tid; j < L; j += T) {
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+      const int k1 = __ldg(lp + j + 1);
+      for (int k = __ldg(lp + j); k < k1; ++k) {
+        const int pk = __ldg(la + k);
+        const int le = pk >> 4, a = pk & 15;
+        s0 += ye[(3 * a + 0) * T + le];
+        s1 += ye[(3 * a + 1) * T + le];
+        s2 += ye[(3 * a + 2) * T + le];
+      }
+      const int64_t g = __ldg(tnodes + n0 + j);
+      if (masked) {
+        const uint8_t m = __ldg(mask + g);
+        if (m & 1) s0 = 0.f;
+        if (m & 2) s1 = 0.f;
+        if (m & 4) s2 = 0.f;
+      }
+      const int slot = __ldg(tbslot + n0 + j);
+      if (slot < 0) {
+        y[3 * g] = s0;
+        y[3 * g + 1] = s1;
+        y[3 * g + 2] = s2;
+        if (part) dot += vdot[3 * g] * (double)s0 + vdot[3 * g + 1] * (double)s1 + vdot[3 * g + 2] * (double)s2;
+      } else {
+        bpart[3 * (int64_t)slot] = s0;
+        bpart[3 * (int64_t)slot + 1] = s1;
+        bpart[3 * (int64_t)slot + 2] = s2;
+      }
+    }
+    __syncthreads();
+  }
+  if (!ok) raise_error(err, JFEM_ERR_NAN);
+  if (part) {
+    const double b = block_sum(dot, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = b;
+  }
+}
 
 // ---------------------------------------------------------------------------
 // launch helpers, instantiated once per element type (jfem_apply_<type>.cu)
@@ -331,6 +451,46 @@ static void dispatch_kin(Ctx* c, const R* geo, const double* v, const float2* v2
     if (MODE == 1) launch_elem<ET, R, AFFINE, KIN_NH, false, 1>(c, geo, v, nullptr, ye, stop, false);
     else if (c->geom) launch_elem<ET, R, AFFINE, KIN_NH, true, 0>(c, geo, v, v2, ye, stop, mask_in);
     else launch_elem<ET, R, AFFINE, KIN_NH, false, 0>(c, geo, v, v2, ye, stop, mask_in);
+  }
+}
+
+template <int ET, bool AFFINE, int KIN, bool GEOM>
+static void launch_tile_k(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part,
+                          const int* stop) {
+  constexpr int NN = Elem<ET>::NN;
+  const size_t sm = (size_t)3 * NN * JFEM_TILE * sizeof(float) + (size_t)3 * c->tile_Lmax * sizeof(float2) +
+                    ((KIN != KIN_SMALL) ? (size_t)3 * c->tile_Lmax * sizeof(float) : 0);
+  cudaFuncSetAttribute(k_tile_apply<ET, AFFINE, KIN, GEOM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const unsigned g = (unsigned)(c->ntiles < JFEM_RED_BLOCKS ? JFEM_RED_BLOCKS : JFEM_RED_BLOCKS);
+  k_tile_apply<ET, AFFINE, KIN, GEOM><<<g, JFEM_TILE, sm, c->stream>>>(
+      c->ntiles, c->Epad, c->tnode_ptr, c->tnodes, c->tconn, c->geoT32, c->tadj_ptr, c->tadj, c->tbslot, c->tperm,
+      v2, vdot, c->u_state, c->mask, masked ? 1 : 0, c->tile_Lmax, y, c->bpart, part, c->d_err, stop);
+  c->launches += 1;
+}
+
+// Tiled FP32 element + in-tile gather launch (the boundary sum is a separate kernel).
+template <int ET>
+void launch_tile_et(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part,
+                    const int* stop) {
+  const int kin = !c->finite ? KIN_SMALL : (c->model == JFEM_NEO_HOOKEAN ? KIN_NH : KIN_SVK);
+  if (c->geo_affine) {
+    if (kin == KIN_SMALL) launch_tile_k<ET, true, KIN_SMALL, false>(c, v2, vdot, y, masked, part, stop);
+    else if (kin == KIN_SVK) {
+      if (c->geom) launch_tile_k<ET, true, KIN_SVK, true>(c, v2, vdot, y, masked, part, stop);
+      else launch_tile_k<ET, true, KIN_SVK, false>(c, v2, vdot, y, masked, part, stop);
+    } else {
+      if (c->geom) launch_tile_k<ET, true, KIN_NH, true>(c, v2, vdot, y, masked, part, stop);
+      else launch_tile_k<ET, true, KIN_NH, false>(c, v2, vdot, y, masked, part, stop);
+    }
+  } else {
+    if (kin == KIN_SMALL) launch_tile_k<ET, false, KIN_SMALL, false>(c, v2, vdot, y, masked, part, stop);
+    else if (kin == KIN_SVK) {
+      if (c->geom) launch_tile_k<ET, false, KIN_SVK, true>(c, v2, vdot, y, masked, part, stop);
+      else launch_tile_k<ET, false, KIN_SVK, false>(c, v2, vdot, y, masked, part, stop);
+    } else {
+      if (c->geom) launch_tile_k<ET, false, KIN_NH, true>(c, v2, vdot, y, masked, part, stop);
+      else launch_tile_k<ET, false, KIN_NH, false>(c, v2, vdot, y, masked, part, stop);
+    }
   }
 }
 

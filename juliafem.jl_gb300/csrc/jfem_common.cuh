@@ -24,6 +24,7 @@
 #define JFEM_MAX_NEIGHBOURS 512   // unique neighbour nodes per node (pattern build)
 #define JFEM_RED_BLOCKS 1216      // fixed reduction grid: 152 SMs x 8 → deterministic sums
 #define JFEM_RED_THREADS 256
+#define JFEM_TILE 256             // elements per tile of the shared-memory apply
 
 namespace jfem {
 
@@ -221,6 +222,22 @@ struct Ctx {
   double* geo64 = nullptr;
   float* geo32 = nullptr;
 
+  // element tiles of the shared-memory FP32 apply (jfem_tiles.cu)
+  int64_t ntiles = 0, Epad = 0, n_bnodes = 0, n_bslots = 0;
+  int tile_Lmax = 0;
+  int* tperm = nullptr;         // [Epad] tile position → element (−1 padding)
+  uint16_t* tconn = nullptr;    // [n_en][Epad] tile-local node of each element node
+  int* tnode_ptr = nullptr;     // [ntiles+1]
+  int* tnodes = nullptr;        // global node of each tile node
+  uint16_t* tadj_ptr = nullptr; // per tile: L+1 offsets into the tile's adjacency block
+  uint16_t* tadj = nullptr;     // [ntiles][T·n_en] (local element << 4 | local node)
+  int* tbslot = nullptr;        // boundary slot of each tile node, −1 when interior
+  int* bnodes = nullptr;        // nodes shared by several tiles
+  int* bptr = nullptr;          // [n_bnodes+1] into bslots
+  int* bslots = nullptr;        // slots of each shared node, ascending tile
+  float* bpart = nullptr;       // [n_bslots][3] tile partial sums
+  float* geoT32 = nullptr;      // geometry records in tile order
+
   // scratch
   float* ye32 = nullptr;
   double* ye64 = nullptr;
@@ -276,6 +293,8 @@ inline int grid_for(int64_t n, int threads, int64_t cap = 152LL * 64) {
 // jfem_mesh.cu
 int mesh_setup(Ctx* c, int et, int64_t N, const double* X, int64_t E, const int64_t* conn, int base);
 int faces_setup(Ctx* c, int ft, int64_t F, const int64_t* fconn, const double* t, const double* p, int base);
+// jfem_tiles.cu
+int tiles_build(Ctx* c, const double* X, const int64_t* conn, int base);
 int exclusive_scan_i32(Ctx* c, const int* in, int* out, int64_t n, int64_t* total);
 // jfem_assemble.cu
 int assemble_csc_device(Ctx* c, int base, int64_t* colptr_d, int64_t* rowval_d, double* nzval_d,
@@ -288,6 +307,7 @@ int geometry_invalidate(Ctx* c);
 void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, bool mask_in, double* part,
                    const int* stop, const float2* v2);
 void enqueue_split(Ctx* c, const double* v, float2* v2);
+bool apply_is_tiled(const Ctx* c, bool fp32, const float2* v2);
 void enqueue_internal_force(Ctx* c, double* f);
 int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, double* partial_pAp);
 int internal_force_device(Ctx* c, double* f_d);

@@ -366,6 +366,8 @@ int mesh_setup(Ctx* c, int et, int64_t N, const double* X, int64_t E, const int6
   if (h_err) return set_err(c, JFEM_ERR_INVALID, "a node has more than 512 neighbours");
   c->n_blocks = nb_total;
 
+  if ((rc = tiles_build(c, X, conn_h, base))) return rc;
+
   // per-mesh scratch and solver vectors
   const int64_t n = 3 * N;
   if ((rc = dalloc(c, &c->ye32, E * nn * 3))) return rc;

@@ -34,10 +34,11 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_pcg_update1(int64_t n, con
                                                                   const double* __restrict__ p,
                                                                   const double* __restrict__ Ap,
                                                                   const double* __restrict__ dinv,
-                                                                  double* __restrict__ part) {
+                                                                  double* __restrict__ part, int tiled) {
   __shared__ double sh[32];
   if (sc->done[slot]) return;
-  const double pAp = reduce_partials(part, G_, sh);
+  // p·Ap partials: part[0..G) (+ part[3G..4G) from the tile-boundary kernel)
+  const double pAp = reduce_partials(part, G_, sh) + (tiled ? reduce_partials(part + 3 * G_, G_, sh) : 0.0);
   const double alpha = sc->rz[slot] / pAp;
   double rz = 0.0, rr = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -271,8 +272,9 @@ static int true_residual(Ctx* c, const double* f, const double* xv, double* r, d
 
 static void enqueue_iteration(Ctx* c, bool fp32, int slot) {
   enqueue_apply(c, c->p, c->Ap, fp32, true, false, c->part, &c->sc->done[slot], fp32 ? c->p2 : nullptr);
+  const int tiled = apply_is_tiled(c, fp32, fp32 ? c->p2 : nullptr) ? 1 : 0;
   k_pcg_update1<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->sc, slot, c->x, c->r, c->z, c->p, c->Ap,
-                                                       c->dinv, c->part);
+                                                       c->dinv, c->part, tiled);
   k_pcg_update2<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->sc, slot, c->p, c->z, c->part,
                                                        fp32 ? c->p2 : nullptr);
   c->launches += 2;
@@ -280,7 +282,7 @@ static void enqueue_iteration(Ctx* c, bool fp32, int slot) {
 
 static int graph_key(Ctx* c, bool fp32) {
   return (fp32 ? 1 : 0) | (c->finite << 1) | (c->model << 2) | (c->geom << 3) | ((c->geo_affine ? 1 : 0) << 4) |
-         (c->et << 5);
+         (c->et << 5) | ((c->geoT32 ? 1 : 0) << 10);
 }
 
 static int build_graph(Ctx* c, bool fp32) {
