@@ -494,21 +494,34 @@ void launch_tile_et(Ctx* c, const float2* v2, const double* vdot, double* y, boo
   }
 }
 
-// mode 0: y = K v (tangent for finite strain); mode 1: f_int(u) (finite strain only).
-// v2 (FP32 only): split copy of v, see k_apply_elem.
+// FP32 element pass (mode 0 only).  v2: split copy of v, see k_apply_elem.
 template <int ET>
-void launch_apply_et(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in,
-                     const int* stop) {
-  if (fp32) {
-    if (c->geo_affine) dispatch_kin<ET, float, true, 0>(c, c->geo32, v, v2, c->ye32, mask_in, stop);
-    else dispatch_kin<ET, float, false, 0>(c, c->geo32, v, v2, c->ye32, mask_in, stop);
-  } else if (mode == 0) {
+void launch_apply_f32_et(Ctx* c, const double* v, const float2* v2, bool mask_in, const int* stop) {
+  if (c->geo_affine) dispatch_kin<ET, float, true, 0>(c, c->geo32, v, v2, c->ye32, mask_in, stop);
+  else dispatch_kin<ET, float, false, 0>(c, c->geo32, v, v2, c->ye32, mask_in, stop);
+}
+
+// FP64 element pass.  mode 0: y = K v (tangent for finite strain); mode 1: f_int(u).
+template <int ET>
+void launch_apply_f64_et(Ctx* c, int mode, const double* v, bool mask_in, const int* stop) {
+  if (mode == 0) {
     if (c->geo_affine) dispatch_kin<ET, double, true, 0>(c, c->geo64, v, nullptr, c->ye64, mask_in, stop);
     else dispatch_kin<ET, double, false, 0>(c, c->geo64, v, nullptr, c->ye64, mask_in, stop);
   } else {
     if (c->geo_affine) dispatch_kin<ET, double, true, 1>(c, c->geo64, v, nullptr, c->ye64, false, stop);
     else dispatch_kin<ET, double, false, 1>(c, c->geo64, v, nullptr, c->ye64, false, stop);
   }
+}
+
+// Both passes in one translation unit (the cheap Tet4 instantiations).  The
+// Tet10 and Hex8 passes are compiled in separate translation units
+// (jfem_apply_<type>_f32.cu, jfem_apply_<type>_f64.cu) so the build runs them
+// in parallel.
+template <int ET>
+void launch_apply_et(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in,
+                     const int* stop) {
+  if (fp32) launch_apply_f32_et<ET>(c, v, v2, mask_in, stop);
+  else launch_apply_f64_et<ET>(c, mode, v, mask_in, stop);
 }
 
 }  // namespace jfem
