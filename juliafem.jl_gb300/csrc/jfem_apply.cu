@@ -20,15 +20,16 @@
 //   flux P (σ, or the tangent δP = F δS + ∇v S),  Q[c][a] = w detJ Σ_d P[c][d] J⁻¹[d][a]
 //   y_i[c] += Σ_a Q[c][a] dN_i[a]
 #include "jfem_common.cuh"
+#include "jfem_df.cuh"
 
 namespace jfem {
 
 void launch_apply_tet4(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in, const int* stop);
 void launch_apply_tet10(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in, const int* stop);
 void launch_apply_hex8(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in, const int* stop);
-void launch_tile_tet4(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part, const int* stop);
-void launch_tile_tet10(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part, const int* stop);
-void launch_tile_hex8(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part, const int* stop);
+void launch_tile_tet4(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop);
+void launch_tile_tet10(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop);
+void launch_tile_hex8(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop);
 
 // ---------------------------------------------------------------------------
 // geometry preparation (FP64)
@@ -194,18 +195,23 @@ __global__ void k_split(int64_t n, const double* __restrict__ v, float2* __restr
 }
 
 // Boundary nodes of the tiled apply: sum the tile partials in ascending tile
-// order; optional v·y partials into part[blockIdx.x].
+// order into y (FP32); optional v·y partials (double-float products, v the
+// split input) into part[3G + blockIdx.x].  With sc (mixed PCG), the last block
+// to finish forms p·Ap = Σ part[0..G) + Σ part[3G..4G) in FP64, in index order,
+// and α = r·z / p·Ap for the update kernel.  Launched with G = JFEM_RED_BLOCKS
+// blocks.
 __global__ void __launch_bounds__(JFEM_RED_THREADS) k_tile_boundary(int64_t nb, const int* __restrict__ bnodes,
                                                                     const int* __restrict__ bptr,
                                                                     const int* __restrict__ bslots,
                                                                     const float* __restrict__ bpart,
                                                                     const uint8_t* __restrict__ mask, int masked,
-                                                                    const double* __restrict__ vdot,
-                                                                    double* __restrict__ y, double* __restrict__ part,
+                                                                    const float2* __restrict__ vdot,
+                                                                    float* __restrict__ y, double* __restrict__ part,
+                                                                    SolverScalars* __restrict__ sc,
                                                                     const int* __restrict__ stop) {
   __shared__ double sh[32];
   if (stop && *stop) return;
-  double dot = 0.0;
+  float2 dot = make_float2(0.f, 0.f);
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nb; k += (int64_t)gridDim.x * blockDim.x) {
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
     const int i1 = __ldg(bptr + k + 1);
@@ -225,12 +231,32 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_tile_boundary(int64_t nb, 
     y[3 * g] = s0;
     y[3 * g + 1] = s1;
     y[3 * g + 2] = s2;
-    if (part) dot += vdot[3 * g] * (double)s0 + vdot[3 * g + 1] * (double)s1 + vdot[3 * g + 2] * (double)s2;
+    if (part) {
+      dot = df_add(dot, df_mul_f(__ldg(vdot + 3 * g), s0));
+      dot = df_add(dot, df_mul_f(__ldg(vdot + 3 * g + 1), s1));
+      dot = df_add(dot, df_mul_f(__ldg(vdot + 3 * g + 2), s2));
+    }
   }
   if (part) {
-    const double b = block_sum(dot, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = b;
+    const double b = block_sum_df(dot, sh);
+    if (threadIdx.x == 0) part[3 * JFEM_RED_BLOCKS + blockIdx.x] = b;
+    if (sc && arrive_last(&sc->arrive[0])) {
+      const double pAp = reduce_partials_cg(part, JFEM_RED_BLOCKS, sh) +
+                         reduce_partials_cg(part + 3 * JFEM_RED_BLOCKS, JFEM_RED_BLOCKS, sh);
+      if (threadIdx.x == 0) {
+        const double a = sc->rz[0] / pAp;
+        sc->alpha = a;
+        sc->alpha_df = df_from_double(a);
+        sc->arrive[0] = 0;
+      }
+    }
   }
+}
+
+// y (FP64) = y32 (FP32), for callers of the FP32 apply that want doubles
+__global__ void k_widen(int64_t n, const float* __restrict__ a, double* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
 }
 
 // geometry records to tile order (padding zero)
@@ -336,31 +362,34 @@ static void launch_gather(Ctx* c, bool fp32, bool masked, const double* v, doubl
 // FP32 with a split input and a built tiling → the tiled apply (interior
 // partials in part[0..G), boundary partials in part[3G..4G)); otherwise the
 // two-phase apply (partials in part[0..G)).
-bool apply_is_tiled(const Ctx* c, bool fp32, const float2* v2) { return fp32 && v2 && c->geoT32 && c->ntiles > 0; }
+bool apply_is_tiled(const Ctx* c) { return c->geoT32 && c->ntiles > 0; }
 
-static void launch_tiles(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part,
-                         const int* stop) {
+static void launch_tiles(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
   switch (c->et) {
-    case JFEM_TET4: launch_tile_tet4(c, v2, vdot, y, masked, part, stop); break;
-    case JFEM_TET10: launch_tile_tet10(c, v2, vdot, y, masked, part, stop); break;
-    default: launch_tile_hex8(c, v2, vdot, y, masked, part, stop); break;
+    case JFEM_TET4: launch_tile_tet4(c, v2, y, masked, part, stop); break;
+    case JFEM_TET10: launch_tile_tet10(c, v2, y, masked, part, stop); break;
+    default: launch_tile_hex8(c, v2, y, masked, part, stop); break;
   }
 }
 
-static void launch_tile_boundary(Ctx* c, const double* vdot, double* y, bool masked, double* part, const int* stop) {
+static void launch_tile_boundary(Ctx* c, const float2* vdot, float* y, bool masked, double* part, const int* stop,
+                                 SolverScalars* sc = nullptr) {
   k_tile_boundary<<<JFEM_RED_BLOCKS, JFEM_RED_THREADS, 0, c->stream>>>(
-      c->n_bnodes, c->bnodes, c->bptr, c->bslots, c->bpart, c->mask, masked ? 1 : 0, vdot, y,
-      part ? part + 3 * JFEM_RED_BLOCKS : nullptr, stop);
+      c->n_bnodes, c->bnodes, c->bptr, c->bslots, c->bpart, c->mask, masked ? 1 : 0, vdot, y, part, sc, stop);
   c->launches += 1;
+}
+
+// Tiled FP32 apply of the split input v2: tile pass + boundary pass, y FP32;
+// v·y partials (double-float products) into part[0..G) and part[3G..4G).
+// With sc (mixed PCG): the boundary pass also forms α (see k_tile_boundary).
+void enqueue_apply_tiled(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop,
+                         SolverScalars* sc) {
+  launch_tiles(c, v2, y, masked, part, stop);
+  launch_tile_boundary(c, v2, y, masked, part, stop, sc);
 }
 
 void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, bool mask_in, double* part,
                    const int* stop, const float2* v2) {
-  if (apply_is_tiled(c, fp32, v2)) {
-    launch_tiles(c, v2, v, y, masked || mask_in, part, stop);
-    launch_tile_boundary(c, v, y, masked || mask_in, part, stop);
-    return;
-  }
   launch_elements(c, fp32, 0, v, fp32 ? v2 : nullptr, mask_in, stop);
   launch_gather(c, fp32, masked, v, y, part, stop);
 }
@@ -370,8 +399,15 @@ int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, dou
   if (rc) return rc;
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
   cudaEventRecord(c->ev0, c->stream);
-  if (fp32) enqueue_split(c, v, c->p2);
-  enqueue_apply(c, v, y, fp32, masked, masked, part, nullptr, fp32 ? c->p2 : nullptr);
+  if (fp32 && apply_is_tiled(c)) {
+    enqueue_split(c, v, c->p2);
+    enqueue_apply_tiled(c, c->p2, c->Apf, masked, part, nullptr);
+    k_widen<<<grid_for(3 * c->N, 256), 256, 0, c->stream>>>(3 * c->N, c->Apf, y);
+    c->launches += 1;
+  } else {
+    if (fp32) enqueue_split(c, v, c->p2);
+    enqueue_apply(c, v, y, fp32, masked, masked, part, nullptr, fp32 ? c->p2 : nullptr);
+  }
   cudaEventRecord(c->ev1, c->stream);
   int h_err = 0;
   cudaMemcpyAsync(&h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
@@ -427,10 +463,10 @@ int time_apply(Ctx* c, bool fp32, bool masked, int reps, double* ms_elem, double
   double se = 0.0, sg = 0.0;
   for (int r = 0; r < reps; ++r) {
     cudaEventRecord(e0, c->stream);
-    if (apply_is_tiled(c, fp32, c->p2)) {
-      launch_tiles(c, c->p2, c->tmp, c->tmp2, masked, c->part, nullptr);
+    if (fp32 && apply_is_tiled(c)) {
+      launch_tiles(c, c->p2, c->Apf, masked, c->part, nullptr);
       cudaEventRecord(e1, c->stream);
-      launch_tile_boundary(c, c->tmp, c->tmp2, masked, c->part, nullptr);
+      launch_tile_boundary(c, c->p2, c->Apf, masked, c->part, nullptr);
     } else {
       launch_elements(c, fp32, 0, c->tmp, fp32 ? c->p2 : nullptr, masked, nullptr);
       cudaEventRecord(e1, c->stream);

@@ -3,6 +3,7 @@
 // type so the instantiations compile in parallel.
 #pragma once
 #include "jfem_common.cuh"
+#include "jfem_df.cuh"
 
 namespace jfem {
 
@@ -321,16 +322,17 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
 //   ye  [3·NN][T] f32   element vectors of the tile
 //   vs  [3·Lmax]  float2 (hi, lo) of the tile's nodes (masked DOFs zero)
 //   us  [3·Lmax]  f32   state u of the tile's nodes (finite strain only)
-// Interior nodes → y (FP64) directly, boundary nodes → bpart[slot] (f32 × 3);
-// optional v·y partial over interior nodes into part[blockIdx.x].
+// Interior nodes → y (FP32) directly, boundary nodes → bpart[slot] (f32 × 3);
+// optional v·y partial over interior nodes (double-float, v = hi + lo as staged)
+// into part[blockIdx.x] (FP64).
 // ---------------------------------------------------------------------------
 template <int ET, bool AFFINE, int KIN, bool GEOM>
 __global__ void __launch_bounds__(JFEM_TILE) k_tile_apply(
     int64_t ntiles, int64_t Epad, const int* __restrict__ tnode_ptr, const int* __restrict__ tnodes,
     const uint16_t* __restrict__ tconn, const float* __restrict__ geo, const uint16_t* __restrict__ tadj_ptr,
     const uint16_t* __restrict__ tadj, const int* __restrict__ tbslot, const int* __restrict__ tperm,
-    const float2* __restrict__ v2, const double* __restrict__ vdot, const double* __restrict__ u,
-    const uint8_t* __restrict__ mask, int masked, int Lmax, double* __restrict__ y, float* __restrict__ bpart,
+    const float2* __restrict__ v2, const double* __restrict__ u,
+    const uint8_t* __restrict__ mask, int masked, int Lmax, float* __restrict__ y, float* __restrict__ bpart,
     double* __restrict__ part, int* err, const int* __restrict__ stop) {
   constexpr int NN = Elem<ET>::NN;
   constexpr int T = JFEM_TILE;
@@ -342,7 +344,7 @@ __global__ void __launch_bounds__(JFEM_TILE) k_tile_apply(
   __shared__ double sh[32];
   if (stop && *stop) return;
   const int tid = threadIdx.x;
-  double dot = 0.0;
+  float2 dot = make_float2(0.f, 0.f);
   bool ok = true;
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int n0 = __ldg(tnode_ptr + t);
@@ -405,7 +407,11 @@ __global__ void __launch_bounds__(JFEM_TILE) k_tile_apply(
         y[3 * g] = s0;
         y[3 * g + 1] = s1;
         y[3 * g + 2] = s2;
-        if (part) dot += vdot[3 * g] * (double)s0 + vdot[3 * g + 1] * (double)s1 + vdot[3 * g + 2] * (double)s2;
+        if (part) {   // v·y in double-float from the staged (masked) v
+          dot = df_add(dot, df_mul_f(vs[3 * j], s0));
+          dot = df_add(dot, df_mul_f(vs[3 * j + 1], s1));
+          dot = df_add(dot, df_mul_f(vs[3 * j + 2], s2));
+        }
       } else {
         bpart[3 * (int64_t)slot] = s0;
         bpart[3 * (int64_t)slot + 1] = s1;
@@ -416,7 +422,7 @@ __global__ void __launch_bounds__(JFEM_TILE) k_tile_apply(
   }
   if (!ok) raise_error(err, JFEM_ERR_NAN);
   if (part) {
-    const double b = block_sum(dot, sh);
+    const double b = block_sum_df(dot, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = b;
   }
 }
@@ -455,8 +461,7 @@ static void dispatch_kin(Ctx* c, const R* geo, const double* v, const float2* v2
 }
 
 template <int ET, bool AFFINE, int KIN, bool GEOM>
-static void launch_tile_k(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part,
-                          const int* stop) {
+static void launch_tile_k(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
   constexpr int NN = Elem<ET>::NN;
   const size_t sm = (size_t)3 * NN * JFEM_TILE * sizeof(float) + (size_t)3 * c->tile_Lmax * sizeof(float2) +
                     ((KIN != KIN_SMALL) ? (size_t)3 * c->tile_Lmax * sizeof(float) : 0);
@@ -464,32 +469,31 @@ static void launch_tile_k(Ctx* c, const float2* v2, const double* vdot, double* 
   const unsigned g = (unsigned)(c->ntiles < JFEM_RED_BLOCKS ? JFEM_RED_BLOCKS : JFEM_RED_BLOCKS);
   k_tile_apply<ET, AFFINE, KIN, GEOM><<<g, JFEM_TILE, sm, c->stream>>>(
       c->ntiles, c->Epad, c->tnode_ptr, c->tnodes, c->tconn, c->geoT32, c->tadj_ptr, c->tadj, c->tbslot, c->tperm,
-      v2, vdot, c->u_state, c->mask, masked ? 1 : 0, c->tile_Lmax, y, c->bpart, part, c->d_err, stop);
+      v2, c->u_state, c->mask, masked ? 1 : 0, c->tile_Lmax, y, c->bpart, part, c->d_err, stop);
   c->launches += 1;
 }
 
 // Tiled FP32 element + in-tile gather launch (the boundary sum is a separate kernel).
 template <int ET>
-void launch_tile_et(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part,
-                    const int* stop) {
+void launch_tile_et(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
   const int kin = !c->finite ? KIN_SMALL : (c->model == JFEM_NEO_HOOKEAN ? KIN_NH : KIN_SVK);
   if (c->geo_affine) {
-    if (kin == KIN_SMALL) launch_tile_k<ET, true, KIN_SMALL, false>(c, v2, vdot, y, masked, part, stop);
+    if (kin == KIN_SMALL) launch_tile_k<ET, true, KIN_SMALL, false>(c, v2, y, masked, part, stop);
     else if (kin == KIN_SVK) {
-      if (c->geom) launch_tile_k<ET, true, KIN_SVK, true>(c, v2, vdot, y, masked, part, stop);
-      else launch_tile_k<ET, true, KIN_SVK, false>(c, v2, vdot, y, masked, part, stop);
+      if (c->geom) launch_tile_k<ET, true, KIN_SVK, true>(c, v2, y, masked, part, stop);
+      else launch_tile_k<ET, true, KIN_SVK, false>(c, v2, y, masked, part, stop);
     } else {
-      if (c->geom) launch_tile_k<ET, true, KIN_NH, true>(c, v2, vdot, y, masked, part, stop);
-      else launch_tile_k<ET, true, KIN_NH, false>(c, v2, vdot, y, masked, part, stop);
+      if (c->geom) launch_tile_k<ET, true, KIN_NH, true>(c, v2, y, masked, part, stop);
+      else launch_tile_k<ET, true, KIN_NH, false>(c, v2, y, masked, part, stop);
     }
   } else {
-    if (kin == KIN_SMALL) launch_tile_k<ET, false, KIN_SMALL, false>(c, v2, vdot, y, masked, part, stop);
+    if (kin == KIN_SMALL) launch_tile_k<ET, false, KIN_SMALL, false>(c, v2, y, masked, part, stop);
     else if (kin == KIN_SVK) {
-      if (c->geom) launch_tile_k<ET, false, KIN_SVK, true>(c, v2, vdot, y, masked, part, stop);
-      else launch_tile_k<ET, false, KIN_SVK, false>(c, v2, vdot, y, masked, part, stop);
+      if (c->geom) launch_tile_k<ET, false, KIN_SVK, true>(c, v2, y, masked, part, stop);
+      else launch_tile_k<ET, false, KIN_SVK, false>(c, v2, y, masked, part, stop);
     } else {
-      if (c->geom) launch_tile_k<ET, false, KIN_NH, true>(c, v2, vdot, y, masked, part, stop);
-      else launch_tile_k<ET, false, KIN_NH, false>(c, v2, vdot, y, masked, part, stop);
+      if (c->geom) launch_tile_k<ET, false, KIN_NH, true>(c, v2, y, masked, part, stop);
+      else launch_tile_k<ET, false, KIN_NH, false>(c, v2, y, masked, part, stop);
     }
   }
 }

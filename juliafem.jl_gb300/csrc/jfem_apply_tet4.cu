@@ -6,8 +6,7 @@ void launch_apply_tet4(Ctx* c, bool fp32, int mode, const double* v, const float
                         const int* stop) {
   launch_apply_et<JFEM_TET4>(c, fp32, mode, v, v2, mask_in, stop);
 }
-void launch_tile_tet4(Ctx* c, const float2* v2, const double* vdot, double* y, bool masked, double* part,
-                      const int* stop) {
-  launch_tile_et<JFEM_TET4>(c, v2, vdot, y, masked, part, stop);
+void launch_tile_tet4(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
+  launch_tile_et<JFEM_TET4>(c, v2, y, masked, part, stop);
 }
 }  // namespace jfem

@@ -162,6 +162,11 @@ struct SolverScalars {
   int done[2];       // stop flag by iteration parity
   int iters;
   int max_iters;
+  // mixed (double-float) solver: one slot, scalars formed by the last block
+  // of the launch that completes the reduction
+  double alpha, beta;
+  float2 alpha_df, beta_df;
+  unsigned arrive[2];   // last-block counters (return to 0 after every use)
 };
 
 struct Ctx {
@@ -248,7 +253,10 @@ struct Ctx {
   // solver
   double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *Ap = nullptr,
          *dinv = nullptr, *b = nullptr, *tmp = nullptr, *tmp2 = nullptr, *xbest = nullptr;
-  float2* p2 = nullptr;       // FP32 (hi, lo) split of p for the FP32 apply
+  float2* p2 = nullptr;       // p as double-float (hi, lo): the mixed solver's direction, the FP32 apply input
+  float2 *xd = nullptr, *rd = nullptr;   // mixed solver: x and r as double-float
+  float* Apf = nullptr;       // FP32 apply output
+  float* dinvf = nullptr;     // Jacobi inverse diagonal (FP32: an exact SPD preconditioner in its own right)
   double* part = nullptr;     // reduction partials (4 × JFEM_RED_BLOCKS)
   SolverScalars* sc = nullptr;
   SolverScalars* sc_host = nullptr;   // pinned mirror
@@ -307,7 +315,9 @@ int geometry_invalidate(Ctx* c);
 void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, bool mask_in, double* part,
                    const int* stop, const float2* v2);
 void enqueue_split(Ctx* c, const double* v, float2* v2);
-bool apply_is_tiled(const Ctx* c, bool fp32, const float2* v2);
+bool apply_is_tiled(const Ctx* c);
+void enqueue_apply_tiled(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop,
+                         SolverScalars* sc = nullptr);
 void enqueue_internal_force(Ctx* c, double* f);
 int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, double* partial_pAp);
 int internal_force_device(Ctx* c, double* f_d);

@@ -380,10 +380,16 @@ int mesh_setup(Ctx* c, int et, int64_t N, const double* X, int64_t E, const int6
   for (double** v : vecs)
     if ((rc = dalloc(c, v, n))) return rc;
   if ((rc = dalloc(c, &c->p2, n))) return rc;
+  if ((rc = dalloc(c, &c->xd, n))) return rc;
+  if ((rc = dalloc(c, &c->rd, n))) return rc;
+  if ((rc = dalloc(c, &c->Apf, n))) return rc;
+  if ((rc = dalloc(c, &c->dinvf, n))) return rc;
   if ((rc = dalloc(c, &c->part, 4 * JFEM_RED_BLOCKS))) return rc;
   if ((rc = dalloc(c, &c->sc, 1))) return rc;
   if ((rc = dalloc(c, &c->norms, 2))) return rc;
   cudaMemsetAsync(c->mask, 0, N, c->stream);
+  cudaMemsetAsync(c->sc, 0, sizeof(SolverScalars), c->stream);
+  cudaMemsetAsync(c->Apf, 0, n * sizeof(float), c->stream);
   cudaMemsetAsync(c->gvals, 0, n * sizeof(double), c->stream);
   cudaMemsetAsync(c->f_ext, 0, n * sizeof(double), c->stream);
   cudaMemsetAsync(c->u_state, 0, n * sizeof(double), c->stream);

@@ -8,19 +8,34 @@
 // ext/JuliaFEMCUDAExt.jl:685-854 (η = min(forcing_max, ‖R‖^forcing_power),
 // :723-724,819-820); legacy Newton src/solvers.jl:575-620.
 //
-// Device loop: one PCG iteration is four launches — element apply, node gather
-// (+ p·Ap partials), update 1 (x, r, z, r·z and r·r partials), update 2 (p and
-// the scalars).  Reductions are fixed-shape block partials summed in a fixed
-// order, so every run gives bit-identical iterates.  Scalars and the stop flag
-// live in two slots selected by iteration parity: iteration k reads slot s and
-// only block 0 of its last launch writes slot 1−s, so no launch reads what it
-// writes.  Chunks of PCG_CHUNK (even) iterations are captured once into a CUDA
-// graph; the host reads the scalars between chunks only.  After convergence
-// every launch returns at entry, so overshoot inside a chunk costs nothing.
+// Two device loops, both four launches per iteration:
+//
+// FP64 (precision JFEM_FP64): element apply, node gather (+ p·Ap partials),
+// update 1 (x, r, z, r·z and r·r partials), update 2 (p and the scalars), all
+// in double.  Scalars and the stop flag live in two slots selected by
+// iteration parity: iteration k reads slot s and only block 0 of its last
+// launch writes slot 1−s, so no launch reads what it writes.
+//
+// Mixed (JFEM_MIXED): GB300 runs FP64 at ~1/64 of its FP32 rate, so the
+// recursion runs in double-float (jfem_df.cuh, 48-bit significand) on the FP32
+// pipe, with x, r, p stored as float2 pairs in HBM: tiled FP32 apply of p
+// (v·y partials in double-float), boundary pass whose last block forms
+// α = r·z / p·Ap in FP64, update 1 (δx += αp, r −= αAp, r·z and r·r) whose
+// last block forms β and the stop flag, update 2 (p = D⁻¹r + βp).  z is never
+// stored.  x itself stays FP64: δx, the correction since the last refinement,
+// is folded into it at every refinement.  The true residual f − K x, its norm
+// and the stopping test stay FP64.
+//
+// Reductions are fixed-shape block partials summed in a fixed order, so every
+// run gives bit-identical iterates.  Chunks of PCG_CHUNK (even) iterations are
+// captured once into a CUDA graph; the host reads the scalars between chunks
+// only.  After convergence every launch returns at entry, so overshoot inside a
+// chunk costs nothing.
 #include <chrono>
 #include <cmath>
 
 #include "jfem_common.cuh"
+#include "jfem_df.cuh"
 
 namespace jfem {
 
@@ -155,6 +170,107 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_precond(int64_t n, const d
   }
 }
 
+// ---------------------------------------------------------------------------
+// mixed solver (double-float vectors)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_dfcg_update1(int64_t n, SolverScalars* __restrict__ sc,
+                                                                   float2* __restrict__ x, float2* __restrict__ r,
+                                                                   const float2* __restrict__ p,
+                                                                   const float* __restrict__ Ap,
+                                                                   const float* __restrict__ dinv,
+                                                                   double* __restrict__ part) {
+  __shared__ double sh[32];
+  if (sc->done[0]) return;
+  const float2 a = sc->alpha_df, na = df_neg(a);
+  float2 rz = make_float2(0.f, 0.f), rr = make_float2(0.f, 0.f);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = df_add(x[i], df_mul(a, p[i]));
+    const float2 ri = df_add(r[i], df_mul_f(na, Ap[i]));
+    r[i] = ri;
+    rz = df_add(rz, df_mul(ri, df_mul_f(ri, dinv[i])));
+    rr = df_add(rr, df_mul(ri, ri));
+  }
+  const double rzb = block_sum_df(rz, sh);
+  const double rrb = block_sum_df(rr, sh);
+  if (threadIdx.x == 0) {
+    part[G_ + blockIdx.x] = rzb;
+    part[2 * G_ + blockIdx.x] = rrb;
+  }
+  if (arrive_last(&sc->arrive[1])) {
+    const double rz_new = reduce_partials_cg(part + G_, G_, sh);
+    const double rr_new = reduce_partials_cg(part + 2 * G_, G_, sh);
+    if (threadIdx.x == 0) {
+      const double beta = rz_new / sc->rz[0];
+      sc->beta = beta;
+      sc->beta_df = df_from_double(beta);
+      sc->rz[0] = rz_new;
+      sc->rr[0] = rr_new;
+      const int it = sc->iters + 1;
+      sc->iters = it;
+      sc->done[0] = (rr_new <= sc->tol2 || it >= sc->max_iters || !(rr_new == rr_new)) ? 1 : 0;
+      sc->arrive[1] = 0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_dfcg_update2(int64_t n, const SolverScalars* __restrict__ sc,
+                                                                   float2* __restrict__ p,
+                                                                   const float2* __restrict__ r,
+                                                                   const float* __restrict__ dinv) {
+  if (sc->done[0]) return;
+  const float2 b = sc->beta_df;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = df_add(df_mul_f(r[i], dinv[i]), df_mul(b, p[i]));
+}
+
+// r·z → part[G..2G), r·r → part[2G..3G) from the double-float r; p = D⁻¹r on restart
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_dfcg_precond(int64_t n, const float2* __restrict__ r,
+                                                                   const float* __restrict__ dinv,
+                                                                   float2* __restrict__ p, int restart,
+                                                                   double* __restrict__ part) {
+  __shared__ double sh[32];
+  float2 rz = make_float2(0.f, 0.f), rr = make_float2(0.f, 0.f);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 ri = r[i];
+    const float2 zi = df_mul_f(ri, dinv[i]);
+    if (restart) p[i] = zi;
+    rz = df_add(rz, df_mul(ri, zi));
+    rr = df_add(rr, df_mul(ri, ri));
+  }
+  const double rzb = block_sum_df(rz, sh);
+  const double rrb = block_sum_df(rr, sh);
+  if (threadIdx.x == 0) {
+    part[G_ + blockIdx.x] = rzb;
+    part[2 * G_ + blockIdx.x] = rrb;
+  }
+}
+
+__global__ void k_df_from_double(int64_t n, const double* __restrict__ a, float2* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = df_from_double(a[i]);
+}
+
+// x (FP64) += δx (double-float); δx ← 0.  The mixed solver accumulates the
+// correction since the last refinement in double-float and folds it into the
+// FP64 iterate at every refinement, so x keeps FP64 precision (a 48-bit x would
+// floor the true residual at ≈2⁻⁴⁸‖K‖‖x‖, above 1e-8 on slender cantilevers).
+__global__ void k_df_absorb(int64_t n, float2* __restrict__ dx, double* __restrict__ x) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += df_to_double(dx[i]);
+    dx[i] = make_float2(0.f, 0.f);
+  }
+}
+
+__global__ void k_df_to_double(int64_t n, const float2* __restrict__ a, double* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = df_to_double(a[i]);
+}
+
+__global__ void k_narrow(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
 // slot 0 ← (r·z, r·r) of k_precond; optionally bb ← r·r and tol2 = tol² bb
 __global__ void k_scalars_reset(SolverScalars* __restrict__ sc, const double* __restrict__ part, int set_bb,
                                 double tol, int max_iters, int reset_iters) {
@@ -172,6 +288,8 @@ __global__ void k_scalars_reset(SolverScalars* __restrict__ sc, const double* __
     sc->max_iters = max_iters;
     sc->done[0] = (rr <= sc->tol2 || sc->iters >= max_iters) ? 1 : 0;
     sc->done[1] = 0;
+    sc->arrive[0] = 0;
+    sc->arrive[1] = 0;
   }
 }
 
@@ -271,12 +389,19 @@ static int true_residual(Ctx* c, const double* f, const double* xv, double* r, d
 }
 
 static void enqueue_iteration(Ctx* c, bool fp32, int slot) {
-  enqueue_apply(c, c->p, c->Ap, fp32, true, false, c->part, &c->sc->done[slot], fp32 ? c->p2 : nullptr);
-  const int tiled = apply_is_tiled(c, fp32, fp32 ? c->p2 : nullptr) ? 1 : 0;
-  k_pcg_update1<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->sc, slot, c->x, c->r, c->z, c->p, c->Ap,
-                                                       c->dinv, c->part, tiled);
-  k_pcg_update2<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->sc, slot, c->p, c->z, c->part,
-                                                       fp32 ? c->p2 : nullptr);
+  const int64_t n = 3 * c->N;
+  if (fp32) {   // mixed: double-float vectors, tiled FP32 apply
+    enqueue_apply_tiled(c, c->p2, c->Apf, true, c->part, &c->sc->done[0], c->sc);
+    k_dfcg_update1<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->xd, c->rd, c->p2, c->Apf, c->dinvf,
+                                                          c->part);
+    k_dfcg_update2<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->p2, c->rd, c->dinvf);
+    c->launches += 2;
+    return;
+  }
+  enqueue_apply(c, c->p, c->Ap, false, true, false, c->part, &c->sc->done[slot], nullptr);
+  k_pcg_update1<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, slot, c->x, c->r, c->z, c->p, c->Ap,
+                                                       c->dinv, c->part, 0);
+  k_pcg_update2<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, slot, c->p, c->z, c->part, nullptr);
   c->launches += 2;
 }
 
@@ -296,7 +421,7 @@ static int build_graph(Ctx* c, bool fp32) {
   const int64_t l0 = c->launches;
   cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_check(c, e, "begin capture");
-  for (int k = 0; k < PCG_CHUNK; ++k) enqueue_iteration(c, fp32, k & 1);
+  for (int k = 0; k < PCG_CHUNK; ++k) enqueue_iteration(c, fp32, fp32 ? 0 : (k & 1));
   e = cudaStreamEndCapture(c->stream, &g);
   if (e != cudaSuccess) return cuda_check(c, e, "end capture");
   e = cudaGraphInstantiate(&c->pcg_graph, g, 0);
@@ -334,6 +459,9 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
                bool reliable, bool x_zero, PcgResult* res, double drop = 1e-2) {
   int rc = 0;
   double rr0 = 0.0;
+  const int64_t n = 3 * c->N;
+  const unsigned gv = grid_for(n, 256);
+  if (fp32 && !apply_is_tiled(c)) return set_err(c, JFEM_ERR_INVALID, "mixed solve needs the tiled apply");
   if (x_zero) {
     k_residual<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, f, 1.0, nullptr, c->mask, c->r, 0, c->part);
     c->launches += 1;
@@ -341,10 +469,18 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
   } else if ((rc = true_residual(c, f, c->x, c->r, &rr0))) {
     return rc;
   }
-  k_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->r, c->dinv, c->z, c->p, 1, c->part,
-                                                   fp32 ? c->p2 : nullptr);
+  if (fp32) {   // double-float state: δx, r, p; FP32 Jacobi diagonal
+    k_narrow<<<gv, 256, 0, c->stream>>>(n, c->dinv, c->dinvf);
+    cudaMemsetAsync(c->xd, 0, n * sizeof(float2), c->stream);   // correction δx since the last refinement
+    k_df_from_double<<<gv, 256, 0, c->stream>>>(n, c->r, c->rd);
+    k_dfcg_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->rd, c->dinvf, c->p2, 1, c->part);
+    c->launches += 4;
+  } else {
+    k_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->r, c->dinv, c->z, c->p, 1, c->part, nullptr);
+    c->launches += 1;
+  }
   k_scalars_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 1, tol, max_iter, 1);
-  c->launches += 2;
+  c->launches += 1;
   if ((rc = read_scalars(c))) return rc;
   const double bb = c->sc_host->bb;
   res->iters = 0;
@@ -373,6 +509,11 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
     const bool check = s.done[0] || bad || (reliable && rr < ru * rr_true_last);
     if (check) {
       double rr_t = 0.0, drift2 = 0.0;
+      if (fp32) {   // x += δx (FP64); FP64 copy of the recursive r for the drift
+        k_df_absorb<<<gv, 256, 0, c->stream>>>(n, c->xd, c->x);
+        k_df_to_double<<<gv, 256, 0, c->stream>>>(n, c->rd, c->r);
+        c->launches += 2;
+      }
       if ((rc = true_residual(c, f, c->x, c->r, &rr_t, &drift2))) return rc;
       ++refinements;
       const bool finite = rr_t == rr_t && rr_t < 1e300;
@@ -398,13 +539,20 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
         cudaMemcpyAsync(c->x, c->xbest, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
         if ((rc = true_residual(c, f, c->x, c->r, &rr_t))) return rc;
         rr_true_last = rr_t;
+        if (fp32) cudaMemsetAsync(c->xd, 0, n * sizeof(float2), c->stream);
       }
       // refinement: r ← true residual; keep p when the drift is small, else restart
       const int restart = (finite && drift2 < 0.01 * rr_t) ? 0 : 1;
-      k_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(3 * c->N, c->r, c->dinv, c->z, c->p, restart, c->part,
-                                                   fp32 ? c->p2 : nullptr);
+      if (fp32) {
+        k_df_from_double<<<gv, 256, 0, c->stream>>>(n, c->r, c->rd);
+        k_dfcg_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->rd, c->dinvf, c->p2, restart, c->part);
+        c->launches += 2;
+      } else {
+        k_precond<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->r, c->dinv, c->z, c->p, restart, c->part, nullptr);
+        c->launches += 1;
+      }
       k_scalars_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 0, tol, max_iter, 0);
-      c->launches += 2;
+      c->launches += 1;
       if ((rc = read_scalars(c))) return rc;
     }
     if (time_budget > 0.0 && now_s() - t_start > time_budget)
