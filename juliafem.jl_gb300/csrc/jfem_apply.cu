@@ -202,8 +202,7 @@ __global__ void k_split(int64_t n, const double* __restrict__ v, float2* __restr
 // blocks.
 __global__ void __launch_bounds__(JFEM_RED_THREADS) k_tile_boundary(int64_t nb, const int* __restrict__ bnodes,
                                                                     const int* __restrict__ bptr,
-                                                                    const int* __restrict__ bslots,
-                                                                    const float* __restrict__ bpart,
+                                                                    const float4* __restrict__ bpart,
                                                                     const uint8_t* __restrict__ mask, int masked,
                                                                     const float2* __restrict__ vdot,
                                                                     float* __restrict__ y, double* __restrict__ part,
@@ -216,10 +215,10 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_tile_boundary(int64_t nb, 
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
     const int i1 = __ldg(bptr + k + 1);
     for (int i = __ldg(bptr + k); i < i1; ++i) {
-      const int64_t sl = __ldg(bslots + i);
-      s0 += __ldg(bpart + 3 * sl);
-      s1 += __ldg(bpart + 3 * sl + 1);
-      s2 += __ldg(bpart + 3 * sl + 2);
+      const float4 q = __ldcs(bpart + i);   // read once: stream past L1
+      s0 += q.x;
+      s1 += q.y;
+      s2 += q.z;
     }
     const int64_t g = __ldg(bnodes + k);
     if (masked) {
@@ -375,7 +374,7 @@ static void launch_tiles(Ctx* c, const float2* v2, float* y, bool masked, double
 static void launch_tile_boundary(Ctx* c, const float2* vdot, float* y, bool masked, double* part, const int* stop,
                                  SolverScalars* sc = nullptr) {
   k_tile_boundary<<<JFEM_RED_BLOCKS, JFEM_RED_THREADS, 0, c->stream>>>(
-      c->n_bnodes, c->bnodes, c->bptr, c->bslots, c->bpart, c->mask, masked ? 1 : 0, vdot, y, part, sc, stop);
+      c->n_bnodes, c->bnodes, c->bptr, c->bpart, c->mask, masked ? 1 : 0, vdot, y, part, sc, stop);
   c->launches += 1;
 }
 

@@ -149,17 +149,30 @@ __host__ __device__ constexpr R dnr(int et, int q, int i, int a) {
   return -s;
 }
 
+// Geometry record sources for element_op: record k of the element, either read
+// from the SoA array in HBM or from values already loaded into registers.
+template <typename R>
+struct GeoGlobal {
+  const R* p;
+  int64_t stride;
+  __device__ __forceinline__ R operator()(int k) const { return __ldg(p + (int64_t)k * stride); }
+};
+template <typename R>
+struct GeoRegs {
+  const R* r;
+  __device__ __forceinline__ R operator()(int k) const { return r[k]; }
+};
+
 // ---------------------------------------------------------------------------
 // Element operator from element-local differences.
 //   dv[i] = v_i − v_0, du[i] = u_i − u_0 (i ≥ 1; index 0 unused).
-//   geo: record base pointer, records strided by `stride` (SoA).
+//   geo: record source (GeoGlobal / GeoRegs), record k = geo(k).
 //   MODE 0: y = K v (linear) / K_T(u) v (finite); MODE 1: y = f_int(u).
 // Returns false when the material state is invalid (det C ≤ 0).
 // ---------------------------------------------------------------------------
-template <int ET, typename R, bool AFFINE, int KIN, bool GEOM, int MODE>
+template <int ET, typename R, bool AFFINE, int KIN, bool GEOM, int MODE, class GEO>
 __device__ __forceinline__ bool element_op(const R (&dv)[Elem<ET>::NN][3], const R (&du)[Elem<ET>::NN][3],
-                                           const R* __restrict__ geo, int64_t stride,
-                                           R (&y)[Elem<ET>::NN][3]) {
+                                           const GEO& geo, R (&y)[Elem<ET>::NN][3]) {
   constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
   constexpr bool NEED_U = (KIN != KIN_SMALL);
   constexpr bool NEED_V = (MODE == 0);
@@ -168,20 +181,20 @@ __device__ __forceinline__ bool element_op(const R (&dv)[Elem<ET>::NN][3], const
   R iJ[9], lam, mu, det = R(1);
   if (AFFINE) {
 #pragma unroll
-    for (int k = 0; k < 9; ++k) iJ[k] = __ldg(geo + (int64_t)k * stride);
-    lam = __ldg(geo + (int64_t)9 * stride);
-    mu = __ldg(geo + (int64_t)10 * stride);
+    for (int k = 0; k < 9; ++k) iJ[k] = geo(k);
+    lam = geo(9);
+    mu = geo(10);
   } else {
-    lam = __ldg(geo + (int64_t)(10 * NQ) * stride);
-    mu = __ldg(geo + (int64_t)(10 * NQ + 1) * stride);
+    lam = geo(10 * NQ);
+    mu = geo(10 * NQ + 1);
   }
   bool ok = true;
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     if (!AFFINE) {
 #pragma unroll
-      for (int k = 0; k < 9; ++k) iJ[k] = __ldg(geo + (int64_t)(10 * q + k) * stride);
-      det = __ldg(geo + (int64_t)(10 * q + 9) * stride);
+      for (int k = 0; k < 9; ++k) iJ[k] = geo(10 * q + k);
+      det = geo(10 * q + 9);
     }
     R gv[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, gu[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     if (NEED_V) {
@@ -307,7 +320,7 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
       }
     }
     R y[NN][3];
-    const bool ok = element_op<ET, R, AFFINE, KIN, GEOM, MODE>(dv, du, geo + e, E, y);
+    const bool ok = element_op<ET, R, AFFINE, KIN, GEOM, MODE>(dv, du, GeoGlobal<R>{geo + e, E}, y);
     if (!ok) raise_error(err, JFEM_ERR_NAN);
 #pragma unroll
     for (int i = 0; i < NN; ++i)
@@ -318,28 +331,44 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
 
 // ---------------------------------------------------------------------------
 // tiled FP32 apply (see jfem_tiles.cu).  One CTA of JFEM_TILE threads per tile
-// (persistent over tiles); dynamic shared memory:
-//   ye  [3·NN][T] f32   element vectors of the tile
-//   vs  [3·Lmax]  float2 (hi, lo) of the tile's nodes (masked DOFs zero)
-//   us  [3·Lmax]  f32   state u of the tile's nodes (finite strain only)
-// Interior nodes → y (FP32) directly, boundary nodes → bpart[slot] (f32 × 3);
-// optional v·y partial over interior nodes (double-float, v = hi + lo as staged)
-// into part[blockIdx.x] (FP64).
+// (persistent over tiles); dynamic shared memory, in this order:
+//   ye   [3·NN][T]   f32    element vectors of the tile
+//   sadj [T·NN]      u16    the tile's node → (element, local node) lists
+//   sptr [Lmax+1]    u16    their offsets (padded to 8 entries)
+//   vs   [3·Lmax]    float2 (hi, lo) of the tile's nodes (masked DOFs zero)
+//   us   [3·Lmax]    f32    state u of the tile's nodes (finite strain only)
+// Each thread issues its element's connectivity and (affine) geometry loads
+// before staging, so they are in flight while the tile's nodes are gathered.
+// Interior nodes → y (FP32) directly, boundary nodes → bpart[slot] (float4);
+// optional v·y partial over interior nodes (double-float, v = hi + lo as
+// staged) into part[blockIdx.x] (FP64).
 // ---------------------------------------------------------------------------
+__host__ __device__ constexpr int tile_sptr_len(int Lmax) { return (Lmax + 8) & ~7; }
+
+template <int NN, bool NEED_U>
+__host__ __device__ constexpr size_t tile_smem_bytes(int Lmax) {
+  return (size_t)3 * NN * JFEM_TILE * sizeof(float) + (size_t)JFEM_TILE * NN * sizeof(uint16_t) +
+         (size_t)tile_sptr_len(Lmax) * sizeof(uint16_t) + (size_t)3 * Lmax * sizeof(float2) +
+         (NEED_U ? (size_t)3 * Lmax * sizeof(float) : 0);
+}
+
 template <int ET, bool AFFINE, int KIN, bool GEOM>
-__global__ void __launch_bounds__(JFEM_TILE) k_tile_apply(
-    int64_t ntiles, int64_t Epad, const int* __restrict__ tnode_ptr, const int* __restrict__ tnodes,
+__global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? 4 : 1) k_tile_apply(
+    int64_t ntiles, int64_t E, int64_t Epad, const int* __restrict__ tnode_ptr, const int* __restrict__ tnodes,
     const uint16_t* __restrict__ tconn, const float* __restrict__ geo, const uint16_t* __restrict__ tadj_ptr,
-    const uint16_t* __restrict__ tadj, const int* __restrict__ tbslot, const int* __restrict__ tperm,
+    const uint16_t* __restrict__ tadj, const int* __restrict__ tbslot,
     const float2* __restrict__ v2, const double* __restrict__ u,
-    const uint8_t* __restrict__ mask, int masked, int Lmax, float* __restrict__ y, float* __restrict__ bpart,
+    const uint8_t* __restrict__ mask, int masked, int Lmax, float* __restrict__ y, float4* __restrict__ bpart,
     double* __restrict__ part, int* err, const int* __restrict__ stop) {
   constexpr int NN = Elem<ET>::NN;
   constexpr int T = JFEM_TILE;
+  constexpr int NADJ = T * NN;   // adjacency entries per tile; NADJ·2 bytes is a multiple of 16
   constexpr bool NEED_U = (KIN != KIN_SMALL);
   extern __shared__ float4 smem_f4[];
   float* ye = reinterpret_cast<float*>(smem_f4);
-  float2* vs = reinterpret_cast<float2*>(ye + 3 * NN * T);
+  uint16_t* sadj = reinterpret_cast<uint16_t*>(ye + 3 * NN * T);
+  uint16_t* sptr = sadj + NADJ;
+  float2* vs = reinterpret_cast<float2*>(sptr + tile_sptr_len(Lmax));
   float* us = reinterpret_cast<float*>(vs + 3 * Lmax);
   __shared__ double sh[32];
   if (stop && *stop) return;
@@ -349,6 +378,24 @@ __global__ void __launch_bounds__(JFEM_TILE) k_tile_apply(
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int n0 = __ldg(tnode_ptr + t);
     const int L = __ldg(tnode_ptr + t + 1) - n0;
+    const int64_t e = t * T + tid;
+    const bool valid = e < E;
+    int li[NN];
+    float rec[11];
+    if (valid) {
+#pragma unroll
+      for (int a = 0; a < NN; ++a) li[a] = __ldg(tconn + (int64_t)a * Epad + e);
+      if constexpr (AFFINE) {
+#pragma unroll
+        for (int k = 0; k < 11; ++k) rec[k] = __ldg(geo + (int64_t)k * Epad + e);
+      }
+    }
+    {
+      const uint4* src = reinterpret_cast<const uint4*>(tadj + t * (int64_t)NADJ);
+      uint4* dst = reinterpret_cast<uint4*>(sadj);
+      for (int k = tid; k < NADJ / 8; k += T) dst[k] = __ldg(src + k);
+    }
+    for (int j = tid; j <= L; j += T) sptr[j] = __ldg(tadj_ptr + n0 + t + j);
     for (int j = tid; j < 3 * L; j += T) {
       const int ln = j / 3, c = j - 3 * (j / 3);
       const int64_t g = __ldg(tnodes + n0 + ln);
@@ -358,11 +405,7 @@ __global__ void __launch_bounds__(JFEM_TILE) k_tile_apply(
       if (NEED_U) us[j] = (float)__ldg(u + 3 * g + c);
     }
     __syncthreads();
-    const int64_t e = t * T + tid;
-    if (__ldg(tperm + e) >= 0) {
-      int li[NN];
-#pragma unroll
-      for (int a = 0; a < NN; ++a) li[a] = __ldg(tconn + (int64_t)a * Epad + e);
+    if (valid) {
       float dv[NN][3], du[NN][3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -376,33 +419,30 @@ __global__ void __launch_bounds__(JFEM_TILE) k_tile_apply(
         }
       }
       float yl[NN][3];
-      ok &= element_op<ET, float, AFFINE, KIN, GEOM, 0>(dv, du, geo + e, Epad, yl);
+      if constexpr (AFFINE) ok &= element_op<ET, float, true, KIN, GEOM, 0>(dv, du, GeoRegs<float>{rec}, yl);
+      else ok &= element_op<ET, float, false, KIN, GEOM, 0>(dv, du, GeoGlobal<float>{geo + e, Epad}, yl);
 #pragma unroll
       for (int a = 0; a < NN; ++a)
 #pragma unroll
         for (int c = 0; c < 3; ++c) ye[(3 * a + c) * T + tid] = yl[a][c];
     }
     __syncthreads();
-    const uint16_t* lp = tadj_ptr + n0 + t;
-    const uint16_t* la = tadj + t * (int64_t)T * NN;
     for (int j = tid; j < L; j += T) {
+      const int64_t g = __ldg(tnodes + n0 + j);
+      const int slot = __ldg(tbslot + n0 + j);
+      const uint8_t m = masked ? __ldg(mask + g) : (uint8_t)0;
       float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-      const int k1 = __ldg(lp + j + 1);
-      for (int k = __ldg(lp + j); k < k1; ++k) {
-        const int pk = __ldg(la + k);
+      const int k1 = sptr[j + 1];
+      for (int k = sptr[j]; k < k1; ++k) {
+        const int pk = sadj[k];
         const int le = pk >> 4, a = pk & 15;
         s0 += ye[(3 * a + 0) * T + le];
         s1 += ye[(3 * a + 1) * T + le];
         s2 += ye[(3 * a + 2) * T + le];
       }
-      const int64_t g = __ldg(tnodes + n0 + j);
-      if (masked) {
-        const uint8_t m = __ldg(mask + g);
-        if (m & 1) s0 = 0.f;
-        if (m & 2) s1 = 0.f;
-        if (m & 4) s2 = 0.f;
-      }
-      const int slot = __ldg(tbslot + n0 + j);
+      if (m & 1) s0 = 0.f;
+      if (m & 2) s1 = 0.f;
+      if (m & 4) s2 = 0.f;
       if (slot < 0) {
         y[3 * g] = s0;
         y[3 * g + 1] = s1;
@@ -413,9 +453,7 @@ __global__ void __launch_bounds__(JFEM_TILE) k_tile_apply(
           dot = df_add(dot, df_mul_f(vs[3 * j + 2], s2));
         }
       } else {
-        bpart[3 * (int64_t)slot] = s0;
-        bpart[3 * (int64_t)slot + 1] = s1;
-        bpart[3 * (int64_t)slot + 2] = s2;
+        bpart[slot] = make_float4(s0, s1, s2, 0.f);
       }
     }
     __syncthreads();
@@ -463,12 +501,11 @@ static void dispatch_kin(Ctx* c, const R* geo, const double* v, const float2* v2
 template <int ET, bool AFFINE, int KIN, bool GEOM>
 static void launch_tile_k(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
   constexpr int NN = Elem<ET>::NN;
-  const size_t sm = (size_t)3 * NN * JFEM_TILE * sizeof(float) + (size_t)3 * c->tile_Lmax * sizeof(float2) +
-                    ((KIN != KIN_SMALL) ? (size_t)3 * c->tile_Lmax * sizeof(float) : 0);
+  const size_t sm = tile_smem_bytes<NN, KIN != KIN_SMALL>(c->tile_Lmax);
   cudaFuncSetAttribute(k_tile_apply<ET, AFFINE, KIN, GEOM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   const unsigned g = (unsigned)(c->ntiles < JFEM_RED_BLOCKS ? JFEM_RED_BLOCKS : JFEM_RED_BLOCKS);
   k_tile_apply<ET, AFFINE, KIN, GEOM><<<g, JFEM_TILE, sm, c->stream>>>(
-      c->ntiles, c->Epad, c->tnode_ptr, c->tnodes, c->tconn, c->geoT32, c->tadj_ptr, c->tadj, c->tbslot, c->tperm,
+      c->ntiles, c->E, c->Epad, c->tnode_ptr, c->tnodes, c->tconn, c->geoT32, c->tadj_ptr, c->tadj, c->tbslot,
       v2, c->u_state, c->mask, masked ? 1 : 0, c->tile_Lmax, y, c->bpart, part, c->d_err, stop);
   c->launches += 1;
 }

@@ -236,11 +236,10 @@ struct Ctx {
   int* tnodes = nullptr;        // global node of each tile node
   uint16_t* tadj_ptr = nullptr; // per tile: L+1 offsets into the tile's adjacency block
   uint16_t* tadj = nullptr;     // [ntiles][T·n_en] (local element << 4 | local node)
-  int* tbslot = nullptr;        // boundary slot of each tile node, −1 when interior
+  int* tbslot = nullptr;        // bpart position of each tile node, −1 when interior
   int* bnodes = nullptr;        // nodes shared by several tiles
-  int* bptr = nullptr;          // [n_bnodes+1] into bslots
-  int* bslots = nullptr;        // slots of each shared node, ascending tile
-  float* bpart = nullptr;       // [n_bslots][3] tile partial sums
+  int* bptr = nullptr;          // [n_bnodes+1] runs of bpart per shared node
+  float4* bpart = nullptr;      // [n_bslots] tile partial sums (x, y, z, unused), grouped by node, ascending tile
   float* geoT32 = nullptr;      // geometry records in tile order
 
   // scratch

@@ -7,9 +7,11 @@
 // JFEM_TILE consecutive elements; one CTA per tile stages the tile's nodes in
 // shared memory, computes the element vectors into shared memory, sums them per
 // local node in a fixed order, writes the nodes owned entirely by the tile to y
-// and only the tile-boundary partial sums to HBM.  A second kernel adds the
-// boundary partials of each shared node in ascending tile order.  Results are
-// deterministic (fixed summation orders) and independent of scheduling.
+// and only the tile-boundary partial sums to HBM (one float4 per (node, tile),
+// grouped by node).  A second kernel adds the boundary partials of each shared
+// node in ascending tile order.  Results are deterministic (fixed summation
+// orders) and independent of scheduling.  Padding elements exist only past E
+// (in the last tile), so a tile position is valid iff its index is below E.
 //
 // Built once per mesh on the host from the caller's arrays (O(E log E)).
 #include <algorithm>
@@ -126,21 +128,24 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
       }
     }
   }
-  // boundary nodes: slots grouped by node, ascending slot (= ascending tile)
+  // boundary nodes: partial-sum slots grouped by node, ascending tile within a
+  // node, so the boundary pass reads each node's partials as one contiguous run
   std::stable_sort(brec.begin(), brec.end(),
                    [](const std::pair<int64_t, int64_t>& a, const std::pair<int64_t, int64_t>& b) {
                      return a.first < b.first;
                    });
-  std::vector<int> bnodes, bptr(1, 0), bslots;
+  std::vector<int> bnodes, bptr(1, 0), pos_of_slot((size_t)nslots, 0);
   for (size_t i = 0; i < brec.size(); ++i) {
     if (i == 0 || brec[i].first != brec[i - 1].first) {
       if (i) bptr.push_back((int)i);
       bnodes.push_back((int)brec[i].first);
     }
-    bslots.push_back((int)brec[i].second);
+    pos_of_slot[(size_t)brec[i].second] = (int)i;
   }
   bptr.push_back((int)brec.size());
   if (bnodes.empty()) bptr.assign(1, 0);
+  for (int& sl : tbslot)
+    if (sl >= 0) sl = pos_of_slot[(size_t)sl];
 
   // upload
   int rc = 0;
@@ -161,8 +166,7 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   if ((rc = up(&c->tbslot, tbslot))) return rc;
   if ((rc = up(&c->bnodes, bnodes))) return rc;
   if ((rc = up(&c->bptr, bptr))) return rc;
-  if ((rc = up(&c->bslots, bslots))) return rc;
-  if ((rc = dalloc(c, &c->bpart, 3 * std::max<int64_t>(nslots, 1)))) return rc;
+  if ((rc = dalloc(c, &c->bpart, std::max<int64_t>(nslots, 1)))) return rc;
   c->ntiles = ntiles;
   c->Epad = Epad;
   c->tile_Lmax = Lmax;
