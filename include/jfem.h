@@ -182,6 +182,42 @@ int jfem_apply_noalloc(int elem_type, int64_t n_nodes, const double* X_device, i
                        const double* nu_device, const double* v_device, double* y_device,
                        void* stream);
 
+/* ------------------------------------------------------------------------
+ * Learned preconditioner for flexible CG (method JFEM_FCG_LEARNED).  No
+ * counterpart in the reference (its solvers are unpreconditioned CG,
+ * src/backend/cpu.jl:221-254, ext/JuliaFEMCUDAExt.jl:531-577): a message-passing
+ * network on the mesh node graph (nodes i ~ j when they share an element),
+ * 3 layers of width JFEM_MPNN_WIDTH, tanh, no biases, BF16 weights with FP32
+ * accumulation:
+ *   h1 = tanh(x Ws1ᵀ + agg(x) Wn1ᵀ), h2, h3 likewise, o = mask ⊙ h3 Woᵀ,
+ *   agg(h)_i = mean of h over the neighbours of i;
+ * preconditioner z = D⁻¹r + s·o(mask ⊙ D⁻¹r / s), s = RMS of D⁻¹r over the
+ * free DOFs (Jacobi plus a learned correction; o(−x) = −o(x)).  The weights
+ * belong to the context and survive jfem_set_mesh; training pairs do not.
+ * Weight layout (row-major [out][in]): Ws1 32×3, Wn1 32×3, Ws2, Wn2, Ws3, Wn3
+ * 32×32, Wo 3×32. */
+#define JFEM_MPNN_WIDTH  32
+#define JFEM_MPNN_PARAMS 4384
+/* Seeded random weights (Glorot-uniform, output layer ×0.05). */
+int jfem_mpnn_init(jfem_ctx* ctx, uint64_t seed);
+/* JFEM_MPNN_PARAMS float values, rounded to BF16 on the way in. */
+int jfem_mpnn_set_weights(jfem_ctx* ctx, const float* w);
+int jfem_mpnn_get_weights(jfem_ctx* ctx, float* w);
+/* Solve the current system (FP64 Jacobi-PCG to tol) and append up to max_pairs
+ * (residual, error) pairs taken from its own iterates x_k (k = 0, 16, 32, 64, …):
+ * e = x* − x_k, r = K e.  Returns the number of pairs held, or < 0. */
+int jfem_mpnn_collect(jfem_ctx* ctx, int max_pairs, double tol);
+int jfem_mpnn_clear(jfem_ctx* ctx);
+/* Adam on the held pairs: loss = mean over pairs of
+ * Σ d (x + o − t)² / Σ d t², t = mask ⊙ e / s, d = diag K.  losses[epochs]
+ * (may be NULL) receives the mean loss of each epoch. */
+int jfem_mpnn_train(jfem_ctx* ctx, int epochs, int batch, double lr, uint64_t seed, double* losses);
+/* Loss and gradient (JFEM_MPNN_PARAMS) of one pair (r, e) given on the host,
+ * through the training kernels — for gradient checks. */
+int jfem_mpnn_loss_grad(jfem_ctx* ctx, const double* r, const double* e, double* loss, float* grad);
+/* z = D⁻¹r + s·o(x) for a host residual r (3 n_nodes), through the inference kernels. */
+int jfem_mpnn_precondition(jfem_ctx* ctx, const double* r, double* z);
+
 /* Kernels launched by the library on this context since its creation. */
 int64_t jfem_kernel_launches(const jfem_ctx* ctx);
 /* Event-timed duration (ms) of the last matrix-free apply launch sequence. */

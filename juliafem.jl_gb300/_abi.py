@@ -24,6 +24,7 @@ PCG_JACOBI, FCG_LEARNED, NEWTON = 0, 1, 2
 FP64, MIXED = 0, 1
 APPLY_FP32, APPLY_MASKED = 1, 2
 HISTORY_MAX = 256
+MPNN_WIDTH, MPNN_PARAMS = 32, 4384
 
 NEN = {TET4: 4, TET10: 10, HEX8: 8}
 NFN = {TRI3: 3, TRI6: 6, QUAD4: 4}
@@ -62,6 +63,7 @@ _P = C.c_void_p
 _i64 = C.c_int64
 _i64p = C.POINTER(C.c_int64)
 _f64p = C.POINTER(C.c_double)
+_f32p = C.POINTER(C.c_float)
 SIGNATURES = {
     "jfem_version": (C.c_char_p, []),
     "jfem_default_opts": (None, [C.POINTER(SolveOpts)]),
@@ -86,6 +88,14 @@ SIGNATURES = {
     "jfem_stream": (C.c_void_p, [_P]),
     "jfem_time_apply": (C.c_int, [_P, C.c_int, C.c_int, _f64p, _f64p]),
     "jfem_apply_noalloc": (C.c_int, [C.c_int, _i64, _P, _i64, _P, C.c_int, _P, _P, _P, _P, _P]),
+    "jfem_mpnn_init": (C.c_int, [_P, C.c_uint64]),
+    "jfem_mpnn_set_weights": (C.c_int, [_P, _f32p]),
+    "jfem_mpnn_get_weights": (C.c_int, [_P, _f32p]),
+    "jfem_mpnn_collect": (C.c_int, [_P, C.c_int, C.c_double]),
+    "jfem_mpnn_clear": (C.c_int, [_P]),
+    "jfem_mpnn_train": (C.c_int, [_P, C.c_int, C.c_int, C.c_double, C.c_uint64, _f64p]),
+    "jfem_mpnn_loss_grad": (C.c_int, [_P, _f64p, _f64p, _f64p, _f32p]),
+    "jfem_mpnn_precondition": (C.c_int, [_P, _f64p, _f64p]),
 }
 
 _lib = None
@@ -257,6 +267,49 @@ class Context:
     @property
     def stream(self) -> int:
         return int(self._lib.jfem_stream(self._h) or 0)
+
+    # -- learned preconditioner ---------------------------------------------------
+    def mpnn_init(self, seed: int = 0):
+        self._check(self._lib.jfem_mpnn_init(self._h, int(seed)))
+
+    def mpnn_set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        if w.size != MPNN_PARAMS:
+            raise ValueError(f"expected {MPNN_PARAMS} weights, got {w.size}")
+        self._check(self._lib.jfem_mpnn_set_weights(self._h, _ptr(w, _f32p)))
+
+    def mpnn_get_weights(self):
+        w = np.empty(MPNN_PARAMS, np.float32)
+        self._check(self._lib.jfem_mpnn_get_weights(self._h, _ptr(w, _f32p)))
+        return w
+
+    def mpnn_collect(self, max_pairs: int = 6, tol: float = 1e-10) -> int:
+        """Solve the current system and keep (residual, error) pairs from its iterates."""
+        return self._check(self._lib.jfem_mpnn_collect(self._h, int(max_pairs), float(tol)))
+
+    def mpnn_clear(self):
+        self._check(self._lib.jfem_mpnn_clear(self._h))
+
+    def mpnn_train(self, epochs: int, batch: int = 32, lr: float = 1e-3, seed: int = 0):
+        losses = np.zeros(epochs)
+        self._check(self._lib.jfem_mpnn_train(self._h, int(epochs), int(batch), float(lr), int(seed),
+                                              _ptr(losses, _f64p)))
+        return losses
+
+    def mpnn_loss_grad(self, r, e):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        e = np.ascontiguousarray(e, dtype=np.float64)
+        L = C.c_double(0)
+        g = np.empty(MPNN_PARAMS, np.float32)
+        self._check(self._lib.jfem_mpnn_loss_grad(self._h, _ptr(r, _f64p), _ptr(e, _f64p), C.byref(L),
+                                                  _ptr(g, _f32p)))
+        return L.value, g
+
+    def mpnn_precondition(self, r):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = np.empty_like(r)
+        self._check(self._lib.jfem_mpnn_precondition(self._h, _ptr(r, _f64p), _ptr(z, _f64p)))
+        return z
 
     def time_apply(self, reps: int = 20, fp32: bool = True, masked: bool = True):
         """Mean CUDA-event ms of (element kernel, gather kernel) of one apply."""

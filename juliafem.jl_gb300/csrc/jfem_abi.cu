@@ -54,6 +54,7 @@ void free_mesh(Ctx* c) {
   fresh.ev1 = c->ev1;
   fresh.sc_host = c->sc_host;
   fresh.norms_host = c->norms_host;
+  fresh.mp = c->mp;
   fresh.launches = c->launches;
   fresh.err = c->err;
   *c = fresh;
@@ -123,6 +124,15 @@ int jfem_destroy(jfem_ctx* h) {
   cudaSetDevice(h->c.device);
   Ctx* c = &h->c;
   jfem::free_mesh(c);
+  if (c->mp) {
+    cudaFree(c->mp->w32);
+    cudaFree(c->mp->wbf);
+    cudaFree(c->mp->m);
+    cudaFree(c->mp->v);
+    cudaFree(c->mp->g);
+    delete c->mp;
+    c->mp = nullptr;
+  }
   if (c->sc_host) cudaFreeHost(c->sc_host);
   if (c->norms_host) cudaFreeHost(c->norms_host);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -361,6 +371,58 @@ int jfem_solve(jfem_ctx* h, const jfem_solve_opts* opts, double* u, jfem_stats* 
   if (stats && rc < 0) stats->status = rc;
   cudaFree(d_u);
   return rc;
+}
+
+int jfem_mpnn_init(jfem_ctx* h, uint64_t seed) {
+  ENTER(h);
+  return jfem::mpnn_init(&h->c, seed);
+}
+
+int jfem_mpnn_set_weights(jfem_ctx* h, const float* w) {
+  ENTER(h);
+  if (!w) return jfem::set_err(&h->c, JFEM_ERR_INVALID, "NULL weights");
+  return jfem::mpnn_set_weights(&h->c, w);
+}
+
+int jfem_mpnn_get_weights(jfem_ctx* h, float* w) {
+  ENTER(h);
+  if (!w) return jfem::set_err(&h->c, JFEM_ERR_INVALID, "NULL weights");
+  return jfem::mpnn_get_weights(&h->c, w);
+}
+
+int jfem_mpnn_collect(jfem_ctx* h, int max_pairs, double tol) {
+  ENTER(h);
+  Ctx* c = &h->c;
+  if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
+  if (!(tol > 0.0)) return jfem::set_err(c, JFEM_ERR_INVALID, "tol must be positive");
+  return jfem::mpnn_collect(c, max_pairs, tol);
+}
+
+int jfem_mpnn_clear(jfem_ctx* h) {
+  ENTER(h);
+  h->c.mp_pairs = 0;
+  return JFEM_OK;
+}
+
+int jfem_mpnn_train(jfem_ctx* h, int epochs, int batch, double lr, uint64_t seed, double* losses) {
+  ENTER(h);
+  return jfem::mpnn_train(&h->c, epochs, batch, lr, seed, losses);
+}
+
+int jfem_mpnn_loss_grad(jfem_ctx* h, const double* r, const double* e, double* loss, float* grad) {
+  ENTER(h);
+  Ctx* c = &h->c;
+  if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
+  if (!r || !e || !loss || !grad) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL argument");
+  return jfem::mpnn_loss_grad(c, r, e, loss, grad);
+}
+
+int jfem_mpnn_precondition(jfem_ctx* h, const double* r, double* z) {
+  ENTER(h);
+  Ctx* c = &h->c;
+  if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
+  if (!r || !z) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL vector");
+  return jfem::mpnn_precondition(c, r, z);
 }
 
 }  // extern "C"

@@ -244,6 +244,7 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_tile_boundary(int64_t nb, 
                          reduce_partials_cg(part + 3 * JFEM_RED_BLOCKS, JFEM_RED_BLOCKS, sh);
       if (threadIdx.x == 0) {
         const double a = sc->rz[0] / pAp;
+        sc->pAp = pAp;
         sc->alpha = a;
         sc->alpha_df = df_from_double(a);
         sc->arrive[0] = 0;

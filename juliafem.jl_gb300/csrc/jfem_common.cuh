@@ -13,6 +13,7 @@
 //   ye32/ye64 [n_en*3][E]      per-element apply results (SoA), gathered per node
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -166,7 +167,42 @@ struct SolverScalars {
   // of the launch that completes the reduction
   double alpha, beta;
   float2 alpha_df, beta_df;
-  unsigned arrive[2];   // last-block counters (return to 0 after every use)
+  unsigned arrive[4];   // last-block counters (return to 0 after every use)
+  // flexible CG with the learned preconditioner
+  double pAp;           // p·Ap of the last apply (denominator of the next β)
+  int restart;          // next direction is z itself (β = 0)
+};
+
+// Learned preconditioner weights (jfem_mpnn.cu): owned by the context, kept
+// across meshes.  Flat layout of JFEM_MPNN_PARAMS values, row-major [out][in].
+#define MP_W 32
+#define MP_W1S 0
+#define MP_W1N (MP_W1S + MP_W * 3)
+#define MP_W2S (MP_W1N + MP_W * 3)
+#define MP_W2N (MP_W2S + MP_W * MP_W)
+#define MP_W3S (MP_W2N + MP_W * MP_W)
+#define MP_W3N (MP_W3S + MP_W * MP_W)
+#define MP_WO (MP_W3N + MP_W * MP_W)
+#define MP_P (MP_WO + 3 * MP_W)
+static_assert(MP_P == JFEM_MPNN_PARAMS, "parameter layout");
+// Per-sample activation buffers of the network ([B][N][C] each).  Two forward
+// passes are kept while training (pass 0 on y, pass 1 on the loss gradient ĝ).
+struct MpBufs {
+  float *a1[2] = {nullptr, nullptr}, *h1[2] = {nullptr, nullptr}, *a2[2] = {nullptr, nullptr},
+        *h2[2] = {nullptr, nullptr}, *a3[2] = {nullptr, nullptr}, *h3[2] = {nullptr, nullptr};
+  float *dA = nullptr, *dB = nullptr, *gn = nullptr;          // 32 channels
+  float *y = nullptr, *u = nullptr, *v = nullptr, *ghat = nullptr, *w = nullptr, *t3a = nullptr,
+        *t3b = nullptr, *kz = nullptr;                          // 3 channels
+};
+
+struct MpnnState {
+  float* w32 = nullptr;          // FP32 master weights (Adam state lives beside them)
+  __nv_bfloat16* wbf = nullptr;  // BF16 weights used by every forward pass
+  float* m = nullptr;
+  float* v = nullptr;
+  float* g = nullptr;            // last gradient
+  int64_t step = 0;
+  bool ready = false;
 };
 
 struct Ctx {
@@ -265,6 +301,19 @@ struct Ctx {
   int pcg_graph_key = -1;
   int64_t chunk_launches = 0;
 
+  // learned preconditioner: weights (kept across meshes) and, per mesh, the
+  // training pairs [pairs][N][3] (x, t, d), activations for B samples, FCG z
+  MpnnState* mp = nullptr;
+  float *mp_x = nullptr, *mp_t = nullptr, *mp_d = nullptr, *mp_den = nullptr;
+  int64_t mp_pairs = 0, mp_cap = 0;
+  MpBufs mb;                  // activations and scratch for m_actB samples (one arena)
+  float* marena = nullptr;
+  float* mgpart = nullptr;    // weight-gradient block partials
+  double* mdots = nullptr;    // loss dot-product partials of a training batch
+  float* mcoef = nullptr;     // per-pair loss-gradient coefficients
+  int64_t m_actB = 0, m_gpart_cap = 0;
+  float* zf = nullptr;        // FCG: preconditioned residual (FP32)
+
   std::vector<void*> owned;   // everything cudaMalloc'ed for this mesh
 };
 
@@ -321,7 +370,20 @@ void enqueue_internal_force(Ctx* c, double* f);
 int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, double* partial_pAp);
 int internal_force_device(Ctx* c, double* f_d);
 int time_apply(Ctx* c, bool fp32, bool masked, int reps, double* ms_elem, double* ms_gather);
+// jfem_mpnn.cu
+int mpnn_ensure(Ctx* c);
+int mpnn_init(Ctx* c, uint64_t seed);
+int mpnn_set_weights(Ctx* c, const float* w);
+int mpnn_get_weights(Ctx* c, float* w);
+int mpnn_collect(Ctx* c, int max_pairs, double tol);
+int mpnn_train(Ctx* c, int epochs, int batch, double lr, uint64_t seed, double* losses);
+int mpnn_loss_grad(Ctx* c, const double* r, const double* e, double* loss, float* grad);
+int mpnn_precondition(Ctx* c, const double* r, double* z);
+int mpnn_ensure_act(Ctx* c, int64_t B);
+void enqueue_mpnn_spd(Ctx* c, const float* y, float* v);   // v = NᵀN y for one sample (y, v: [N][3])
 // jfem_solver.cu
+int pcg_fp64_snapshots(Ctx* c, const double* f, double tol, int max_iter, double* snaps, int max_snaps,
+                       int* n_snaps, int* snap_iters, int* iters_out, double* relres_out);
 void enqueue_axpy(Ctx* c, int64_t n, double a, const double* x, double* y);
 int solve_device(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stats* st);
 

@@ -1,0 +1,867 @@
+// jfem_mpnn.cu — learned preconditioner: a message-passing network on the mesh
+// node graph, its forward, adjoint and gradient kernels, Adam, training-pair
+// collection from the solver's own iterates, and the ABI around them.  No
+// counterpart in the reference (its CG is unpreconditioned:
+// src/backend/cpu.jl:221-254, ext/JuliaFEMCUDAExt.jl:531-577); the semantics
+// are those of oracle/mpnn_oracle.py.
+//
+// Graph: node i's neighbours are the nodes that share an element with it — the
+// 3×3-block sparsity pattern (nb_ptr, nbr) without i itself.  N is linear
+// message passing, 3 layers of width 32:
+//   a_i = (1/deg_i) Σ_{j~i} h_j,   h'_i = Ws h_i + Wn a_i     (3 → 32 → 32 → 32)
+//   N(y)_i = mask_i ⊙ (Wo h3_i)                               (32 → 3)
+// and the preconditioner is z = D^{-1/2}(y + NᵀN y), y = mask ⊙ D^{-1/2} r:
+// symmetric positive definite for any weights, so flexible CG keeps PCG's
+// convergence (a non-symmetric or nonlinear learned map loses the Krylov
+// acceleration).  Nᵀ is the network's backward-data pass.  Weights are BF16
+// (converted to FP32 in shared memory), activations and accumulation FP32.
+// Training loss per pair (scaled units, r̃ = D^{1/2} y = K t):
+//   ℓ = 1 − (zᵀr̃)² / ((zᵀKz)(tᵀr̃)) = 1 − cos²_K(z, t)
+// with K z from the tiled FP32 apply, one apply per pair per step.  Rows are (sample, node) pairs, row-major [B][N][C]; one
+// thread per row.  Every reduction (weight gradients, loss) is a fixed-shape
+// block partial followed by an in-order sum: training is bit-reproducible.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <vector>
+
+#include "jfem_common.cuh"
+#include "jfem_df.cuh"
+
+namespace jfem {
+
+#define MP_THREADS 128
+#define MP_DOT_BLOCKS 32   // blocks per pair of the loss dot products
+
+__device__ __forceinline__ bool dof_free(const uint8_t* mask, int64_t i, int c) { return !((mask[i] >> c) & 1); }
+
+// ---------------------------------------------------------------------------
+// forward
+// ---------------------------------------------------------------------------
+template <int CIN>
+__device__ __forceinline__ void load_row(const float* __restrict__ p, float (&h)[CIN]) {
+  if constexpr (CIN % 4 == 0) {
+    const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int c = 0; c < CIN / 4; ++c) {
+      const float4 v = __ldg(q + c);
+      h[4 * c] = v.x;
+      h[4 * c + 1] = v.y;
+      h[4 * c + 2] = v.z;
+      h[4 * c + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < CIN; ++c) h[c] = __ldg(p + c);
+  }
+}
+
+template <int C>
+__device__ __forceinline__ void store_row(float* __restrict__ p, const float (&h)[C]) {
+  if constexpr (C % 4 == 0) {
+    float4* q = reinterpret_cast<float4*>(p);
+#pragma unroll
+    for (int c = 0; c < C / 4; ++c) q[c] = make_float4(h[4 * c], h[4 * c + 1], h[4 * c + 2], h[4 * c + 3]);
+  } else {
+#pragma unroll
+    for (int c = 0; c < C; ++c) p[c] = h[c];
+  }
+}
+
+// mean over the neighbours j ≠ i of rows j of sample block hb
+template <int CIN>
+__device__ __forceinline__ void neighbour_mean(const float* __restrict__ hb, const int* __restrict__ nb_ptr,
+                                               const int* __restrict__ nbr, int64_t i, float (&a)[CIN]) {
+#pragma unroll
+  for (int c = 0; c < CIN; ++c) a[c] = 0.f;
+  const int j0 = __ldg(nb_ptr + i), j1 = __ldg(nb_ptr + i + 1);
+  for (int jj = j0; jj < j1; ++jj) {
+    const int64_t j = __ldg(nbr + jj);
+    if (j == i) continue;
+    float hj[CIN];
+    load_row<CIN>(hb + j * CIN, hj);
+#pragma unroll
+    for (int c = 0; c < CIN; ++c) a[c] += hj[c];
+  }
+  const int deg = j1 - j0 - 1;
+  const float id = deg > 0 ? 1.f / (float)deg : 0.f;
+#pragma unroll
+  for (int c = 0; c < CIN; ++c) a[c] *= id;
+}
+
+__device__ __forceinline__ float inv_degree(const int* __restrict__ nb_ptr, int64_t i) {
+  const int deg = __ldg(nb_ptr + i + 1) - __ldg(nb_ptr + i) - 1;
+  return deg > 0 ? 1.f / (float)deg : 0.f;
+}
+
+// One layer over B samples: hout = Ws h + Wn agg(h).  agg (may be null) keeps
+// the neighbour means for the weight gradient.
+template <int CIN>
+__global__ void __launch_bounds__(MP_THREADS) k_mp_layer(int64_t rows, int64_t N, const int* __restrict__ nb_ptr,
+                                                         const int* __restrict__ nbr, const float* __restrict__ hin,
+                                                         const __nv_bfloat16* __restrict__ Ws,
+                                                         const __nv_bfloat16* __restrict__ Wn,
+                                                         float* __restrict__ agg, float* __restrict__ hout) {
+  __shared__ float ws[MP_W * CIN], wn[MP_W * CIN];
+  for (int k = threadIdx.x; k < MP_W * CIN; k += blockDim.x) {
+    ws[k] = __bfloat162float(Ws[k]);
+    wn[k] = __bfloat162float(Wn[k]);
+  }
+  __syncthreads();
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < rows;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = row / N, i = row - b * N;
+    const float* hb = hin + b * N * CIN;
+    float h[CIN], a[CIN];
+    load_row<CIN>(hb + i * CIN, h);
+    neighbour_mean<CIN>(hb, nb_ptr, nbr, i, a);
+    if (agg) store_row<CIN>(agg + row * CIN, a);
+    float out[MP_W];
+#pragma unroll
+    for (int k = 0; k < MP_W; ++k) {
+      float s = 0.f;
+#pragma unroll
+      for (int c = 0; c < CIN; ++c) s = fmaf(ws[k * CIN + c], h[c], fmaf(wn[k * CIN + c], a[c], s));
+      out[k] = s;
+    }
+    store_row<MP_W>(hout + row * MP_W, out);
+  }
+}
+
+// u = mask ⊙ Wo h3
+__global__ void __launch_bounds__(MP_THREADS) k_mp_out(int64_t rows, int64_t N, const float* __restrict__ h3,
+                                                       const __nv_bfloat16* __restrict__ Wo,
+                                                       const uint8_t* __restrict__ mask, float* __restrict__ u) {
+  __shared__ float wo[3 * MP_W];
+  for (int k = threadIdx.x; k < 3 * MP_W; k += blockDim.x) wo[k] = __bfloat162float(Wo[k]);
+  __syncthreads();
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < rows;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = row % N;
+    float h[MP_W];
+    load_row<MP_W>(h3 + row * MP_W, h);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float s = 0.f;
+#pragma unroll
+      for (int c = 0; c < MP_W; ++c) s = fmaf(wo[k * MP_W + c], h[c], s);
+      u[row * 3 + k] = dof_free(mask, i, k) ? s : 0.f;
+    }
+  }
+}
+
+// Block partial of Σ_rows u ⊗ v (KU × KV) from rows staged in shared memory.
+template <int KU, int KV>
+__device__ __forceinline__ void outer_partial(const float* su, const float* sv, int nrows, float* __restrict__ out) {
+  for (int e = threadIdx.x; e < KU * KV; e += blockDim.x) {
+    const int k = e / KV, c = e - (e / KV) * KV;
+    float s = 0.f;
+    for (int r = 0; r < nrows; ++r) s = fmaf(su[r * KU + k], sv[r * KV + c], s);
+    out[e] = s;
+  }
+}
+
+// Output layer backward: dh3 = Woᵀ (mask ⊙ dout); gradient partial of Wo
+// (3 × 32) per block when gpart is set.  One row per thread, grid =
+// ceil(rows / MP_THREADS) when gpart is set.
+__global__ void __launch_bounds__(MP_THREADS) k_mp_bwd_out(int64_t rows, int64_t N, const float* __restrict__ dout,
+                                                           const float* __restrict__ h3,
+                                                           const __nv_bfloat16* __restrict__ Wo,
+                                                           const uint8_t* __restrict__ mask, float* __restrict__ dh3,
+                                                           float* __restrict__ gpart) {
+  __shared__ float wo[3 * MP_W];
+  __shared__ float su[MP_THREADS * 3];
+  __shared__ float sv[MP_THREADS * MP_W];
+  for (int k = threadIdx.x; k < 3 * MP_W; k += blockDim.x) wo[k] = __bfloat162float(Wo[k]);
+  __syncthreads();
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = threadIdx.x;
+  float g[3] = {0.f, 0.f, 0.f};
+  if (row < rows) {
+    const int64_t i = row % N;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) g[k] = dof_free(mask, i, k) ? dout[row * 3 + k] : 0.f;
+    float dh[MP_W];
+#pragma unroll
+    for (int c = 0; c < MP_W; ++c) dh[c] = g[0] * wo[c] + g[1] * wo[MP_W + c] + g[2] * wo[2 * MP_W + c];
+    store_row<MP_W>(dh3 + row * MP_W, dh);
+  }
+  if (!gpart) return;
+  float h[MP_W];
+  if (row < rows) load_row<MP_W>(h3 + row * MP_W, h);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) su[r * 3 + k] = g[k];
+#pragma unroll
+  for (int c = 0; c < MP_W; ++c) sv[r * MP_W + c] = row < rows ? h[c] : 0.f;
+  __syncthreads();
+  outer_partial<3, MP_W>(su, sv, MP_THREADS, gpart + (int64_t)blockIdx.x * (3 * MP_W));
+}
+
+// Hidden layer backward (linear): with dout = ∂/∂hout, the self part of
+// ∂/∂hin (Wsᵀ dout → dh_self) and gn = Wnᵀ dout / deg for the neighbour part
+// (when NEED_DH); gradient partials of Ws, Wn (Σ dout ⊗ hin, Σ dout ⊗ agg) per
+// block when gpart is set.  Dynamic shared memory when gpart is set:
+// MP_THREADS × (MP_W + 2·CIN) floats.
+template <int CIN, bool NEED_DH>
+__global__ void __launch_bounds__(MP_THREADS) k_mp_bwd_layer(int64_t rows, int64_t N, const int* __restrict__ nb_ptr,
+                                                             const float* __restrict__ dout,
+                                                             const float* __restrict__ hin,
+                                                             const float* __restrict__ agg,
+                                                             const __nv_bfloat16* __restrict__ Ws,
+                                                             const __nv_bfloat16* __restrict__ Wn,
+                                                             float* __restrict__ dh_self, float* __restrict__ gn,
+                                                             float* __restrict__ gpart) {
+  __shared__ float ws[MP_W * CIN], wn[MP_W * CIN];
+  extern __shared__ float4 mp_dyn[];
+  for (int k = threadIdx.x; k < MP_W * CIN; k += blockDim.x) {
+    ws[k] = __bfloat162float(Ws[k]);
+    wn[k] = __bfloat162float(Wn[k]);
+  }
+  __syncthreads();
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = threadIdx.x;
+  float dp[MP_W];
+#pragma unroll
+  for (int k = 0; k < MP_W; ++k) dp[k] = 0.f;
+  if (row < rows) {
+    load_row<MP_W>(dout + row * MP_W, dp);
+    if (NEED_DH) {
+      const float id = inv_degree(nb_ptr, row % N);
+      float ds[CIN], g[CIN];
+#pragma unroll
+      for (int c = 0; c < CIN; ++c) {
+        float s1 = 0.f, s2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < MP_W; ++k) {
+          s1 = fmaf(ws[k * CIN + c], dp[k], s1);
+          s2 = fmaf(wn[k * CIN + c], dp[k], s2);
+        }
+        ds[c] = s1;
+        g[c] = s2 * id;
+      }
+      store_row<CIN>(dh_self + row * CIN, ds);
+      store_row<CIN>(gn + row * CIN, g);
+    }
+  }
+  if (!gpart) return;
+  float* su = reinterpret_cast<float*>(mp_dyn);
+  float* sh_ = su + MP_THREADS * MP_W;
+  float* sa = sh_ + MP_THREADS * CIN;
+  float h[CIN], a[CIN];
+#pragma unroll
+  for (int c = 0; c < CIN; ++c) h[c] = a[c] = 0.f;
+  if (row < rows) {
+    load_row<CIN>(hin + row * CIN, h);
+    load_row<CIN>(agg + row * CIN, a);
+  }
+#pragma unroll
+  for (int k = 0; k < MP_W; ++k) su[r * MP_W + k] = dp[k];
+#pragma unroll
+  for (int c = 0; c < CIN; ++c) {
+    sh_[r * CIN + c] = h[c];
+    sa[r * CIN + c] = a[c];
+  }
+  __syncthreads();
+  float* gp = gpart + (int64_t)blockIdx.x * (2 * MP_W * CIN);
+  outer_partial<MP_W, CIN>(su, sh_, MP_THREADS, gp);
+  outer_partial<MP_W, CIN>(su, sa, MP_THREADS, gp + MP_W * CIN);
+}
+
+// dh_i = dh_self_i + Σ_{k~i} gn_k  (the transpose of the neighbour mean)
+template <int C>
+__global__ void __launch_bounds__(MP_THREADS) k_mp_bwd_agg(int64_t rows, int64_t N, const int* __restrict__ nb_ptr,
+                                                           const int* __restrict__ nbr,
+                                                           const float* __restrict__ dh_self,
+                                                           const float* __restrict__ gn, float* __restrict__ dh) {
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < rows;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = row / N, i = row - b * N;
+    const float* gb = gn + b * N * C;
+    float s[C];
+    load_row<C>(dh_self + row * C, s);
+    const int j0 = __ldg(nb_ptr + i), j1 = __ldg(nb_ptr + i + 1);
+    for (int jj = j0; jj < j1; ++jj) {
+      const int64_t j = __ldg(nbr + jj);
+      if (j == i) continue;
+      float g[C];
+      load_row<C>(gb + j * C, g);
+#pragma unroll
+      for (int c = 0; c < C; ++c) s[c] += g[c];
+    }
+    store_row<C>(dh + row * C, s);
+  }
+}
+
+// grad[e] (+)= Σ_blocks gpart[blk][e] in block order (FP64 accumulation)
+__global__ void k_mp_grad_reduce(int nblk, int width, const float* __restrict__ gpart, float* __restrict__ grad,
+                                 int accumulate) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < width; e += gridDim.x * blockDim.x) {
+    double s = accumulate ? (double)grad[e] : 0.0;
+    for (int k = 0; k < nblk; ++k) s += (double)gpart[(int64_t)k * width + e];
+    grad[e] = (float)s;
+  }
+}
+
+__global__ void k_mp_adam(int n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                          float* __restrict__ v, __nv_bfloat16* __restrict__ wbf, float lr, float b1, float b2,
+                          float eps, float c1, float c2) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const float gk = g[k];
+    const float mk = b1 * m[k] + (1.f - b1) * gk;
+    const float vk = b2 * v[k] + (1.f - b2) * gk * gk;
+    m[k] = mk;
+    v[k] = vk;
+    const float wk = w[k] - lr * (mk / c1) / (sqrtf(vk / c2) + eps);
+    w[k] = wk;
+    wbf[k] = __float2bfloat16_rn(wk);
+  }
+}
+
+__global__ void k_mp_to_bf16(int n, float* __restrict__ w, __nv_bfloat16* __restrict__ wbf) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const __nv_bfloat16 b = __float2bfloat16_rn(w[k]);
+    wbf[k] = b;
+    w[k] = __bfloat162float(b);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// loss (energy-norm cosine) and its gradient with respect to z
+// ---------------------------------------------------------------------------
+// z = mask ⊙ (y + v) / sq of one pair as the double-float input of the tiled apply
+__global__ void k_mp_zsplit(int64_t n3, const float* __restrict__ y, const float* __restrict__ v,
+                            const float* __restrict__ sq, float2* __restrict__ p2) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n3; q += (int64_t)gridDim.x * blockDim.x)
+    p2[q] = make_float2(sq[q] > 0.f ? (y[q] + v[q]) / sq[q] : 0.f, 0.f);
+}
+
+// per pair b = blockIdx.y: partials of a_b = zᵀr̃ = Σ (y + v) y and q_b = zᵀKz
+// into dots[(b·gridDim.x + blockIdx.x)·2 + {0, 1}]
+__global__ void __launch_bounds__(256) k_mp_cos_dots(int64_t n3, const float* __restrict__ y,
+                                                     const float* __restrict__ v, const float* __restrict__ sq,
+                                                     const float* __restrict__ kz, double* __restrict__ dots) {
+  __shared__ double sh[32];
+  const int64_t b = blockIdx.y;
+  const float* yb = y + b * n3;
+  const float* vb = v + b * n3;
+  const float* sb = sq + b * n3;
+  const float* kb = kz + b * n3;
+  double a = 0.0, q = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x) {
+    const double yv = (double)yb[i] + (double)vb[i];
+    a += yv * (double)yb[i];
+    q += (sb[i] > 0.f ? (double)((yb[i] + vb[i]) / sb[i]) : 0.0) * (double)kb[i];
+  }
+  a = block_sum(a, sh);
+  q = block_sum(q, sh);
+  if (threadIdx.x == 0) {
+    dots[(b * gridDim.x + blockIdx.x) * 2] = a;
+    dots[(b * gridDim.x + blockIdx.x) * 2 + 1] = q;
+  }
+}
+
+// per pair: ℓ_b, and ∂ℓ/∂z = c1 r̃ + c2 Kz with c1 = −2a/(q den), c2 = 2a²/(q² den)
+// (× scale) into coef[2b], coef[2b+1]; Σ scale·ℓ_b → dots[2·B·nbx] (one thread,
+// pair order)
+__global__ void k_mp_cos_coef(int B, int nbx, double* __restrict__ dots, const float* __restrict__ den, float scale,
+                              float* __restrict__ coef) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double L = 0.0;
+  for (int b = 0; b < B; ++b) {
+    double a = 0.0, q = 0.0;
+    for (int k = 0; k < nbx; ++k) {
+      a += dots[((int64_t)b * nbx + k) * 2];
+      q += dots[((int64_t)b * nbx + k) * 2 + 1];
+    }
+    const double dn = (double)den[b];
+    const bool ok = q > 0.0 && dn > 0.0;
+    L += ok ? 1.0 - a * a / (q * dn) : 1.0;
+    coef[2 * b] = ok ? (float)(-2.0 * a / (q * dn) * scale) : 0.f;
+    coef[2 * b + 1] = ok ? (float)(2.0 * a * a / (q * q * dn) * scale) : 0.f;
+  }
+  dots[(int64_t)2 * B * nbx] = L * (double)scale;
+}
+
+// ĝ = D^{-1/2} ∂ℓ/∂z = mask ⊙ (c1 y + c2 Kz / sq)   (r̃ / sq = y)
+__global__ void __launch_bounds__(MP_THREADS) k_mp_cos_ghat(int64_t rows, int64_t N, const float* __restrict__ y,
+                                                            const float* __restrict__ sq,
+                                                            const float* __restrict__ kz,
+                                                            const float* __restrict__ coef,
+                                                            const uint8_t* __restrict__ mask,
+                                                            float* __restrict__ ghat) {
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < rows;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = row / N, i = row - b * N;
+    const float c1 = coef[2 * b], c2 = coef[2 * b + 1];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int64_t q = row * 3 + k;
+      ghat[q] = (dof_free(mask, i, k) && sq[q] > 0.f) ? c1 * y[q] + c2 * kz[q] / sq[q] : 0.f;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// training pairs
+// ---------------------------------------------------------------------------
+// v = D^{-1/2} r on free DOFs; Σ v² partials → part[blockIdx.x]
+__global__ void __launch_bounds__(256) k_mp_sample_norm(int64_t N, const double* __restrict__ r,
+                                                        const double* __restrict__ dinv,
+                                                        const uint8_t* __restrict__ mask, double* __restrict__ part) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * N; q += (int64_t)gridDim.x * blockDim.x) {
+    const double v = dof_free(mask, q / 3, (int)(q % 3)) ? sqrt(dinv[q]) * r[q] : 0.0;
+    s += v * v;
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// y = D^{-1/2} r / s, t = e / s, sq = D^{1/2} (free DOFs; zero elsewhere);
+// partials of tᵀr̃ = Σ t sq y (= ‖t‖²_K)
+__global__ void __launch_bounds__(256) k_mp_make_sample(int64_t N, const double* __restrict__ r,
+                                                        const double* __restrict__ e, const double* __restrict__ dinv,
+                                                        const uint8_t* __restrict__ mask, double inv_s,
+                                                        float* __restrict__ y, float* __restrict__ t,
+                                                        float* __restrict__ sq, double* __restrict__ part) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * N; q += (int64_t)gridDim.x * blockDim.x) {
+    const bool fr = dof_free(mask, q / 3, (int)(q % 3)) && dinv[q] > 0.0;
+    const double isq = fr ? sqrt(dinv[q]) : 0.0;
+    const double sqq = fr ? 1.0 / isq : 0.0;
+    const double tq = fr ? e[q] * inv_s : 0.0;
+    const double yq = isq * r[q] * inv_s;
+    y[q] = (float)yq;
+    t[q] = (float)tq;
+    sq[q] = (float)sqq;
+    s += tq * sqq * yq;
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void k_mp_sub(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ c) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    c[i] = a[i] - b[i];
+}
+
+// y = mask ⊙ D^{-1/2} r (FP64 r, for the host-facing preconditioner)
+__global__ void k_mp_input_d(int64_t N, const double* __restrict__ r, const double* __restrict__ dinv,
+                             const uint8_t* __restrict__ mask, float* __restrict__ y) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * N; q += (int64_t)gridDim.x * blockDim.x)
+    y[q] = dof_free(mask, q / 3, (int)(q % 3)) ? (float)(sqrt(dinv[q]) * r[q]) : 0.f;
+}
+
+// z = D^{-1/2} (y + v) (FP64 out)
+__global__ void k_mp_precond_out(int64_t N, const float* __restrict__ y, const float* __restrict__ v,
+                                 const double* __restrict__ dinv, const uint8_t* __restrict__ mask,
+                                 double* __restrict__ z) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * N; q += (int64_t)gridDim.x * blockDim.x)
+    z[q] = dof_free(mask, q / 3, (int)(q % 3)) ? sqrt(dinv[q]) * ((double)y[q] + (double)v[q]) : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static uint64_t splitmix(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+int mpnn_ensure(Ctx* c) {
+  if (c->mp && c->mp->ready) return 0;
+  if (!c->mp) c->mp = new MpnnState();
+  MpnnState* m = c->mp;
+  if (!m->w32) {
+    if (cudaMalloc(&m->w32, MP_P * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&m->wbf, MP_P * sizeof(__nv_bfloat16)) != cudaSuccess ||
+        cudaMalloc(&m->m, MP_P * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&m->v, MP_P * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&m->g, MP_P * sizeof(float)) != cudaSuccess)
+      return set_err(c, JFEM_ERR_OOM, "network weights");
+  }
+  return 0;
+}
+
+static int upload_weights(Ctx* c, const float* w) {
+  MpnnState* m = c->mp;
+  cudaMemcpyAsync(m->w32, w, MP_P * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+  k_mp_to_bf16<<<grid_for(MP_P, 256), 256, 0, c->stream>>>(MP_P, m->w32, m->wbf);
+  cudaMemsetAsync(m->m, 0, MP_P * sizeof(float), c->stream);
+  cudaMemsetAsync(m->v, 0, MP_P * sizeof(float), c->stream);
+  c->launches += 1;
+  m->step = 0;
+  int rc = sync_and_check(c, "network weights");
+  if (!rc) m->ready = true;
+  return rc;
+}
+
+int mpnn_init(Ctx* c, uint64_t seed) {
+  int rc = mpnn_ensure(c);
+  if (rc) return rc;
+  std::vector<float> w(MP_P);
+  const int shapes[7][2] = {{MP_W, 3}, {MP_W, 3}, {MP_W, MP_W}, {MP_W, MP_W}, {MP_W, MP_W}, {MP_W, MP_W}, {3, MP_W}};
+  uint64_t st = seed;
+  int k = 0;
+  for (int s = 0; s < 7; ++s) {
+    const double lim = 0.5 * std::sqrt(6.0 / (shapes[s][0] + shapes[s][1]));
+    for (int q = 0; q < shapes[s][0] * shapes[s][1]; ++q) {
+      const double u = (double)(splitmix(st) >> 11) * (1.0 / 9007199254740992.0);
+      w[(size_t)k++] = (float)((2.0 * u - 1.0) * lim);
+    }
+  }
+  return upload_weights(c, w.data());
+}
+
+int mpnn_set_weights(Ctx* c, const float* w) {
+  int rc = mpnn_ensure(c);
+  if (rc) return rc;
+  return upload_weights(c, w);
+}
+
+int mpnn_get_weights(Ctx* c, float* w) {
+  if (!c->mp || !c->mp->ready) return set_err(c, JFEM_ERR_INVALID, "no network weights (jfem_mpnn_init first)");
+  cudaMemcpyAsync(w, c->mp->w32, MP_P * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  return sync_and_check(c, "network weights download");
+}
+
+// One arena for B samples: two forward passes (a1 3, h1 32, a2 32, h2 32, a3 32,
+// h3 32 channels each), scratch dA, dB, gn (32) and y, u, v, ĝ, w, t3a, t3b, Kz (3).
+// Every buffer starts on a 256-byte boundary (the 32-channel rows are read and
+// written as float4).
+int mpnn_ensure_act(Ctx* c, int64_t B) {
+  if (c->m_actB >= B) return 0;
+  if (c->marena) dfree(c, c->marena);
+  c->marena = nullptr;
+  const int64_t r = B * c->N;
+  auto padded = [&](int64_t ch) { return (r * ch + 63) / 64 * 64; };
+  const int64_t per_pass = padded(3) + 5 * padded(MP_W);
+  const int64_t total = 2 * per_pass + 3 * padded(MP_W) + 8 * padded(3);
+  int rc = dalloc(c, &c->marena, (size_t)total);
+  if (rc) return rc;
+  float* p = c->marena;
+  auto take = [&](int64_t ch) {
+    float* q = p;
+    p += padded(ch);
+    return q;
+  };
+  MpBufs& b = c->mb;
+  for (int k = 0; k < 2; ++k) {
+    b.a1[k] = take(3);
+    b.h1[k] = take(MP_W);
+    b.a2[k] = take(MP_W);
+    b.h2[k] = take(MP_W);
+    b.a3[k] = take(MP_W);
+    b.h3[k] = take(MP_W);
+  }
+  b.dA = take(MP_W);
+  b.dB = take(MP_W);
+  b.gn = take(MP_W);
+  b.y = take(3);
+  b.u = take(3);
+  b.v = take(3);
+  b.ghat = take(3);
+  b.w = take(3);
+  b.t3a = take(3);
+  b.t3b = take(3);
+  b.kz = take(3);
+  if (c->mdots) dfree(c, c->mdots);
+  if (c->mcoef) dfree(c, c->mcoef);
+  rc = dalloc(c, &c->mdots, (size_t)2 * B * MP_DOT_BLOCKS + 1);
+  if (!rc) rc = dalloc(c, &c->mcoef, (size_t)2 * B);
+  if (rc) return rc;
+  c->m_actB = B;
+  return 0;
+}
+
+static int ensure_gpart(Ctx* c, int64_t nblk) {
+  const int64_t need = nblk * (2 * MP_W * MP_W);
+  if (c->m_gpart_cap >= need) return 0;
+  if (c->mgpart) dfree(c, c->mgpart);
+  int rc = dalloc(c, &c->mgpart, (size_t)need);
+  if (rc) return rc;
+  c->m_gpart_cap = need;
+  return 0;
+}
+
+// u = N(h0) for B samples; pass k keeps its aggregates (for weight gradients)
+// when keep is set.
+static void enqueue_forward(Ctx* c, int64_t B, const float* h0, int k, bool keep, float* u) {
+  const MpnnState* m = c->mp;
+  const MpBufs& b = c->mb;
+  const int64_t rows = B * c->N;
+  const unsigned g = grid_for(rows, MP_THREADS);
+  k_mp_layer<3><<<g, MP_THREADS, 0, c->stream>>>(rows, c->N, c->nb_ptr, c->nbr, h0, m->wbf + MP_W1S,
+                                                 m->wbf + MP_W1N, keep ? b.a1[k] : nullptr, b.h1[k]);
+  k_mp_layer<MP_W><<<g, MP_THREADS, 0, c->stream>>>(rows, c->N, c->nb_ptr, c->nbr, b.h1[k], m->wbf + MP_W2S,
+                                                    m->wbf + MP_W2N, keep ? b.a2[k] : nullptr, b.h2[k]);
+  k_mp_layer<MP_W><<<g, MP_THREADS, 0, c->stream>>>(rows, c->N, c->nb_ptr, c->nbr, b.h2[k], m->wbf + MP_W3S,
+                                                    m->wbf + MP_W3N, keep ? b.a3[k] : nullptr, b.h3[k]);
+  k_mp_out<<<g, MP_THREADS, 0, c->stream>>>(rows, c->N, b.h3[k], m->wbf + MP_WO, c->mask, u);
+  c->launches += 4;
+}
+
+// Backward through N for B samples with output gradient dout (3 channels).
+// With grad (weight gradients of ⟨dout, N(h0)⟩ from the kept pass k, written or
+// accumulated into mp->g) and/or din (the input gradient Nᵀ dout).
+static void enqueue_backward(Ctx* c, int64_t B, const float* dout, int k, const float* h0, bool grad, bool accumulate,
+                             float* din) {
+  const MpnnState* m = c->mp;
+  const MpBufs& b = c->mb;
+  const int64_t rows = B * c->N;
+  const unsigned gs = grid_for(rows, MP_THREADS);
+  const unsigned nblk = (unsigned)((rows + MP_THREADS - 1) / MP_THREADS);
+  float* gp = grad ? c->mgpart : nullptr;
+  const int acc = accumulate ? 1 : 0;
+  const size_t sm32 = grad ? (size_t)MP_THREADS * (MP_W + 2 * MP_W) * sizeof(float) : 0;
+  const size_t sm3 = grad ? (size_t)MP_THREADS * (MP_W + 2 * 3) * sizeof(float) : 0;
+  k_mp_bwd_out<<<nblk, MP_THREADS, 0, c->stream>>>(rows, c->N, dout, b.h3[k], m->wbf + MP_WO, c->mask, b.dA, gp);
+  if (grad) k_mp_grad_reduce<<<1, 128, 0, c->stream>>>((int)nblk, 3 * MP_W, c->mgpart, m->g + MP_WO, acc);
+  // layer 3 (input h2), layer 2 (input h1): dA → dB (self), gn → dA (Σ)
+  const float* hin[2] = {b.h2[k], b.h1[k]};
+  const float* aggs[2] = {b.a3[k], b.a2[k]};
+  const int offs[2] = {MP_W3S, MP_W2S};
+  for (int l = 0; l < 2; ++l) {
+    k_mp_bwd_layer<MP_W, true><<<nblk, MP_THREADS, sm32, c->stream>>>(
+        rows, c->N, c->nb_ptr, b.dA, hin[l], aggs[l], m->wbf + offs[l], m->wbf + offs[l] + MP_W * MP_W, b.dB, b.gn,
+        gp);
+    if (grad)
+      k_mp_grad_reduce<<<16, 128, 0, c->stream>>>((int)nblk, 2 * MP_W * MP_W, c->mgpart, m->g + offs[l], acc);
+    k_mp_bwd_agg<MP_W><<<gs, MP_THREADS, 0, c->stream>>>(rows, c->N, c->nb_ptr, c->nbr, b.dB, b.gn, b.dA);
+  }
+  // layer 1 (input h0, 3 channels)
+  if (din) {
+    k_mp_bwd_layer<3, true><<<nblk, MP_THREADS, sm3, c->stream>>>(rows, c->N, c->nb_ptr, b.dA, h0, b.a1[k],
+                                                                  m->wbf + MP_W1S, m->wbf + MP_W1N, b.t3a, b.t3b, gp);
+    k_mp_bwd_agg<3><<<gs, MP_THREADS, 0, c->stream>>>(rows, c->N, c->nb_ptr, c->nbr, b.t3a, b.t3b, din);
+  } else {
+    k_mp_bwd_layer<3, false><<<nblk, MP_THREADS, sm3, c->stream>>>(rows, c->N, c->nb_ptr, b.dA, h0, b.a1[k],
+                                                                   m->wbf + MP_W1S, m->wbf + MP_W1N, nullptr, nullptr,
+                                                                   gp);
+  }
+  if (grad) k_mp_grad_reduce<<<2, 128, 0, c->stream>>>((int)nblk, 2 * MP_W * 3, c->mgpart, m->g + MP_W1S, acc);
+  c->launches += 8 + (grad ? 4 : 0) + (din ? 1 : 0);
+}
+
+static void set_bwd_smem() {
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(k_mp_bwd_layer<MP_W, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(MP_THREADS * (MP_W + 2 * MP_W) * sizeof(float)));
+  done = true;
+}
+
+// v = NᵀN y for one sample (inference; uses pass 0 without keeping aggregates
+// for the weight gradient — the adjoint still needs a1 of the input layer only
+// when weight gradients are formed, so none is read here)
+void enqueue_mpnn_spd(Ctx* c, const float* y, float* v) {
+  enqueue_forward(c, 1, y, 0, false, c->mb.u);
+  enqueue_backward(c, 1, c->mb.u, 0, y, false, false, v);
+}
+
+// forward, loss and gradient for B pairs (y, sq [B][N][3], den [B]); the
+// gradient of scale·Σ_b ℓ_b lands in mp->g, the loss in *loss_out (if set).
+static int train_step(Ctx* c, int64_t B, const float* y, const float* sq, const float* den, float scale,
+                      double* loss_out) {
+  const int64_t N = c->N, rows = B * N, n3 = 3 * N;
+  const int64_t nblk = (rows + MP_THREADS - 1) / MP_THREADS;
+  int rc = ensure_gpart(c, nblk);
+  if (rc) return rc;
+  set_bwd_smem();
+  MpBufs& b = c->mb;
+  const unsigned gs = grid_for(rows, MP_THREADS);
+  // u = N y (pass 0 kept), v = Nᵀ u
+  enqueue_forward(c, B, y, 0, true, b.u);
+  enqueue_backward(c, B, b.u, 0, y, false, false, b.v);
+  // K z per pair, z = (y + v)/sq (FP32 tiled apply)
+  for (int64_t k = 0; k < B; ++k) {
+    k_mp_zsplit<<<grid_for(n3, 256), 256, 0, c->stream>>>(n3, y + k * n3, b.v + k * n3, sq + k * n3, c->p2);
+    enqueue_apply_tiled(c, c->p2, c->Apf, true, nullptr, nullptr, nullptr);
+    cudaMemcpyAsync(b.kz + k * n3, c->Apf, n3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream);
+    c->launches += 1;
+  }
+  k_mp_cos_dots<<<dim3(MP_DOT_BLOCKS, (unsigned)B), 256, 0, c->stream>>>(n3, y, b.v, sq, b.kz, c->mdots);
+  k_mp_cos_coef<<<1, 32, 0, c->stream>>>((int)B, MP_DOT_BLOCKS, c->mdots, den, scale, c->mcoef);
+  k_mp_cos_ghat<<<gs, MP_THREADS, 0, c->stream>>>(rows, N, y, sq, b.kz, c->mcoef, c->mask, b.ghat);
+  c->launches += 3;
+  // ∂ℓ/∂W = ∂⟨N ĝ, N y⟩/∂W: backward of pass 0 with N ĝ, of pass 1 (on ĝ) with u
+  enqueue_forward(c, B, b.ghat, 1, true, b.w);
+  enqueue_backward(c, B, b.w, 0, y, true, false, nullptr);
+  enqueue_backward(c, B, b.u, 1, b.ghat, true, true, nullptr);
+  if (loss_out) {
+    double L = 0.0;
+    cudaMemcpyAsync(&L, c->mdots + 2 * B * MP_DOT_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if ((rc = sync_and_check(c, "training loss"))) return rc;
+    *loss_out = L;
+  }
+  return 0;
+}
+
+static double sum_partials_host(Ctx* c, int n) {
+  std::vector<double> h((size_t)n);
+  cudaMemcpyAsync(h.data(), c->part, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (sync_and_check(c, "partials")) return NAN;
+  double s = 0.0;
+  for (double v : h) s += v;
+  return s;
+}
+
+// Append (y, t, sq, den) for one pair (r, e) (device, FP64).
+static int append_pair(Ctx* c, const double* r, const double* e) {
+  const int64_t n3 = 3 * c->N;
+  if (c->mp_pairs >= c->mp_cap) {   // grow geometrically
+    const int64_t cap = std::max<int64_t>(16, 2 * c->mp_cap);
+    float *x = nullptr, *t = nullptr, *d = nullptr, *den = nullptr;
+    int rc = dalloc(c, &x, (size_t)cap * n3);
+    if (!rc) rc = dalloc(c, &t, (size_t)cap * n3);
+    if (!rc) rc = dalloc(c, &d, (size_t)cap * n3);
+    if (!rc) rc = dalloc(c, &den, (size_t)cap);
+    if (rc) return rc;
+    if (c->mp_pairs) {
+      cudaMemcpyAsync(x, c->mp_x, c->mp_pairs * n3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream);
+      cudaMemcpyAsync(t, c->mp_t, c->mp_pairs * n3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream);
+      cudaMemcpyAsync(d, c->mp_d, c->mp_pairs * n3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream);
+      cudaMemcpyAsync(den, c->mp_den, c->mp_pairs * sizeof(float), cudaMemcpyDeviceToDevice, c->stream);
+      cudaStreamSynchronize(c->stream);
+    }
+    if (c->mp_x) {
+      dfree(c, c->mp_x);
+      dfree(c, c->mp_t);
+      dfree(c, c->mp_d);
+      dfree(c, c->mp_den);
+    }
+    c->mp_x = x;
+    c->mp_t = t;
+    c->mp_d = d;
+    c->mp_den = den;
+    c->mp_cap = cap;
+  }
+  k_mp_sample_norm<<<JFEM_RED_BLOCKS, 256, 0, c->stream>>>(c->N, r, c->dinv, c->mask, c->part);
+  c->launches += 1;
+  const double nf = (double)(n3 - c->n_fixed);
+  const double ss = sum_partials_host(c, JFEM_RED_BLOCKS);
+  if (!(ss > 0.0) || !(nf > 0.0)) return 0;   // nothing to learn from a zero residual
+  const double s = std::sqrt(ss / nf);
+  const int64_t k = c->mp_pairs;
+  k_mp_make_sample<<<JFEM_RED_BLOCKS, 256, 0, c->stream>>>(c->N, r, e, c->dinv, c->mask, 1.0 / s, c->mp_x + k * n3,
+                                                           c->mp_t + k * n3, c->mp_d + k * n3, c->part);
+  c->launches += 1;
+  const double den = sum_partials_host(c, JFEM_RED_BLOCKS);
+  if (!(den > 0.0)) return 0;
+  const float denf = (float)den;
+  cudaMemcpyAsync(c->mp_den + k, &denf, sizeof(float), cudaMemcpyHostToDevice, c->stream);
+  int rc = sync_and_check(c, "training pair");
+  if (rc) return rc;
+  c->mp_pairs += 1;
+  return 0;
+}
+
+int mpnn_collect(Ctx* c, int max_pairs, double tol) {
+  if (max_pairs <= 0) return set_err(c, JFEM_ERR_INVALID, "max_pairs must be positive");
+  int rc = geometry_prepare(c);
+  if (rc) return rc;
+  const int64_t n3 = 3 * c->N;
+  const int max_snaps = max_pairs - 1;   // plus the x = 0 pair
+  std::vector<int> snap_iters((size_t)std::max(1, max_snaps));
+  double* snaps = nullptr;
+  if (max_snaps > 0 && cudaMalloc(&snaps, (size_t)max_snaps * n3 * sizeof(double)) != cudaSuccess)
+    return set_err(c, JFEM_ERR_OOM, "iterate snapshots");
+  int n_snaps = 0, iters = 0;
+  double relres = 0.0;
+  rc = pcg_fp64_snapshots(c, c->f_ext, tol, 100000, snaps, max_snaps, &n_snaps, snap_iters.data(), &iters, &relres);
+  if (!rc) {
+    // c->x = x*; pairs e_k = x* − x_k (x_0 = prescribed values only), r_k = K e_k (masked)
+    double* e = c->b;
+    for (int k = -1; k < n_snaps && !rc; ++k) {
+      if (k < 0) k_mp_sub<<<grid_for(n3, 256), 256, 0, c->stream>>>(n3, c->x, c->gvals, e);
+      else k_mp_sub<<<grid_for(n3, 256), 256, 0, c->stream>>>(n3, c->x, snaps + (int64_t)k * n3, e);
+      c->launches += 1;
+      enqueue_apply(c, e, c->tmp, false, true, true, nullptr, nullptr, nullptr);
+      rc = append_pair(c, c->tmp, e);
+    }
+  }
+  if (snaps) cudaFree(snaps);
+  return rc ? rc : (int)c->mp_pairs;
+}
+
+int mpnn_train(Ctx* c, int epochs, int batch, double lr, uint64_t seed, double* losses) {
+  if (!c->mp || !c->mp->ready) return set_err(c, JFEM_ERR_INVALID, "no network weights (jfem_mpnn_init first)");
+  if (c->mp_pairs <= 0) return set_err(c, JFEM_ERR_INVALID, "no training pairs (jfem_mpnn_collect first)");
+  if (epochs <= 0 || batch <= 0 || !(lr > 0.0)) return set_err(c, JFEM_ERR_INVALID, "epochs, batch, lr must be positive");
+  const int64_t B = std::min<int64_t>(batch, c->mp_pairs);
+  int rc = geometry_prepare(c);
+  if (rc) return rc;
+  if ((rc = mpnn_ensure_act(c, B))) return rc;
+  MpnnState* m = c->mp;
+  const int64_t nb = (c->mp_pairs + B - 1) / B;
+  std::vector<int64_t> order((size_t)nb);
+  uint64_t st = seed;
+  for (int ep = 0; ep < epochs; ++ep) {
+    std::iota(order.begin(), order.end(), 0);
+    for (int64_t k = nb - 1; k > 0; --k) std::swap(order[(size_t)k], order[(size_t)(splitmix(st) % (uint64_t)(k + 1))]);
+    double ep_loss = 0.0;
+    for (int64_t q = 0; q < nb; ++q) {
+      const int64_t s0 = order[(size_t)q] * B;
+      const int64_t Bq = std::min<int64_t>(B, c->mp_pairs - s0);
+      const int64_t off = s0 * 3 * c->N;
+      double lq = 0.0;
+      rc = train_step(c, Bq, c->mp_x + off, c->mp_d + off, c->mp_den + s0, 1.f / (float)Bq, losses ? &lq : nullptr);
+      if (rc) return rc;
+      m->step += 1;
+      const float c1 = 1.f - std::pow(0.9f, (float)m->step), c2 = 1.f - std::pow(0.999f, (float)m->step);
+      k_mp_adam<<<grid_for(MP_P, 256), 256, 0, c->stream>>>(MP_P, m->w32, m->g, m->m, m->v, m->wbf, (float)lr, 0.9f,
+                                                            0.999f, 1e-8f, c1, c2);
+      c->launches += 1;
+      if (losses) ep_loss += lq * (double)Bq;
+    }
+    if (losses) losses[ep] = ep_loss / (double)c->mp_pairs;
+  }
+  return sync_and_check(c, "training");
+}
+
+int mpnn_loss_grad(Ctx* c, const double* r_h, const double* e_h, double* loss, float* grad) {
+  if (!c->mp || !c->mp->ready) return set_err(c, JFEM_ERR_INVALID, "no network weights (jfem_mpnn_init first)");
+  int rc = geometry_prepare(c);
+  if (rc) return rc;
+  if ((rc = jacobi_diag_device(c, c->dinv))) return rc;
+  if ((rc = mpnn_ensure_act(c, 1))) return rc;
+  const int64_t n3 = 3 * c->N;
+  cudaMemcpyAsync(c->tmp, r_h, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(c->b, e_h, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  const int64_t keep = c->mp_pairs;   // the pair goes to slot `keep` and is dropped again below
+  if ((rc = append_pair(c, c->tmp, c->b))) return rc;
+  if (c->mp_pairs == keep) return set_err(c, JFEM_ERR_INVALID, "zero residual or error");
+  const int64_t off = keep * n3;
+  double L = 0.0;
+  rc = train_step(c, 1, c->mp_x + off, c->mp_d + off, c->mp_den + keep, 1.f, &L);
+  c->mp_pairs = keep;
+  if (rc) return rc;
+  cudaMemcpyAsync(grad, c->mp->g, MP_P * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  if ((rc = sync_and_check(c, "gradient"))) return rc;
+  *loss = L;
+  return 0;
+}
+
+int mpnn_precondition(Ctx* c, const double* r_h, double* z_h) {
+  if (!c->mp || !c->mp->ready) return set_err(c, JFEM_ERR_INVALID, "no network weights (jfem_mpnn_init first)");
+  int rc = geometry_prepare(c);
+  if (rc) return rc;
+  if ((rc = jacobi_diag_device(c, c->dinv))) return rc;
+  if ((rc = mpnn_ensure_act(c, 1))) return rc;
+  const int64_t n3 = 3 * c->N;
+  cudaMemcpyAsync(c->tmp, r_h, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  k_mp_input_d<<<grid_for(n3, 256), 256, 0, c->stream>>>(c->N, c->tmp, c->dinv, c->mask, c->mb.y);
+  enqueue_mpnn_spd(c, c->mb.y, c->mb.v);
+  k_mp_precond_out<<<grid_for(n3, 256), 256, 0, c->stream>>>(c->N, c->mb.y, c->mb.v, c->dinv, c->mask, c->tmp2);
+  c->launches += 2;
+  cudaMemcpyAsync(z_h, c->tmp2, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  return sync_and_check(c, "preconditioner");
+}
+
+}  // namespace jfem

@@ -288,8 +288,7 @@ __global__ void k_scalars_reset(SolverScalars* __restrict__ sc, const double* __
     sc->max_iters = max_iters;
     sc->done[0] = (rr <= sc->tol2 || sc->iters >= max_iters) ? 1 : 0;
     sc->done[1] = 0;
-    sc->arrive[0] = 0;
-    sc->arrive[1] = 0;
+    for (int k = 0; k < 4; ++k) sc->arrive[k] = 0;
   }
 }
 
@@ -356,6 +355,157 @@ void enqueue_axpy(Ctx* c, int64_t n, double a, const double* x, double* y) {
 }
 
 // ---------------------------------------------------------------------------
+// flexible CG (Notay's FCG with one stored direction) for the learned
+// preconditioner, double-float vectors like the mixed PCG:
+//   z = B(r);  β = z·q_old / p_old·q_old (0 on restart);  p = z − βp;
+//   q = K p;  α = p·r / p·q;  δx += αp;  r −= αq
+// With a fixed SPD preconditioner this is PCG; with the network (nonlinear in
+// r) the explicit orthogonalisation against the previous direction keeps the
+// recursion consistent; the learned preconditioner is symmetric positive
+// definite, for which FCG is PCG.  part regions: [0,G) tile p·q, [3G,4G)
+// boundary p·q, [G,2G) z·q then r·r, [2G,3G) p·r.
+// ---------------------------------------------------------------------------
+// y = mask ⊙ D^{-1/2} r (FP32), the network input
+__global__ void __launch_bounds__(256) k_fcg_input(int64_t N, const float2* __restrict__ r,
+                                                   const float* __restrict__ dinv, const uint8_t* __restrict__ mask,
+                                                   const SolverScalars* __restrict__ sc, float* __restrict__ y) {
+  if (sc->done[0]) return;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * N; q += (int64_t)gridDim.x * blockDim.x) {
+    const bool fr = !((mask[q / 3] >> (int)(q % 3)) & 1);
+    const float2 rq = r[q];
+    y[q] = fr ? sqrtf(dinv[q]) * (rq.x + rq.y) : 0.f;
+  }
+}
+
+// z = D^{-1/2}(y + NᵀN y) (NN; y, v = NᵀN y given) or z = D⁻¹r (Jacobi); z·q_old
+// partials → the last block forms β = z·q_old / p_old·q_old (0 on restart)
+template <bool NN>
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_z(int64_t n, const float* __restrict__ y,
+                                                            const float* __restrict__ v,
+                                                            const float2* __restrict__ r,
+                                                            const float* __restrict__ dinv,
+                                                            const uint8_t* __restrict__ mask,
+                                                            const float* __restrict__ qold,
+                                                            SolverScalars* __restrict__ sc, float* __restrict__ z,
+                                                            double* __restrict__ part) {
+  __shared__ double sh[32];
+  if (sc->done[0]) return;
+  float2 dot = make_float2(0.f, 0.f);
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const bool fr = !((mask[q / 3] >> (int)(q % 3)) & 1);
+    float zq;
+    if (NN) {
+      zq = fr ? sqrtf(dinv[q]) * (y[q] + v[q]) : 0.f;
+    } else {
+      const float2 rq = r[q];
+      zq = fr ? dinv[q] * (rq.x + rq.y) : 0.f;
+    }
+    z[q] = zq;
+    dot = df_add(dot, df_two_prod(zq, qold[q]));
+  }
+  const double b = block_sum_df(dot, sh);
+  if (threadIdx.x == 0) part[G_ + blockIdx.x] = b;
+  if (arrive_last(&sc->arrive[2])) {
+    const double zq = reduce_partials_cg(part + G_, G_, sh);
+    if (threadIdx.x == 0) {
+      const double beta = sc->restart ? 0.0 : zq / sc->pAp;
+      sc->beta = beta;
+      sc->beta_df = df_from_double(beta);
+      sc->restart = 0;
+      sc->arrive[2] = 0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_p(int64_t n, const float* __restrict__ z,
+                                                            float2* __restrict__ p, const float2* __restrict__ r,
+                                                            SolverScalars* __restrict__ sc, double* __restrict__ part) {
+  __shared__ double sh[32];
+  if (sc->done[0]) return;
+  const float2 nb = df_neg(sc->beta_df);
+  const bool keep = sc->beta != 0.0;
+  float2 dot = make_float2(0.f, 0.f);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float2 pi = make_float2(z[i], 0.f);
+    if (keep) pi = df_add(pi, df_mul(nb, p[i]));
+    p[i] = pi;
+    dot = df_add(dot, df_mul(pi, r[i]));
+  }
+  const double b = block_sum_df(dot, sh);
+  if (threadIdx.x == 0) part[2 * G_ + blockIdx.x] = b;
+  if (arrive_last(&sc->arrive[3])) {
+    const double pr = reduce_partials_cg(part + 2 * G_, G_, sh);
+    if (threadIdx.x == 0) {
+      sc->rz[0] = pr;
+      sc->arrive[3] = 0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_update(int64_t n, SolverScalars* __restrict__ sc,
+                                                                 float2* __restrict__ x, float2* __restrict__ r,
+                                                                 const float2* __restrict__ p,
+                                                                 const float* __restrict__ q,
+                                                                 double* __restrict__ part) {
+  __shared__ double sh[32];
+  if (sc->done[0]) return;
+  const float2 a = sc->alpha_df, na = df_neg(a);
+  float2 rr = make_float2(0.f, 0.f);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = df_add(x[i], df_mul(a, p[i]));
+    const float2 ri = df_add(r[i], df_mul_f(na, q[i]));
+    r[i] = ri;
+    rr = df_add(rr, df_mul(ri, ri));
+  }
+  const double rrb = block_sum_df(rr, sh);
+  if (threadIdx.x == 0) part[G_ + blockIdx.x] = rrb;
+  if (arrive_last(&sc->arrive[1])) {
+    const double rr_new = reduce_partials_cg(part + G_, G_, sh);
+    if (threadIdx.x == 0) {
+      sc->rr[0] = rr_new;
+      sc->rz[0] = rr_new;   // reported in place of r·z (positive while the solve is healthy)
+      const int it = sc->iters + 1;
+      sc->iters = it;
+      sc->done[0] = (rr_new <= sc->tol2 || it >= sc->max_iters || !(rr_new == rr_new)) ? 1 : 0;
+      sc->arrive[1] = 0;
+    }
+  }
+}
+
+// r·r → part[G..2G) for a (re)start
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_norms(int64_t n, const float2* __restrict__ r,
+                                                                double* __restrict__ part) {
+  __shared__ double sh[32];
+  float2 rr = make_float2(0.f, 0.f);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 ri = r[i];
+    rr = df_add(rr, df_mul(ri, ri));
+  }
+  const double rrb = block_sum_df(rr, sh);
+  if (threadIdx.x == 0) part[G_ + blockIdx.x] = rrb;
+}
+
+__global__ void k_fcg_reset(SolverScalars* __restrict__ sc, const double* __restrict__ part, int set_bb, double tol,
+                            int max_iters, int reset_iters, int restart) {
+  __shared__ double sh[32];
+  const double rr = reduce_partials(part + G_, G_, sh);
+  if (threadIdx.x == 0) {
+    sc->rz[0] = rr;
+    sc->rr[0] = rr;
+    if (set_bb) {
+      sc->bb = rr;
+      sc->tol2 = tol * tol * rr;
+    }
+    if (reset_iters) sc->iters = 0;
+    sc->max_iters = max_iters;
+    sc->restart = restart;
+    sc->done[0] = (rr <= sc->tol2 || sc->iters >= max_iters) ? 1 : 0;
+    sc->done[1] = 0;
+    for (int k = 0; k < 4; ++k) sc->arrive[k] = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host orchestration
 // ---------------------------------------------------------------------------
 static double now_s() {
@@ -388,6 +538,25 @@ static int true_residual(Ctx* c, const double* f, const double* xv, double* r, d
   return read_norms(c, rr_out, drift2);
 }
 
+static void enqueue_fcg_iteration(Ctx* c, bool nn) {
+  const int64_t n = 3 * c->N;
+  if (nn) {
+    k_fcg_input<<<grid_for(n, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, c->mb.y);
+    enqueue_mpnn_spd(c, c->mb.y, c->mb.v);
+    k_fcg_z<true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->mb.y, c->mb.v, c->rd, c->dinvf, c->mask, c->Apf,
+                                                           c->sc, c->zf, c->part);
+    c->launches += 2;
+  } else {
+    k_fcg_z<false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, nullptr, nullptr, c->rd, c->dinvf, c->mask, c->Apf,
+                                                            c->sc, c->zf, c->part);
+    c->launches += 1;
+  }
+  k_fcg_p<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->zf, c->p2, c->rd, c->sc, c->part);
+  enqueue_apply_tiled(c, c->p2, c->Apf, true, c->part, &c->sc->done[0], c->sc);
+  k_fcg_update<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->xd, c->rd, c->p2, c->Apf, c->part);
+  c->launches += 2;
+}
+
 static void enqueue_iteration(Ctx* c, bool fp32, int slot) {
   const int64_t n = 3 * c->N;
   if (fp32) {   // mixed: double-float vectors, tiled FP32 apply
@@ -405,13 +574,14 @@ static void enqueue_iteration(Ctx* c, bool fp32, int slot) {
   c->launches += 2;
 }
 
-static int graph_key(Ctx* c, bool fp32) {
-  return (fp32 ? 1 : 0) | (c->finite << 1) | (c->model << 2) | (c->geom << 3) | ((c->geo_affine ? 1 : 0) << 4) |
-         (c->et << 5) | ((c->geoT32 ? 1 : 0) << 10);
+// kind: 0 FP64 PCG, 1 mixed PCG, 2 FCG Jacobi, 3 FCG learned
+static int graph_key(Ctx* c, int kind) {
+  return kind | (c->finite << 2) | (c->model << 3) | (c->geom << 4) | ((c->geo_affine ? 1 : 0) << 5) |
+         (c->et << 6) | ((c->geoT32 ? 1 : 0) << 11);
 }
 
-static int build_graph(Ctx* c, bool fp32) {
-  const int key = graph_key(c, fp32);
+static int build_graph(Ctx* c, int kind) {
+  const int key = graph_key(c, kind);
   if (c->pcg_graph && c->pcg_graph_key == key) return 0;
   if (c->pcg_graph) {
     cudaGraphExecDestroy(c->pcg_graph);
@@ -421,7 +591,10 @@ static int build_graph(Ctx* c, bool fp32) {
   const int64_t l0 = c->launches;
   cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_check(c, e, "begin capture");
-  for (int k = 0; k < PCG_CHUNK; ++k) enqueue_iteration(c, fp32, fp32 ? 0 : (k & 1));
+  for (int k = 0; k < PCG_CHUNK; ++k) {
+    if (kind >= 2) enqueue_fcg_iteration(c, kind == 3);
+    else enqueue_iteration(c, kind == 1, kind == 1 ? 0 : (k & 1));
+  }
   e = cudaStreamEndCapture(c->stream, &g);
   if (e != cudaSuccess) return cuda_check(c, e, "end capture");
   e = cudaGraphInstantiate(&c->pcg_graph, g, 0);
@@ -438,6 +611,15 @@ struct PcgResult {
   int refinements = 0;
   double relres = 0.0;
   int status = 0;
+  int fallbacks = 0;
+};
+
+// FP64 iterates captured at iteration counts first, 2·first, 4·first, … (after
+// the graph chunk that reaches them), for training-pair collection.
+struct PcgSnap {
+  double* buf = nullptr;   // [max][3N]
+  int max = 0, count = 0, next = 16;
+  int* iters = nullptr;
 };
 
 // PCG on the masked operator for K x = f over the free DOFs; x holds the
@@ -456,7 +638,7 @@ struct PcgResult {
 // reached the attainable accuracy of the arithmetic: the best iterate is kept
 // and JFEM_NOT_CONVERGED returned.
 static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, double time_budget, double t_start,
-               bool reliable, bool x_zero, PcgResult* res, double drop = 1e-2) {
+               bool reliable, bool x_zero, PcgResult* res, double drop = 1e-2, PcgSnap* snap = nullptr) {
   int rc = 0;
   double rr0 = 0.0;
   const int64_t n = 3 * c->N;
@@ -488,7 +670,7 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
   res->relres = 0.0;
   res->status = 0;
   if (!(bb > 0.0)) return 0;
-  if ((rc = build_graph(c, fp32))) return rc;
+  if ((rc = build_graph(c, fp32 ? 1 : 0))) return rc;
   const double ru = fp32 ? drop * drop : 0.0;
   const double goal = tol * tol * bb;
   double rr_true_last = rr0, rr_best = rr0;
@@ -500,6 +682,12 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
       if (e != cudaSuccess) return cuda_check(c, e, "graph launch");
       c->launches += c->chunk_launches;
       if ((rc = read_scalars(c))) return rc;
+      if (snap && !fp32 && snap->count < snap->max && c->sc_host->iters >= snap->next && !c->sc_host->done[0]) {
+        cudaMemcpyAsync(snap->buf + (int64_t)snap->count * 3 * c->N, c->x, 3 * c->N * sizeof(double),
+                        cudaMemcpyDeviceToDevice, c->stream);
+        snap->iters[snap->count++] = c->sc_host->iters;
+        snap->next *= 2;
+      }
     }
     const SolverScalars& s = *c->sc_host;
     const double rr = s.rr[0];
@@ -560,6 +748,122 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
   }
 }
 
+// Flexible CG with the learned preconditioner (nn) or Jacobi, mixed precision
+// (double-float vectors, FP32 tiled apply, FP64 true residual as the judge).
+// Refinements as in pcg() (the direction is kept when the recursive and true
+// residuals agree to 10 %).  When the learned preconditioner stalls (two
+// refinements without a 4× gain in the true residual, or no 10 % progress of
+// the recursive residual norm over `window` iterations — generous, since CG
+// residual norms are not monotone) the solve continues with Jacobi from the
+// best iterate (res->fallbacks = 1).
+static int fcg(Ctx* c, const double* f, bool nn, double tol, int max_iter, double time_budget, double t_start,
+               bool x_zero, PcgResult* res, double drop) {
+  int rc = 0;
+  double rr0 = 0.0;
+  const int64_t n = 3 * c->N;
+  const unsigned gv = grid_for(n, 256);
+  if (!apply_is_tiled(c)) return set_err(c, JFEM_ERR_INVALID, "flexible CG needs the tiled apply");
+  if (nn && (!c->mp || !c->mp->ready)) return set_err(c, JFEM_ERR_INVALID, "no network weights (jfem_mpnn_init)");
+  if (nn && (rc = mpnn_ensure_act(c, 1))) return rc;
+  if (!c->zf && (rc = dalloc(c, &c->zf, (size_t)n))) return rc;
+  if (x_zero) {
+    k_residual<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, f, 1.0, nullptr, c->mask, c->r, 0, c->part);
+    c->launches += 1;
+    if ((rc = read_norms(c, &rr0, nullptr))) return rc;
+  } else if ((rc = true_residual(c, f, c->x, c->r, &rr0))) {
+    return rc;
+  }
+  k_narrow<<<gv, 256, 0, c->stream>>>(n, c->dinv, c->dinvf);
+  cudaMemsetAsync(c->xd, 0, n * sizeof(float2), c->stream);
+  cudaMemsetAsync(c->Apf, 0, n * sizeof(float), c->stream);
+  k_df_from_double<<<gv, 256, 0, c->stream>>>(n, c->r, c->rd);
+  k_fcg_norms<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->rd, c->part);
+  k_fcg_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 1, tol, max_iter, 1, 1);
+  c->launches += 4;
+  if ((rc = read_scalars(c))) return rc;
+  const double bb = c->sc_host->bb;
+  *res = PcgResult();
+  if (!(bb > 0.0)) return 0;
+  if ((rc = build_graph(c, nn ? 3 : 2))) return rc;
+  const double ru = drop * drop;
+  const double goal = tol * tol * bb;
+  const int window = 4096;
+  double rr_true_last = rr0, rr_best = rr0, rr_rec_best = rr0;
+  int rec_best_it = 0;
+  cudaMemcpyAsync(c->xbest, c->x, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  int refinements = 0, stalls = 0, fallbacks = 0;
+  for (;;) {
+    if (!c->sc_host->done[0]) {
+      cudaError_t e = cudaGraphLaunch(c->pcg_graph, c->stream);
+      if (e != cudaSuccess) return cuda_check(c, e, "graph launch");
+      c->launches += c->chunk_launches;
+      if ((rc = read_scalars(c))) return rc;
+    }
+    const SolverScalars& s = *c->sc_host;
+    const double rr = s.rr[0];
+    const int iters = s.iters;
+    const bool at_cap = iters >= max_iter;
+    const bool bad = !(rr == rr) || rr > 1e30 * bb;
+    if (rr < 0.9 * rr_rec_best) {
+      rr_rec_best = rr;
+      rec_best_it = iters;
+    }
+    const bool stagnant = nn && iters - rec_best_it >= window;
+    const bool check = s.done[0] || bad || rr < ru * rr_true_last || stagnant;
+    if (check) {
+      double rr_t = 0.0, drift2 = 0.0;
+      k_df_absorb<<<gv, 256, 0, c->stream>>>(n, c->xd, c->x);
+      k_df_to_double<<<gv, 256, 0, c->stream>>>(n, c->rd, c->r);
+      c->launches += 2;
+      if ((rc = true_residual(c, f, c->x, c->r, &rr_t, &drift2))) return rc;
+      ++refinements;
+      const bool finite = rr_t == rr_t && rr_t < 1e300;
+      if (finite && rr_t < rr_best) {
+        rr_best = rr_t;
+        cudaMemcpyAsync(c->xbest, c->x, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+      }
+      stalls = (finite && rr_t < 0.25 * rr_true_last && !stagnant) ? 0 : stalls + 1;
+      const bool converged = finite && rr_t <= goal;
+      bool switch_jacobi = false;
+      if (!converged && !at_cap && (stalls >= 2 || !finite) && nn) {   // learned preconditioner stalled
+        switch_jacobi = true;
+        nn = false;
+        fallbacks = 1;
+        stalls = 0;
+      }
+      if (converged || at_cap || (!switch_jacobi && (stalls >= 2 || !finite))) {
+        if (!converged) {
+          cudaMemcpyAsync(c->x, c->xbest, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+          if ((rc = sync_and_check(c, "best iterate"))) return rc;
+        }
+        res->iters = iters;
+        res->refinements = refinements;
+        res->fallbacks = fallbacks;
+        res->relres = std::sqrt((converged ? rr_t : rr_best) / bb);
+        res->status = converged ? (fallbacks ? JFEM_STALL : 0) : JFEM_NOT_CONVERGED;
+        return 0;
+      }
+      rr_true_last = rr_t;
+      if (!finite || switch_jacobi) {   // continue from the best iterate
+        cudaMemcpyAsync(c->x, c->xbest, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+        if ((rc = true_residual(c, f, c->x, c->r, &rr_t))) return rc;
+        rr_true_last = rr_t;
+      }
+      if (switch_jacobi && (rc = build_graph(c, 2))) return rc;
+      rr_rec_best = rr_t;
+      rec_best_it = iters;
+      const int restart = (!finite || switch_jacobi || !(drift2 < 0.01 * rr_t)) ? 1 : 0;
+      k_df_from_double<<<gv, 256, 0, c->stream>>>(n, c->r, c->rd);
+      k_fcg_norms<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->rd, c->part);
+      k_fcg_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 0, tol, max_iter, 0, restart);
+      c->launches += 3;
+      if ((rc = read_scalars(c))) return rc;
+    }
+    if (time_budget > 0.0 && now_s() - t_start > time_budget)
+      return set_err(c, JFEM_ERR_TIMEOUT, "solve exceeded its time budget");
+  }
+}
+
 static int prepare_rhs(Ctx* c) {
   if (c->f_ext_dirty) {
     int rc = traction_device(c, c->f_ext);
@@ -589,14 +893,45 @@ static int solve_linear(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
   cudaMemcpyAsync(c->x, c->gvals, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   const bool fp32 = o->precision == JFEM_MIXED;
   PcgResult pr;
-  rc = pcg(c, c->f_ext, fp32, o->tol, o->max_iter, o->time_budget_s, t0, true, c->n_fixed_nonzero == 0, &pr,
-           o->refine_drop > 0.0 ? o->refine_drop : 0.3);
+  const double drop = o->refine_drop > 0.0 ? o->refine_drop : 0.3;
+  if (o->method == JFEM_FCG_LEARNED)
+    rc = fcg(c, c->f_ext, true, o->tol, o->max_iter, o->time_budget_s, t0, c->n_fixed_nonzero == 0, &pr, drop);
+  else
+    rc = pcg(c, c->f_ext, fp32, o->tol, o->max_iter, o->time_budget_s, t0, true, c->n_fixed_nonzero == 0, &pr,
+             drop);
   if (rc) return rc;
   cudaMemcpyAsync(u_d, c->x, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   if ((rc = sync_and_check(c, "solution copy"))) return rc;
   fill_stats(st, pr.status, 1, pr.iters, pr.refinements, pr.relres, now_s() - t0);
-  if (st) st->history_len = 0;
+  if (st) {
+    st->history_len = 0;
+    st->fallbacks = pr.fallbacks;
+  }
   return pr.status;
+}
+
+// FP64 Jacobi-PCG of the current system from x = prescribed values to tol,
+// keeping iterates at 16, 32, 64, … iterations (training-pair collection).
+// Leaves x* in c->x, D⁻¹ in c->dinv.
+int pcg_fp64_snapshots(Ctx* c, const double* f, double tol, int max_iter, double* snaps, int max_snaps,
+                       int* n_snaps, int* snap_iters, int* iters_out, double* relres_out) {
+  int rc = 0;
+  if ((rc = geometry_prepare(c))) return rc;
+  if ((rc = prepare_rhs(c))) return rc;
+  if ((rc = jacobi_diag_device(c, c->dinv))) return rc;
+  cudaMemcpyAsync(c->x, c->gvals, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  PcgSnap sn;
+  sn.buf = snaps;
+  sn.max = max_snaps;
+  sn.iters = snap_iters;
+  PcgResult pr;
+  rc = pcg(c, f == c->f_ext ? c->f_ext : f, false, tol, max_iter, 0.0, now_s(), false, c->n_fixed_nonzero == 0,
+           &pr, 1e-2, &sn);
+  if (rc) return rc;
+  *n_snaps = sn.count;
+  *iters_out = pr.iters;
+  *relres_out = pr.relres;
+  return sync_and_check(c, "snapshots");
 }
 
 // Inexact Newton–Krylov with load stepping.  Step s of S applies s/S of the
@@ -691,7 +1026,8 @@ int solve_device(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stats* st) 
   if (o->method == JFEM_NEWTON && (o->max_newton <= 0 || o->max_cg_per_newton <= 0 || !(o->newton_tol > 0.0)))
     return set_err(c, JFEM_ERR_INVALID, "Newton options must be positive");
   switch (o->method) {
-    case JFEM_PCG_JACOBI: return solve_linear(c, o, u_d, st);
+    case JFEM_PCG_JACOBI:
+    case JFEM_FCG_LEARNED: return solve_linear(c, o, u_d, st);
     case JFEM_NEWTON: return solve_newton(c, o, u_d, st);
     default: return set_err(c, JFEM_ERR_INVALID, "unknown solve method");
   }

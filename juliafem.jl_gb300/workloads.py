@@ -110,3 +110,48 @@ def batch_instances(count: int = 256, nmin: int = 8, nmax: int = 32, seed_item: 
         w = cantilever(_mesh.TET4, n, k, k, 4.0, 1.0, 1.0, E=E, nu=nu, traction=t, name=f"batch_{i}")
         out.append(w)
     return out
+
+
+def learned_family(count: int, seed_item: int = 40, nx: int = 40, ny: int = 4, nz: int = 4,
+                   L: float = 10.0, W: float = 1.0, H: float = 1.0, sigma_log: float = 0.5,
+                   patches: int = 2, elem_type: int = _mesh.TET10):
+    """Training / evaluation systems of the learned preconditioner: the Tet10
+    cantilever on [0,10]×[0,1]² (40×4×4 cubes, the geometry of the Tet4
+    parity case) with per-element E = 210e3·exp(σ z), z ~ N(0,1) (σ = 0.5),
+    ν = 0.3, x = 0 clamped, and `patches` tractions with components N(0,1) on
+    random rectangular patches of the five unclamped faces.  Item k of a family
+    draws from the generator of seed_item + k, so a family of unseen systems is
+    a disjoint seed range."""
+    m = _mesh.box_mesh(elem_type, nx, ny, nz, L, W, H)
+    clamp = m.nodes_where(0, 0.0)
+    dofs = _mesh.clamp_dofs(clamp)
+    sides = [(0, 1), (1, 0), (1, 1), (2, 0), (2, 1)]
+    face_sets = []
+    for axis, side in sides:
+        ft, faces = m.face(axis, side)
+        face_sets.append((axis, ft, faces, m.X[faces].mean(axis=1)))
+    out = []
+    for k in range(count):
+        g = rng(seed_item + k)
+        E = 210e3 * np.exp(sigma_log * g.standard_normal(m.n_elem))
+        sel_faces, sel_t = [], []
+        for _ in range(patches):
+            axis, ft, faces, cen = face_sets[int(g.integers(len(face_sets)))]
+            u_ax, v_ax = [d for d in range(3) if d != axis]
+            lu, lv = m.size[u_ax], m.size[v_ax]
+            u = np.sort(g.uniform(0.0, lu, 2))
+            v = np.sort(g.uniform(0.0, lv, 2))
+            inside = ((cen[:, u_ax] >= u[0]) & (cen[:, u_ax] <= u[1]) &
+                      (cen[:, v_ax] >= v[0]) & (cen[:, v_ax] <= v[1]))
+            if not inside.any():   # at least the face nearest the patch centre
+                c = np.array([0.0, 0.0, 0.0])
+                c[u_ax], c[v_ax] = u.mean(), v.mean()
+                inside[np.argmin(np.sum((cen[:, [u_ax, v_ax]] - c[[u_ax, v_ax]]) ** 2, axis=1))] = True
+            t = g.standard_normal(3)
+            sel_faces.append(faces[inside])
+            sel_t.append(np.broadcast_to(t, (int(inside.sum()), 3)))
+        faces = np.concatenate(sel_faces)
+        trac = np.ascontiguousarray(np.concatenate(sel_t))
+        out.append(Workload(f"learned_{seed_item + k}", m, E, 0.3, dofs, np.zeros(dofs.size),
+                            face_sets[0][1], faces, trac))
+    return out
