@@ -130,6 +130,7 @@ int jfem_destroy(jfem_ctx* h) {
     cudaFree(c->mp->m);
     cudaFree(c->mp->v);
     cudaFree(c->mp->g);
+    cudaFree(c->mp->poly);
     delete c->mp;
     c->mp = nullptr;
   }

@@ -203,6 +203,12 @@ struct MpnnState {
   float* g = nullptr;            // last gradient
   int64_t step = 0;
   bool ready = false;
+  // Inference form of the (linear) network: N = Σ_{k=0..3} C_k ⊗ A^k with A the
+  // neighbour mean and C_k the 3×3 sums of the layer products (Wo·X3·X2·X1,
+  // X_l ∈ {Ws_l, Wn_l}, k of them Wn).  Formed in FP64 from the BF16 weights
+  // whenever they change; FP32 on the device.
+  float* poly = nullptr;         // C_0..C_3 row-major, 36 values
+  bool poly_fresh = false;
 };
 
 struct Ctx {
@@ -313,6 +319,7 @@ struct Ctx {
   float* mcoef = nullptr;     // per-pair loss-gradient coefficients
   int64_t m_actB = 0, m_gpart_cap = 0;
   float* zf = nullptr;        // FCG: preconditioned residual (FP32)
+  float* invdeg = nullptr;    // 1 / (neighbours of each node), the mean-aggregation weights
 
   std::vector<void*> owned;   // everything cudaMalloc'ed for this mesh
 };
@@ -380,6 +387,7 @@ int mpnn_train(Ctx* c, int epochs, int batch, double lr, uint64_t seed, double* 
 int mpnn_loss_grad(Ctx* c, const double* r, const double* e, double* loss, float* grad);
 int mpnn_precondition(Ctx* c, const double* r, double* z);
 int mpnn_ensure_act(Ctx* c, int64_t B);
+int mpnn_refresh_poly(Ctx* c);
 void enqueue_mpnn_spd(Ctx* c, const float* y, float* v);   // v = NᵀN y for one sample (y, v: [N][3])
 // jfem_solver.cu
 int pcg_fp64_snapshots(Ctx* c, const double* f, double tol, int max_iter, double* snaps, int max_snaps,

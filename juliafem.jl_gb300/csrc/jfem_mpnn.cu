@@ -465,6 +465,104 @@ __global__ void k_mp_precond_out(int64_t N, const float* __restrict__ y, const f
 }
 
 // ---------------------------------------------------------------------------
+// inference in polynomial form (3 channels): N y = mask ⊙ Σ_k C_k A^k y and
+// Nᵀ u = Σ_k (Aᵀ)^k C_kᵀ u by Horner's rule.  A y_i = invdeg_i Σ_{j~i} y_j;
+// Aᵀ g_i = Σ_{j~i} invdeg_j g_j (the node graph is symmetric).
+// ---------------------------------------------------------------------------
+__global__ void k_mp_invdeg(int64_t N, const int* __restrict__ nb_ptr, float* __restrict__ invdeg) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    const int deg = nb_ptr[i + 1] - nb_ptr[i] - 1;
+    invdeg[i] = deg > 0 ? 1.f / (float)deg : 0.f;
+  }
+}
+
+__device__ __forceinline__ void mat3_acc(const float* __restrict__ C, bool transpose, const float (&x)[3],
+                                         float (&y)[3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) y[a] = fmaf(transpose ? C[3 * b + a] : C[3 * a + b], x[b], y[a]);
+}
+
+// out = A in  (FORWARD_LAST = false), or, for the last forward step,
+// u = mask ⊙ (C0 y + C1 a1 + C2 a2 + C3 A a2) and h = C3ᵀ u
+template <bool LAST>
+__global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __restrict__ nb_ptr,
+                                                     const int* __restrict__ nbr, const float* __restrict__ invdeg,
+                                                     const float* __restrict__ in, const float* __restrict__ y,
+                                                     const float* __restrict__ a1, const float* __restrict__ poly,
+                                                     const uint8_t* __restrict__ mask, float* __restrict__ out,
+                                                     float* __restrict__ h) {
+  __shared__ float C[36];
+  if (threadIdx.x < 36) C[threadIdx.x] = poly[threadIdx.x];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    float s[3] = {0.f, 0.f, 0.f};
+    const int j0 = __ldg(nb_ptr + i), j1 = __ldg(nb_ptr + i + 1);
+    for (int jj = j0; jj < j1; ++jj) {
+      const int64_t j = __ldg(nbr + jj);
+      if (j == i) continue;
+      s[0] += __ldg(in + 3 * j);
+      s[1] += __ldg(in + 3 * j + 1);
+      s[2] += __ldg(in + 3 * j + 2);
+    }
+    const float id = __ldg(invdeg + i);
+    float a[3] = {s[0] * id, s[1] * id, s[2] * id};
+    if (!LAST) {
+      out[3 * i] = a[0];
+      out[3 * i + 1] = a[1];
+      out[3 * i + 2] = a[2];
+    } else {
+      const float yv[3] = {y[3 * i], y[3 * i + 1], y[3 * i + 2]};
+      const float a1v[3] = {a1[3 * i], a1[3 * i + 1], a1[3 * i + 2]};
+      const float a2v[3] = {in[3 * i], in[3 * i + 1], in[3 * i + 2]};
+      float u[3] = {0.f, 0.f, 0.f};
+      mat3_acc(C, false, yv, u);
+      mat3_acc(C + 9, false, a1v, u);
+      mat3_acc(C + 18, false, a2v, u);
+      mat3_acc(C + 27, false, a, u);
+      const uint8_t m = mask[i];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) u[k] = ((m >> k) & 1) ? 0.f : u[k];
+      float hv[3] = {0.f, 0.f, 0.f};
+      mat3_acc(C + 27, true, u, hv);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        out[3 * i + k] = u[k];
+        h[3 * i + k] = hv[k];
+      }
+    }
+  }
+}
+
+// Horner step of the adjoint: out = C_kᵀ u + Aᵀ g
+__global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __restrict__ nb_ptr,
+                                                     const int* __restrict__ nbr, const float* __restrict__ invdeg,
+                                                     const float* __restrict__ g, const float* __restrict__ u,
+                                                     const float* __restrict__ poly, int k, float* __restrict__ out) {
+  __shared__ float C[9];
+  if (threadIdx.x < 9) C[threadIdx.x] = poly[9 * k + threadIdx.x];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    float s[3] = {0.f, 0.f, 0.f};
+    const int j0 = __ldg(nb_ptr + i), j1 = __ldg(nb_ptr + i + 1);
+    for (int jj = j0; jj < j1; ++jj) {
+      const int64_t j = __ldg(nbr + jj);
+      if (j == i) continue;
+      const float w = __ldg(invdeg + j);
+      s[0] = fmaf(w, __ldg(g + 3 * j), s[0]);
+      s[1] = fmaf(w, __ldg(g + 3 * j + 1), s[1]);
+      s[2] = fmaf(w, __ldg(g + 3 * j + 2), s[2]);
+    }
+    const float uv[3] = {u[3 * i], u[3 * i + 1], u[3 * i + 2]};
+    mat3_acc(C, true, uv, s);
+    out[3 * i] = s[0];
+    out[3 * i + 1] = s[1];
+    out[3 * i + 2] = s[2];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 static uint64_t splitmix(uint64_t& s) {
@@ -483,7 +581,8 @@ int mpnn_ensure(Ctx* c) {
         cudaMalloc(&m->wbf, MP_P * sizeof(__nv_bfloat16)) != cudaSuccess ||
         cudaMalloc(&m->m, MP_P * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&m->v, MP_P * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&m->g, MP_P * sizeof(float)) != cudaSuccess)
+        cudaMalloc(&m->g, MP_P * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&m->poly, 36 * sizeof(float)) != cudaSuccess)
       return set_err(c, JFEM_ERR_OOM, "network weights");
   }
   return 0;
@@ -497,6 +596,7 @@ static int upload_weights(Ctx* c, const float* w) {
   cudaMemsetAsync(m->v, 0, MP_P * sizeof(float), c->stream);
   c->launches += 1;
   m->step = 0;
+  m->poly_fresh = false;
   int rc = sync_and_check(c, "network weights");
   if (!rc) m->ready = true;
   return rc;
@@ -537,6 +637,12 @@ int mpnn_get_weights(Ctx* c, float* w) {
 // written as float4).
 int mpnn_ensure_act(Ctx* c, int64_t B) {
   if (c->m_actB >= B) return 0;
+  if (c->pcg_graph) {   // a captured solve graph holds the old buffer addresses
+    cudaStreamSynchronize(c->stream);
+    cudaGraphExecDestroy(c->pcg_graph);
+    c->pcg_graph = nullptr;
+    c->pcg_graph_key = -1;
+  }
   if (c->marena) dfree(c, c->marena);
   c->marena = nullptr;
   const int64_t r = B * c->N;
@@ -657,12 +763,75 @@ static void set_bwd_smem() {
   done = true;
 }
 
-// v = NᵀN y for one sample (inference; uses pass 0 without keeping aggregates
-// for the weight gradient — the adjoint still needs a1 of the input layer only
-// when weight gradients are formed, so none is read here)
+// C_0..C_3 of the polynomial form from the current (BF16-valued) weights, FP64
+// on the host; also the per-node mean weights of the mesh.
+int mpnn_refresh_poly(Ctx* c) {
+  MpnnState* m = c->mp;
+  if (!c->invdeg) {
+    int rc = dalloc(c, &c->invdeg, (size_t)c->N);
+    if (rc) return rc;
+    k_mp_invdeg<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->nb_ptr, c->invdeg);
+    c->launches += 1;
+  }
+  if (m->poly_fresh) return sync_and_check(c, "aggregation weights");
+  std::vector<float> w(MP_P);
+  cudaMemcpyAsync(w.data(), m->w32, MP_P * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  int rc = sync_and_check(c, "network weights");
+  if (rc) return rc;
+  auto W = [&](int off, int rows, int cols, int r, int col) { return (double)w[(size_t)(off + r * cols + col)]; };
+  double C[4][3][3] = {};
+  for (int path = 0; path < 8; ++path) {   // bit l set: layer l+1 uses Wn
+    // T = X1 (32×3), then X2·T, X3·T, Wo·T
+    double T[MP_W][3], U[MP_W][3];
+    const int o1 = (path & 1) ? MP_W1N : MP_W1S;
+    for (int a = 0; a < MP_W; ++a)
+      for (int b = 0; b < 3; ++b) T[a][b] = W(o1, MP_W, 3, a, b);
+    const int offs[2] = {(path & 2) ? MP_W2N : MP_W2S, (path & 4) ? MP_W3N : MP_W3S};
+    for (int l = 0; l < 2; ++l) {
+      for (int a = 0; a < MP_W; ++a)
+        for (int b = 0; b < 3; ++b) {
+          double s2 = 0.0;
+          for (int q = 0; q < MP_W; ++q) s2 += W(offs[l], MP_W, MP_W, a, q) * T[q][b];
+          U[a][b] = s2;
+        }
+      std::memcpy(T, U, sizeof(T));
+    }
+    const int k = ((path >> 0) & 1) + ((path >> 1) & 1) + ((path >> 2) & 1);
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) {
+        double s2 = 0.0;
+        for (int q = 0; q < MP_W; ++q) s2 += W(MP_WO, 3, MP_W, a, q) * T[q][b];
+        C[k][a][b] += s2;
+      }
+  }
+  float cf[36];
+  for (int k = 0; k < 4; ++k)
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) cf[9 * k + 3 * a + b] = (float)C[k][a][b];
+  cudaMemcpyAsync(m->poly, cf, sizeof(cf), cudaMemcpyHostToDevice, c->stream);
+  rc = sync_and_check(c, "aggregation polynomial");
+  if (!rc) m->poly_fresh = true;
+  return rc;
+}
+
+// v = NᵀN y for one sample in polynomial form (mpnn_refresh_poly first):
+// a1 = A y, a2 = A a1, u = mask ⊙ Σ C_k A^k y, then Horner for Nᵀ u.  Uses the
+// 3-channel scratch of the activation arena (B ≥ 1).
 void enqueue_mpnn_spd(Ctx* c, const float* y, float* v) {
-  enqueue_forward(c, 1, y, 0, false, c->mb.u);
-  enqueue_backward(c, 1, c->mb.u, 0, y, false, false, v);
+  const MpBufs& b = c->mb;
+  const float* P = c->mp->poly;
+  const unsigned g = grid_for(c->N, 256);
+  float *a1 = b.t3a, *a2 = b.t3b, *u = b.u, *h = b.w, *g2 = b.ghat;
+  k_mp_poly_fwd<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, y, nullptr, nullptr, P, c->mask,
+                                                  a1, nullptr);
+  k_mp_poly_fwd<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, a1, nullptr, nullptr, P,
+                                                  c->mask, a2, nullptr);
+  k_mp_poly_fwd<true><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, a2, y, a1, P, c->mask, u, h);
+  // h = C3ᵀu;  g2 = C2ᵀu + Aᵀh;  h = C1ᵀu + Aᵀg2;  v = C0ᵀu + Aᵀh
+  k_mp_poly_adj<<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 2, g2);
+  k_mp_poly_adj<<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, g2, u, P, 1, h);
+  k_mp_poly_adj<<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 0, v);
+  c->launches += 6;
 }
 
 // forward, loss and gradient for B pairs (y, sq [B][N][3], den [B]); the
@@ -822,6 +991,7 @@ int mpnn_train(Ctx* c, int epochs, int batch, double lr, uint64_t seed, double* 
     }
     if (losses) losses[ep] = ep_loss / (double)c->mp_pairs;
   }
+  m->poly_fresh = false;
   return sync_and_check(c, "training");
 }
 
@@ -854,6 +1024,7 @@ int mpnn_precondition(Ctx* c, const double* r_h, double* z_h) {
   if (rc) return rc;
   if ((rc = jacobi_diag_device(c, c->dinv))) return rc;
   if ((rc = mpnn_ensure_act(c, 1))) return rc;
+  if ((rc = mpnn_refresh_poly(c))) return rc;
   const int64_t n3 = 3 * c->N;
   cudaMemcpyAsync(c->tmp, r_h, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
   k_mp_input_d<<<grid_for(n3, 256), 256, 0, c->stream>>>(c->N, c->tmp, c->dinv, c->mask, c->mb.y);

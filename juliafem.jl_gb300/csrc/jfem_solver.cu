@@ -765,6 +765,7 @@ static int fcg(Ctx* c, const double* f, bool nn, double tol, int max_iter, doubl
   if (!apply_is_tiled(c)) return set_err(c, JFEM_ERR_INVALID, "flexible CG needs the tiled apply");
   if (nn && (!c->mp || !c->mp->ready)) return set_err(c, JFEM_ERR_INVALID, "no network weights (jfem_mpnn_init)");
   if (nn && (rc = mpnn_ensure_act(c, 1))) return rc;
+  if (nn && (rc = mpnn_refresh_poly(c))) return rc;
   if (!c->zf && (rc = dalloc(c, &c->zf, (size_t)n))) return rc;
   if (x_zero) {
     k_residual<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, f, 1.0, nullptr, c->mask, c->r, 0, c->part);
