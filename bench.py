@@ -53,6 +53,12 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-div", type=int, default=4, help="CPU sample = 1/div of the cubes along x")
     p.add_argument("--cpu-sample-iters", type=int, default=200)
+    p.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner leg")
+    p.add_argument("--learned-train", type=int, default=64, help="training systems of the Tet10 family")
+    p.add_argument("--learned-eval", type=int, default=16, help="unseen evaluation systems")
+    p.add_argument("--learned-epochs", type=int, default=60)
+    p.add_argument("--no-batch", action="store_true", help="skip the batched-solves leg")
+    p.add_argument("--batch-count", type=int, default=256)
     return p.parse_args()
 
 
@@ -145,6 +151,110 @@ def workload_config(size):
             "dofs": 3 * (2 * nx + 1) * (2 * ny + 1) * (2 * nz + 1), "solver": "Jacobi-PCG",
             "tol": TOL, "apply": "matrix-free FP32, FP64 vectors/dots/residual",
             "l2": "flushed before every step (256 MiB write)"}
+
+
+# ---------------------------------------------------------------------------
+# learned preconditioner leg
+# ---------------------------------------------------------------------------
+def _set_system(ctx, w, mesh=True):
+    m = w.mesh
+    if mesh:
+        ctx.set_mesh(m.elem_type, m.X, m.conn)
+    ctx.set_material(w.E, w.nu)
+    if mesh:
+        ctx.set_dirichlet(w.fixed_dofs, w.fixed_values)
+    ctx.set_traction(w.face_type, w.faces, w.traction)
+
+
+def learned_leg(jfem, args, device, big_workload):
+    """Train the network on solver-generated pairs of the Tet10 family (40×4×4
+    cubes on [0,10]×[0,1]², lognormal E with σ_log 0.5, random surface-patch
+    tractions), then time Jacobi-PCG and learned flexible CG to the FP64
+    relative residual 1e-8 on unseen seeds of the family and on the 2M-DOF
+    cantilever.  Times are host wall clock around a synchronous solve (second
+    of two runs)."""
+    abi = jfem._abi
+    fam = jfem.workloads.learned_family(args.learned_train, seed_item=40)
+    ev = jfem.workloads.learned_family(args.learned_eval, seed_item=40 + 100000)
+
+    def timed(ctx, method):
+        o = jfem.default_opts(method=method, precision=abi.MIXED, tol=TOL, max_iter=500000)
+        ctx.solve(o)
+        t0 = time.perf_counter()
+        _, st, rc = ctx.solve(o)
+        dt = time.perf_counter() - t0
+        if rc not in (0, abi.STALL):
+            raise RuntimeError(f"solve did not converge: status {rc}")
+        return st.cg_iterations, dt, st.fallbacks
+
+    out = {}
+    with jfem.Context(device) as ctx:
+        _set_system(ctx, fam[0])
+        ctx.mpnn_init(3)
+        t0 = time.perf_counter()
+        for w in fam:
+            _set_system(ctx, w, mesh=False)
+            pairs = ctx.mpnn_collect(8, 1e-10)
+        t1 = time.perf_counter()
+        l1 = ctx.mpnn_train(args.learned_epochs, 32, 3e-3, seed=1)
+        l2 = ctx.mpnn_train(args.learned_epochs, 32, 1e-3, seed=2)
+        t2 = time.perf_counter()
+        trained = ctx.mpnn_get_weights()
+        rows = []
+        for w in ev:
+            _set_system(ctx, w, mesh=False)
+            rows.append(timed(ctx, abi.PCG_JACOBI) + timed(ctx, abi.FCG_LEARNED))
+        r = np.array(rows, dtype=np.float64)
+        out["family"] = {"workload": "tet10_cantilever_40x4x4 family (19,683 DOFs)", "train_systems": len(fam),
+                         "pairs": int(pairs), "epochs": 2 * args.learned_epochs, "collect_s": t1 - t0,
+                         "train_s": t2 - t1, "loss_first": float(l1[0]), "loss_last": float(l2[-1]),
+                         "eval_systems": len(ev),
+                         "jacobi_pcg": {"iterations": float(r[:, 0].mean()), "s": float(r[:, 1].mean())},
+                         "learned_fcg": {"iterations": float(r[:, 3].mean()), "s": float(r[:, 4].mean()),
+                                         "fallbacks": int(r[:, 5].sum())},
+                         "iteration_ratio": float(r[:, 0].mean() / r[:, 3].mean()),
+                         "wall_time_ratio": float(r[:, 1].mean() / r[:, 4].mean())}
+        _set_system(ctx, big_workload)
+        ctx.mpnn_set_weights(trained)
+        pj = timed(ctx, abi.PCG_JACOBI)
+        pl = timed(ctx, abi.FCG_LEARNED)
+        out["tet10_2M"] = {"jacobi_pcg": {"iterations": pj[0], "s": pj[1]},
+                           "learned_fcg": {"iterations": pl[0], "s": pl[1], "fallbacks": pl[2]},
+                           "wall_time_ratio": pj[1] / pl[1]}
+    return out
+
+
+# ---------------------------------------------------------------------------
+# batched solves leg
+# ---------------------------------------------------------------------------
+def batch_leg(jfem, args, device):
+    """256 uneven Tet4 cantilevers (n ~ U{8..32} cubes along x, n/4 across;
+    E ~ U[50e3, 300e3], ν ~ U[0.2, 0.45], random end traction) solved by
+    Jacobi-PCG to the FP64 relative residual 1e-8 in one persistent,
+    graph-captured launch; launch configuration from the autotuner.  solves/s
+    = instances ÷ launch time (CUDA events, mean of `steps` launches after the
+    autotuning launches); latency = per-instance time on the GPU."""
+    ws = jfem.workloads.batch_instances(count=args.batch_count, nmin=8, nmax=32, seed_item=5)
+    with jfem.Batch(device) as b:
+        for w in ws:
+            b.add_workload(w)
+        t0 = time.perf_counter()
+        b.solve(tol=TOL, max_iter=200000, block_size=0)          # autotune + first solve
+        t_tune = time.perf_counter() - t0
+        bs, grid = b.config()
+        times, lats, its, ok = [], [], None, True
+        for _ in range(max(1, args.steps)):
+            _, its, st, res, lat, t = b.solve(tol=TOL, max_iter=200000, block_size=bs)
+            times.append(t)
+            lats.append(lat)
+            ok = ok and bool(np.all(st == 0)) and bool(np.all(res <= TOL))
+    t = statistics.mean(times)
+    lat = np.concatenate(lats)
+    dofs = [w.mesh.n_dofs for w in ws]
+    return {"workload": f"{len(ws)} Tet4 cantilevers, n ~ U{{8..32}} (DOFs {min(dofs)}..{max(dofs)})",
+            "solves_per_s": len(ws) / t, "launch_ms": t * 1e3, "p50_latency_ms": float(np.percentile(lat, 50)) * 1e3,
+            "p99_latency_ms": float(np.percentile(lat, 99)) * 1e3, "block_size": bs, "grid": grid,
+            "autotune_s": t_tune, "iterations_mean": float(np.mean(its)), "all_converged": ok}
 
 
 # ---------------------------------------------------------------------------
@@ -318,6 +428,10 @@ def run_gpu(args):
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                 "gpu_launches": int(launches),
                 "clocks": clk}
+        if ws == 1 and not args.no_batch:
+            line["batched"] = batch_leg(jfem, args, local)
+        if ws == 1 and not args.no_learned:
+            line["learned_preconditioner"] = learned_leg(jfem, args, local, w)
         if ws == 1 and not args.no_cpu_baseline:
             cb = cpu_sample(jfem, args.size, args.cpu_sample_div, args.cpu_sample_iters)
             line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

@@ -218,6 +218,34 @@ int jfem_mpnn_loss_grad(jfem_ctx* ctx, const double* r, const double* e, double*
 /* z = D⁻¹r + s·o(x) for a host residual r (3 n_nodes), through the inference kernels. */
 int jfem_mpnn_precondition(jfem_ctx* ctx, const double* r, double* z);
 
+/* ------------------------------------------------------------------------
+ * Batched solves: many small independent linear-elastic Tet4 problems solved
+ * by Jacobi-PCG to an FP64 relative residual in one persistent, graph-captured
+ * launch (one CTA per instance at a time, instances taken largest first).  No
+ * counterpart in the reference, which runs one solve! per problem
+ * (src/solvers.jl:273-344).  Instances: mesh (X 3 × n_nodes, conn 4 × n_elem,
+ * numbers from index_base), E and nu, prescribed DOFs (value zero) and a
+ * constant traction t (3 × n_faces) on Tri3 faces (face_conn 3 × n_faces),
+ * integrated consistently (problems_elasticity.jl:454-502).  jfem_batch_add
+ * returns the instance number (≥ 0) or an error. */
+typedef struct jfem_batch jfem_batch;
+int jfem_batch_create(jfem_batch** out, int device_ordinal);
+int jfem_batch_destroy(jfem_batch* batch);
+const char* jfem_batch_last_error(const jfem_batch* batch);
+int jfem_batch_add(jfem_batch* batch, int64_t n_nodes, const double* X, int64_t n_elem, const int64_t* conn,
+                   int index_base, double E, double nu, int64_t n_fixed, const int64_t* fixed_dofs,
+                   int64_t n_faces, const int64_t* face_conn, const double* t);
+/* Solve every instance to tol.  block_size 0 = autotune (block size and CTAs
+ * per SM timed on the whole batch, fastest kept), else 128/256/512/1024.
+ * Outputs (each may be NULL): u (3 × total nodes, instances in order),
+ * per-instance iterations, status (0 / JFEM_NOT_CONVERGED), final relative
+ * residual and latency (seconds from the instance's start to its end on the
+ * GPU); solve_s = the launch's CUDA-event time. */
+int jfem_batch_solve(jfem_batch* batch, double tol, int max_iter, int block_size, double* u, int* iterations,
+                     int* status, double* residual, double* latency_s, double* solve_s);
+/* Launch configuration of the last solve (the autotuner's choice when it ran). */
+int jfem_batch_config(const jfem_batch* batch, int* block_size, int* grid);
+
 /* Kernels launched by the library on this context since its creation. */
 int64_t jfem_kernel_launches(const jfem_ctx* ctx);
 /* Event-timed duration (ms) of the last matrix-free apply launch sequence. */

@@ -8,7 +8,7 @@ The directory name contains a dot, so it is loaded by path; ``load_package()``
 in __graft_entry__.py (and tests/conftest.py) registers it as ``jfem_gb300``.
 """
 from . import _abi, abaqus, mesh, workloads
-from ._abi import Context, JFEMError, SolveOpts, Stats, default_opts, load
+from ._abi import Batch, Context, JFEMError, SolveOpts, Stats, default_opts, load
 from .problem import (CPU, GPU, Analysis, Auto, Dirichlet, DirichletBC, Elasticity, ElasticitySolution,
                       Element, Hex8, Linear, NeumannBC, Physics, Problem, Quad4, Tet4, Tet10, Tri3, Tri6,
                       add_dirichlet_, add_elements_, add_neumann_, add_problems_, assemble_, get_gdofs,

@@ -96,6 +96,14 @@ SIGNATURES = {
     "jfem_mpnn_train": (C.c_int, [_P, C.c_int, C.c_int, C.c_double, C.c_uint64, _f64p]),
     "jfem_mpnn_loss_grad": (C.c_int, [_P, _f64p, _f64p, _f64p, _f32p]),
     "jfem_mpnn_precondition": (C.c_int, [_P, _f64p, _f64p]),
+    "jfem_batch_create": (C.c_int, [C.POINTER(_P), C.c_int]),
+    "jfem_batch_destroy": (C.c_int, [_P]),
+    "jfem_batch_last_error": (C.c_char_p, [_P]),
+    "jfem_batch_add": (C.c_int, [_P, _i64, _f64p, _i64, _i64p, C.c_int, C.c_double, C.c_double, _i64, _i64p,
+                                 _i64, _i64p, _f64p]),
+    "jfem_batch_solve": (C.c_int, [_P, C.c_double, C.c_int, C.c_int, _f64p, C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int), _f64p, _f64p, _f64p]),
+    "jfem_batch_config": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
 }
 
 _lib = None
@@ -317,3 +325,76 @@ class Context:
         flags = (APPLY_FP32 if fp32 else 0) | (APPLY_MASKED if masked else 0)
         self._check(self._lib.jfem_time_apply(self._h, flags, int(reps), C.byref(a), C.byref(b)))
         return a.value, b.value
+
+
+class Batch:
+    """Many small independent Tet4 solves in one persistent launch (jfem_batch_*)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        h = C.c_void_p()
+        rc = self._lib.jfem_batch_create(C.byref(h), int(device))
+        if rc != 0:
+            raise JFEMError(rc, "jfem_batch_create failed (no usable CUDA device?)")
+        self._h = h
+        self.node_counts = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.jfem_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int) -> int:
+        if rc < 0:
+            raise JFEMError(rc, self._lib.jfem_batch_last_error(self._h).decode())
+        return rc
+
+    def add(self, X, conn, E: float, nu: float, fixed_dofs, face_conn, t, index_base: int = 0) -> int:
+        X = np.ascontiguousarray(X, dtype=np.float64).reshape(-1, 3)
+        conn = np.ascontiguousarray(conn, dtype=np.int64).reshape(-1, 4)
+        fd = np.ascontiguousarray(fixed_dofs, dtype=np.int64)
+        fc = np.ascontiguousarray(face_conn, dtype=np.int64).reshape(-1, 3)
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(t, dtype=np.float64), (fc.shape[0], 3)))
+        k = self._check(self._lib.jfem_batch_add(self._h, X.shape[0], _ptr(X, _f64p), conn.shape[0], _ptr(conn, _i64p),
+                                                 index_base, float(E), float(nu), fd.size, _ptr(fd, _i64p),
+                                                 fc.shape[0], _ptr(fc, _i64p), _ptr(t, _f64p)))
+        self.node_counts.append(X.shape[0])
+        return k
+
+    def add_workload(self, w) -> int:
+        return self.add(w.mesh.X, w.mesh.conn, w.E, w.nu, w.fixed_dofs, w.faces, w.traction)
+
+    def solve(self, tol: float = 1e-8, max_iter: int = 100000, block_size: int = 0):
+        """Returns (list of u per instance, iterations, status, residual, latency_s, solve_s)."""
+        n = len(self.node_counts)
+        tot = 3 * sum(self.node_counts)
+        u = np.empty(tot)
+        it = np.empty(n, np.int32)
+        stv = np.empty(n, np.int32)
+        res = np.empty(n)
+        lat = np.empty(n)
+        t = C.c_double(0)
+        self._check(self._lib.jfem_batch_solve(self._h, float(tol), int(max_iter), int(block_size), _ptr(u, _f64p),
+                                               it.ctypes.data_as(C.POINTER(C.c_int)),
+                                               stv.ctypes.data_as(C.POINTER(C.c_int)), _ptr(res, _f64p),
+                                               _ptr(lat, _f64p), C.byref(t)))
+        offs = np.concatenate([[0], np.cumsum(3 * np.asarray(self.node_counts))])
+        us = [u[offs[k]:offs[k + 1]] for k in range(n)]
+        return us, it, stv, res, lat, t.value
+
+    def config(self):
+        bs, g = C.c_int(0), C.c_int(0)
+        self._check(self._lib.jfem_batch_config(self._h, C.byref(bs), C.byref(g)))
+        return bs.value, g.value

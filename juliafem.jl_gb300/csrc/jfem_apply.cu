@@ -122,6 +122,12 @@ __global__ void k_prepare_geo(int64_t E, const int* __restrict__ conn, const dou
   }
 }
 
+// Affine Tet4 records for a concatenated batch of meshes (jfem_batch.cu).
+void prepare_geo_tet4_affine(int64_t E, const int* conn, const double* X, const double* lam, const double* mu,
+                             double* g64, float* g32, cudaStream_t stream) {
+  k_prepare_geo<JFEM_TET4><<<grid_for(E, 128), 128, 0, stream>>>(E, conn, X, lam, mu, 1, g64, g32);
+}
+
 // ---------------------------------------------------------------------------
 // phase 2: node gather (ascending element order), masking and optional v·y partials.
 // One thread per node (GATHER_GL = 1; with GL > 1 lanes split a node's entries

@@ -375,6 +375,8 @@ void enqueue_apply_tiled(Ctx* c, const float2* v2, float* y, bool masked, double
                          SolverScalars* sc = nullptr);
 void enqueue_internal_force(Ctx* c, double* f);
 int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, double* partial_pAp);
+void prepare_geo_tet4_affine(int64_t E, const int* conn, const double* X, const double* lam, const double* mu,
+                             double* g64, float* g32, cudaStream_t stream);
 int internal_force_device(Ctx* c, double* f_d);
 int time_apply(Ctx* c, bool fp32, bool masked, int reps, double* ms_elem, double* ms_gather);
 // jfem_mpnn.cu

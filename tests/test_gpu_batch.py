@@ -1,0 +1,67 @@
+"""Batched persistent solves (jfem_batch_*) against the oracle's direct solves."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_u(orc, w):
+    m = w.mesh
+    cp, rv, nz, _ = orc.assemble_coo(4, m.X, m.conn, w.E, w.nu)
+    f = orc.traction(w.face_type, w.faces, m.X, w.traction)
+    return orc.direct_solve(cp, rv, nz, f, w.fixed_mask().astype(bool))
+
+
+def test_batch_matches_oracle_and_is_deterministic(jfem, orc):
+    """Uneven Tet4 cantilevers (8..14 cubes along x, random E, ν, end traction)
+    solved together to 1e-10: each displacement within 1e-8 of the oracle's
+    direct solve; a second launch gives identical bits."""
+    ws = jfem.workloads.batch_instances(count=12, nmin=8, nmax=14, seed_item=77)
+    with jfem.Batch(0) as b:
+        for k, w in enumerate(ws):
+            assert b.add_workload(w) == k
+        us, it, st, res, lat, t = b.solve(tol=1e-10, max_iter=50000, block_size=256)
+        us2, it2, *_ = b.solve(tol=1e-10, max_iter=50000, block_size=256)
+    assert np.all(st == 0) and np.all(res <= 1e-10) and np.all(it > 0)
+    assert np.all(lat > 0) and t > 0 and lat.max() <= t * 1.01
+    for w, u in zip(ws, us):
+        assert rel_err(u, _oracle_u(orc, w)) <= 1e-8
+        assert np.all(u[w.fixed_dofs] == 0.0)
+    assert all(np.array_equal(a, c) for a, c in zip(us, us2)) and np.array_equal(it, it2)
+
+
+def test_batch_autotune_and_block_sizes_agree(jfem):
+    ws = jfem.workloads.batch_instances(count=6, nmin=8, nmax=10, seed_item=78)
+    with jfem.Batch(0) as b:
+        for w in ws:
+            b.add_workload(w)
+        ref, *_ = b.solve(tol=1e-9, block_size=128)
+        for bs in (512, 1024):
+            us, _, st, *_ = b.solve(tol=1e-9, block_size=bs)
+            assert np.all(st == 0)
+            for a, c in zip(us, ref):
+                assert rel_err(a, c) <= 1e-7
+        us, _, st, *_ = b.solve(tol=1e-9, block_size=0)
+        bs, grid = b.config()
+        assert bs in (128, 256, 512, 1024) and 1 <= grid <= len(ws)
+        assert np.all(st == 0)
+
+
+def test_batch_rejects_invalid_instances(jfem):
+    w = jfem.workloads.batch_instances(count=1, nmin=8, nmax=8, seed_item=79)[0]
+    m = w.mesh
+    with jfem.Batch(0) as b:
+        bad = m.conn.copy()
+        bad[0, 0] = m.n_nodes + 5
+        with pytest.raises(jfem.JFEMError):
+            b.add(m.X, bad, w.E, w.nu, w.fixed_dofs, w.faces, w.traction)
+        flipped = m.conn.copy()
+        flipped[:, [1, 2]] = flipped[:, [2, 1]]
+        with pytest.raises(jfem.JFEMError):
+            b.add(m.X, flipped, w.E, w.nu, w.fixed_dofs, w.faces, w.traction)
+        with pytest.raises(jfem.JFEMError):
+            b.add(m.X, m.conn, -1.0, w.nu, w.fixed_dofs, w.faces, w.traction)
+        with pytest.raises(jfem.JFEMError):
+            b.solve()                    # nothing added
