@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--learned-eval", type=int, default=16, help="unseen evaluation systems")
     p.add_argument("--learned-epochs", type=int, default=60)
     p.add_argument("--no-batch", action="store_true", help="skip the batched-solves leg")
+    p.add_argument("--no-newton", action="store_true", help="skip the Newton–Krylov leg")
+    p.add_argument("--newton-n", type=int, default=128, help="Hex8 cells per side of the Newton cube")
     p.add_argument("--batch-count", type=int, default=256)
     return p.parse_args()
 
@@ -222,6 +224,43 @@ def learned_leg(jfem, args, device, big_workload):
                            "learned_fcg": {"iterations": pl[0], "s": pl[1], "fallbacks": pl[2]},
                            "wall_time_ratio": pj[1] / pl[1]}
     return out
+
+
+# ---------------------------------------------------------------------------
+# Newton–Krylov leg
+# ---------------------------------------------------------------------------
+def newton_leg(jfem, args, device):
+    """Hex8 Neo-Hookean unit cube, n³ cells (128³: 2,097,152 elements,
+    6,440,067 DOFs), 2×2×2 Gauss, per-element E = 210e3·exp(0.2 z) (seeded),
+    ν = 0.3, bottom clamped, top u_z ramped to −0.1 over 10 load steps;
+    Newton–Krylov with the FP32 tiled tangent apply, double-float PCG vectors,
+    FP64 residuals and Eisenstat–Walker forcing, Newton tol 1e-8.  One timed
+    solve (CUDA events on the context stream) after the mesh is resident."""
+    import torch
+    w = jfem.workloads.cube_compression(n=args.newton_n, steps=10)
+    m = w.mesh
+    abi = jfem._abi
+    with jfem.Context(device) as ctx:
+        ctx.set_mesh(m.elem_type, m.X, m.conn)
+        ctx.set_material(w.E, w.nu, w.model)
+        ctx.set_formulation(True, True)
+        ctx.set_dirichlet(w.fixed_dofs, w.fixed_values)
+        o = jfem.default_opts(method=abi.NEWTON, precision=abi.MIXED, tol=1e-8, newton_tol=1e-8, max_newton=30,
+                              max_cg_per_newton=50000, n_load_steps=10, max_iter=50000)
+        dev = torch.device("cuda", device)
+        u = torch.empty(m.n_dofs, dtype=torch.float64, device=dev)
+        stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        st, rc = ctx.solve_device(u.data_ptr(), o)
+        e1.record(stream)
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+    return {"workload": f"hex8_neohookean_{args.newton_n}^3", "elements": m.n_elem, "dofs": m.n_dofs,
+            "load_steps": 10, "status": int(rc), "newton_iterations": int(st.newton_iterations),
+            "cg_iterations": int(st.cg_iterations), "refinements": int(st.refinements),
+            "final_relative_residual": float(st.residual), "s": t, "s_per_load_step": t / 10}
 
 
 # ---------------------------------------------------------------------------
@@ -428,6 +467,8 @@ def run_gpu(args):
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                 "gpu_launches": int(launches),
                 "clocks": clk}
+        if ws == 1 and not args.no_newton:
+            line["newton"] = newton_leg(jfem, args, local)
         if ws == 1 and not args.no_batch:
             line["batched"] = batch_leg(jfem, args, local)
         if ws == 1 and not args.no_learned:

@@ -991,6 +991,10 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
         c->launches += 1;
       }
       double eta = std::pow(last_rel, o->forcing_power);
+      // An iteration that only carries a prescribed-value increment (‖R‖ = 0)
+      // has no residual to scale the forcing term by; solve it to 1e-2 instead
+      // of to the floor (Newton corrects the rest in the next iteration).
+      if (first && dgg > 0.0 && !(rn > 0.0)) eta = 1e-2;
       if (eta > o->forcing_max) eta = o->forcing_max;
       if (eta < 1e-12) eta = 1e-12;
       cudaMemsetAsync(c->x, 0, n * sizeof(double), c->stream);
