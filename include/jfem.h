@@ -246,6 +246,15 @@ int jfem_batch_solve(jfem_batch* batch, double tol, int max_iter, int block_size
 /* Launch configuration of the last solve (the autotuner's choice when it ran). */
 int jfem_batch_config(const jfem_batch* batch, int* block_size, int* grid);
 
+/* Reverse Cuthill–McKee renumbering of the mesh's node graph (nodes sharing an
+ * element), as symrcm in src/graph/graph_ordering.jl:21-98: search from node
+ * `start`, neighbours in increasing-degree order, reversed.  perm[k] (n_nodes,
+ * numbers from index_base) is the old node placed at new position k.  The
+ * bandwidths 2·max|v−w|+1 before and after (graph_ordering.jl:21-29) may be
+ * NULL.  Host code; needs no device. */
+int jfem_rcm(int64_t n_nodes, int64_t n_elem, int nodes_per_elem, const int64_t* conn, int index_base,
+             int64_t start, int64_t* perm, int64_t* bandwidth_before, int64_t* bandwidth_after);
+
 /* Kernels launched by the library on this context since its creation. */
 int64_t jfem_kernel_launches(const jfem_ctx* ctx);
 /* Event-timed duration (ms) of the last matrix-free apply launch sequence. */

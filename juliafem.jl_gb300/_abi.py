@@ -104,6 +104,7 @@ SIGNATURES = {
     "jfem_batch_solve": (C.c_int, [_P, C.c_double, C.c_int, C.c_int, _f64p, C.POINTER(C.c_int),
                                    C.POINTER(C.c_int), _f64p, _f64p, _f64p]),
     "jfem_batch_config": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "jfem_rcm": (C.c_int, [_i64, _i64, C.c_int, _i64p, C.c_int, _i64, _i64p, _i64p, _i64p]),
 }
 
 _lib = None
@@ -398,3 +399,17 @@ class Batch:
         bs, g = C.c_int(0), C.c_int(0)
         self._check(self._lib.jfem_batch_config(self._h, C.byref(bs), C.byref(g)))
         return bs.value, g.value
+
+
+def rcm(conn, n_nodes: int, start: int = 0, index_base: int = 0):
+    """Reverse Cuthill–McKee order of the node graph (jfem_rcm): returns
+    (perm, bandwidth_before, bandwidth_after); perm[k] = old node at position k."""
+    conn = np.ascontiguousarray(conn, dtype=np.int64)
+    nen = conn.shape[1] if conn.ndim == 2 else 1
+    perm = np.empty(n_nodes, np.int64)
+    b0, b1 = C.c_int64(0), C.c_int64(0)
+    rc = load().jfem_rcm(int(n_nodes), conn.shape[0], nen, _ptr(conn, _i64p), index_base, int(start),
+                         _ptr(perm, _i64p), C.byref(b0), C.byref(b1))
+    if rc != 0:
+        raise JFEMError(rc, "jfem_rcm: invalid arguments")
+    return perm, b0.value, b1.value

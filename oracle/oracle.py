@@ -283,3 +283,40 @@ def newton(et, X, conn, E, nu, fixed, g_final, f_ext=None, n_steps=10, tol=1e-8,
             u += du
         its.append(k)
     return u, its
+
+
+def rcm(conn, n_nodes, start=0):
+    """Reverse Cuthill–McKee as symrcm of src/graph/graph_ordering.jl:21-98
+    (breadth-first from `start`, neighbours by increasing degree with a stable
+    sort, reversed), on the node graph with ascending adjacency lists; nodes
+    unreachable from `start` continue from the lowest unvisited node.
+    Pure Python: small graphs only."""
+    conn = np.asarray(conn, dtype=np.int64)
+    nb = [set() for _ in range(n_nodes)]
+    for el in conn:
+        for a in el:
+            nb[a].update(int(b) for b in el if b != a)
+    adj = [sorted(s) for s in nb]
+    deg = [len(a) for a in adj]
+    visited = [False] * n_nodes
+    order = []
+    s = start
+    while len(order) < n_nodes:
+        visited[s] = True
+        head = len(order)
+        order.append(s)
+        while head < len(order):
+            v = order[head]
+            head += 1
+            for w in sorted(adj[v], key=lambda j: deg[j]):      # stable: ties keep ascending order
+                if not visited[w]:
+                    visited[w] = True
+                    order.append(w)
+        rest = [k for k in range(n_nodes) if not visited[k]]
+        if rest:
+            s = rest[0]
+    perm = np.array(order[::-1], dtype=np.int64)
+    newpos = np.empty(n_nodes, np.int64)
+    newpos[perm] = np.arange(n_nodes)
+    bw = lambda pos: 2 * max(abs(int(pos[v]) - int(pos[w])) for v in range(n_nodes) for w in adj[v]) + 1
+    return perm, bw(np.arange(n_nodes)), bw(newpos)

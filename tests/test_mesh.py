@@ -99,3 +99,22 @@ def test_abaqus_reader_reference_fixture(jfem):
     import numpy as np
     d = np.load(Path(__file__).parent / "golden" / "cube_tet4.npz")
     assert np.array_equal(d["X"], X) and np.array_equal(d["conn"], conn)
+
+
+def test_rcm_matches_reference_restatement(jfem, orc):
+    """jfem_rcm (C++ in the library) against the Python restatement of the
+    reference's symrcm, on a shuffled Tet10 box and a mesh with two parts."""
+    m = jfem.mesh.box_mesh(10, 4, 2, 2, 2.0, 1.0, 1.0)
+    g = np.random.default_rng(5)
+    shuffle = g.permutation(m.n_nodes)
+    conn = shuffle[m.conn]                       # scramble the numbering
+    perm, b0, b1 = jfem._abi.rcm(conn, m.n_nodes, start=int(shuffle[0]))
+    op, ob0, ob1 = orc.rcm(conn, m.n_nodes, start=int(shuffle[0]))
+    assert np.array_equal(perm, op) and (b0, b1) == (ob0, ob1)
+    assert sorted(perm) == list(range(m.n_nodes)) and b1 < b0 / 2
+    two = np.concatenate([m.conn, m.conn + m.n_nodes])
+    perm2, _, _ = jfem._abi.rcm(two, 2 * m.n_nodes, start=3)
+    op2, _, _ = orc.rcm(two, 2 * m.n_nodes, start=3)
+    assert np.array_equal(perm2, op2)
+    perm1, _, _ = jfem._abi.rcm(conn + 1, m.n_nodes, start=int(shuffle[0]) + 1, index_base=1)
+    assert np.array_equal(perm1, perm + 1)
