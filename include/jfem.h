@@ -246,6 +246,18 @@ int jfem_batch_solve(jfem_batch* batch, double tol, int max_iter, int block_size
 /* Launch configuration of the last solve (the autotuner's choice when it ran). */
 int jfem_batch_config(const jfem_batch* batch, int* block_size, int* grid);
 
+/* Nodal strain or stress by a least-squares fit (postprocess!(problem, time,
+ * Val{:strain} / Val{:stress}) with lsq_fit, src/problems_elasticity.jl:521-594):
+ * the integration-point field of the displacement u (3 n_nodes, host) —
+ * small strain ε = sym ∇u or σ = λ tr(ε) I + 2μ ε, order 11, 22, 33, 12, 23, 13,
+ * tensor shear — projected onto the nodal shape functions.  The mass-matrix
+ * system is solved in FP64 by Jacobi-PCG on its six columns to the relative
+ * residual tol (the reference factorises it).  nodal: 6 × n_nodes (host). */
+#define JFEM_FIELD_STRAIN 0
+#define JFEM_FIELD_STRESS 1
+int jfem_recover_field(jfem_ctx* ctx, const double* u, int field, double tol, int max_iter, double* nodal,
+                       int* iterations);
+
 /* Reverse Cuthill–McKee renumbering of the mesh's node graph (nodes sharing an
  * element), as symrcm in src/graph/graph_ordering.jl:21-98: search from node
  * `start`, neighbours in increasing-degree order, reversed.  perm[k] (n_nodes,

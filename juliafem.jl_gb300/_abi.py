@@ -105,6 +105,7 @@ SIGNATURES = {
                                    C.POINTER(C.c_int), _f64p, _f64p, _f64p]),
     "jfem_batch_config": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "jfem_rcm": (C.c_int, [_i64, _i64, C.c_int, _i64p, C.c_int, _i64, _i64p, _i64p, _i64p]),
+    "jfem_recover_field": (C.c_int, [_P, _f64p, C.c_int, C.c_double, C.c_int, _f64p, C.POINTER(C.c_int)]),
 }
 
 _lib = None
@@ -276,6 +277,16 @@ class Context:
     @property
     def stream(self) -> int:
         return int(self._lib.jfem_stream(self._h) or 0)
+
+    def recover_field(self, u, field: int = 1, tol: float = 1e-12, max_iter: int = 10000):
+        """Nodal strain (field 0) or stress (field 1) by the least-squares fit:
+        array [n_nodes, 6] (11, 22, 33, 12, 23, 13)."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        out = np.empty((self.n_nodes, 6))
+        it = C.c_int(0)
+        self._check(self._lib.jfem_recover_field(self._h, _ptr(u, _f64p), int(field), float(tol), int(max_iter),
+                                                 _ptr(out, _f64p), C.byref(it)))
+        return out
 
     # -- learned preconditioner ---------------------------------------------------
     def mpnn_init(self, seed: int = 0):

@@ -374,6 +374,18 @@ int jfem_solve(jfem_ctx* h, const jfem_solve_opts* opts, double* u, jfem_stats* 
   return rc;
 }
 
+int jfem_recover_field(jfem_ctx* h, const double* u, int field, double tol, int max_iter, double* nodal,
+                       int* iterations) {
+  ENTER(h);
+  Ctx* c = &h->c;
+  if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
+  if (!u || !nodal) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL array");
+  if (field != JFEM_FIELD_STRAIN && field != JFEM_FIELD_STRESS)
+    return jfem::set_err(c, JFEM_ERR_INVALID, "field must be JFEM_FIELD_STRAIN or JFEM_FIELD_STRESS");
+  if (!(tol > 0.0) || max_iter <= 0) return jfem::set_err(c, JFEM_ERR_INVALID, "tol and max_iter must be positive");
+  return jfem::recover_field(c, u, field, tol, max_iter, nodal, iterations);
+}
+
 int jfem_mpnn_init(jfem_ctx* h, uint64_t seed) {
   ENTER(h);
   return jfem::mpnn_init(&h->c, seed);

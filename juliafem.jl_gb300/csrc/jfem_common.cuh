@@ -391,6 +391,8 @@ int mpnn_precondition(Ctx* c, const double* r, double* z);
 int mpnn_ensure_act(Ctx* c, int64_t B);
 int mpnn_refresh_poly(Ctx* c);
 void enqueue_mpnn_spd(Ctx* c, const float* y, float* v);   // v = NᵀN y for one sample (y, v: [N][3])
+// jfem_recovery.cu
+int recover_field(Ctx* c, const double* u_h, int field, double tol, int max_iter, double* nodal_h, int* iters_out);
 // jfem_solver.cu
 int pcg_fp64_snapshots(Ctx* c, const double* f, double tol, int max_iter, double* snaps, int max_snaps,
                        int* n_snaps, int* snap_iters, int* iters_out, double* relres_out);

@@ -192,3 +192,69 @@ def traction(ft, fconn, X, t):
         contrib = (wq * area)[:, None, None] * t[:, None, :] * N[None, :, None]
         np.add.at(f, (3 * fconn[:, :, None] + np.arange(3)).ravel(), contrib.ravel())
     return f
+
+
+def mass_rule(et):
+    """Rules exact for N·Nᵀ: GLTET4 (Tet4), GLTET15 (Tet10, the points and
+    weights of src/quadrature/gltet.jl:46-63), GLHEX8 (Hex8)."""
+    if et == 4:
+        return rule(10)
+    if et == 8:
+        return rule(8)
+    s15 = np.sqrt(15.0)
+    a = 0.25
+    b1, b2 = (7 + s15) / 34, (7 - s15) / 34
+    c1, c2 = (13 - 3 * s15) / 34, (13 + 3 * s15) / 34
+    d, f = (5 - s15) / 20, (5 + s15) / 20
+    w1, w2, w3, w4 = 8 / 405, (2665 - 14 * s15) / 226800, (2665 + 14 * s15) / 226800, 5 / 567
+    pts = [(a, a, a), (b1, b1, b1), (b1, b1, c1), (b1, c1, b1), (c1, b1, b1), (b2, b2, b2), (b2, b2, c2),
+           (b2, c2, b2), (c2, b2, b2), (d, d, f), (d, f, d), (f, d, d), (d, f, f), (f, d, f), (f, f, d)]
+    return np.array(pts), np.array([w1] + [w2] * 4 + [w3] * 4 + [w4] * 6)
+
+
+def lsq_fit(et, X, conn, E, nu, u, field):
+    """Least-squares nodal fit of the small-strain strain (field 0) or stress
+    (field 1) vector (order 11, 22, 33, 12, 23, 13, tensor shear components) as
+    lsq_fit + get_strain_vector / get_stress_vector of
+    src/problems_elasticity.jl:521-583: A = Σ w N Nᵀ, b = Σ w N f, A x = b on
+    the nodes the elements touch (scipy's spsolve standing in for ldlt).  The
+    integration uses mass_rule(et): the elements' own rules (GLTET1 / GLTET4)
+    make A singular on simplices, a defect not replicated."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    X = np.asarray(X, dtype=np.float64)
+    conn = np.asarray(conn, dtype=np.int64)
+    ne, nn = conn.shape
+    nnode = X.shape[0]
+    la, mu = lame(np.broadcast_to(E, (ne,)), np.broadcast_to(nu, (ne,)))
+    Xe = X[conn]
+    ue = np.asarray(u, dtype=np.float64).reshape(-1, 3)[conn]
+    pts, wts = mass_rule(et)
+    rows, cols, vals = [], [], []
+    b = np.zeros((nnode, 6))
+    I3 = np.eye(3)
+    for xi, wq in zip(pts, wts):
+        N, dN = basis(et, xi)
+        J = np.einsum("ak,eab->ekb", dN, Xe)
+        detJ = np.linalg.det(J)
+        g = np.einsum("ekl,al->eak", np.linalg.inv(J), dN)
+        gu = np.einsum("eai,eaj->eij", ue, g)
+        eps = 0.5 * (gu + gu.transpose(0, 2, 1))
+        if field == 0:
+            t = eps
+        else:
+            t = (la * np.trace(eps, axis1=1, axis2=2))[:, None, None] * I3 + 2 * mu[:, None, None] * eps
+        f = np.stack([t[:, 0, 0], t[:, 1, 1], t[:, 2, 2], t[:, 0, 1], t[:, 1, 2], t[:, 0, 2]], axis=1)
+        w = wq * detJ
+        for a in range(nn):
+            np.add.at(b, conn[:, a], (w * N[a])[:, None] * f)
+            for c in range(nn):
+                rows.append(conn[:, a])
+                cols.append(conn[:, c])
+                vals.append(w * N[a] * N[c])
+    A = sp.csc_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(nnode, nnode))
+    A = 0.5 * (A + A.T)
+    nz = np.unique(conn)
+    x = np.zeros((nnode, 6))
+    x[nz] = spla.spsolve(A[nz][:, nz].tocsc(), b[nz])
+    return x

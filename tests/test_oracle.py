@@ -133,3 +133,19 @@ def test_newton_oracle_golden(jfem, orc):
                         n_steps=5, tol=1e-10, max_newton=25, model=1)
     assert rel_err(u, d["u"]) < 1e-9
     assert max(its) <= 8
+
+
+@pytest.mark.parametrize("et", [4, 10, 8])
+def test_lsq_fit_reproduces_a_uniform_field(jfem, npo, et):
+    """The least-squares nodal fit (problems_elasticity.jl:554-583) of a linear
+    displacement field returns its constant strain and stress at every node."""
+    m = jfem.mesh.box_mesh(et, 3, 2, 2, 1.5, 1.0, 0.8)
+    Gd = np.array([[1e-3, 2e-4, -3e-4], [5e-4, -2e-3, 1e-4], [0.0, 3e-4, 1.5e-3]])
+    u = (m.X @ Gd.T).reshape(-1)
+    eps = 0.5 * (Gd + Gd.T)
+    la, mu = npo.lame(210e3, 0.3)
+    sig = la * np.trace(eps) * np.eye(3) + 2 * mu * eps
+    for field, t in ((0, eps), (1, sig)):
+        x = npo.lsq_fit(et, m.X, m.conn, 210e3, 0.3, u, field)
+        ref = np.array([t[0, 0], t[1, 1], t[2, 2], t[0, 1], t[1, 2], t[0, 2]])
+        assert np.abs(x - ref).max() <= 1e-10 * np.abs(ref).max()
