@@ -332,8 +332,9 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
 // ---------------------------------------------------------------------------
 // tiled FP32 apply (see jfem_tiles.cu).  One CTA of JFEM_TILE threads per tile
 // (persistent over tiles); dynamic shared memory, in this order:
-//   ye   [3·NN][T]   f32    element vectors of the tile
-//   sadj [T·NN]      u16    the tile's node → (element, local node) lists
+//   yxy  [NN][T]     float2 x, y components of the element vectors of the tile
+//   yz   [NN][T]     f32    their z components
+//   sadj [T·NN]      u16    the tile's node → slot (local node · T + element) lists
 //   sptr [Lmax+1]    u16    their offsets (padded to 8 entries)
 //   vs   [3·Lmax]    float2 (hi, lo) of the tile's nodes (masked DOFs zero)
 //   us   [3·Lmax]    f32    state u of the tile's nodes (finite strain only)
@@ -347,7 +348,7 @@ __host__ __device__ constexpr int tile_sptr_len(int Lmax) { return (Lmax + 8) & 
 
 template <int NN, bool NEED_U>
 __host__ __device__ constexpr size_t tile_smem_bytes(int Lmax) {
-  return (size_t)3 * NN * JFEM_TILE * sizeof(float) + (size_t)JFEM_TILE * NN * sizeof(uint16_t) +
+  return (size_t)NN * JFEM_TILE * (sizeof(float2) + sizeof(float)) + (size_t)JFEM_TILE * NN * sizeof(uint16_t) +
          (size_t)tile_sptr_len(Lmax) * sizeof(uint16_t) + (size_t)3 * Lmax * sizeof(float2) +
          (NEED_U ? (size_t)3 * Lmax * sizeof(float) : 0);
 }
@@ -365,8 +366,9 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? 4 : 1) k_tile_ap
   constexpr int NADJ = T * NN;   // adjacency entries per tile; NADJ·2 bytes is a multiple of 16
   constexpr bool NEED_U = (KIN != KIN_SMALL);
   extern __shared__ float4 smem_f4[];
-  float* ye = reinterpret_cast<float*>(smem_f4);
-  uint16_t* sadj = reinterpret_cast<uint16_t*>(ye + 3 * NN * T);
+  float2* yxy = reinterpret_cast<float2*>(smem_f4);
+  float* yz = reinterpret_cast<float*>(yxy + NN * T);
+  uint16_t* sadj = reinterpret_cast<uint16_t*>(yz + NN * T);
   uint16_t* sptr = sadj + NADJ;
   float2* vs = reinterpret_cast<float2*>(sptr + tile_sptr_len(Lmax));
   float* us = reinterpret_cast<float*>(vs + 3 * Lmax);
@@ -396,13 +398,15 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? 4 : 1) k_tile_ap
       for (int k = tid; k < NADJ / 8; k += T) dst[k] = __ldg(src + k);
     }
     for (int j = tid; j <= L; j += T) sptr[j] = __ldg(tadj_ptr + n0 + t + j);
-    for (int j = tid; j < 3 * L; j += T) {
-      const int ln = j / 3, c = j - 3 * (j / 3);
-      const int64_t g = __ldg(tnodes + n0 + ln);
-      float2 h = __ldg(v2 + 3 * g + c);
-      if (masked && ((__ldg(mask + g) >> c) & 1)) h = make_float2(0.f, 0.f);
-      vs[j] = h;
-      if (NEED_U) us[j] = (float)__ldg(u + 3 * g + c);
+    for (int j = tid; j < L; j += T) {   // one node per thread: its three (hi, lo) pairs
+      const int64_t g = __ldg(tnodes + n0 + j);
+      const uint8_t m = masked ? __ldg(mask + g) : (uint8_t)0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float2 h = __ldg(v2 + 3 * g + c);
+        vs[3 * j + c] = ((m >> c) & 1) ? make_float2(0.f, 0.f) : h;
+        if (NEED_U) us[3 * j + c] = (float)__ldg(u + 3 * g + c);
+      }
     }
     __syncthreads();
     if (valid) {
@@ -422,9 +426,10 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? 4 : 1) k_tile_ap
       if constexpr (AFFINE) ok &= element_op<ET, float, true, KIN, GEOM, 0>(dv, du, GeoRegs<float>{rec}, yl);
       else ok &= element_op<ET, float, false, KIN, GEOM, 0>(dv, du, GeoGlobal<float>{geo + e, Epad}, yl);
 #pragma unroll
-      for (int a = 0; a < NN; ++a)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) ye[(3 * a + c) * T + tid] = yl[a][c];
+      for (int a = 0; a < NN; ++a) {
+        yxy[a * T + tid] = make_float2(yl[a][0], yl[a][1]);
+        yz[a * T + tid] = yl[a][2];
+      }
     }
     __syncthreads();
     for (int j = tid; j < L; j += T) {
@@ -434,11 +439,11 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? 4 : 1) k_tile_ap
       float s0 = 0.f, s1 = 0.f, s2 = 0.f;
       const int k1 = sptr[j + 1];
       for (int k = sptr[j]; k < k1; ++k) {
-        const int pk = sadj[k];
-        const int le = pk >> 4, a = pk & 15;
-        s0 += ye[(3 * a + 0) * T + le];
-        s1 += ye[(3 * a + 1) * T + le];
-        s2 += ye[(3 * a + 2) * T + le];
+        const int sl = sadj[k];
+        const float2 q = yxy[sl];
+        s0 += q.x;
+        s1 += q.y;
+        s2 += yz[sl];
       }
       if (m & 1) s0 = 0.f;
       if (m & 2) s1 = 0.f;

@@ -277,7 +277,7 @@ struct Ctx {
   int* tnode_ptr = nullptr;     // [ntiles+1]
   int* tnodes = nullptr;        // global node of each tile node
   uint16_t* tadj_ptr = nullptr; // per tile: L+1 offsets into the tile's adjacency block
-  uint16_t* tadj = nullptr;     // [ntiles][T·n_en] (local element << 4 | local node)
+  uint16_t* tadj = nullptr;     // [ntiles][T·n_en] local node · T + local element (an element-vector slot)
   int* tbslot = nullptr;        // bpart position of each tile node, −1 when interior
   int* bnodes = nullptr;        // nodes shared by several tiles
   int* bptr = nullptr;          // [n_bnodes+1] runs of bpart per shared node

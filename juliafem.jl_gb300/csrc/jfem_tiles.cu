@@ -112,7 +112,7 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
       if (e < 0) continue;
       for (int a = 0; a < nn; ++a) {
         const int li = tconn[(size_t)a * Epad + t * T + k];
-        tadj[(size_t)t * T * nn + cur[(size_t)li]++] = (uint16_t)((k << 4) | a);
+        tadj[(size_t)t * T * nn + cur[(size_t)li]++] = (uint16_t)(a * T + k);   // slot of (k, a) in [n_en][T]
       }
     }
     for (int j = 0; j < L; ++j) {
