@@ -334,81 +334,182 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
 // (persistent over tiles); dynamic shared memory, in this order:
 //   yxy  [NN][T]     float2 x, y components of the element vectors of the tile
 //   yz   [NN][T]     f32    their z components
+//     (before the element pass the same bytes hold the staged element data:
+//      sconn [NN][T] u16 local connectivity, srec [11][T] f32 affine records)
 //   sadj [T·NN]      u16    the tile's node → slot (local node · T + element) lists
-//   sptr [Lmax+1]    u16    their offsets (padded to 8 entries)
+//   sptr [Lmax+1]    u16    end offsets into sadj (bits 0-12) and the node's
+//                           Dirichlet mask (bits 13-15; entry j+1 is node j's)
 //   vs   [3·Lmax]    float2 (hi, lo) of the tile's nodes (masked DOFs zero)
 //   us   [3·Lmax]    f32    state u of the tile's nodes (finite strain only)
-// Each thread issues its element's connectivity and (affine) geometry loads
-// before staging, so they are in flight while the tile's nodes are gathered.
-// Interior nodes → y (FP32) directly, boundary nodes → bpart[slot] (float4);
-// optional v·y partial over interior nodes (double-float, v = hi + lo as
-// staged) into part[blockIdx.x] (FP64).
+// The loads of one tile are issued in two waves, so a tile waits for about
+// three global-memory latencies instead of one per node round:
+//   header   n0, L                                   (tnode_ptr)
+//   wave 1   bulk async copies (cp.async.bulk, one mbarrier, issued by the
+//            lanes of warp 0): the adjacency block, the NN connectivity rows
+//            and the 11 affine record rows of the tile (all 16-byte aligned:
+//            rows of T elements of a tile-padded [k][Epad] array);
+//            per node: global index, adjacency end offset
+//   wave 2   per node (depends on wave 1): mask byte, v (hi, lo) and u
+// The node gather then loads one output word per node (tout: the global node
+// when interior, −1 − slot when shared), sums its element slots from shared
+// memory and writes y (interior) or bpart[slot] (shared).  Optional v·y
+// partial over interior nodes (double-float, v = hi + lo as staged) into
+// part[blockIdx.x] (FP64).
 // ---------------------------------------------------------------------------
 __host__ __device__ constexpr int tile_sptr_len(int Lmax) { return (Lmax + 8) & ~7; }
 
-template <int NN, bool NEED_U>
+// bytes of the element-vector region (also holds the staged element data)
+template <int NN, bool AFFINE>
+__host__ __device__ constexpr size_t tile_elem_region_bytes() {
+  constexpr size_t yb = (size_t)NN * JFEM_TILE * (sizeof(float2) + sizeof(float));
+  constexpr size_t sb = (size_t)NN * JFEM_TILE * sizeof(uint16_t) + (AFFINE ? (size_t)11 * JFEM_TILE * sizeof(float) : 0);
+  return ((yb > sb ? yb : sb) + 15) & ~(size_t)15;
+}
+
+template <int NN, bool NEED_U, bool AFFINE>
 __host__ __device__ constexpr size_t tile_smem_bytes(int Lmax) {
-  return (size_t)NN * JFEM_TILE * (sizeof(float2) + sizeof(float)) + (size_t)JFEM_TILE * NN * sizeof(uint16_t) +
+  return tile_elem_region_bytes<NN, AFFINE>() + (size_t)JFEM_TILE * NN * sizeof(uint16_t) +
          (size_t)tile_sptr_len(Lmax) * sizeof(uint16_t) + (size_t)3 * Lmax * sizeof(float2) +
          (NEED_U ? (size_t)3 * Lmax * sizeof(float) : 0);
 }
 
+// node rounds per thread covered by the unrolled waves (tiles of JFEM_TILE
+// Morton-ordered elements hold ≈ 0.4, 1.3 and 2.6 nodes per element for Tet4,
+// Hex8 and Tet10); nodes beyond are staged by a plain loop
+template <int ET>
+__host__ __device__ constexpr int tile_node_rounds() {
+  return ET == JFEM_TET4 ? 1 : ET == JFEM_HEX8 ? 2 : 3;
+}
+constexpr int TILE_PTR_BITS = 13;   // sadj offsets < 2^13 (T·NN ≤ 2560)
+static_assert(JFEM_TILE * 10 < (1 << TILE_PTR_BITS), "tile adjacency offsets must fit 13 bits");
+
 template <int ET, bool AFFINE, int KIN, bool GEOM>
-__global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? 4 : 1) k_tile_apply(
+__global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS : 1) k_tile_apply(
     int64_t ntiles, int64_t E, int64_t Epad, const int* __restrict__ tnode_ptr, const int* __restrict__ tnodes,
     const uint16_t* __restrict__ tconn, const float* __restrict__ geo, const uint16_t* __restrict__ tadj_ptr,
-    const uint16_t* __restrict__ tadj, const int* __restrict__ tbslot,
+    const uint16_t* __restrict__ tadj, const int* __restrict__ tout,
     const float2* __restrict__ v2, const double* __restrict__ u,
     const uint8_t* __restrict__ mask, int masked, int Lmax, float* __restrict__ y, float4* __restrict__ bpart,
     double* __restrict__ part, int* err, const int* __restrict__ stop) {
   constexpr int NN = Elem<ET>::NN;
   constexpr int T = JFEM_TILE;
   constexpr int NADJ = T * NN;   // adjacency entries per tile; NADJ·2 bytes is a multiple of 16
+  constexpr int NR = tile_node_rounds<ET>();
+  constexpr unsigned PMASK = (1u << TILE_PTR_BITS) - 1;
   constexpr bool NEED_U = (KIN != KIN_SMALL);
+  constexpr int NCOPY = 1 + NN + (AFFINE ? 11 : 0);   // bulk copies per tile
+  constexpr unsigned TILE_BYTES = (unsigned)((NADJ + NN * T) * sizeof(uint16_t) + (AFFINE ? 11 * T * sizeof(float) : 0));
+  static_assert(NCOPY <= 32, "one bulk copy per lane of warp 0");
+  static_assert((T * sizeof(uint16_t)) % 16 == 0 && (T * sizeof(float)) % 16 == 0, "bulk copy rows: 16-byte multiples");
+  static_assert((NN * T * sizeof(uint16_t)) % 16 == 0, "srec must start 16-byte aligned");
   extern __shared__ float4 smem_f4[];
   float2* yxy = reinterpret_cast<float2*>(smem_f4);
   float* yz = reinterpret_cast<float*>(yxy + NN * T);
-  uint16_t* sadj = reinterpret_cast<uint16_t*>(yz + NN * T);
+  uint16_t* sconn = reinterpret_cast<uint16_t*>(smem_f4);
+  float* srec = reinterpret_cast<float*>(sconn + NN * T);
+  uint16_t* sadj = reinterpret_cast<uint16_t*>(reinterpret_cast<char*>(smem_f4) + tile_elem_region_bytes<NN, AFFINE>());
   uint16_t* sptr = sadj + NADJ;
   float2* vs = reinterpret_cast<float2*>(sptr + tile_sptr_len(Lmax));
   float* us = reinterpret_cast<float*>(vs + 3 * Lmax);
   __shared__ double sh[32];
+  __shared__ uint64_t tile_bar;
   if (stop && *stop) return;
   const int tid = threadIdx.x;
+  if (tid == 0) mbar_init(&tile_bar, 1);
+  __syncthreads();
   float2 dot = make_float2(0.f, 0.f);
   bool ok = true;
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  unsigned phase = 0;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, phase ^= 1u) {
+    if (tid < 32) {   // wave 1, bulk part (the previous tile's readers passed the loop-end barrier)
+      if (tid == 0) mbar_expect_tx(&tile_bar, TILE_BYTES);
+      __syncwarp();
+      if (tid < NCOPY) {
+        fence_proxy_async_smem();
+        if (tid == 0) {
+          bulk_copy_g2s(sadj, tadj + t * (int64_t)NADJ, NADJ * sizeof(uint16_t), &tile_bar);
+        } else if (tid <= NN) {
+          const int a = tid - 1;
+          bulk_copy_g2s(sconn + a * T, tconn + (int64_t)a * Epad + t * T, T * sizeof(uint16_t), &tile_bar);
+        } else {
+          const int k = tid - 1 - NN;
+          bulk_copy_g2s(srec + k * T, geo + (int64_t)k * Epad + t * T, T * sizeof(float), &tile_bar);
+        }
+      }
+    }
     const int n0 = __ldg(tnode_ptr + t);
     const int L = __ldg(tnode_ptr + t + 1) - n0;
     const int64_t e = t * T + tid;
     const bool valid = e < E;
+    {   // node staging, wave 1: global index and adjacency end offset per node
+      int gn[NR];
+      unsigned pe[NR];
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        const int j = tid + r * T;
+        gn[r] = 0;
+        pe[r] = 0;
+        if (j < L) {
+          gn[r] = __ldg(tnodes + n0 + j);
+          pe[r] = __ldg(tadj_ptr + n0 + t + j + 1);
+        }
+      }
+      // wave 2: mask, v (hi, lo), u
+      unsigned mk[NR];
+      float2 h[NR][3];
+      float uu[NR][3];
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        const int j = tid + r * T;
+        mk[r] = 0;
+        if (j < L) {
+          const int64_t g = gn[r];
+          mk[r] = masked ? (unsigned)__ldg(mask + g) : 0u;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            h[r][c] = __ldg(v2 + 3 * g + c);
+            if (NEED_U) uu[r][c] = (float)__ldg(u + 3 * g + c);
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        const int j = tid + r * T;
+        if (j < L) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            vs[3 * j + c] = ((mk[r] >> c) & 1) ? make_float2(0.f, 0.f) : h[r][c];
+            if (NEED_U) us[3 * j + c] = uu[r][c];
+          }
+          sptr[j + 1] = (uint16_t)(pe[r] | (mk[r] << TILE_PTR_BITS));
+        }
+      }
+      if (tid == 0) sptr[0] = 0;
+      for (int j = tid + NR * T; j < L; j += T) {   // tiles with more nodes than the unrolled rounds
+        const int64_t g = __ldg(tnodes + n0 + j);
+        const unsigned m = masked ? (unsigned)__ldg(mask + g) : 0u;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float2 hv = __ldg(v2 + 3 * g + c);
+          vs[3 * j + c] = ((m >> c) & 1) ? make_float2(0.f, 0.f) : hv;
+          if (NEED_U) us[3 * j + c] = (float)__ldg(u + 3 * g + c);
+        }
+        sptr[j + 1] = (uint16_t)(__ldg(tadj_ptr + n0 + t + j + 1) | (m << TILE_PTR_BITS));
+      }
+    }
+    const bool have_tile = mbar_wait_bounded(&tile_bar, phase, err);
+    if (__syncthreads_or(!have_tile)) break;   // a bulk copy never completed: error raised, stop
     int li[NN];
     float rec[11];
     if (valid) {
 #pragma unroll
-      for (int a = 0; a < NN; ++a) li[a] = __ldg(tconn + (int64_t)a * Epad + e);
+      for (int a = 0; a < NN; ++a) li[a] = sconn[a * T + tid];
       if constexpr (AFFINE) {
 #pragma unroll
-        for (int k = 0; k < 11; ++k) rec[k] = __ldg(geo + (int64_t)k * Epad + e);
+        for (int k = 0; k < 11; ++k) rec[k] = srec[k * T + tid];
       }
     }
-    {
-      const uint4* src = reinterpret_cast<const uint4*>(tadj + t * (int64_t)NADJ);
-      uint4* dst = reinterpret_cast<uint4*>(sadj);
-      for (int k = tid; k < NADJ / 8; k += T) dst[k] = __ldg(src + k);
-    }
-    for (int j = tid; j <= L; j += T) sptr[j] = __ldg(tadj_ptr + n0 + t + j);
-    for (int j = tid; j < L; j += T) {   // one node per thread: its three (hi, lo) pairs
-      const int64_t g = __ldg(tnodes + n0 + j);
-      const uint8_t m = masked ? __ldg(mask + g) : (uint8_t)0;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float2 h = __ldg(v2 + 3 * g + c);
-        vs[3 * j + c] = ((m >> c) & 1) ? make_float2(0.f, 0.f) : h;
-        if (NEED_U) us[3 * j + c] = (float)__ldg(u + 3 * g + c);
-      }
-    }
-    __syncthreads();
+    __syncthreads();   // the element vectors below overwrite the staged element data
     if (valid) {
       float dv[NN][3], du[NN][3];
 #pragma unroll
@@ -432,34 +533,48 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? 4 : 1) k_tile_ap
       }
     }
     __syncthreads();
-    for (int j = tid; j < L; j += T) {
-      const int64_t g = __ldg(tnodes + n0 + j);
-      const int slot = __ldg(tbslot + n0 + j);
-      const uint8_t m = masked ? __ldg(mask + g) : (uint8_t)0;
-      float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-      const int k1 = sptr[j + 1];
-      for (int k = sptr[j]; k < k1; ++k) {
-        const int sl = sadj[k];
-        const float2 q = yxy[sl];
-        s0 += q.x;
-        s1 += q.y;
-        s2 += yz[sl];
+    {   // node gather
+      int on[NR];
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        const int j = tid + r * T;
+        on[r] = j < L ? __ldg(tout + n0 + j) : 0;
       }
-      if (m & 1) s0 = 0.f;
-      if (m & 2) s1 = 0.f;
-      if (m & 4) s2 = 0.f;
-      if (slot < 0) {
-        y[3 * g] = s0;
-        y[3 * g + 1] = s1;
-        y[3 * g + 2] = s2;
-        if (part) {   // v·y in double-float from the staged (masked) v
-          dot = df_add(dot, df_mul_f(vs[3 * j], s0));
-          dot = df_add(dot, df_mul_f(vs[3 * j + 1], s1));
-          dot = df_add(dot, df_mul_f(vs[3 * j + 2], s2));
+      auto gather = [&](int j, int o) {
+        const unsigned w1 = sptr[j + 1];
+        const int k1 = (int)(w1 & PMASK);
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+        for (int k = (int)(sptr[j] & PMASK); k < k1; ++k) {
+          const int sl = sadj[k];
+          const float2 q = yxy[sl];
+          s0 += q.x;
+          s1 += q.y;
+          s2 += yz[sl];
         }
-      } else {
-        bpart[slot] = make_float4(s0, s1, s2, 0.f);
+        if (o >= 0) {
+          const unsigned m = w1 >> TILE_PTR_BITS;
+          if (m & 1) s0 = 0.f;
+          if (m & 2) s1 = 0.f;
+          if (m & 4) s2 = 0.f;
+          const int64_t g = o;
+          y[3 * g] = s0;
+          y[3 * g + 1] = s1;
+          y[3 * g + 2] = s2;
+          if (part) {   // v·y in double-float from the staged (masked) v
+            dot = df_add(dot, df_mul_f(vs[3 * j], s0));
+            dot = df_add(dot, df_mul_f(vs[3 * j + 1], s1));
+            dot = df_add(dot, df_mul_f(vs[3 * j + 2], s2));
+          }
+        } else {   // shared node: partial sum; the boundary pass applies the mask
+          bpart[-1 - o] = make_float4(s0, s1, s2, 0.f);
+        }
+      };
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        const int j = tid + r * T;
+        if (j < L) gather(j, on[r]);
       }
+      for (int j = tid + NR * T; j < L; j += T) gather(j, __ldg(tout + n0 + j));
     }
     __syncthreads();
   }
@@ -506,11 +621,12 @@ static void dispatch_kin(Ctx* c, const R* geo, const double* v, const float2* v2
 template <int ET, bool AFFINE, int KIN, bool GEOM>
 static void launch_tile_k(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
   constexpr int NN = Elem<ET>::NN;
-  const size_t sm = tile_smem_bytes<NN, KIN != KIN_SMALL>(c->tile_Lmax);
-  cudaFuncSetAttribute(k_tile_apply<ET, AFFINE, KIN, GEOM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  const unsigned g = (unsigned)(c->ntiles < JFEM_RED_BLOCKS ? JFEM_RED_BLOCKS : JFEM_RED_BLOCKS);
-  k_tile_apply<ET, AFFINE, KIN, GEOM><<<g, JFEM_TILE, sm, c->stream>>>(
-      c->ntiles, c->E, c->Epad, c->tnode_ptr, c->tnodes, c->tconn, c->geoT32, c->tadj_ptr, c->tadj, c->tbslot,
+  const size_t sm = tile_smem_bytes<NN, KIN != KIN_SMALL, AFFINE>(c->tile_Lmax);
+  auto kern = k_tile_apply<ET, AFFINE, KIN, GEOM>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const unsigned g = JFEM_RED_BLOCKS;   // CTAs take tiles b, b + g, …
+  kern<<<g, JFEM_TILE, sm, c->stream>>>(
+      c->ntiles, c->E, c->Epad, c->tnode_ptr, c->tnodes, c->tconn, c->geoT32, c->tadj_ptr, c->tadj, c->tout,
       v2, c->u_state, c->mask, masked ? 1 : 0, c->tile_Lmax, y, c->bpart, part, c->d_err, stop);
   c->launches += 1;
 }

@@ -26,6 +26,7 @@
 #define JFEM_RED_BLOCKS 1216      // fixed reduction grid: 152 SMs x 8 → deterministic sums
 #define JFEM_RED_THREADS 256
 #define JFEM_TILE 256             // elements per tile of the shared-memory apply
+#define JFEM_TILE_CTAS 3          // resident CTAs per SM the small-strain tile kernel is compiled for
 
 namespace jfem {
 
@@ -153,6 +154,50 @@ __device__ __forceinline__ double reduce_partials(const double* __restrict__ par
 __device__ __forceinline__ void raise_error(int* flag, int code) { atomicCAS(flag, 0, code); }
 
 // ---------------------------------------------------------------------------
+// bulk asynchronous copies global → shared (cp.async.bulk, completion counted
+// in bytes on a shared-memory mbarrier).  Addresses 16-byte aligned, sizes a
+// multiple of 16 bytes.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// Orders this thread's earlier generic-proxy shared-memory accesses before
+// later async-proxy (bulk copy) writes to the same memory.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Wait for the phase of the given parity with a bounded number of polls;
+// false (and JFEM_ERR_TIMEOUT raised) when the budget runs out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, int* err) {
+  for (unsigned k = 0; k < (1u << 20); ++k)
+    if (mbar_try_wait(bar, parity)) return true;
+  raise_error(err, JFEM_ERR_TIMEOUT);
+  return false;
+}
+
+// ---------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------
 struct SolverScalars {
@@ -278,7 +323,7 @@ struct Ctx {
   int* tnodes = nullptr;        // global node of each tile node
   uint16_t* tadj_ptr = nullptr; // per tile: L+1 offsets into the tile's adjacency block
   uint16_t* tadj = nullptr;     // [ntiles][T·n_en] local node · T + local element (an element-vector slot)
-  int* tbslot = nullptr;        // bpart position of each tile node, −1 when interior
+  int* tout = nullptr;          // per tile node: its global node when interior, −1 − (bpart position) when shared
   int* bnodes = nullptr;        // nodes shared by several tiles
   int* bptr = nullptr;          // [n_bnodes+1] runs of bpart per shared node
   float4* bpart = nullptr;      // [n_bslots] tile partial sums (x, y, z, unused), grouped by node, ascending tile

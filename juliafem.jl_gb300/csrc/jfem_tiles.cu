@@ -70,7 +70,7 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   for (int64_t t = 0; t < E * nn; ++t) cntg[(size_t)(conn_h[t] - base)]++;
 
   std::vector<uint16_t> tconn((size_t)nn * Epad, 0);
-  std::vector<int> tnode_ptr((size_t)ntiles + 1, 0), tnodes, tbslot;
+  std::vector<int> tnode_ptr((size_t)ntiles + 1, 0), tnodes, tout;
   std::vector<uint16_t> tadj_ptr, tadj((size_t)ntiles * T * nn, 0);
   std::vector<std::pair<int64_t, int64_t>> brec;   // (node, slot), slots ascend with tile
   tnodes.reserve((size_t)E * 2);
@@ -120,9 +120,9 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
       tnodes.push_back(g);
       const int here = lcnt[(size_t)j + 1] - lcnt[(size_t)j];
       if (here == cntg[(size_t)g]) {
-        tbslot.push_back(-1);
+        tout.push_back(g);
       } else {
-        tbslot.push_back((int)nslots);
+        tout.push_back(-1 - (int)nslots);
         brec.push_back({g, nslots});
         ++nslots;
       }
@@ -144,8 +144,8 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   }
   bptr.push_back((int)brec.size());
   if (bnodes.empty()) bptr.assign(1, 0);
-  for (int& sl : tbslot)
-    if (sl >= 0) sl = pos_of_slot[(size_t)sl];
+  for (int& o : tout)
+    if (o < 0) o = -1 - pos_of_slot[(size_t)(-1 - o)];
 
   // upload
   int rc = 0;
@@ -163,7 +163,7 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   if ((rc = up(&c->tnodes, tnodes))) return rc;
   if ((rc = up(&c->tadj_ptr, tadj_ptr))) return rc;
   if ((rc = up(&c->tadj, tadj))) return rc;
-  if ((rc = up(&c->tbslot, tbslot))) return rc;
+  if ((rc = up(&c->tout, tout))) return rc;
   if ((rc = up(&c->bnodes, bnodes))) return rc;
   if ((rc = up(&c->bptr, bptr))) return rc;
   if ((rc = dalloc(c, &c->bpart, std::max<int64_t>(nslots, 1)))) return rc;
