@@ -205,8 +205,15 @@ __global__ void k_split(int64_t n, const double* __restrict__ v, float2* __restr
 // split input) into part[3G + blockIdx.x].  With sc (mixed PCG), the last block
 // to finish forms p·Ap = Σ part[0..G) + Σ part[3G..4G) in FP64, in index order,
 // and α = r·z / p·Ap for the update kernel.  Launched with G = JFEM_RED_BLOCKS
-// blocks.
-__global__ void __launch_bounds__(JFEM_RED_THREADS) k_tile_boundary(int64_t nb, const int* __restrict__ bnodes,
+// blocks.  Each thread takes BND_ROUNDS nodes (k, k + stride, …) and issues
+// their loads in two waves (node and run offsets; then the first BND_UNROLL
+// partials of each run, the mask byte and v), so a thread waits for about two
+// memory latencies; runs longer than BND_UNROLL (nodes shared by more tiles)
+// finish in a loop.
+constexpr int BND_ROUNDS = 1;
+constexpr int BND_UNROLL = 4;
+
+__global__ void __launch_bounds__(JFEM_RED_THREADS, 4) k_tile_boundary(int64_t nb, const int* __restrict__ bnodes,
                                                                     const int* __restrict__ bptr,
                                                                     const float4* __restrict__ bpart,
                                                                     const uint8_t* __restrict__ mask, int masked,
@@ -217,37 +224,72 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_tile_boundary(int64_t nb, 
   __shared__ double sh[32];
   if (stop && *stop) return;
   float2 dot = make_float2(0.f, 0.f);
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nb; k += (int64_t)gridDim.x * blockDim.x) {
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    const int i1 = __ldg(bptr + k + 1);
-    for (int i = __ldg(bptr + k); i < i1; ++i) {
-      const float4 q = __ldcs(bpart + i);   // read once: stream past L1
-      s0 += q.x;
-      s1 += q.y;
-      s2 += q.z;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k0 < nb; k0 += BND_ROUNDS * stride) {
+    int g[BND_ROUNDS], i0[BND_ROUNDS], i1[BND_ROUNDS];
+#pragma unroll
+    for (int r = 0; r < BND_ROUNDS; ++r) {   // wave 1
+      const int64_t k = k0 + r * stride;
+      g[r] = 0;
+      i0[r] = i1[r] = 0;
+      if (k < nb) {
+        g[r] = __ldg(bnodes + k);
+        i0[r] = __ldg(bptr + k);
+        i1[r] = __ldg(bptr + k + 1);
+      }
     }
-    const int64_t g = __ldg(bnodes + k);
-    if (masked) {
-      const uint8_t m = __ldg(mask + g);
-      if (m & 1) s0 = 0.f;
-      if (m & 2) s1 = 0.f;
-      if (m & 4) s2 = 0.f;
+    float4 q[BND_ROUNDS][BND_UNROLL];
+    unsigned m[BND_ROUNDS];
+    float2 vv[BND_ROUNDS][3];
+#pragma unroll
+    for (int r = 0; r < BND_ROUNDS; ++r) {   // wave 2
+      const int64_t k = k0 + r * stride;
+#pragma unroll
+      for (int u = 0; u < BND_UNROLL; ++u)
+        q[r][u] = i0[r] + u < i1[r] ? __ldcs(bpart + i0[r] + u) : make_float4(0.f, 0.f, 0.f, 0.f);   // read once
+      m[r] = (k < nb && masked) ? (unsigned)__ldg(mask + g[r]) : 0u;
+      if (part && k < nb) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vv[r][c] = __ldg(vdot + 3 * (int64_t)g[r] + c);
+      }
     }
-    y[3 * g] = s0;
-    y[3 * g + 1] = s1;
-    y[3 * g + 2] = s2;
-    if (part) {
-      dot = df_add(dot, df_mul_f(__ldg(vdot + 3 * g), s0));
-      dot = df_add(dot, df_mul_f(__ldg(vdot + 3 * g + 1), s1));
-      dot = df_add(dot, df_mul_f(__ldg(vdot + 3 * g + 2), s2));
+#pragma unroll
+    for (int r = 0; r < BND_ROUNDS; ++r) {
+      const int64_t k = k0 + r * stride;
+      if (k >= nb) continue;
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll
+      for (int u = 0; u < BND_UNROLL; ++u) {   // ascending tile order, as the loop below continues it
+        s0 += q[r][u].x;
+        s1 += q[r][u].y;
+        s2 += q[r][u].z;
+      }
+      for (int i = i0[r] + BND_UNROLL; i < i1[r]; ++i) {
+        const float4 t = __ldcs(bpart + i);
+        s0 += t.x;
+        s1 += t.y;
+        s2 += t.z;
+      }
+      if (m[r] & 1) s0 = 0.f;
+      if (m[r] & 2) s1 = 0.f;
+      if (m[r] & 4) s2 = 0.f;
+      const int64_t gg = g[r];
+      y[3 * gg] = s0;
+      y[3 * gg + 1] = s1;
+      y[3 * gg + 2] = s2;
+      if (part) {
+        dot = df_add(dot, df_mul_f(vv[r][0], s0));
+        dot = df_add(dot, df_mul_f(vv[r][1], s1));
+        dot = df_add(dot, df_mul_f(vv[r][2], s2));
+      }
     }
   }
   if (part) {
     const double b = block_sum_df(dot, sh);
     if (threadIdx.x == 0) part[3 * JFEM_RED_BLOCKS + blockIdx.x] = b;
     if (sc && arrive_last(&sc->arrive[0])) {
-      const double pAp = reduce_partials_cg(part, JFEM_RED_BLOCKS, sh) +
-                         reduce_partials_cg(part + 3 * JFEM_RED_BLOCKS, JFEM_RED_BLOCKS, sh);
+      const double2 ab = reduce_partials2_cg(part, part + 3 * JFEM_RED_BLOCKS, JFEM_RED_BLOCKS, sh);
+      const double pAp = ab.x + ab.y;
       if (threadIdx.x == 0) {
         const double a = sc->rz[0] / pAp;
         sc->pAp = pAp;

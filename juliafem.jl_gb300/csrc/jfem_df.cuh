@@ -90,6 +90,36 @@ __device__ __forceinline__ double block_sum_df(float2 v, double* sh /* ≥ 32 en
   return r;
 }
 
+// Two block sums in one pass (same order per value as block_sum_df; ≤ 16 warps).
+__device__ __forceinline__ double2 block_sum2_df(float2 u, float2 v, double* sh /* ≥ 32 entries */) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const float2 wu = make_float2(__shfl_down_sync(0xffffffffu, u.x, o), __shfl_down_sync(0xffffffffu, u.y, o));
+    const float2 wv = make_float2(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o));
+    u = df_add(u, wu);
+    v = df_add(v, wv);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) {
+    sh[w] = df_to_double(u);
+    sh[16 + w] = df_to_double(v);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0, t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      s += sh[k];
+      t += sh[16 + k];
+    }
+    sh[0] = s;
+    sh[16] = t;
+  }
+  __syncthreads();
+  const double2 r = make_double2(sh[0], sh[16]);
+  __syncthreads();
+  return r;
+}
+
 // "Last block" detection for a fixed-order grid reduction without a second
 // launch: each block publishes its partial, fences, and counts itself in; the
 // block that arrives last (every partial is then visible) reduces all partials
@@ -124,6 +154,40 @@ __device__ __forceinline__ double reduce_partials_cg(const double* part, int n, 
   }
   __syncthreads();
   const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// Two fixed-order sums of n partials each in one pass (same order per value as
+// reduce_partials_cg; ≤ 16 warps).
+__device__ __forceinline__ double2 reduce_partials2_cg(const double* a, const double* b, int n, double* sh) {
+  double s = 0.0, t = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    s += __ldcg(a + i);
+    t += __ldcg(b + i);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_down_sync(0xffffffffu, s, o);
+    t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) {
+    sh[w] = s;
+    sh[16 + w] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double u = 0.0, v = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      u += sh[k];
+      v += sh[16 + k];
+    }
+    sh[0] = u;
+    sh[16] = v;
+  }
+  __syncthreads();
+  const double2 r = make_double2(sh[0], sh[16]);
   __syncthreads();
   return r;
 }

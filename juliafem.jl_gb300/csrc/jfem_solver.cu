@@ -190,15 +190,14 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_dfcg_update1(int64_t n, So
     rz = df_add(rz, df_mul(ri, df_mul_f(ri, dinv[i])));
     rr = df_add(rr, df_mul(ri, ri));
   }
-  const double rzb = block_sum_df(rz, sh);
-  const double rrb = block_sum_df(rr, sh);
+  const double2 zr = block_sum2_df(rz, rr, sh);
   if (threadIdx.x == 0) {
-    part[G_ + blockIdx.x] = rzb;
-    part[2 * G_ + blockIdx.x] = rrb;
+    part[G_ + blockIdx.x] = zr.x;
+    part[2 * G_ + blockIdx.x] = zr.y;
   }
   if (arrive_last(&sc->arrive[1])) {
-    const double rz_new = reduce_partials_cg(part + G_, G_, sh);
-    const double rr_new = reduce_partials_cg(part + 2 * G_, G_, sh);
+    const double2 t = reduce_partials2_cg(part + G_, part + 2 * G_, G_, sh);
+    const double rz_new = t.x, rr_new = t.y;
     if (threadIdx.x == 0) {
       const double beta = rz_new / sc->rz[0];
       sc->beta = beta;
