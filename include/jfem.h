@@ -278,6 +278,12 @@ void* jfem_stream(const jfem_ctx* ctx);
  * gather kernel (ms), each measured on the context stream.  No counterpart in the
  * reference (measurement hook). */
 int jfem_time_apply(jfem_ctx* ctx, int flags, int reps, double* ms_element, double* ms_gather);
+/* Runs the FP64 assembly of K's values and f_int (the integration-point kernel
+ * and the CSC scatter of jfem_assemble_csc, without the pattern and without
+ * the download) reps times into device scratch and returns the mean CUDA-event
+ * duration of each kernel (ms) and the number of stored entries.  No
+ * counterpart in the reference (measurement hook). */
+int jfem_time_assembly(jfem_ctx* ctx, int reps, double* ms_qpoint, double* ms_scatter, int64_t* nnz);
 
 #ifdef __cplusplus
 }

@@ -87,6 +87,7 @@ SIGNATURES = {
     "jfem_last_apply_ms": (C.c_double, [_P]),
     "jfem_stream": (C.c_void_p, [_P]),
     "jfem_time_apply": (C.c_int, [_P, C.c_int, C.c_int, _f64p, _f64p]),
+    "jfem_time_assembly": (C.c_int, [_P, C.c_int, _f64p, _f64p, _i64p]),
     "jfem_apply_noalloc": (C.c_int, [C.c_int, _i64, _P, _i64, _P, C.c_int, _P, _P, _P, _P, _P]),
     "jfem_mpnn_init": (C.c_int, [_P, C.c_uint64]),
     "jfem_mpnn_set_weights": (C.c_int, [_P, _f32p]),
@@ -337,6 +338,13 @@ class Context:
         flags = (APPLY_FP32 if fp32 else 0) | (APPLY_MASKED if masked else 0)
         self._check(self._lib.jfem_time_apply(self._h, flags, int(reps), C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def time_assembly(self, reps: int = 3):
+        """Mean CUDA-event ms of (integration-point kernel, CSC scatter kernel) of
+        the FP64 assembly of K's values and f_int, and K's stored entry count."""
+        a, b, n = C.c_double(0), C.c_double(0), C.c_int64(0)
+        self._check(self._lib.jfem_time_assembly(self._h, int(reps), C.byref(a), C.byref(b), C.byref(n)))
+        return a.value, b.value, n.value
 
 
 class Batch:

@@ -160,6 +160,15 @@ int jfem_time_apply(jfem_ctx* h, int flags, int reps, double* ms_element, double
                           ms_gather);
 }
 
+int jfem_time_assembly(jfem_ctx* h, int reps, double* ms_qpoint, double* ms_scatter, int64_t* nnz) {
+  ENTER(h);
+  Ctx* c = &h->c;
+  if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
+  if (!ms_qpoint || !ms_scatter || !nnz) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL output");
+  *nnz = 9 * c->n_blocks;
+  return jfem::time_assembly(c, reps, ms_qpoint, ms_scatter);
+}
+
 int jfem_set_mesh(jfem_ctx* h, int elem_type, int64_t n_nodes, const double* X, int64_t n_elem, const int64_t* conn,
                   int index_base) {
   ENTER(h);

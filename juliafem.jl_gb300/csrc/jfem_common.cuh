@@ -424,6 +424,7 @@ void prepare_geo_tet4_affine(int64_t E, const int* conn, const double* X, const 
                              double* g64, float* g32, cudaStream_t stream);
 int internal_force_device(Ctx* c, double* f_d);
 int time_apply(Ctx* c, bool fp32, bool masked, int reps, double* ms_elem, double* ms_gather);
+int time_assembly(Ctx* c, int reps, double* ms_qpoint, double* ms_scatter);
 // jfem_mpnn.cu
 int mpnn_ensure(Ctx* c);
 int mpnn_init(Ctx* c, uint64_t seed);

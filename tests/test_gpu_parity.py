@@ -77,6 +77,21 @@ def test_assembly_is_deterministic(jfem, gpu_ctx_factory):
         assert np.array_equal(x, y)
 
 
+def test_assembly_timing_hook_runs_the_same_assembly(jfem, gpu_ctx_factory):
+    """jfem_time_assembly times the two assembly launches into scratch and
+    leaves the assembled K unchanged; its entry count is K's."""
+    w = jfem.workloads.cantilever(10, 6, 3, 3, 3.0, 1.0, 1.0)
+    with gpu_ctx_factory(w) as ctx:
+        a = ctx.assemble_csc(0)
+        ms_q, ms_s, nnz = ctx.time_assembly(reps=2)
+        b = ctx.assemble_csc(0)
+        with pytest.raises(jfem.JFEMError):
+            ctx.time_assembly(reps=0)
+    assert ms_q > 0.0 and ms_s > 0.0 and nnz == a[2].size
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
 @pytest.mark.parametrize("et", [4, 10, 8])
 def test_apply_fp64_and_fp32(jfem, orc, gpu_ctx_factory, et):
     m = jfem.mesh.box_mesh(et, 5, 3, 3, 5.0, 1.0, 1.0)
