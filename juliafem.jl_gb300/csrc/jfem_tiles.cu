@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cstring>
 #include <numeric>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -34,6 +35,22 @@ static inline uint64_t spread3(uint64_t v) {   // 21 bits → every third bit
   return v;
 }
 
+// Runs body(i0, i1) over contiguous ranges of [0, n) on up to 16 host threads;
+// every range's work is independent, so results do not depend on the split.
+template <class F>
+static void parallel_tiles(int64_t n, F body) {
+  const int64_t hw = std::max<int64_t>(1, std::min<int64_t>(16, std::thread::hardware_concurrency()));
+  const int64_t nt = std::min<int64_t>(hw, std::max<int64_t>(1, n / 16));
+  if (nt <= 1) {
+    body(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve((size_t)nt);
+  for (int64_t k = 0; k < nt; ++k) th.emplace_back(body, n * k / nt, n * (k + 1) / nt);
+  for (auto& x : th) x.join();
+}
+
 int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   const int64_t N = c->N, E = c->E;
   const int nn = c->nn;
@@ -49,17 +66,19 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   for (int d = 0; d < 3; ++d) span = std::max(span, hi[d] - lo[d]);
   if (!(span > 0.0)) span = 1.0;
   std::vector<std::pair<uint64_t, int64_t>> key((size_t)E);
-  for (int64_t e = 0; e < E; ++e) {
-    double cen[3] = {0, 0, 0};
-    for (int a = 0; a < nn; ++a)
-      for (int d = 0; d < 3; ++d) cen[d] += X[3 * (conn_h[e * nn + a] - base) + d];
-    uint64_t code = 0;
-    for (int d = 0; d < 3; ++d) {
-      const double q = (cen[d] / nn - lo[d]) / span * 2097151.0;
-      code |= spread3((uint64_t)std::max(0.0, std::min(2097151.0, q))) << d;
+  parallel_tiles(E, [&](int64_t e0, int64_t e1) {
+    for (int64_t e = e0; e < e1; ++e) {
+      double cen[3] = {0, 0, 0};
+      for (int a = 0; a < nn; ++a)
+        for (int d = 0; d < 3; ++d) cen[d] += X[3 * (conn_h[e * nn + a] - base) + d];
+      uint64_t code = 0;
+      for (int d = 0; d < 3; ++d) {
+        const double q = (cen[d] / nn - lo[d]) / span * 2097151.0;
+        code |= spread3((uint64_t)std::max(0.0, std::min(2097151.0, q))) << d;
+      }
+      key[(size_t)e] = {code, e};
     }
-    key[(size_t)e] = {code, e};
-  }
+  });
   std::sort(key.begin(), key.end());
   const int64_t ntiles = (E + T - 1) / T;
   const int64_t Epad = ntiles * T;
@@ -70,15 +89,19 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   for (int64_t t = 0; t < E * nn; ++t) cntg[(size_t)(conn_h[t] - base)]++;
 
   std::vector<uint16_t> tconn((size_t)nn * Epad, 0);
-  std::vector<int> tnode_ptr((size_t)ntiles + 1, 0), tnodes, tout;
-  std::vector<uint16_t> tadj_ptr, tadj((size_t)ntiles * T * nn, 0);
-  std::vector<std::pair<int64_t, int64_t>> brec;   // (node, slot), slots ascend with tile
-  tnodes.reserve((size_t)E * 2);
-  int Lmax = 0;
-  int64_t nslots = 0;
-  std::vector<int> loc;     // (node) of the tile, sorted unique
-  std::vector<int> lcnt;
-  for (int64_t t = 0; t < ntiles; ++t) {
+  std::vector<uint16_t> tadj((size_t)ntiles * T * nn, 0);
+  // Per tile (independent, built on host threads): its sorted unique nodes,
+  // their adjacency offsets, and which of them other tiles share.
+  struct TileNodes {
+    std::vector<int> loc;            // global nodes of the tile, ascending
+    std::vector<uint16_t> ptr;       // L + 1 offsets into the tile's adjacency block
+    std::vector<uint8_t> shared;     // node also in another tile
+    int nshared = 0;
+  };
+  std::vector<TileNodes> tn((size_t)ntiles);
+  auto build_tile = [&](int64_t t, std::vector<int>& lcnt) {
+    TileNodes& o = tn[(size_t)t];
+    std::vector<int>& loc = o.loc;
     loc.clear();
     for (int k = 0; k < T; ++k) {
       const int e = perm[(size_t)(t * T + k)];
@@ -88,9 +111,6 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
     std::sort(loc.begin(), loc.end());
     loc.erase(std::unique(loc.begin(), loc.end()), loc.end());
     const int L = (int)loc.size();
-    if (L > 65535) return set_err(c, JFEM_ERR_INVALID, "tile has too many nodes");
-    Lmax = std::max(Lmax, L);
-    tnode_ptr[(size_t)t + 1] = tnode_ptr[(size_t)t] + L;
     lcnt.assign((size_t)L + 1, 0);
     // local connectivity and counts
     for (int k = 0; k < T; ++k) {
@@ -104,7 +124,7 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
       }
     }
     for (int j = 0; j < L; ++j) lcnt[(size_t)j + 1] += lcnt[(size_t)j];
-    for (int j = 0; j <= L; ++j) tadj_ptr.push_back((uint16_t)lcnt[(size_t)j]);
+    o.ptr.assign(lcnt.begin(), lcnt.end());
     // local adjacency, ascending local element then local node index
     std::vector<int> cur(lcnt.begin(), lcnt.end() - 1);
     for (int k = 0; k < T; ++k) {
@@ -115,37 +135,71 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
         tadj[(size_t)t * T * nn + cur[(size_t)li]++] = (uint16_t)(a * T + k);   // slot of (k, a) in [n_en][T]
       }
     }
-    for (int j = 0; j < L; ++j) {
-      const int g = loc[(size_t)j];
-      tnodes.push_back(g);
-      const int here = lcnt[(size_t)j + 1] - lcnt[(size_t)j];
-      if (here == cntg[(size_t)g]) {
-        tout.push_back(g);
-      } else {
-        tout.push_back(-1 - (int)nslots);
-        brec.push_back({g, nslots});
-        ++nslots;
+    o.shared.assign((size_t)L, 0);
+    o.nshared = 0;
+    for (int j = 0; j < L; ++j)
+      if (lcnt[(size_t)j + 1] - lcnt[(size_t)j] != cntg[(size_t)loc[(size_t)j]]) {
+        o.shared[(size_t)j] = 1;
+        ++o.nshared;
       }
-    }
+  };
+  parallel_tiles(ntiles, [&](int64_t t0, int64_t t1) {
+    std::vector<int> lcnt;
+    for (int64_t t = t0; t < t1; ++t) build_tile(t, lcnt);
+  });
+  // tile offsets (serial prefix sums in tile order)
+  std::vector<int> tnode_ptr((size_t)ntiles + 1, 0);
+  std::vector<int64_t> slot_base((size_t)ntiles + 1, 0);
+  int Lmax = 0;
+  for (int64_t t = 0; t < ntiles; ++t) {
+    const int L = (int)tn[(size_t)t].loc.size();
+    if (L > 65535) return set_err(c, JFEM_ERR_INVALID, "tile has too many nodes");
+    Lmax = std::max(Lmax, L);
+    tnode_ptr[(size_t)t + 1] = tnode_ptr[(size_t)t] + L;
+    slot_base[(size_t)t + 1] = slot_base[(size_t)t] + tn[(size_t)t].nshared;
   }
-  // boundary nodes: partial-sum slots grouped by node, ascending tile within a
-  // node, so the boundary pass reads each node's partials as one contiguous run
-  std::stable_sort(brec.begin(), brec.end(),
-                   [](const std::pair<int64_t, int64_t>& a, const std::pair<int64_t, int64_t>& b) {
-                     return a.first < b.first;
-                   });
-  std::vector<int> bnodes, bptr(1, 0), pos_of_slot((size_t)nslots, 0);
-  for (size_t i = 0; i < brec.size(); ++i) {
-    if (i == 0 || brec[i].first != brec[i - 1].first) {
-      if (i) bptr.push_back((int)i);
-      bnodes.push_back((int)brec[i].first);
+  const int64_t total = tnode_ptr[(size_t)ntiles];
+  const int64_t nslots = slot_base[(size_t)ntiles];
+  // Shared nodes: one partial-sum slot per (node, tile), numbered in tile order;
+  // the boundary pass reads each node's partials as one contiguous run in
+  // ascending tile order, so positions are grouped by node (counting sort over
+  // the slots in tile order keeps tiles ascending within a node).
+  std::vector<int> slot_node((size_t)nslots);
+  std::vector<int> tnodes((size_t)total), tout((size_t)total);
+  std::vector<uint16_t> tadj_ptr((size_t)(total + ntiles));
+  parallel_tiles(ntiles, [&](int64_t t0, int64_t t1) {
+    for (int64_t t = t0; t < t1; ++t) {
+      const TileNodes& o = tn[(size_t)t];
+      const int64_t n0 = tnode_ptr[(size_t)t];
+      int64_t sl = slot_base[(size_t)t];
+      for (size_t j = 0; j < o.loc.size(); ++j) {
+        tnodes[(size_t)(n0 + j)] = o.loc[j];
+        if (o.shared[j]) slot_node[(size_t)sl++] = o.loc[j];
+      }
+      for (size_t j = 0; j < o.ptr.size(); ++j) tadj_ptr[(size_t)(n0 + t + j)] = o.ptr[j];
     }
-    pos_of_slot[(size_t)brec[i].second] = (int)i;
-  }
-  bptr.push_back((int)brec.size());
-  if (bnodes.empty()) bptr.assign(1, 0);
-  for (int& o : tout)
-    if (o < 0) o = -1 - pos_of_slot[(size_t)(-1 - o)];
+  });
+  std::vector<int> bcnt((size_t)N + 1, 0);
+  for (int64_t s2 = 0; s2 < nslots; ++s2) bcnt[(size_t)slot_node[(size_t)s2] + 1]++;
+  std::vector<int> bnodes, bptr(1, 0), bidx((size_t)N, -1);
+  for (int64_t g = 0; g < N; ++g)
+    if (bcnt[(size_t)g + 1] > 0) {
+      bidx[(size_t)g] = (int)bnodes.size();
+      bnodes.push_back((int)g);
+      bptr.push_back(bptr.back() + bcnt[(size_t)g + 1]);
+    }
+  std::vector<int> pos_of_slot((size_t)nslots, 0), fill(bptr.begin(), bptr.end() - 1);
+  for (int64_t s2 = 0; s2 < nslots; ++s2) pos_of_slot[(size_t)s2] = fill[(size_t)bidx[(size_t)slot_node[(size_t)s2]]]++;
+  parallel_tiles(ntiles, [&](int64_t t0, int64_t t1) {
+    for (int64_t t = t0; t < t1; ++t) {
+      const TileNodes& o = tn[(size_t)t];
+      const int64_t n0 = tnode_ptr[(size_t)t];
+      int64_t sl = slot_base[(size_t)t];
+      for (size_t j = 0; j < o.loc.size(); ++j)
+        tout[(size_t)(n0 + j)] = o.shared[j] ? -1 - pos_of_slot[(size_t)sl++] : o.loc[j];
+    }
+  });
+  std::vector<TileNodes>().swap(tn);
 
   // upload
   int rc = 0;
