@@ -269,8 +269,9 @@ def newton_leg(jfem, args, device):
 def batch_leg(jfem, args, device):
     """256 uneven Tet4 cantilevers (n ~ U{8..32} cubes along x, n/4 across;
     E ~ U[50e3, 300e3], ν ~ U[0.2, 0.45], random end traction) solved by
-    Jacobi-PCG to the FP64 relative residual 1e-8 in one persistent,
-    graph-captured launch; launch configuration from the autotuner.  solves/s
+    Jacobi-PCG to the FP64 relative residual 1e-8 in one graph-captured solve
+    (persistent launches: the largest instances on thread-block clusters when
+    the autotuner finds that faster, the rest one CTA each).  solves/s
     = instances ÷ launch time (CUDA events, mean of `steps` launches after the
     autotuning launches); latency = per-instance time on the GPU."""
     ws = jfem.workloads.batch_instances(count=args.batch_count, nmin=8, nmax=32, seed_item=5)
@@ -281,9 +282,10 @@ def batch_leg(jfem, args, device):
         b.solve(tol=TOL, max_iter=200000, block_size=0)          # autotune + first solve
         t_tune = time.perf_counter() - t0
         bs, grid = b.config()
+        cluster, n_clustered, bs_c = b.cluster_config()
         times, lats, its, ok = [], [], None, True
         for _ in range(max(1, args.steps)):
-            _, its, st, res, lat, t = b.solve(tol=TOL, max_iter=200000, block_size=bs)
+            _, its, st, res, lat, t = b.solve(tol=TOL, max_iter=200000, block_size=0)   # the tuned configuration
             times.append(t)
             lats.append(lat)
             ok = ok and bool(np.all(st == 0)) and bool(np.all(res <= TOL))
@@ -293,6 +295,7 @@ def batch_leg(jfem, args, device):
     return {"workload": f"{len(ws)} Tet4 cantilevers, n ~ U{{8..32}} (DOFs {min(dofs)}..{max(dofs)})",
             "solves_per_s": len(ws) / t, "launch_ms": t * 1e3, "p50_latency_ms": float(np.percentile(lat, 50)) * 1e3,
             "p99_latency_ms": float(np.percentile(lat, 99)) * 1e3, "block_size": bs, "grid": grid,
+            "cluster_size": cluster, "clustered_instances": n_clustered, "cluster_block_size": bs_c,
             "autotune_s": t_tune, "iterations_mean": float(np.mean(its)), "all_converged": ok}
 
 

@@ -235,16 +235,26 @@ const char* jfem_batch_last_error(const jfem_batch* batch);
 int jfem_batch_add(jfem_batch* batch, int64_t n_nodes, const double* X, int64_t n_elem, const int64_t* conn,
                    int index_base, double E, double nu, int64_t n_fixed, const int64_t* fixed_dofs,
                    int64_t n_faces, const int64_t* face_conn, const double* t);
-/* Solve every instance to tol.  block_size 0 = autotune (block size and CTAs
- * per SM timed on the whole batch, fastest kept), else 128/256/512/1024.
+/* Solve every instance to tol.  block_size 0 = autotune (block size, CTAs per
+ * SM, and whether the largest instances run on thread-block clusters of 2, 4
+ * or 8 CTAs, each cluster solving one instance; every candidate timed on the
+ * whole batch, fastest kept), else 128/256/512/1024 with one CTA per instance.
  * Outputs (each may be NULL): u (3 × total nodes, instances in order),
  * per-instance iterations, status (0 / JFEM_NOT_CONVERGED), final relative
  * residual and latency (seconds from the instance's start to its end on the
  * GPU); solve_s = the launch's CUDA-event time. */
 int jfem_batch_solve(jfem_batch* batch, double tol, int max_iter, int block_size, double* u, int* iterations,
                      int* status, double* residual, double* latency_s, double* solve_s);
-/* Launch configuration of the last solve (the autotuner's choice when it ran). */
+/* Launch configuration of the last solve (the autotuner's choice when it ran):
+ * the single-CTA launch, and the cluster launch of the largest instances
+ * (cluster_size 1 and n_clustered 0 when there is none). */
 int jfem_batch_config(const jfem_batch* batch, int* block_size, int* grid);
+int jfem_batch_cluster_config(const jfem_batch* batch, int* cluster_size, int* n_clustered, int* cluster_block);
+/* Fix the configuration jfem_batch_solve uses when its block_size is 0 (instead
+ * of the autotuner): single-CTA block size, cluster size (1, 2, 4, 8), the
+ * number of largest instances solved on clusters and their block size (256 or
+ * 512).  block_size 0 returns to the autotuner. */
+int jfem_batch_set_config(jfem_batch* batch, int block_size, int cluster_size, int n_clustered, int cluster_block);
 
 /* Nodal strain or stress by a least-squares fit (postprocess!(problem, time,
  * Val{:strain} / Val{:stress}) with lsq_fit, src/problems_elasticity.jl:521-594):

@@ -105,6 +105,8 @@ SIGNATURES = {
     "jfem_batch_solve": (C.c_int, [_P, C.c_double, C.c_int, C.c_int, _f64p, C.POINTER(C.c_int),
                                    C.POINTER(C.c_int), _f64p, _f64p, _f64p]),
     "jfem_batch_config": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "jfem_batch_cluster_config": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "jfem_batch_set_config": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int]),
     "jfem_rcm": (C.c_int, [_i64, _i64, C.c_int, _i64p, C.c_int, _i64, _i64p, _i64p, _i64p]),
     "jfem_recover_field": (C.c_int, [_P, _f64p, C.c_int, C.c_double, C.c_int, _f64p, C.POINTER(C.c_int)]),
 }
@@ -418,6 +420,18 @@ class Batch:
         bs, g = C.c_int(0), C.c_int(0)
         self._check(self._lib.jfem_batch_config(self._h, C.byref(bs), C.byref(g)))
         return bs.value, g.value
+
+    def set_config(self, block_size: int, cluster_size: int = 1, n_clustered: int = 0, cluster_block: int = 0):
+        """Fix the launch configuration used by solve(block_size=0); block_size 0
+        returns to the autotuner."""
+        self._check(self._lib.jfem_batch_set_config(self._h, int(block_size), int(cluster_size), int(n_clustered),
+                                                     int(cluster_block)))
+
+    def cluster_config(self):
+        """(cluster size, number of instances solved on clusters, their block size)."""
+        cs, nl, bc = C.c_int(0), C.c_int(0), C.c_int(0)
+        self._check(self._lib.jfem_batch_cluster_config(self._h, C.byref(cs), C.byref(nl), C.byref(bc)))
+        return cs.value, nl.value, bc.value
 
 
 def rcm(conn, n_nodes: int, start: int = 0, index_base: int = 0):

@@ -57,7 +57,7 @@ struct BatchDev {
   float2* p = nullptr;
   float* Ap = nullptr;
   double* r64 = nullptr;
-  int* next = nullptr;                 // work counter (zeroed before every launch)
+  int* next = nullptr;                 // [2] work counters of the two launches (zeroed before every solve)
   int* iters = nullptr;                // [n_inst]
   int* status = nullptr;
   double* relres = nullptr;
@@ -72,14 +72,78 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 __device__ __forceinline__ bool dfree3(const uint8_t* mask, int64_t node, int c) { return !((mask[node] >> c) & 1); }
 
+// The CTAs that solve one instance: one CTA (C = 1), or the C CTAs of a thread-
+// block cluster.  Loops over the instance's elements, nodes and DOFs are
+// strided over all C·blockDim threads; sync() is a block barrier (C = 1) or a
+// cluster barrier with release/acquire order (global writes before it are
+// visible to every CTA of the cluster after it); sum() adds one value per CTA
+// in rank order through distributed shared memory, so every CTA gets the same,
+// deterministic total.  Nothing spins: cluster barriers are hardware barriers.
+__device__ __forceinline__ int cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return (int)r;
+}
+template <typename T>
+__device__ __forceinline__ T dsmem_load(const T* p, int rank);
+template <>
+__device__ __forceinline__ double dsmem_load<double>(const double* p, int rank) {
+  unsigned ra;
+  double v;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_u32(p)), "r"(rank));
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(ra) : "memory");
+  return v;
+}
+template <>
+__device__ __forceinline__ int dsmem_load<int>(const int* p, int rank) {
+  unsigned ra;
+  int v;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_u32(p)), "r"(rank));
+  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(ra) : "memory");
+  return v;
+}
+
+template <int C>
+struct Team {
+  int rank = 0;
+  double* xch = nullptr;   // __shared__ double[2]: this CTA's published partial, double-buffered
+  int par = 0;
+  __device__ __forceinline__ int64_t tid() const { return (int64_t)rank * blockDim.x + threadIdx.x; }
+  __device__ __forceinline__ int64_t nthr() const { return (int64_t)C * blockDim.x; }
+  __device__ __forceinline__ void sync() const {
+    if constexpr (C == 1) {
+      __syncthreads();
+    } else {
+      __threadfence();
+      __syncwarp();   // the .aligned barrier wants converged warps (callers may follow a thread-0 branch)
+      asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    }
+  }
+  // v: this CTA's value (the same in all its threads) → Σ over the team's CTAs
+  __device__ __forceinline__ double sum(double v) {
+    if constexpr (C == 1) {
+      return v;
+    } else {
+      if (threadIdx.x == 0) xch[par] = v;
+      sync();
+      double s = 0.0;
+#pragma unroll
+      for (int r = 0; r < C; ++r) s += dsmem_load(xch + par, r);
+      par ^= 1;   // the next sum writes the other slot: every CTA has read this one before passing that sum's barrier
+      return s;
+    }
+  }
+};
+
 // y = K v over the instance's elements (FP32: v double-float; FP64: v double)
 // into ye, then the node gather into out (masked).  Returns Σ v·out over the
 // instance (double-float products for FP32) when want_dot.
-template <bool FP32>
-__device__ double batch_apply(const BatchDev& a, int64_t n0, int64_t n1, int64_t e0, int64_t e1, const float2* v2,
-                              const double* v64, float* out32, double* out64, bool want_dot, double* sh) {
+template <bool FP32, int C>
+__device__ double batch_apply(const BatchDev& a, Team<C>& tm, int64_t n0, int64_t n1, int64_t e0, int64_t e1,
+                              const float2* v2, const double* v64, float* out32, double* out64, bool want_dot,
+                              double* sh) {
   constexpr int ET = JFEM_TET4;
-  for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+  for (int64_t e = e0 + tm.tid(); e < e1; e += tm.nthr()) {
     int nd[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) nd[i] = __ldg(a.conn + (int64_t)i * a.E + e);
@@ -116,10 +180,10 @@ __device__ double batch_apply(const BatchDev& a, int64_t n0, int64_t n1, int64_t
         for (int c = 0; c < 3; ++c) a.ye64[e * 12 + 3 * i + c] = y[i][c];
     }
   }
-  __syncthreads();
+  tm.sync();
   float2 dot = make_float2(0.f, 0.f);
   double dot64 = 0.0;
-  for (int64_t j = n0 + threadIdx.x; j < n1; j += blockDim.x) {
+  for (int64_t j = n0 + tm.tid(); j < n1; j += tm.nthr()) {
     const int k1 = __ldg(a.adj_ptr + j + 1);
     if (FP32) {
       float s[3] = {0.f, 0.f, 0.f};
@@ -154,17 +218,18 @@ __device__ double batch_apply(const BatchDev& a, int64_t n0, int64_t n1, int64_t
     }
   }
   double res = 0.0;
-  if (want_dot) res = FP32 ? block_sum_df(dot, sh) : block_sum(dot64, sh);
-  __syncthreads();
+  if (want_dot) res = tm.sum(FP32 ? block_sum_df(dot, sh) : block_sum(dot64, sh));
+  tm.sync();
   return res;
 }
 
 // Jacobi diagonal: per element the (i, c) diagonal of K_e for small strain,
 // w(μ(|g_i|² + g_ic²) + λ g_ic²) with g_i = ∇N_i, then a node gather.
-__device__ void batch_diag(const BatchDev& a, int64_t n0, int64_t n1, int64_t e0, int64_t e1) {
+template <int C>
+__device__ void batch_diag(const BatchDev& a, Team<C>& tm, int64_t n0, int64_t n1, int64_t e0, int64_t e1) {
   constexpr int ET = JFEM_TET4;
   const double w = qp_weight(ET, 0);
-  for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+  for (int64_t e = e0 + tm.tid(); e < e1; e += tm.nthr()) {
     double iJ[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) iJ[k] = a.g64[(int64_t)k * a.E + e];
@@ -180,8 +245,8 @@ __device__ void batch_diag(const BatchDev& a, int64_t n0, int64_t n1, int64_t e0
       for (int c = 0; c < 3; ++c) a.ye64[e * 12 + 3 * i + c] = w * (mu * (gg + g[c] * g[c]) + lam * g[c] * g[c]);
     }
   }
-  __syncthreads();
-  for (int64_t j = n0 + threadIdx.x; j < n1; j += blockDim.x) {
+  tm.sync();
+  for (int64_t j = n0 + tm.tid(); j < n1; j += tm.nthr()) {
     double s[3] = {0.0, 0.0, 0.0};
     const int k1 = __ldg(a.adj_ptr + j + 1);
     for (int k = __ldg(a.adj_ptr + j); k < k1; ++k) {
@@ -198,21 +263,22 @@ __device__ void batch_diag(const BatchDev& a, int64_t n0, int64_t n1, int64_t e0
       a.dinvf[3 * j + c] = (float)d;
     }
   }
-  __syncthreads();
+  tm.sync();
 }
 
 // r_rec → FP64 true residual: x += δx, r64 = f − K x (masked); returns
 // (‖r64‖², ‖r64 − r_rec‖²) and replaces r by r64 (double-float).
-__device__ void batch_refine(const BatchDev& a, int64_t n0, int64_t n1, int64_t e0, int64_t e1, double* sh,
-                             double* rr_t, double* drift2) {
-  for (int64_t q = 3 * n0 + threadIdx.x; q < 3 * n1; q += blockDim.x) {
+template <int C>
+__device__ void batch_refine(const BatchDev& a, Team<C>& tm, int64_t n0, int64_t n1, int64_t e0, int64_t e1,
+                             double* sh, double* rr_t, double* drift2) {
+  for (int64_t q = 3 * n0 + tm.tid(); q < 3 * n1; q += tm.nthr()) {
     a.x[q] += df_to_double(a.dx[q]);
     a.dx[q] = make_float2(0.f, 0.f);
   }
-  __syncthreads();
-  batch_apply<false>(a, n0, n1, e0, e1, nullptr, a.x, nullptr, a.r64, false, sh);
+  tm.sync();
+  batch_apply<false>(a, tm, n0, n1, e0, e1, nullptr, a.x, nullptr, a.r64, false, sh);
   double s1 = 0.0, s2 = 0.0;
-  for (int64_t q = 3 * n0 + threadIdx.x; q < 3 * n1; q += blockDim.x) {
+  for (int64_t q = 3 * n0 + tm.tid(); q < 3 * n1; q += tm.nthr()) {
     const bool fr = dfree3(a.mask, q / 3, (int)(q % 3));
     const double v = fr ? a.f[q] - a.r64[q] : 0.0;
     const double d = v - df_to_double(a.r[q]);
@@ -220,70 +286,72 @@ __device__ void batch_refine(const BatchDev& a, int64_t n0, int64_t n1, int64_t 
     s2 += d * d;
     a.r[q] = df_from_double(v);
   }
-  *rr_t = block_sum(s1, sh);
-  *drift2 = block_sum(s2, sh);
+  *rr_t = tm.sum(block_sum(s1, sh));
+  *drift2 = tm.sum(block_sum(s2, sh));
 }
 
 // z = D⁻¹ r (double-float), optionally p = z; returns r·z
-__device__ double batch_precond(const BatchDev& a, int64_t n0, int64_t n1, bool restart, double* sh) {
+template <int C>
+__device__ double batch_precond(const BatchDev& a, Team<C>& tm, int64_t n0, int64_t n1, bool restart, double* sh) {
   float2 rz = make_float2(0.f, 0.f);
-  for (int64_t q = 3 * n0 + threadIdx.x; q < 3 * n1; q += blockDim.x) {
+  for (int64_t q = 3 * n0 + tm.tid(); q < 3 * n1; q += tm.nthr()) {
     const float2 rq = a.r[q];
     const float2 zq = df_mul_f(rq, a.dinvf[q]);
     if (restart) a.p[q] = zq;
     rz = df_add(rz, df_mul(rq, zq));
   }
-  return block_sum_df(rz, sh);
+  return tm.sum(block_sum_df(rz, sh));
 }
 
-__device__ void batch_solve_instance(const BatchDev& a, int inst, double* sh) {
+template <int C>
+__device__ void batch_solve_instance(const BatchDev& a, Team<C>& tm, int inst, double* sh) {
   const int64_t n0 = a.node_off[inst], n1 = a.node_off[inst + 1];
   const int64_t e0 = a.elem_off[inst], e1 = a.elem_off[inst + 1];
-  batch_diag(a, n0, n1, e0, e1);
+  batch_diag(a, tm, n0, n1, e0, e1);
   // x = 0 (the batch's prescribed values are zero), r = f on the free DOFs
   double s = 0.0;
-  for (int64_t q = 3 * n0 + threadIdx.x; q < 3 * n1; q += blockDim.x) {
+  for (int64_t q = 3 * n0 + tm.tid(); q < 3 * n1; q += tm.nthr()) {
     const double v = dfree3(a.mask, q / 3, (int)(q % 3)) ? a.f[q] : 0.0;
     a.x[q] = 0.0;
     a.dx[q] = make_float2(0.f, 0.f);
     a.r[q] = df_from_double(v);
     s += v * v;
   }
-  const double bb = block_sum(s, sh);
+  const double bb = tm.sum(block_sum(s, sh));
   int it = 0, status = 0;
   double relres = 0.0;
   if (bb > 0.0) {
     const double goal = a.tol * a.tol * bb;
     double rr_true_last = bb, rr_best = bb;
-    double rz = batch_precond(a, n0, n1, true, sh);
+    double rz = batch_precond(a, tm, n0, n1, true, sh);
     int stalls = 0;
     status = JFEM_NOT_CONVERGED;
     relres = 1.0;
     for (;;) {
-      const double pAp = batch_apply<true>(a, n0, n1, e0, e1, a.p, nullptr, a.Ap, nullptr, true, sh);
+      const double pAp = batch_apply<true>(a, tm, n0, n1, e0, e1, a.p, nullptr, a.Ap, nullptr, true, sh);
       const double alpha = rz / pAp;
       const float2 al = df_from_double(alpha), nal = df_neg(al);
       float2 rzn = make_float2(0.f, 0.f), rrn = make_float2(0.f, 0.f);
-      for (int64_t q = 3 * n0 + threadIdx.x; q < 3 * n1; q += blockDim.x) {
+      for (int64_t q = 3 * n0 + tm.tid(); q < 3 * n1; q += tm.nthr()) {
         a.dx[q] = df_add(a.dx[q], df_mul(al, a.p[q]));
         const float2 rq = df_add(a.r[q], df_mul_f(nal, a.Ap[q]));
         a.r[q] = rq;
         rzn = df_add(rzn, df_mul(rq, df_mul_f(rq, a.dinvf[q])));
         rrn = df_add(rrn, df_mul(rq, rq));
       }
-      const double rz_new = block_sum_df(rzn, sh);
-      const double rr = block_sum_df(rrn, sh);
+      const double rz_new = tm.sum(block_sum_df(rzn, sh));
+      const double rr = tm.sum(block_sum_df(rrn, sh));
       ++it;
       // next direction first: a refinement keeps it (p·r = r·z holds for it)
       const float2 be = df_from_double(rz_new / rz);
-      for (int64_t q = 3 * n0 + threadIdx.x; q < 3 * n1; q += blockDim.x)
+      for (int64_t q = 3 * n0 + tm.tid(); q < 3 * n1; q += tm.nthr())
         a.p[q] = df_add(df_mul_f(a.r[q], a.dinvf[q]), df_mul(be, a.p[q]));
       rz = rz_new;
-      __syncthreads();
+      tm.sync();
       const bool bad = !(rr == rr) || !(pAp > 0.0);
       if (rr <= goal || rr < a.drop * a.drop * rr_true_last || it >= a.max_iter || bad) {
         double rr_t = 0.0, drift2 = 0.0;
-        batch_refine(a, n0, n1, e0, e1, sh, &rr_t, &drift2);
+        batch_refine(a, tm, n0, n1, e0, e1, sh, &rr_t, &drift2);
         const bool finite = rr_t == rr_t && rr_t < 1e300;
         if (finite && rr_t < rr_best) rr_best = rr_t;
         stalls = (finite && rr_t < 0.25 * rr_true_last) ? 0 : stalls + 1;
@@ -297,33 +365,47 @@ __device__ void batch_solve_instance(const BatchDev& a, int inst, double* sh) {
           break;
         }
         rr_true_last = rr_t;
-        rz = batch_precond(a, n0, n1, !(drift2 < 0.01 * rr_t), sh);
+        rz = batch_precond(a, tm, n0, n1, !(drift2 < 0.01 * rr_t), sh);
       }
     }
   }
-  if (threadIdx.x == 0) {
+  if (tm.rank == 0 && threadIdx.x == 0) {
     a.iters[inst] = it;
     a.status[inst] = status;
     a.relres[inst] = bb > 0.0 ? relres : 0.0;
   }
 }
 
-template <int BS>
-__global__ void __launch_bounds__(BS) k_batch_pcg(BatchDev a) {
+// Persistent solver over the instances order[k_begin..k_end): a team (one CTA,
+// or one cluster of C CTAs) takes the next position from the counter and
+// solves that instance.
+template <int BS, int C>
+__global__ void __launch_bounds__(BS) k_batch_pcg(BatchDev a, int* __restrict__ next, int k_begin, int k_end) {
   __shared__ double sh[32];
+  __shared__ double xch[2];
   __shared__ int s_k;
+  Team<C> tm;
+  tm.xch = xch;
+  if constexpr (C > 1) tm.rank = cluster_rank();
   for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) s_k = atomicAdd(a.next, 1);
-    __syncthreads();
-    const int k = s_k;
-    if (k >= a.n_inst) break;
+    tm.sync();
+    if (tm.rank == 0 && threadIdx.x == 0) s_k = k_begin + atomicAdd(next, 1);
+    tm.sync();
+    int k;
+    if constexpr (C == 1) {
+      k = s_k;
+    } else {
+      k = dsmem_load(&s_k, 0);
+      tm.sync();   // every CTA has read rank 0's s_k before it is written again
+    }
+    if (k >= k_end) break;
     const int inst = a.order[k];
     const unsigned long long t0 = global_ns();
-    batch_solve_instance(a, inst, sh);
-    __syncthreads();
-    if (threadIdx.x == 0) a.t_ns[inst] = global_ns() - t0;
+    batch_solve_instance(a, tm, inst, sh);
+    tm.sync();
+    if (tm.rank == 0 && threadIdx.x == 0) a.t_ns[inst] = global_ns() - t0;
   }
+  tm.sync();   // no CTA leaves while another may still read its shared memory
 }
 
 // ---------------------------------------------------------------------------
@@ -332,6 +414,8 @@ __global__ void __launch_bounds__(BS) k_batch_pcg(BatchDev a) {
 struct BatchHost {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;             // second branch of the captured solve
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::string err;
   // instances (host, FP64)
   std::vector<double> X;           // [N][3]
@@ -344,8 +428,17 @@ struct BatchHost {
   BatchDev d;
   std::vector<void*> owned;
   cudaGraphExec_t graph = nullptr;
-  int graph_bs = 0, graph_grid = 0;
-  int tuned_bs = 0, tuned_grid = 0;
+  struct Config {
+    int bs = 0, grid = 0;        // single-CTA launch over order[n_large..n_inst)
+    int cluster = 1, bs_c = 0;   // cluster launch over order[0..n_large), C CTAs per instance
+    int grid_c = 0, n_large = 0;
+    bool operator==(const Config& o) const {
+      return bs == o.bs && grid == o.grid && cluster == o.cluster && bs_c == o.bs_c && grid_c == o.grid_c &&
+             n_large == o.n_large;
+    }
+  };
+  Config graph_cfg, tuned;
+  Config forced;                 // set by jfem_batch_set_config (bs 0: none)
   double tuned_ms = 0.0;
   int64_t launches = 0;
 };
@@ -371,7 +464,7 @@ static void bfree_device(BatchHost* b) {
   for (void* p : b->owned) cudaFree(p);
   b->owned.clear();
   b->uploaded = false;
-  b->tuned_bs = b->tuned_grid = 0;
+  b->tuned = BatchHost::Config();
 }
 
 static int batch_upload(BatchHost* b) {
@@ -438,7 +531,7 @@ static int batch_upload(BatchHost* b) {
       (rc = bupload(b, &dinvf, ef, (size_t)3 * N)) || (rc = bupload(b, &dx, ef2, (size_t)3 * N)) ||
       (rc = bupload(b, &r, ef2, (size_t)3 * N)) || (rc = bupload(b, &p, ef2, (size_t)3 * N)) ||
       (rc = bupload(b, &Ap, ef, (size_t)3 * N)) || (rc = bupload(b, &r64, edb, (size_t)3 * N)) ||
-      (rc = bupload(b, &next, ei, 1)) || (rc = bupload(b, &iters, ei, (size_t)n_inst)) ||
+      (rc = bupload(b, &next, ei, 2)) || (rc = bupload(b, &iters, ei, (size_t)n_inst)) ||
       (rc = bupload(b, &status, ei, (size_t)n_inst)) || (rc = bupload(b, &relres, edb, (size_t)n_inst)) ||
       (rc = bupload(b, &tns, eu, (size_t)n_inst)))
     return rc;
@@ -468,50 +561,130 @@ static int batch_upload(BatchHost* b) {
 }
 
 template <int BS>
-static void launch_batch(BatchHost* b, int grid) {
-  k_batch_pcg<BS><<<grid, BS, 0, b->stream>>>(b->d);
+static void launch_single(BatchHost* b, cudaStream_t st, int grid, int k0, int k1) {
+  k_batch_pcg<BS, 1><<<grid, BS, 0, st>>>(b->d, b->d.next + 1, k0, k1);
 }
 
-static void enqueue_batch(BatchHost* b, int bs, int grid) {
-  cudaMemsetAsync(b->d.next, 0, sizeof(int), b->stream);
-  switch (bs) {
-    case 128: launch_batch<128>(b, grid); break;
-    case 256: launch_batch<256>(b, grid); break;
-    case 512: launch_batch<512>(b, grid); break;
-    default: launch_batch<1024>(b, grid); break;
+template <int BS, int C>
+static cudaError_t launch_cluster(BatchHost* b, int grid, int k0, int k1) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(BS);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = b->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_batch_pcg<BS, C>, b->d, b->d.next, k0, k1);
+}
+
+// Clusters of C CTAs of BS threads the device can hold at once (0: the shape
+// cannot be scheduled, so the autotuner skips it).
+template <int BS, int C>
+static int max_clusters(BatchHost* b, int grid) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(BS);
+  cfg.stream = b->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_batch_pcg<BS, C>, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
   }
-  b->launches += 1;
+  return n;
 }
 
-static int batch_graph(BatchHost* b, int bs, int grid) {
-  if (b->graph && b->graph_bs == bs && b->graph_grid == grid) return 0;
+static int max_clusters_for(BatchHost* b, int bs, int C, int grid) {
+  if (bs == 256) return C == 2 ? max_clusters<256, 2>(b, grid) : C == 4 ? max_clusters<256, 4>(b, grid) : max_clusters<256, 8>(b, grid);
+  return C == 2 ? max_clusters<512, 2>(b, grid) : C == 4 ? max_clusters<512, 4>(b, grid) : max_clusters<512, 8>(b, grid);
+}
+
+template <int BS>
+static cudaError_t launch_cluster_c(BatchHost* b, int C, int grid, int k0, int k1) {
+  switch (C) {
+    case 2: return launch_cluster<BS, 2>(b, grid, k0, k1);
+    case 4: return launch_cluster<BS, 4>(b, grid, k0, k1);
+    default: return launch_cluster<BS, 8>(b, grid, k0, k1);
+  }
+}
+
+// The largest n_large instances (the order is largest first) on clusters and
+// the rest on single CTAs, as two branches of the captured graph that run at
+// the same time (the side stream forks from and joins back into the main one;
+// the two kernels share no data and take work from separate counters).
+static int enqueue_batch(BatchHost* b, const BatchHost::Config& cf) {
+  cudaMemsetAsync(b->d.next, 0, 2 * sizeof(int), b->stream);
+  const bool both = cf.n_large > 0 && cf.n_large < b->d.n_inst;
+  cudaStream_t st_single = both ? b->side : b->stream;
+  if (both) {
+    cudaEventRecord(b->ev_fork, b->stream);
+    cudaStreamWaitEvent(b->side, b->ev_fork, 0);
+  }
+  if (cf.n_large > 0) {
+    const cudaError_t e = cf.bs_c == 256 ? launch_cluster_c<256>(b, cf.cluster, cf.grid_c, 0, cf.n_large)
+                                         : launch_cluster_c<512>(b, cf.cluster, cf.grid_c, 0, cf.n_large);
+    if (e != cudaSuccess) return bset_err(b, JFEM_ERR_CUDA, std::string("cluster launch: ") + cudaGetErrorString(e));
+    b->launches += 1;
+  }
+  if (cf.n_large < b->d.n_inst) {
+    switch (cf.bs) {
+      case 128: launch_single<128>(b, st_single, cf.grid, cf.n_large, b->d.n_inst); break;
+      case 256: launch_single<256>(b, st_single, cf.grid, cf.n_large, b->d.n_inst); break;
+      case 512: launch_single<512>(b, st_single, cf.grid, cf.n_large, b->d.n_inst); break;
+      default: launch_single<1024>(b, st_single, cf.grid, cf.n_large, b->d.n_inst); break;
+    }
+    b->launches += 1;
+  }
+  if (both) {
+    cudaEventRecord(b->ev_join, b->side);
+    cudaStreamWaitEvent(b->stream, b->ev_join, 0);
+  }
+  return 0;
+}
+
+static int batch_graph(BatchHost* b, const BatchHost::Config& cf) {
+  if (b->graph && b->graph_cfg == cf) return 0;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   b->graph = nullptr;
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return bset_err(b, JFEM_ERR_CUDA, "batch capture");
   const int64_t l0 = b->launches;
-  enqueue_batch(b, bs, grid);
+  const int rc = enqueue_batch(b, cf);
   b->launches = l0;
   e = cudaStreamEndCapture(b->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
   if (e != cudaSuccess) return bset_err(b, JFEM_ERR_CUDA, "batch capture end");
   e = cudaGraphInstantiate(&b->graph, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return bset_err(b, JFEM_ERR_CUDA, "batch graph instantiate");
-  b->graph_bs = bs;
-  b->graph_grid = grid;
+  b->graph_cfg = cf;
   return 0;
 }
 
-static int batch_run(BatchHost* b, int bs, int grid, float* ms) {
-  int rc = batch_graph(b, bs, grid);
+static int batch_run(BatchHost* b, const BatchHost::Config& cf, float* ms) {
+  int rc = batch_graph(b, cf);
   if (rc) return rc;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, b->stream);
   cudaError_t e = cudaGraphLaunch(b->graph, b->stream);
-  b->launches += 1;
+  b->launches += (cf.n_large > 0) + (cf.n_large < b->d.n_inst);
   cudaEventRecord(e1, b->stream);
   if (e == cudaSuccess) e = cudaEventSynchronize(e1);
   if (e == cudaSuccess) e = cudaGetLastError();
@@ -530,27 +703,48 @@ static int sm_count(int device) {
   return n > 0 ? n : 1;
 }
 
-// Times the whole batch for every (block size, CTAs per SM) candidate and keeps
-// the fastest; the ties go to the smaller configuration.
+// Times the whole batch for every candidate configuration and keeps the
+// fastest (ties to the earlier, simpler one): single-CTA teams for all
+// instances at block sizes 128–1024 and 1/2/4 CTAs per SM; then the largest
+// 1/8, 1/4 or 1/2 of the instances on clusters of 2, 4 or 8 CTAs (block 256 or
+// 512) running beside the rest on single CTAs of the best size above.
 static int batch_autotune(BatchHost* b) {
-  if (b->tuned_bs) return 0;
+  if (b->tuned.bs) return 0;
   const int sms = sm_count(b->device);
-  const int sizes[4] = {128, 256, 512, 1024};
-  const int per_sm[3] = {1, 2, 4};
+  const int n = b->d.n_inst;
   float best = 1e30f;
-  for (int bs : sizes)
-    for (int k : per_sm) {
-      if (bs * k > 2048) continue;
-      const int grid = std::min(b->d.n_inst, sms * k);
-      float ms = 0.f;
-      int rc = batch_run(b, bs, grid, &ms);
-      if (rc) return rc;
-      if (ms < best) {
-        best = ms;
-        b->tuned_bs = bs;
-        b->tuned_grid = grid;
-      }
+  auto try_cfg = [&](const BatchHost::Config& cf) -> int {
+    float ms = 0.f;
+    const int rc = batch_run(b, cf, &ms);
+    if (rc) return rc;
+    if (ms < best) {
+      best = ms;
+      b->tuned = cf;
     }
+    return 0;
+  };
+  for (int bs : {128, 256, 512, 1024})
+    for (int k : {1, 2, 4}) {
+      if (bs * k > 2048) continue;
+      BatchHost::Config cf;
+      cf.bs = bs;
+      cf.grid = std::min(n, sms * k);
+      if (int rc = try_cfg(cf)) return rc;
+    }
+  const BatchHost::Config single = b->tuned;
+  for (int frac : {8, 4, 2})
+    for (int C : {2, 4, 8})
+      for (int bs_c : {256, 512}) {
+        const int nl = n / frac;
+        if (nl < 1 || sms < C) continue;
+        BatchHost::Config cf = single;
+        cf.cluster = C;
+        cf.bs_c = bs_c;
+        cf.n_large = nl;
+        cf.grid_c = std::min(nl, sms / C) * C;
+        if (max_clusters_for(b, bs_c, C, cf.grid_c) < 1) continue;   // shape not schedulable here
+        if (int rc = try_cfg(cf)) return rc;
+      }
   b->tuned_ms = best;
   return 0;
 }
@@ -575,7 +769,14 @@ int jfem_batch_create(jfem_batch** out, int device) {
   jfem_batch* h = new (std::nothrow) jfem_batch();
   if (!h) return JFEM_ERR_OOM;
   h->b.device = device;
-  if (cudaStreamCreateWithFlags(&h->b.stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&h->b.stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->b.side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->b.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->b.ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    if (h->b.stream) cudaStreamDestroy(h->b.stream);
+    if (h->b.side) cudaStreamDestroy(h->b.side);
+    if (h->b.ev_fork) cudaEventDestroy(h->b.ev_fork);
+    if (h->b.ev_join) cudaEventDestroy(h->b.ev_join);
     delete h;
     return JFEM_ERR_CUDA;
   }
@@ -588,6 +789,9 @@ int jfem_batch_destroy(jfem_batch* h) {
   cudaSetDevice(h->b.device);
   jfem::bfree_device(&h->b);
   if (h->b.stream) cudaStreamDestroy(h->b.stream);
+  if (h->b.side) cudaStreamDestroy(h->b.side);
+  if (h->b.ev_fork) cudaEventDestroy(h->b.ev_fork);
+  if (h->b.ev_join) cudaEventDestroy(h->b.ev_join);
   delete h;
   return JFEM_OK;
 }
@@ -677,18 +881,28 @@ int jfem_batch_solve(jfem_batch* h, double tol, int max_iter, int block_size, do
     b->d.max_iter = max_iter;
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
-    b->tuned_bs = 0;
+    b->tuned = BatchHost::Config();
   }
-  int bs = block_size, grid = 0;
-  if (bs == 0) {
+  BatchHost::Config cf;
+  const int sms = jfem::sm_count(b->device);
+  if (block_size == 0 && b->forced.bs) {
+    cf = b->forced;
+    cf.n_large = std::min(cf.n_large, b->d.n_inst);
+    cf.grid = std::min(std::max(b->d.n_inst - cf.n_large, 1), sms * std::max(1, 1024 / cf.bs));
+    if (cf.n_large > 0) {
+      cf.grid_c = std::min(cf.n_large, std::max(sms / cf.cluster, 1)) * cf.cluster;
+      if (jfem::max_clusters_for(b, cf.bs_c, cf.cluster, cf.grid_c) < 1)
+        return jfem::bset_err(b, JFEM_ERR_INVALID, "cluster shape cannot be scheduled on this device");
+    }
+  } else if (block_size == 0) {
     if ((rc = jfem::batch_autotune(b))) return rc;
-    bs = b->tuned_bs;
-    grid = b->tuned_grid;
+    cf = b->tuned;
   } else {
-    grid = std::min(b->d.n_inst, jfem::sm_count(b->device) * std::max(1, 1024 / bs));
+    cf.bs = block_size;
+    cf.grid = std::min(b->d.n_inst, jfem::sm_count(b->device) * std::max(1, 1024 / block_size));
   }
   float ms = 0.f;
-  if ((rc = jfem::batch_run(b, bs, grid, &ms))) return rc;
+  if ((rc = jfem::batch_run(b, cf, &ms))) return rc;
   const int n = b->d.n_inst;
   std::vector<unsigned long long> tns((size_t)n);
   if (u) cudaMemcpyAsync(u, b->d.x, 3 * b->d.N * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
@@ -706,8 +920,40 @@ int jfem_batch_solve(jfem_batch* h, double tol, int max_iter, int block_size, do
 
 int jfem_batch_config(const jfem_batch* h, int* block_size, int* grid) {
   if (!h) return JFEM_ERR_INVALID;
-  if (block_size) *block_size = h->b.tuned_bs ? h->b.tuned_bs : h->b.graph_bs;
-  if (grid) *grid = h->b.tuned_bs ? h->b.tuned_grid : h->b.graph_grid;
+  const BatchHost::Config& cf = h->b.graph_cfg;
+  if (block_size) *block_size = cf.bs;
+  if (grid) *grid = cf.grid;
+  return JFEM_OK;
+}
+
+int jfem_batch_set_config(jfem_batch* h, int block_size, int cluster_size, int n_clustered, int cluster_block) {
+  if (!h) return JFEM_ERR_INVALID;
+  BatchHost* b = &h->b;
+  if (block_size == 0) {
+    b->forced = BatchHost::Config();
+    return JFEM_OK;
+  }
+  if (block_size != 128 && block_size != 256 && block_size != 512 && block_size != 1024)
+    return jfem::bset_err(b, JFEM_ERR_INVALID, "block_size must be 0 (autotune), 128, 256, 512 or 1024");
+  if (cluster_size != 1 && cluster_size != 2 && cluster_size != 4 && cluster_size != 8)
+    return jfem::bset_err(b, JFEM_ERR_INVALID, "cluster_size must be 1, 2, 4 or 8");
+  if (n_clustered < 0 || (cluster_size > 1 && cluster_block != 256 && cluster_block != 512))
+    return jfem::bset_err(b, JFEM_ERR_INVALID, "n_clustered must be >= 0 and cluster_block 256 or 512");
+  BatchHost::Config cf;
+  cf.bs = block_size;
+  cf.cluster = cluster_size;
+  cf.n_large = cluster_size > 1 ? n_clustered : 0;
+  cf.bs_c = cluster_size > 1 ? cluster_block : 0;
+  b->forced = cf;
+  return JFEM_OK;
+}
+
+int jfem_batch_cluster_config(const jfem_batch* h, int* cluster_size, int* n_clustered, int* cluster_block) {
+  if (!h) return JFEM_ERR_INVALID;
+  const BatchHost::Config& cf = h->b.graph_cfg;
+  if (cluster_size) *cluster_size = cf.n_large > 0 ? cf.cluster : 1;
+  if (n_clustered) *n_clustered = cf.n_large;
+  if (cluster_block) *cluster_block = cf.n_large > 0 ? cf.bs_c : 0;
   return JFEM_OK;
 }
 

@@ -49,6 +49,31 @@ def test_batch_autotune_and_block_sizes_agree(jfem):
         assert np.all(st == 0)
 
 
+@pytest.mark.parametrize("cluster,block", [(2, 512), (4, 256), (8, 256)])
+def test_cluster_teams_match_single_cta_teams(jfem, cluster, block):
+    """The largest half of the instances solved by thread-block clusters (one
+    instance per cluster, cluster-barrier synchronised, sums exchanged through
+    distributed shared memory in rank order) gives the single-CTA solutions to
+    the solver tolerance, every instance converged, and repeats bit for bit."""
+    ws = jfem.workloads.batch_instances(count=10, nmin=8, nmax=16, seed_item=80)
+    with jfem.Batch(0) as b:
+        for w in ws:
+            b.add_workload(w)
+        b.set_config(256)
+        ref, it0, st0, *_ = b.solve(tol=1e-9, max_iter=50000)
+        assert b.cluster_config() == (1, 0, 0)
+        b.set_config(256, cluster, 5, block)
+        us, it, st, res, lat, t = b.solve(tol=1e-9, max_iter=50000)
+        us2, it2, *_ = b.solve(tol=1e-9, max_iter=50000)
+        assert b.cluster_config() == (cluster, 5, block)
+        with pytest.raises(jfem.JFEMError):
+            b.set_config(256, 3, 5, block)
+    assert np.all(st0 == 0) and np.all(st == 0) and np.all(res <= 1e-9) and np.all(lat > 0)
+    for a, c in zip(us, ref):
+        assert rel_err(a, c) <= 1e-6
+    assert all(np.array_equal(a, c) for a, c in zip(us, us2)) and np.array_equal(it, it2)
+
+
 def test_batch_rejects_invalid_instances(jfem):
     w = jfem.workloads.batch_instances(count=1, nmin=8, nmax=8, seed_item=79)[0]
     m = w.mesh
