@@ -41,6 +41,10 @@ TOL = 1e-8
 # arithmetic, measured by the GPU arm of this benchmark); the CPU arm times a
 # bounded sample of iterations and scales to this count.
 FULL_PCG_ITERS = 6883
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one FP32 apply of
+# the 200×20×20 Tet10 beam, tile pass (73,905,152 + 3,734,016) plus boundary
+# pass (34,161,920 + 768), from one ncu capture of this benchmark's solve.
+APPLY_TRAFFIC_BYTES = {(200, 20, 20): 111_801_856}
 
 
 def parse():
@@ -473,7 +477,7 @@ def run_gpu(args):
                 "assembly": assembly,
                 "setup_s": t_setup,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": None,
+                             "frac": achieved / peak, "traffic": APPLY_TRAFFIC_BYTES.get(tuple(args.size)),
                              "kernel": "matrix-free FP32 apply (element + node-gather launches)",
                              "algorithmic_bytes": alg_bytes, "peak_kind": peak_kind},
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
