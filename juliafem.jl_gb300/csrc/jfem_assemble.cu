@@ -34,6 +34,20 @@ struct QD {
   static constexpr int SIZE = P + 9;
 };
 
+// Integration-point record of the isotropic small-strain scatter: the factors
+// every lane of a block column would otherwise recompute.
+template <int ET>
+struct QDI {
+  static constexpr int NN = Elem<ET>::NN;
+  static constexpr int G = 0;                 // ∇N         [NN][3]
+  static constexpr int SL = 3 * NN;           // w·λ·∇N     [NN][3]
+  static constexpr int SM = 6 * NN;           // w·μ·∇N     [NN][3]
+  static constexpr int GR = 9 * NN;           // w·μ·∇N_a·∇N_b [NN][NN]
+  static constexpr int W = GR + NN * NN;      // w·detJ
+  static constexpr int P = W + 1;             // σ [3][3] (P = σ for small strain)
+  static constexpr int SIZE = P + 9;
+};
+
 // Material law at one integration point (FP64).  gu = ∇u.  Returns 0 or an error.
 __device__ int material64(int model, bool finite, double lam, double mu, const double gu[3][3],
                           double F[3][3], double S6[6], double D[6][6]) {
@@ -91,7 +105,7 @@ __device__ int material64(int model, bool finite, double lam, double mu, const d
 }
 
 // Kernel 1: one thread per (element, integration point).
-template <int ET>
+template <int ET, bool ISO>
 __global__ void __launch_bounds__(128) k_qpoint64(int64_t E, const int* __restrict__ conn,
                                                   const double* __restrict__ X,
                                                   const double* __restrict__ u, int use_u,
@@ -100,6 +114,8 @@ __global__ void __launch_bounds__(128) k_qpoint64(int64_t E, const int* __restri
                                                   double* __restrict__ qd, int* err) {
   constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
   using L = QD<ET>;
+  using LI = QDI<ET>;
+  constexpr int RSIZE = ISO ? LI::SIZE : L::SIZE;
   const int64_t total = E * NQ;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (int64_t)gridDim.x * blockDim.x) {
@@ -124,10 +140,10 @@ __global__ void __launch_bounds__(128) k_qpoint64(int64_t E, const int* __restri
       }
     }
     const double det = det3(J);
-    double* out = qd + t * L::SIZE;
+    double* out = qd + t * RSIZE;
     if (!(det > 0.0)) {
       raise_error(err, JFEM_ERR_NEG_JACOBIAN);
-      for (int k = 0; k < L::SIZE; ++k) out[k] = 0.0;
+      for (int k = 0; k < RSIZE; ++k) out[k] = 0.0;
       continue;
     }
     double iJ[3][3];
@@ -152,6 +168,31 @@ __global__ void __launch_bounds__(128) k_qpoint64(int64_t E, const int* __restri
     double F[3][3], S6[6], D[6][6];
     const int rc = material64(model, finite != 0, lam_e[e], mu_e[e], gu, F, S6, D);
     if (rc) raise_error(err, rc);
+    if constexpr (ISO) {
+      const double w = qp_weight(ET, q) * det;
+      const double wl = w * lam_e[e], wm = w * mu_e[e];
+#pragma unroll
+      for (int i = 0; i < NN; ++i)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          out[LI::G + 3 * i + a] = g[i][a];
+          out[LI::SL + 3 * i + a] = wl * g[i][a];
+          out[LI::SM + 3 * i + a] = wm * g[i][a];
+        }
+#pragma unroll
+      for (int a = 0; a < NN; ++a)
+#pragma unroll
+        for (int b = 0; b < NN; ++b)
+          out[LI::GR + NN * a + b] = wm * (g[a][0] * g[b][0] + g[a][1] * g[b][1] + g[a][2] * g[b][2]);
+      out[LI::W] = w;
+      const int vi[6] = {0, 1, 2, 0, 1, 0}, vj[6] = {0, 1, 2, 1, 2, 2};   // Voigt order (c_VI, c_VJ)
+#pragma unroll
+      for (int I = 0; I < 6; ++I) {
+        out[LI::P + 3 * vi[I] + vj[I]] = S6[I];
+        out[LI::P + 3 * vj[I] + vi[I]] = S6[I];
+      }
+      continue;
+    }
 #pragma unroll
     for (int i = 0; i < NN; ++i)
 #pragma unroll
@@ -183,11 +224,12 @@ __device__ __forceinline__ void bl_column(const double F[9], const double g[3], 
 
 // Kernel 2: warp per node column; shared accumulator per warp laid out exactly as
 // the node's three CSC columns: acc[k][slot][i] ↔ nzval[9 bp + 3 d k + 3 slot + i].
-// ISO (small strain, Hooke): the block is formed from its closed form
+// ISO (small strain, Hooke; QDI records): the block is formed from its closed
+// form
 //   (B_bᵢ)ᵀ 𝔻 B_aₖ = λ ∇N_b,i ∇N_a,k + μ ∇N_a,i ∇N_b,k + μ δ_ik ∇N_a·∇N_b
-// (λ = 𝔻₁₂, μ = 𝔻₄₄ of the record), ≈13 FP64 operations per lane and point
-// instead of the ≈105 of the general BL(F)ᵀ 𝔻 BL(F) product; equal to it up to
-// rounding.
+// with w·λ·∇N, w·μ·∇N and w·μ·∇N_a·∇N_b precomputed per integration point:
+// 7 FP64 operations per lane and point instead of the ≈105 of the general
+// BL(F)ᵀ 𝔻 BL(F) product; equal to it up to rounding.
 template <int ET, bool ISO>
 __global__ void k_scatter64(int64_t N, int64_t E, const int* __restrict__ conn,
                             const int* __restrict__ adj_ptr, const unsigned* __restrict__ adj,
@@ -196,6 +238,7 @@ __global__ void k_scatter64(int64_t N, int64_t E, const int* __restrict__ conn,
                             double* __restrict__ nzval, double* __restrict__ fint) {
   constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
   using L = QD<ET>;
+  using LI = QDI<ET>;
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -213,21 +256,33 @@ __global__ void k_scatter64(int64_t N, int64_t E, const int* __restrict__ conn,
       const int64_t e = pk >> 4;
       const int a = (int)(pk & 15u);
       double K0 = 0.0, K1 = 0.0, K2 = 0.0;
+      if constexpr (ISO) {
+        double Kc = 0.0;   // the μ δ_ik ∇N_a·∇N_b term, added to component i below
+        for (int q = 0; q < NQ; ++q) {
+          const double* rec = qd + (e * NQ + q) * LI::SIZE;
+          const double ga0 = rec[LI::G + 3 * a], ga1 = rec[LI::G + 3 * a + 1], ga2 = rec[LI::G + 3 * a + 2];
+          if (active) {
+            const double gb0 = rec[LI::G + 3 * b], gb1 = rec[LI::G + 3 * b + 1], gb2 = rec[LI::G + 3 * b + 2];
+            const double A = rec[LI::SL + 3 * b + i], B = rec[LI::SM + 3 * a + i];
+            K0 += A * ga0 + B * gb0;
+            K1 += A * ga1 + B * gb1;
+            K2 += A * ga2 + B * gb2;
+            Kc += rec[LI::GR + NN * a + b];
+          }
+          if (lane < 3) {
+            const double* P = rec + LI::P;
+            fa += rec[LI::W] * (P[3 * lane] * ga0 + P[3 * lane + 1] * ga1 + P[3 * lane + 2] * ga2);
+          }
+        }
+        if (i == 0) K0 += Kc;
+        else if (i == 1) K1 += Kc;
+        else K2 += Kc;
+      } else {
       for (int q = 0; q < NQ; ++q) {
         const double* rec = qd + (e * NQ + q) * L::SIZE;
         const double w = rec[L::W];
         const double ga[3] = {rec[L::G + 3 * a], rec[L::G + 3 * a + 1], rec[L::G + 3 * a + 2]};
-        if (ISO && active) {
-          const double gb[3] = {rec[L::G + 3 * b], rec[L::G + 3 * b + 1], rec[L::G + 3 * b + 2]};
-          const double lam = rec[L::D + 1], mu = rec[L::D + 21];
-          const double dot = ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2];
-          const double gbi = i == 0 ? gb[0] : (i == 1 ? gb[1] : gb[2]);   // selects: no local-memory indexing
-          const double gai = i == 0 ? ga[0] : (i == 1 ? ga[1] : ga[2]);
-          const double A = w * lam * gbi, B = w * mu * gai, C = w * mu * dot;
-          K0 += A * ga[0] + B * gb[0] + (i == 0 ? C : 0.0);
-          K1 += A * ga[1] + B * gb[1] + (i == 1 ? C : 0.0);
-          K2 += A * ga[2] + B * gb[2] + (i == 2 ? C : 0.0);
-        } else if (active) {
+        if (active) {
           const double gb[3] = {rec[L::G + 3 * b], rec[L::G + 3 * b + 1], rec[L::G + 3 * b + 2]};
           double Fm[9];
 #pragma unroll
@@ -269,6 +324,7 @@ __global__ void k_scatter64(int64_t N, int64_t E, const int* __restrict__ conn,
           fa += w * (P[3 * lane] * ga[0] + P[3 * lane + 1] * ga[1] + P[3 * lane + 2] * ga[2]);
         }
       }
+      }   // general path
       if (active) {
         const int s = slot[(int64_t)t * NN + b];
         acc[0 * 3 * d + 3 * s + i] += K0;
@@ -421,9 +477,11 @@ int traction_device(Ctx* c, double* f_d) {
   return rc;
 }
 
+static bool iso_assembly(const Ctx* c) { return !c->finite && !c->geom && c->model == JFEM_LINEAR_ELASTIC; }
+
 template <int ET>
 static size_t qpoint_bytes(const Ctx* c) {
-  return (size_t)c->E * Elem<ET>::NQ * QD<ET>::SIZE * sizeof(double);
+  return (size_t)c->E * Elem<ET>::NQ * (iso_assembly(c) ? QDI<ET>::SIZE : QD<ET>::SIZE) * sizeof(double);
 }
 
 // The two assembly launches: integration-point records → qd, then the
@@ -436,14 +494,15 @@ static int enqueue_assembly(Ctx* c, double* qd, double* nzval_d, double* fint_d,
   while (wpb > 1 && (size_t)wpb * 9 * c->dmax * sizeof(double) > 96 * 1024) wpb >>= 1;
   const size_t sm = (size_t)wpb * 9 * c->dmax * sizeof(double);
   if (sm > 200 * 1024) return set_err(c, JFEM_ERR_INVALID, "node degree too large for assembly");
-  const bool iso = !c->finite && !c->geom && c->model == JFEM_LINEAR_ELASTIC;
+  const bool iso = iso_assembly(c);
   auto scatter = iso ? k_scatter64<ET, true> : k_scatter64<ET, false>;
+  auto qpoint = iso ? k_qpoint64<ET, true> : k_qpoint64<ET, false>;
   cudaFuncSetAttribute(scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   int64_t blocks = (c->N + wpb - 1) / wpb;
   if (blocks > 152 * 64) blocks = 152 * 64;
   if (ev) cudaEventRecord(ev[0], c->stream);
-  k_qpoint64<ET><<<grid_for(c->E * NQ, 128), 128, 0, c->stream>>>(
-      c->E, c->conn, c->X64, c->u_state, c->have_state ? 1 : 0, c->lam64, c->mu64, c->model, c->finite, qd, c->d_err);
+  qpoint<<<grid_for(c->E * NQ, 128), 128, 0, c->stream>>>(c->E, c->conn, c->X64, c->u_state, c->have_state ? 1 : 0,
+                                                          c->lam64, c->mu64, c->model, c->finite, qd, c->d_err);
   if (ev) cudaEventRecord(ev[1], c->stream);
   scatter<<<(unsigned)blocks, 32 * wpb, sm, c->stream>>>(c->N, c->E, c->conn, c->adj_ptr, c->adj, c->nb_ptr, c->slot,
                                                          qd, c->geom, c->dmax, nzval_d, fint_d);
