@@ -707,7 +707,8 @@ static int sm_count(int device) {
 // fastest (ties to the earlier, simpler one): single-CTA teams for all
 // instances at block sizes 128–1024 and 1/2/4 CTAs per SM; then the largest
 // 1/8, 1/4 or 1/2 of the instances on clusters of 2, 4 or 8 CTAs (block 256 or
-// 512) running beside the rest on single CTAs of the best size above.
+// 512, one or two cluster CTAs per SM) running beside the rest on single CTAs
+// of the best size above.
 static int batch_autotune(BatchHost* b) {
   if (b->tuned.bs) return 0;
   const int sms = sm_count(b->device);
@@ -734,17 +735,18 @@ static int batch_autotune(BatchHost* b) {
   const BatchHost::Config single = b->tuned;
   for (int frac : {8, 4, 2})
     for (int C : {2, 4, 8})
-      for (int bs_c : {256, 512}) {
-        const int nl = n / frac;
-        if (nl < 1 || sms < C) continue;
-        BatchHost::Config cf = single;
-        cf.cluster = C;
-        cf.bs_c = bs_c;
-        cf.n_large = nl;
-        cf.grid_c = std::min(nl, sms / C) * C;
-        if (max_clusters_for(b, bs_c, C, cf.grid_c) < 1) continue;   // shape not schedulable here
-        if (int rc = try_cfg(cf)) return rc;
-      }
+      for (int bs_c : {256, 512})
+        for (int per_sm : {1, 2}) {
+          const int nl = n / frac;
+          if (nl < 1 || sms < C) continue;
+          BatchHost::Config cf = single;
+          cf.cluster = C;
+          cf.bs_c = bs_c;
+          cf.n_large = nl;
+          cf.grid_c = std::min(nl, per_sm * sms / C) * C;
+          if (max_clusters_for(b, bs_c, C, cf.grid_c) < 1) continue;   // shape not schedulable here
+          if (int rc = try_cfg(cf)) return rc;
+        }
   b->tuned_ms = best;
   return 0;
 }

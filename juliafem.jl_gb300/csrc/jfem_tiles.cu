@@ -79,7 +79,30 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
       key[(size_t)e] = {code, e};
     }
   });
-  std::sort(key.begin(), key.end());
+  // keys are unique (element index in the low half), so any sort gives the
+  // same order: sort contiguous chunks on host threads, then merge pairwise
+  {
+    const int64_t hw = std::max<int64_t>(1, std::min<int64_t>(16, std::thread::hardware_concurrency()));
+    const int64_t nchunk = std::max<int64_t>(1, std::min<int64_t>(hw, E / 4096));
+    std::vector<int64_t> cut((size_t)nchunk + 1);
+    for (int64_t k = 0; k <= nchunk; ++k) cut[(size_t)k] = E * k / nchunk;
+    {
+      std::vector<std::thread> th;
+      for (int64_t k = 0; k < nchunk; ++k)
+        th.emplace_back([&key, &cut, k]() { std::sort(key.begin() + cut[(size_t)k], key.begin() + cut[(size_t)k + 1]); });
+      for (auto& x : th) x.join();
+    }
+    for (int64_t w = 1; w < nchunk; w *= 2) {
+      std::vector<std::thread> th;
+      for (int64_t k = 0; k + w < nchunk; k += 2 * w) {
+        const int64_t lo = cut[(size_t)k], mid = cut[(size_t)(k + w)], hi = cut[(size_t)std::min(k + 2 * w, nchunk)];
+        th.emplace_back([&key, lo, mid, hi]() {
+          std::inplace_merge(key.begin() + lo, key.begin() + mid, key.begin() + hi);
+        });
+      }
+      for (auto& x : th) x.join();
+    }
+  }
   const int64_t ntiles = (E + T - 1) / T;
   const int64_t Epad = ntiles * T;
   std::vector<int> perm((size_t)Epad, -1);
