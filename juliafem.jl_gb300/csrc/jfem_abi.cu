@@ -213,6 +213,7 @@ int jfem_set_formulation(jfem_ctx* h, int finite_strain, int geometric_stiffness
   Ctx* c = &h->c;
   c->finite = finite_strain ? 1 : 0;
   c->geom = geometric_stiffness ? 1 : 0;
+  ++c->state_version;
   return JFEM_OK;
 }
 
@@ -263,6 +264,7 @@ int jfem_set_state(jfem_ctx* h, const double* u) {
     cudaMemcpyAsync(c->u_state, u, 3 * c->N * sizeof(double), cudaMemcpyHostToDevice, c->stream);
     c->have_state = true;
   }
+  ++c->state_version;
   return jfem::sync_and_check(c, "state upload");
 }
 

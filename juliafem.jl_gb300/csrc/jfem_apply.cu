@@ -30,6 +30,9 @@ void launch_apply_hex8(Ctx* c, bool fp32, int mode, const double* v, const float
 void launch_tile_tet4(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop);
 void launch_tile_tet10(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop);
 void launch_tile_hex8(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop);
+void nh_state_tet4(Ctx* c);
+void nh_state_tet10(Ctx* c);
+void nh_state_hex8(Ctx* c);
 
 // ---------------------------------------------------------------------------
 // geometry preparation (FP64)
@@ -337,6 +340,7 @@ int geometry_invalidate(Ctx* c) {
   if (c->geo32) { dfree(c, c->geo32); c->geo32 = nullptr; }
   if (c->geoT32) { dfree(c, c->geoT32); c->geoT32 = nullptr; }
   c->geo_ready = false;
+  ++c->state_version;
   return 0;
 }
 
@@ -411,6 +415,29 @@ static void launch_gather(Ctx* c, bool fp32, bool masked, const double* v, doubl
 // partials in part[0..G), boundary partials in part[3G..4G)); otherwise the
 // two-phase apply (partials in part[0..G)).
 bool apply_is_tiled(const Ctx* c) { return c->geoT32 && c->ntiles > 0; }
+
+// Point state of the Neo-Hookean tangent at the current u_state (enqueued, no
+// sync); later tiled tangent applies read it until u, the material, the
+// formulation or the geometry change (state_version).
+int nh_state_prepare(Ctx* c) {
+  if (!c->finite || c->model != JFEM_NEO_HOOKEAN) return 0;
+  int rc = geometry_prepare(c);
+  if (rc) return rc;
+  if (!apply_is_tiled(c)) return 0;
+  if (nh_cache_ready(c)) return 0;
+  if (!c->nhstate) {
+    const int nq = c->et == JFEM_TET4 ? Elem<JFEM_TET4>::NQ : c->et == JFEM_TET10 ? Elem<JFEM_TET10>::NQ
+                                                                                    : Elem<JFEM_HEX8>::NQ;
+    if ((rc = dalloc(c, &c->nhstate, (size_t)16 * nq * c->Epad))) return rc;
+  }
+  switch (c->et) {
+    case JFEM_TET4: nh_state_tet4(c); break;
+    case JFEM_TET10: nh_state_tet10(c); break;
+    default: nh_state_hex8(c); break;
+  }
+  c->nhstate_version = c->state_version;
+  return 0;
+}
 
 static void launch_tiles(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
   switch (c->et) {

@@ -7,7 +7,9 @@
 
 namespace jfem {
 
-enum Kin { KIN_SMALL = 0, KIN_SVK = 1, KIN_NH = 2 };
+// KIN_NHC: Neo-Hookean tangent from the cached point state (F, C⁻¹, μ − λ ln J)
+enum Kin { KIN_SMALL = 0, KIN_SVK = 1, KIN_NH = 2, KIN_NHC = 3 };
+__host__ __device__ constexpr bool kin_needs_u(int kin) { return kin == KIN_SVK || kin == KIN_NH; }
 
 // ---------------------------------------------------------------------------
 // constitutive flux at one integration point
@@ -97,6 +99,59 @@ __device__ __forceinline__ bool flux_tangent(const R gu[3][3], const R gv[3][3],
   return ok;
 }
 
+// Neo-Hookean tangent action from the cached state of point q (16 values per
+// point: F row-major, C⁻¹ as 00 11 22 01 12 02, cc = μ − λ ln J; the same
+// scaling as the record's λ, μ):  S = μ I − cc C⁻¹,
+// δS = λ (C⁻¹:δE) C⁻¹ + 2 cc C⁻¹ δE C⁻¹,  δP = F δS (+ ∇v S with GEOM).
+template <typename R, bool GEOM, class ST>
+__device__ __forceinline__ void flux_tangent_cached(const ST& st, int q, const R gv[3][3], R lam, R mu,
+                                                    R P[3][3]) {
+  R F[3][3], Ci[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) F[i][j] = st(16 * q + 3 * i + j);
+  Ci[0][0] = st(16 * q + 9);
+  Ci[1][1] = st(16 * q + 10);
+  Ci[2][2] = st(16 * q + 11);
+  Ci[0][1] = Ci[1][0] = st(16 * q + 12);
+  Ci[1][2] = Ci[2][1] = st(16 * q + 13);
+  Ci[0][2] = Ci[2][0] = st(16 * q + 14);
+  const R cc = st(16 * q + 15);
+  R FtG[3][3], dE[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) FtG[i][j] = F[0][i] * gv[0][j] + F[1][i] * gv[1][j] + F[2][i] * gv[2][j];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dE[i][j] = R(0.5) * (FtG[i][j] + FtG[j][i]);
+  R CidE[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) CidE[i][j] = Ci[i][0] * dE[0][j] + Ci[i][1] * dE[1][j] + Ci[i][2] * dE[2][j];
+  const R tr = CidE[0][0] + CidE[1][1] + CidE[2][2];
+  R S[3][3], dS[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      S[i][j] = (i == j ? mu : R(0)) - cc * Ci[i][j];
+      const R CdC = CidE[i][0] * Ci[0][j] + CidE[i][1] * Ci[1][j] + CidE[i][2] * Ci[2][j];
+      dS[i][j] = lam * tr * Ci[i][j] + R(2) * cc * CdC;
+    }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      R v = F[i][0] * dS[0][j] + F[i][1] * dS[1][j] + F[i][2] * dS[2][j];
+      if (GEOM) v += gv[i][0] * S[0][j] + gv[i][1] * S[1][j] + gv[i][2] * S[2][j];
+      P[i][j] = v;
+    }
+}
+
 // First Piola stress P = F S at state u (finite) — internal force flux.
 template <typename R, int KIN>
 __device__ __forceinline__ bool flux_pk1(const R gu[3][3], R lam, R mu, R P[3][3]) {
@@ -170,11 +225,15 @@ struct GeoRegs {
 //   MODE 0: y = K v (linear) / K_T(u) v (finite); MODE 1: y = f_int(u).
 // Returns false when the material state is invalid (det C ≤ 0).
 // ---------------------------------------------------------------------------
-template <int ET, typename R, bool AFFINE, int KIN, bool GEOM, int MODE, class GEO>
+struct NoState {
+  __device__ __forceinline__ float operator()(int) const { return 0.f; }
+};
+
+template <int ET, typename R, bool AFFINE, int KIN, bool GEOM, int MODE, class GEO, class ST = NoState>
 __device__ __forceinline__ bool element_op(const R (&dv)[Elem<ET>::NN][3], const R (&du)[Elem<ET>::NN][3],
-                                           const GEO& geo, R (&y)[Elem<ET>::NN][3]) {
+                                           const GEO& geo, R (&y)[Elem<ET>::NN][3], const ST& st = ST()) {
   constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
-  constexpr bool NEED_U = (KIN != KIN_SMALL);
+  constexpr bool NEED_U = kin_needs_u(KIN);
   constexpr bool NEED_V = (MODE == 0);
 #pragma unroll
   for (int i = 0; i < NN; ++i) y[i][0] = y[i][1] = y[i][2] = R(0);
@@ -240,6 +299,8 @@ __device__ __forceinline__ bool element_op(const R (&dv)[Elem<ET>::NN][3], const
       ok &= flux_pk1<R, KIN>(gu, lam, mu, P);
     } else if (KIN == KIN_SMALL) {
       flux_small<R>(gv, lam, mu, P);
+    } else if (KIN == KIN_NHC) {
+      flux_tangent_cached<R, GEOM>(st, q, gv, lam, mu, P);
     } else {
       ok &= flux_tangent<R, KIN, GEOM>(gu, gv, lam, mu, P);
     }
@@ -284,7 +345,7 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
                                                     int mask_in) {
   constexpr int NN = Elem<ET>::NN;
   if (stop && *stop) return;
-  constexpr bool NEED_U = (KIN != KIN_SMALL);
+  constexpr bool NEED_U = kin_needs_u(KIN);
   constexpr bool NEED_V = (MODE == 0);
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
     int nodes[NN];
@@ -384,19 +445,19 @@ constexpr int TILE_PTR_BITS = 13;   // sadj offsets < 2^13 (T·NN ≤ 2560)
 static_assert(JFEM_TILE * 10 < (1 << TILE_PTR_BITS), "tile adjacency offsets must fit 13 bits");
 
 template <int ET, bool AFFINE, int KIN, bool GEOM>
-__global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS : 1) k_tile_apply(
+__global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS : (KIN == KIN_NHC ? 2 : 1)) k_tile_apply(
     int64_t ntiles, int64_t E, int64_t Epad, const int* __restrict__ tnode_ptr, const int* __restrict__ tnodes,
     const uint16_t* __restrict__ tconn, const float* __restrict__ geo, const uint16_t* __restrict__ tadj_ptr,
     const uint16_t* __restrict__ tadj, const int* __restrict__ tout,
     const float2* __restrict__ v2, const double* __restrict__ u,
     const uint8_t* __restrict__ mask, int masked, int Lmax, float* __restrict__ y, float4* __restrict__ bpart,
-    double* __restrict__ part, int* err, const int* __restrict__ stop) {
+    double* __restrict__ part, const float* __restrict__ nhs, int* err, const int* __restrict__ stop) {
   constexpr int NN = Elem<ET>::NN;
   constexpr int T = JFEM_TILE;
   constexpr int NADJ = T * NN;   // adjacency entries per tile; NADJ·2 bytes is a multiple of 16
   constexpr int NR = tile_node_rounds<ET>();
   constexpr unsigned PMASK = (1u << TILE_PTR_BITS) - 1;
-  constexpr bool NEED_U = (KIN != KIN_SMALL);
+  constexpr bool NEED_U = kin_needs_u(KIN);
   constexpr int NCOPY = 1 + NN + (AFFINE ? 11 : 0);   // bulk copies per tile
   constexpr unsigned TILE_BYTES = (unsigned)((NADJ + NN * T) * sizeof(uint16_t) + (AFFINE ? 11 * T * sizeof(float) : 0));
   static_assert(NCOPY <= 32, "one bulk copy per lane of warp 0");
@@ -524,8 +585,15 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
         }
       }
       float yl[NN][3];
-      if constexpr (AFFINE) ok &= element_op<ET, float, true, KIN, GEOM, 0>(dv, du, GeoRegs<float>{rec}, yl);
-      else ok &= element_op<ET, float, false, KIN, GEOM, 0>(dv, du, GeoGlobal<float>{geo + e, Epad}, yl);
+      if constexpr (KIN == KIN_NHC) {   // point state cached in tile order: [16·n_q][Epad]
+        const GeoGlobal<float> st{nhs + e, Epad};
+        if constexpr (AFFINE) ok &= element_op<ET, float, true, KIN, GEOM, 0>(dv, du, GeoRegs<float>{rec}, yl, st);
+        else ok &= element_op<ET, float, false, KIN, GEOM, 0>(dv, du, GeoGlobal<float>{geo + e, Epad}, yl, st);
+      } else if constexpr (AFFINE) {
+        ok &= element_op<ET, float, true, KIN, GEOM, 0>(dv, du, GeoRegs<float>{rec}, yl);
+      } else {
+        ok &= element_op<ET, float, false, KIN, GEOM, 0>(dv, du, GeoGlobal<float>{geo + e, Epad}, yl);
+      }
 #pragma unroll
       for (int a = 0; a < NN; ++a) {
         yxy[a * T + tid] = make_float2(yl[a][0], yl[a][1]);
@@ -621,20 +689,30 @@ static void dispatch_kin(Ctx* c, const R* geo, const double* v, const float2* v2
 template <int ET, bool AFFINE, int KIN, bool GEOM>
 static void launch_tile_k(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
   constexpr int NN = Elem<ET>::NN;
-  const size_t sm = tile_smem_bytes<NN, KIN != KIN_SMALL, AFFINE>(c->tile_Lmax);
+  const size_t sm = tile_smem_bytes<NN, kin_needs_u(KIN), AFFINE>(c->tile_Lmax);
   auto kern = k_tile_apply<ET, AFFINE, KIN, GEOM>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   const unsigned g = JFEM_RED_BLOCKS;   // CTAs take tiles b, b + g, …
   kern<<<g, JFEM_TILE, sm, c->stream>>>(
       c->ntiles, c->E, c->Epad, c->tnode_ptr, c->tnodes, c->tconn, c->geoT32, c->tadj_ptr, c->tadj, c->tout,
-      v2, c->u_state, c->mask, masked ? 1 : 0, c->tile_Lmax, y, c->bpart, part, c->d_err, stop);
+      v2, c->u_state, c->mask, masked ? 1 : 0, c->tile_Lmax, y, c->bpart, part, c->nhstate, c->d_err, stop);
   c->launches += 1;
 }
 
 // Tiled FP32 element + in-tile gather launch (the boundary sum is a separate kernel).
 template <int ET>
 void launch_tile_et(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
-  const int kin = !c->finite ? KIN_SMALL : (c->model == JFEM_NEO_HOOKEAN ? KIN_NH : KIN_SVK);
+  int kin = !c->finite ? KIN_SMALL : (c->model == JFEM_NEO_HOOKEAN ? KIN_NH : KIN_SVK);
+  if (kin == KIN_NH && nh_cache_ready(c)) {
+    if (c->geo_affine) {
+      if (c->geom) launch_tile_k<ET, true, KIN_NHC, true>(c, v2, y, masked, part, stop);
+      else launch_tile_k<ET, true, KIN_NHC, false>(c, v2, y, masked, part, stop);
+    } else {
+      if (c->geom) launch_tile_k<ET, false, KIN_NHC, true>(c, v2, y, masked, part, stop);
+      else launch_tile_k<ET, false, KIN_NHC, false>(c, v2, y, masked, part, stop);
+    }
+    return;
+  }
   if (c->geo_affine) {
     if (kin == KIN_SMALL) launch_tile_k<ET, true, KIN_SMALL, false>(c, v2, y, masked, part, stop);
     else if (kin == KIN_SVK) {
@@ -654,6 +732,103 @@ void launch_tile_et(Ctx* c, const float2* v2, float* y, bool masked, double* par
       else launch_tile_k<ET, false, KIN_NH, false>(c, v2, y, masked, part, stop);
     }
   }
+}
+
+// Neo-Hookean point state at u (tile order, one thread per tile position):
+// ∇u from the FP32 state differences exactly as the tangent apply forms it,
+// F = I + ∇u, C = FᵀF, C⁻¹, cc = μ − λ ln J with the record's λ, μ.
+template <int ET, bool AFFINE>
+__global__ void __launch_bounds__(128) k_nh_state(int64_t E, int64_t Epad, const int* __restrict__ perm,
+                                                  const int* __restrict__ conn, const double* __restrict__ u,
+                                                  const float* __restrict__ geo, float* __restrict__ st,
+                                                  int* err) {
+  constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < E; p += (int64_t)gridDim.x * blockDim.x) {
+    const int e = perm[p];   // positions below E hold elements
+    float u0[3], du[NN][3];
+    const int64_t g0 = conn[e];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) u0[c] = (float)u[3 * g0 + c];
+#pragma unroll
+    for (int i = 1; i < NN; ++i) {
+      const int64_t g = conn[(int64_t)i * E + e];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) du[i][c] = (float)u[3 * g + c] - u0[c];
+    }
+    const GeoGlobal<float> rec{geo + p, Epad};
+    float iJ[9], lam, mu;
+    if (AFFINE) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) iJ[k] = rec(k);
+      lam = rec(9);
+      mu = rec(10);
+    } else {
+      lam = rec(10 * NQ);
+      mu = rec(10 * NQ + 1);
+    }
+    bool ok = true;
+#pragma unroll 1
+    for (int q = 0; q < NQ; ++q) {
+      if (!AFFINE) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) iJ[k] = rec(10 * q + k);
+      }
+      float G[3][3], F[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          float s = 0.f;
+#pragma unroll
+          for (int i = 1; i < NN; ++i) {
+            const float dn = dnr<float>(ET, q, i, a);
+            if (dn != 0.f) s += du[i][c] * dn;
+          }
+          G[c][a] = s;
+        }
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          F[c][d] = (G[c][0] * iJ[3 * d] + G[c][1] * iJ[3 * d + 1] + G[c][2] * iJ[3 * d + 2]) + (c == d ? 1.f : 0.f);
+      float C[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) C[i][j] = F[0][i] * F[0][j] + F[1][i] * F[1][j] + F[2][i] * F[2][j];
+      const float detC = det3(C);
+      ok &= detC > 0.f;
+      float Ci[3][3];
+      adj3(C, Ci);
+      const float id = 1.f / detC;
+      const float lnJ = 0.5f * logf(detC);
+      float* o = st + p;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) o[(int64_t)(16 * q + 3 * i + j) * Epad] = F[i][j];
+      o[(int64_t)(16 * q + 9) * Epad] = Ci[0][0] * id;
+      o[(int64_t)(16 * q + 10) * Epad] = Ci[1][1] * id;
+      o[(int64_t)(16 * q + 11) * Epad] = Ci[2][2] * id;
+      o[(int64_t)(16 * q + 12) * Epad] = Ci[0][1] * id;
+      o[(int64_t)(16 * q + 13) * Epad] = Ci[1][2] * id;
+      o[(int64_t)(16 * q + 14) * Epad] = Ci[0][2] * id;
+      o[(int64_t)(16 * q + 15) * Epad] = mu - lam * lnJ;
+    }
+    if (!ok) raise_error(err, JFEM_ERR_NAN);
+  }
+}
+
+template <int ET>
+void nh_state_et(Ctx* c) {
+  const unsigned g = grid_for(c->E, 128);
+  if (c->geo_affine)
+    k_nh_state<ET, true><<<g, 128, 0, c->stream>>>(c->E, c->Epad, c->tperm, c->conn, c->u_state, c->geoT32,
+                                                   c->nhstate, c->d_err);
+  else
+    k_nh_state<ET, false><<<g, 128, 0, c->stream>>>(c->E, c->Epad, c->tperm, c->conn, c->u_state, c->geoT32,
+                                                    c->nhstate, c->d_err);
+  c->launches += 1;
 }
 
 // FP32 element pass (mode 0 only).  v2: split copy of v, see k_apply_elem.

@@ -9,4 +9,5 @@ void launch_apply_tet4(Ctx* c, bool fp32, int mode, const double* v, const float
 void launch_tile_tet4(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
   launch_tile_et<JFEM_TET4>(c, v2, y, masked, part, stop);
 }
+void nh_state_tet4(Ctx* c) { nh_state_et<JFEM_TET4>(c); }
 }  // namespace jfem

@@ -328,6 +328,9 @@ struct Ctx {
   int* bptr = nullptr;          // [n_bnodes+1] runs of bpart per shared node
   float4* bpart = nullptr;      // [n_bslots] tile partial sums (x, y, z, unused), grouped by node, ascending tile
   float* geoT32 = nullptr;      // geometry records in tile order
+  float* nhstate = nullptr;     // [16·n_q][Epad] Neo-Hookean point state at u_state (F, C⁻¹ sym, μ − λ ln J), tile order
+  uint64_t state_version = 1;   // bumped whenever u_state, the material, the formulation or the geometry change
+  uint64_t nhstate_version = 0; // state_version nhstate was computed at
 
   // scratch
   float* ye32 = nullptr;
@@ -416,6 +419,10 @@ void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, b
                    const int* stop, const float2* v2);
 void enqueue_split(Ctx* c, const double* v, float2* v2);
 bool apply_is_tiled(const Ctx* c);
+// Neo-Hookean tangent applies read the point state cached for the current u
+// (nh_state_prepare; off the captured graphs) instead of recomputing it.
+inline bool nh_cache_ready(const Ctx* c) { return c->nhstate && c->nhstate_version == c->state_version; }
+int nh_state_prepare(Ctx* c);
 void enqueue_apply_tiled(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop,
                          SolverScalars* sc = nullptr);
 void enqueue_internal_force(Ctx* c, double* f);

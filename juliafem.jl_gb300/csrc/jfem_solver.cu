@@ -576,7 +576,7 @@ static void enqueue_iteration(Ctx* c, bool fp32, int slot) {
 // kind: 0 FP64 PCG, 1 mixed PCG, 2 FCG Jacobi, 3 FCG learned
 static int graph_key(Ctx* c, int kind) {
   return kind | (c->finite << 2) | (c->model << 3) | (c->geom << 4) | ((c->geo_affine ? 1 : 0) << 5) |
-         (c->et << 6) | ((c->geoT32 ? 1 : 0) << 11);
+         (c->et << 6) | ((c->geoT32 ? 1 : 0) << 11) | ((nh_cache_ready(c) ? 1 : 0) << 12);
 }
 
 static int build_graph(Ctx* c, int kind) {
@@ -947,6 +947,7 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
   if (!c->have_state) {
     cudaMemsetAsync(c->u_state, 0, n * sizeof(double), c->stream);
     c->have_state = true;
+    ++c->state_version;
   }
   const int steps = o->n_load_steps > 0 ? o->n_load_steps : 1;
   const bool fp32 = o->precision == JFEM_MIXED;
@@ -997,6 +998,7 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
       if (eta > o->forcing_max) eta = o->forcing_max;
       if (eta < 1e-12) eta = 1e-12;
       cudaMemsetAsync(c->x, 0, n * sizeof(double), c->stream);
+      if (fp32 && (rc = nh_state_prepare(c))) return rc;   // tangent point state at u for this Newton step
       PcgResult pr;
       if ((rc = pcg(c, c->b, fp32, eta, o->max_cg_per_newton, o->time_budget_s, t0, false, true, &pr))) return rc;
       total_cg += pr.iters;
@@ -1005,6 +1007,7 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
       k_update_state<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, c->u_state, c->x, c->gvals, frac, first ? 1 : 0,
                                                             c->mask);
       c->launches += 1;
+      ++c->state_version;
       if (st && hist < JFEM_HISTORY_MAX) {
         st->history[3 * hist] = pr.iters;
         st->history[3 * hist + 1] = rn;
