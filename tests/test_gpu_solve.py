@@ -72,6 +72,28 @@ def test_newton_neo_hookean_cube(jfem, gpu_ctx_factory):
         assert st.history_len == st.newton_iterations > 0
 
 
+def test_newton_tangent_cache_follows_the_state(jfem, gpu_ctx_factory):
+    """The mixed Newton solve reads a per-step cache of the Neo-Hookean point
+    state; after the solve (u moved on) and after set_state, the FP32 tiled
+    tangent apply at the current state must agree with the FP64 apply, so a
+    stale cache cannot be used."""
+    w = jfem.workloads.cube_compression(n=6, steps=3, top_uz=-0.1)
+    v = np.random.default_rng(5).standard_normal(w.mesh.n_dofs)
+    with gpu_ctx_factory(w) as ctx:
+        u, st, rc = ctx.solve(method=2, precision=1, tol=1e-10, newton_tol=1e-10, max_newton=30,
+                              max_cg_per_newton=2000, n_load_steps=3)
+        assert rc == 0 and st.newton_iterations > 0
+        ctx.set_state(u)
+        y32, y64 = ctx.apply(v, fp32=True, masked=True), ctx.apply(v, fp32=False, masked=True)
+        assert rel_err(y32, y64) <= 1e-5
+        ctx.set_state(0.5 * u)
+        z32, z64 = ctx.apply(v, fp32=True, masked=True), ctx.apply(v, fp32=False, masked=True)
+        assert rel_err(z32, z64) <= 1e-5 and rel_err(z64, y64) > 1e-3
+        u2, st2, rc2 = ctx.solve(method=2, precision=1, tol=1e-10, newton_tol=1e-10, max_newton=30,
+                                 max_cg_per_newton=2000, n_load_steps=3)
+    assert rc2 == 0 and rel_err(u2, u) <= 1e-7
+
+
 def test_solve_api_physics(jfem):
     w = jfem.workloads.cfg_tet4_cantilever()
     d = np.load(GOLDEN / "tet4_cantilever.npz")
