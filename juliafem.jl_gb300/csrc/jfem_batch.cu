@@ -634,7 +634,13 @@ static int enqueue_batch(BatchHost* b, const BatchHost::Config& cf) {
   if (cf.n_large > 0) {
     const cudaError_t e = cf.bs_c == 256 ? launch_cluster_c<256>(b, cf.cluster, cf.grid_c, 0, cf.n_large)
                                          : launch_cluster_c<512>(b, cf.cluster, cf.grid_c, 0, cf.n_large);
-    if (e != cudaSuccess) return bset_err(b, JFEM_ERR_CUDA, std::string("cluster launch: ") + cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+      if (both) {   // close the fork so the capture (if any) ends cleanly
+        cudaEventRecord(b->ev_join, b->side);
+        cudaStreamWaitEvent(b->stream, b->ev_join, 0);
+      }
+      return bset_err(b, JFEM_ERR_CUDA, std::string("cluster launch: ") + cudaGetErrorString(e));
+    }
     b->launches += 1;
   }
   if (cf.n_large < b->d.n_inst) {
@@ -745,7 +751,10 @@ static int batch_autotune(BatchHost* b) {
           cf.n_large = nl;
           cf.grid_c = std::min(nl, per_sm * sms / C) * C;
           if (max_clusters_for(b, bs_c, C, cf.grid_c) < 1) continue;   // shape not schedulable here
-          if (int rc = try_cfg(cf)) return rc;
+          if (try_cfg(cf)) {   // a cluster shape the launch refused: keep the configurations that ran
+            cudaGetLastError();
+            b->err.clear();
+          }
         }
   b->tuned_ms = best;
   return 0;
