@@ -98,13 +98,20 @@ def max_over_ranks(ws, v, device=None):
 # ---------------------------------------------------------------------------
 # CPU oracle sample (cpu_baseline and --impl reference)
 # ---------------------------------------------------------------------------
-def cpu_sample(jfem, size, div, iters):
-    """Oracle (C++ FP64, OpenMP on all host cores): assemble a 1/div slab of the
-    workload into CSC and run `iters` Jacobi-PCG iterations on it; scale to the
-    full workload (work is linear in elements / DOFs) and to FULL_PCG_ITERS."""
+def cpu_sample(jfem, size, div, iters, threads=0):
+    """Oracle (C++ FP64, OpenMP on all host cores, or `threads`): assemble a
+    1/div slab of the workload into CSC and run `iters` Jacobi-PCG iterations on
+    it; scale to the full workload (work is linear in elements / DOFs) and to
+    FULL_PCG_ITERS."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
     oracle.build()
+    if threads:
+        oracle.set_threads(threads)
+        try:
+            return cpu_sample(jfem, size, div, iters)
+        finally:
+            oracle.set_threads(0)
     nx, ny, nz = size
     sx = max(1, nx // div)
     w = jfem.workloads.cantilever(10, sx, ny, nz, 20.0 * sx / 200, 2.0 * ny / 20, 2.0 * nz / 20)
@@ -123,7 +130,7 @@ def cpu_sample(jfem, size, div, iters):
     sample = (f"Tet10 {sx}x{ny}x{nz} slab ({m.n_elem} elements, {m.n_dofs} DOFs): CSC assembly + {it} "
               f"Jacobi-PCG iterations, scaled x{scale:g} in size and to {FULL_PCG_ITERS} iterations")
     return dict(value=value, unit=UNIT, cores=oracle.get_threads(), kind="port", sample=sample,
-                assembly_s=t_asm, s_per_iter=t_iter)
+                assembly_s=t_asm, s_per_iter=t_iter, pcg_s=t_iter * FULL_PCG_ITERS)
 
 
 def run_reference(args):
@@ -500,7 +507,11 @@ def run_gpu(args):
             line["learned_preconditioner"] = learned_leg(jfem, args, local, w)
         if ws == 1 and not args.no_cpu_baseline:
             cb = cpu_sample(jfem, args.size, args.cpu_sample_div, args.cpu_sample_iters)
-            line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "assembly_s", "pcg_s")}
+            # one host thread, on a smaller slab and fewer iterations (same scaling)
+            c1 = cpu_sample(jfem, args.size, 4 * args.cpu_sample_div, max(20, args.cpu_sample_iters // 4), threads=1)
+            line["cpu_baseline"]["single_thread"] = {k: c1[k] for k in ("value", "cores", "sample", "assembly_s",
+                                                                         "pcg_s")}
         print(json.dumps(line), flush=True)
     return 0
 
