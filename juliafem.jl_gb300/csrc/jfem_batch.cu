@@ -1,23 +1,28 @@
 // jfem_batch.cu — many small independent linear-elastic Tet4 solves in one
-// persistent, CUDA-graph-captured launch.
+// CUDA-graph-captured solve of persistent launches.
 //
 // The reference solves one problem per solve! call (src/solvers.jl:273-344,
 // ext/JuliaFEMCUDAExt.jl:867-916); a batch of uneven systems there is a loop
 // of host round trips.  Here every instance is an independent Jacobi-PCG solve
-// owned by one CTA: a persistent grid of CTAs takes instances from a device
-// counter in decreasing-size order (longest first), so uneven sizes balance
-// across SMs, and no CTA ever waits for another.  Per instance:
+// owned by one team: a single CTA, or for the largest instances a thread-block
+// cluster of 2, 4 or 8 CTAs that share the instance's loops and exchange their
+// block sums through distributed shared memory.  Persistent grids of teams take
+// instances from device counters in decreasing-size order (longest first), so
+// uneven sizes balance across SMs; the cluster launch and the single-CTA launch
+// are parallel branches of the graph, and no team ever waits for another.  Per
+// instance:
 //   * FP32 matrix-free apply (element pass over the instance's elements into a
-//     per-element scratch, block barrier, node gather in ascending element
+//     per-element scratch, team barrier, node gather in ascending element
 //     order: deterministic) with the same element operator as the main apply;
 //   * double-float vectors (jfem_df.cuh) for r, p and the correction δx, an
 //     FP64 iterate x, FP64 true residual f − K x (FP64 element apply) at
 //     recursive convergence and every time the residual drops by 0.3, as the
 //     single-mesh mixed solver does;
-//   * block-level fixed-order reductions, so results are bit-reproducible.
+//   * fixed-order reductions (block, then cluster rank order), so results are
+//     bit-reproducible for a given configuration.
 // Per-instance latency comes from %globaltimer around each instance.  Block
-// size and CTAs per SM are chosen by an autotuner (timed launches of the whole
-// batch, fastest kept).
+// size, CTAs per SM, cluster size and the share of instances on clusters are
+// chosen by an autotuner (timed solves of the whole batch, fastest kept).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
