@@ -110,6 +110,31 @@ def test_apply_fp64_and_fp32(jfem, orc, gpu_ctx_factory, et):
     assert np.array_equal(y64, y64b)        # deterministic gather
 
 
+@pytest.mark.parametrize("et,dims", [(10, (8, 4, 4)), (8, (8, 6, 6)), (4, (10, 5, 5))])
+def test_apply_fp32_distorted_multi_tile(jfem, orc, gpu_ctx_factory, et, dims):
+    """Tiled FP32 apply on distorted (non-affine for Tet10/Hex8) meshes of
+    several tiles: per-point geometry records read from HBM, tile-shared nodes
+    through the boundary pass; small strain and the Neo-Hookean tangent."""
+    m = jfem.mesh.box_mesh(et, *dims, 2.0, 1.0, 1.0)
+    g = np.random.default_rng(20 + et)
+    X = m.X + 0.01 * g.standard_normal(m.X.shape)
+    E = g.uniform(100e3, 300e3, m.n_elem)
+    v = g.standard_normal(m.n_dofs)
+    u = 0.01 * g.standard_normal(m.n_dofs)
+    with gpu_ctx_factory() as ctx:
+        ctx.set_mesh(et, X, m.conn)
+        ctx.set_material(E, 0.3)
+        y32 = ctx.apply(v, fp32=True)
+        ctx.set_material(E, 0.3, 1)
+        ctx.set_formulation(True, True)
+        ctx.set_state(u)
+        t32 = ctx.apply(v, fp32=True)
+    assert m.n_elem > 256                     # several tiles, so shared nodes exist
+    assert rel_err(y32, orc.apply(et, X, m.conn, E, 0.3, v)) <= 2e-5
+    to = orc.apply(et, X, m.conn, E, 0.3, v, u=u, model=1, finite=True, geom=True)
+    assert rel_err(t32, to) <= 1e-4
+
+
 def test_apply_masked(jfem, gpu_ctx_factory, orc):
     w = jfem.workloads.cantilever(4, 6, 2, 2, 3.0, 1.0, 1.0)
     m = w.mesh
