@@ -107,11 +107,12 @@ def cpu_sample(jfem, size, div, iters, threads=0):
     import oracle
     oracle.build()
     if threads:
+        prev = oracle.get_threads()
         oracle.set_threads(threads)
         try:
             return cpu_sample(jfem, size, div, iters)
         finally:
-            oracle.set_threads(0)
+            oracle.set_threads(prev)
     nx, ny, nz = size
     sx = max(1, nx // div)
     w = jfem.workloads.cantilever(10, sx, ny, nz, 20.0 * sx / 200, 2.0 * ny / 20, 2.0 * nz / 20)
