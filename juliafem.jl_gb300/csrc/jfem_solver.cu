@@ -748,7 +748,7 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
 }
 
 // Flexible CG with the learned preconditioner (nn) or Jacobi, mixed precision
-// (double-float vectors, FP32 tiled apply, FP64 true residual as the judge).
+// (double-float vectors, FP32 tiled apply, the FP64 true residual decides).
 // Refinements as in pcg() (the direction is kept when the recursive and true
 // residuals agree to 10 %).  When the learned preconditioner stalls (two
 // refinements without a 4× gain in the true residual, or no 10 % progress of
