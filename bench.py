@@ -131,7 +131,36 @@ def cpu_sample(jfem, size, div, iters, threads=0):
     sample = (f"Tet10 {sx}x{ny}x{nz} slab ({m.n_elem} elements, {m.n_dofs} DOFs): CSC assembly + {it} "
               f"Jacobi-PCG iterations, scaled x{scale:g} in size and to {FULL_PCG_ITERS} iterations")
     return dict(value=value, unit=UNIT, cores=oracle.get_threads(), kind="port", sample=sample,
-                assembly_s=t_asm, s_per_iter=t_iter, pcg_s=t_iter * FULL_PCG_ITERS)
+                assembly_s=t_asm, s_per_iter=t_iter, pcg_s=t_iter * FULL_PCG_ITERS,
+                scipy_pcg_s=_scipy_pcg_s(cp, rv, nz_, f, w.fixed_mask(), max(5, iters // 10), scale))
+
+
+def _scipy_pcg_s(cp, rv, nz, f, fixed, iters, scale):
+    """Second, independent CPU point: Jacobi-PCG iterations with scipy's CSC
+    SpMV on the same slab, scaled like the oracle's; None if scipy fails."""
+    try:
+        import numpy as _np
+        import scipy.sparse as _sp
+        n = f.size
+        K = _sp.csc_matrix((nz, rv, cp), shape=(n, n))
+        free = (_np.asarray(fixed) == 0).astype(_np.float64)
+        dinv = _np.where(free > 0, 1.0 / K.diagonal(), 0.0)
+        r = f * free
+        z = dinv * r
+        p = z.copy()
+        rz = r @ z
+        t0 = time.perf_counter()
+        for _ in range(iters):
+            q = (K @ (p * free)) * free
+            a = rz / (p @ q)
+            r -= a * q
+            z = dinv * r
+            rzn = r @ z
+            p = z + (rzn / rz) * p
+            rz = rzn
+        return (time.perf_counter() - t0) / max(iters, 1) * scale * FULL_PCG_ITERS
+    except Exception:
+        return None
 
 
 def run_reference(args):
@@ -508,7 +537,8 @@ def run_gpu(args):
             line["learned_preconditioner"] = learned_leg(jfem, args, local, w)
         if ws == 1 and not args.no_cpu_baseline:
             cb = cpu_sample(jfem, args.size, args.cpu_sample_div, args.cpu_sample_iters)
-            line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "assembly_s", "pcg_s")}
+            line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "assembly_s", "pcg_s",
+                                                       "scipy_pcg_s")}
             # one host thread, on a smaller slab and fewer iterations (same scaling)
             c1 = cpu_sample(jfem, args.size, 4 * args.cpu_sample_div, max(20, args.cpu_sample_iters // 4), threads=1)
             line["cpu_baseline"]["single_thread"] = {k: c1[k] for k in ("value", "cores", "sample", "assembly_s",
