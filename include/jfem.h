@@ -65,8 +65,13 @@ typedef struct jfem_ctx jfem_ctx;
 
 /* Keyword arguments of solve!(physics; tol, max_iter, newton_tol, max_newton,
  * max_cg_per_newton) (src/backend/abstract.jl:181-188) and the Eisenstat–Walker
- * parameters of ext/JuliaFEMCUDAExt.jl:685-694.  tol is a relative FP64
- * residual ‖f − K u‖ / ‖f‖ over the free DOFs. */
+ * parameters of ext/JuliaFEMCUDAExt.jl:685-694.
+ * Tolerances: by default tol is a relative FP64 residual ‖f − K u‖ / ‖f − K u₀‖
+ * over the free DOFs (u₀ = prescribed values, free part zero) and Newton stops
+ * when ‖R_free‖ ≤ newton_tol·‖f_int‖.  The reference tests absolute norms
+ * instead — CG ‖r‖ < tol (src/backend/cpu.jl:230,244, ext/JuliaFEMCUDAExt.jl:567,620),
+ * Newton ‖R‖ < newton_tol (ext/JuliaFEMCUDAExt.jl:754,779) — which tol_absolute = 1
+ * selects, so solve!(tol = 1e-6) keeps its meaning through this ABI. */
 typedef struct jfem_solve_opts {
   int method;             /* JFEM_PCG_JACOBI, JFEM_FCG_LEARNED, JFEM_NEWTON */
   int precision;          /* JFEM_FP64 or JFEM_MIXED */
@@ -78,8 +83,12 @@ typedef struct jfem_solve_opts {
   int n_load_steps;       /* Newton: prescribed values and loads ramped over steps */
   double forcing_power;
   double forcing_max;
-  double time_budget_s;   /* 0 = none; else JFEM_ERR_TIMEOUT when exceeded */
+  double time_budget_s;   /* 0 = none; else JFEM_ERR_TIMEOUT when exceeded (checked every 16
+                             CG iterations); u then receives the best iterate found so far
+                             (the last accepted Newton state for JFEM_NEWTON) and stats the
+                             counts up to that point */
   double refine_drop;     /* JFEM_MIXED: FP64 residual each time ‖r‖ drops by this factor (0 → 0.3) */
+  int tol_absolute;       /* 0: relative tests (default); 1: the reference's absolute ‖r‖ and ‖R‖ */
 } jfem_solve_opts;
 
 #define JFEM_HISTORY_MAX 256
@@ -175,8 +184,11 @@ int jfem_solve_device(jfem_ctx* ctx, const jfem_solve_opts* opts, double* u_devi
  * overlap on the GPU race and must be serialised by the caller.  The first call
  * on a device resolves the array's address for that device; make it before any
  * stream capture.  Runs on `stream` (a cudaStream_t, NULL = legacy default) and
- * returns after the stream has finished the work.  Status as elsewhere
- * (JFEM_ERR_INVALID for out-of-range connectivity, JFEM_ERR_NEG_JACOBIAN). */
+ * returns after the stream has finished the work (it synchronises that
+ * stream).  Status as elsewhere: JFEM_ERR_INVALID for node numbers outside
+ * [index_base, index_base + n_nodes) or a material with E ≤ 0 or ν outside
+ * (−1, 1/2) — such elements are skipped, never read out of bounds —,
+ * JFEM_ERR_NEG_JACOBIAN, JFEM_ERR_CUDA when a launch or the stream fails. */
 int jfem_apply_noalloc(int elem_type, int64_t n_nodes, const double* X_device, int64_t n_elem,
                        const int64_t* conn_device, int index_base, const double* E_device,
                        const double* nu_device, const double* v_device, double* y_device,
@@ -185,20 +197,27 @@ int jfem_apply_noalloc(int elem_type, int64_t n_nodes, const double* X_device, i
 /* ------------------------------------------------------------------------
  * Learned preconditioner for flexible CG (method JFEM_FCG_LEARNED).  No
  * counterpart in the reference (its solvers are unpreconditioned CG,
- * src/backend/cpu.jl:221-254, ext/JuliaFEMCUDAExt.jl:531-577): a message-passing
- * network on the mesh node graph (nodes i ~ j when they share an element),
- * 3 layers of width JFEM_MPNN_WIDTH, tanh, no biases, BF16 weights with FP32
- * accumulation:
- *   h1 = tanh(x Ws1ᵀ + agg(x) Wn1ᵀ), h2, h3 likewise, o = mask ⊙ h3 Woᵀ,
- *   agg(h)_i = mean of h over the neighbours of i;
- * preconditioner z = D⁻¹r + s·o(mask ⊙ D⁻¹r / s), s = RMS of D⁻¹r over the
- * free DOFs (Jacobi plus a learned correction; o(−x) = −o(x)).  The weights
- * belong to the context and survive jfem_set_mesh; training pairs do not.
+ * src/backend/cpu.jl:221-254, ext/JuliaFEMCUDAExt.jl:531-577).
+ *
+ * Network N: linear message passing on the mesh node graph (nodes i ~ j when
+ * they share an element), 3 layers of width JFEM_MPNN_WIDTH, no activation and
+ * no biases, BF16 weights with FP32 accumulation:
+ *   h0 = y (3 channels per node),   a_l,i = mean of h_l over the neighbours of i,
+ *   h_{l+1} = Ws_l h_l + Wn_l a_l   (3 → 32 → 32 → 32),   N(y) = mask ⊙ Wo h3.
+ * Preconditioner, symmetric positive definite for any weights (flexible CG
+ * then keeps PCG's convergence):
+ *   y = mask ⊙ D^{-1/2} r,   z = D^{-1/2} (y + Nᵀ N y),   D = diag K,
+ * with Nᵀ the network's backward-data pass.  With all weights zero it is
+ * Jacobi.  Training loss of a pair (r, e), r = K e, averaged over the pairs:
+ *   ℓ = 1 − (zᵀ K e)² / ((zᵀ K z)(eᵀ K e)) = 1 − cos²_K(z, e)
+ * (the share of e's energy left after one optimally scaled step along z; K z
+ * from the FP32 apply).  The weights belong to the context and survive
+ * jfem_set_mesh; training pairs do not.
  * Weight layout (row-major [out][in]): Ws1 32×3, Wn1 32×3, Ws2, Wn2, Ws3, Wn3
  * 32×32, Wo 3×32. */
 #define JFEM_MPNN_WIDTH  32
 #define JFEM_MPNN_PARAMS 4384
-/* Seeded random weights (Glorot-uniform, output layer ×0.05). */
+/* Seeded random weights: uniform in ±0.5·sqrt(6 / (fan_in + fan_out)) per layer. */
 int jfem_mpnn_init(jfem_ctx* ctx, uint64_t seed);
 /* JFEM_MPNN_PARAMS float values, rounded to BF16 on the way in. */
 int jfem_mpnn_set_weights(jfem_ctx* ctx, const float* w);
@@ -208,14 +227,15 @@ int jfem_mpnn_get_weights(jfem_ctx* ctx, float* w);
  * e = x* − x_k, r = K e.  Returns the number of pairs held, or < 0. */
 int jfem_mpnn_collect(jfem_ctx* ctx, int max_pairs, double tol);
 int jfem_mpnn_clear(jfem_ctx* ctx);
-/* Adam on the held pairs: loss = mean over pairs of
- * Σ d (x + o − t)² / Σ d t², t = mask ⊙ e / s, d = diag K.  losses[epochs]
- * (may be NULL) receives the mean loss of each epoch. */
+/* Adam on the held pairs, mini-batches of `batch` pairs in a seeded shuffled
+ * order, minimising the mean of ℓ above.  losses[epochs] (may be NULL)
+ * receives the mean loss of each epoch. */
 int jfem_mpnn_train(jfem_ctx* ctx, int epochs, int batch, double lr, uint64_t seed, double* losses);
-/* Loss and gradient (JFEM_MPNN_PARAMS) of one pair (r, e) given on the host,
- * through the training kernels — for gradient checks. */
+/* Loss ℓ and its gradient (JFEM_MPNN_PARAMS) for one pair (r, e) given on the
+ * host, through the training kernels — for gradient checks. */
 int jfem_mpnn_loss_grad(jfem_ctx* ctx, const double* r, const double* e, double* loss, float* grad);
-/* z = D⁻¹r + s·o(x) for a host residual r (3 n_nodes), through the inference kernels. */
+/* z = D^{-1/2}(y + NᵀN y), y = mask ⊙ D^{-1/2} r, for a host residual r
+ * (3 n_nodes), through the inference kernels. */
 int jfem_mpnn_precondition(jfem_ctx* ctx, const double* r, double* z);
 
 /* ------------------------------------------------------------------------

@@ -44,7 +44,7 @@ class SolveOpts(C.Structure):
     _fields_ = [("method", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int),
                 ("newton_tol", C.c_double), ("max_newton", C.c_int), ("max_cg_per_newton", C.c_int),
                 ("n_load_steps", C.c_int), ("forcing_power", C.c_double), ("forcing_max", C.c_double),
-                ("time_budget_s", C.c_double), ("refine_drop", C.c_double)]
+                ("time_budget_s", C.c_double), ("refine_drop", C.c_double), ("tol_absolute", C.c_int)]
 
 
 class Stats(C.Structure):

@@ -375,12 +375,13 @@ int jfem_solve(jfem_ctx* h, const jfem_solve_opts* opts, double* u, jfem_stats* 
     return jfem::set_err(c, JFEM_ERR_OOM, "solution buffer");
   if (stats) std::memset(stats, 0, sizeof(*stats));
   int rc = jfem::solve_device(c, opts, d_u, stats);
-  if (rc >= 0) {
+  if (rc >= 0 || rc == JFEM_ERR_TIMEOUT) {   // on a timeout u receives the best iterate so far
     cudaMemcpyAsync(u, d_u, 3 * c->N * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     const int rc2 = jfem::sync_and_check(c, "solution download");
     if (rc2) rc = rc2;
   }
   if (stats && rc < 0) stats->status = rc;
+  if (rc == JFEM_ERR_TIMEOUT) jfem::set_err(c, JFEM_ERR_TIMEOUT, "solve exceeded its time budget");
   cudaFree(d_u);
   return rc;
 }

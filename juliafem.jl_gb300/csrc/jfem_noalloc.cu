@@ -131,18 +131,33 @@ __global__ void k_na_sort(const int* __restrict__ ptr, unsigned* __restrict__ ad
   }
 }
 
-// FP64 element kernel, geometry evaluated per integration point from X.
+// FP64 element kernel, geometry evaluated per integration point from X.  An
+// element whose node numbers fall outside [0, N) or whose material is not
+// admissible (E > 0, −1 < ν < 1/2; NaN fails both) is not evaluated: it raises
+// JFEM_ERR_INVALID and writes zeros, so no load ever leaves X's or v's bounds.
 template <int ET>
-__global__ void __launch_bounds__(128) k_na_elem(int64_t E, const int64_t* __restrict__ conn, int base,
+__global__ void __launch_bounds__(128) k_na_elem(int64_t E, int64_t N, const int64_t* __restrict__ conn, int base,
                                                  const double* __restrict__ X, const double* __restrict__ Em,
                                                  const double* __restrict__ num, const double* __restrict__ v,
                                                  double* __restrict__ ye, int* __restrict__ err) {
   constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
     int64_t nodes[NN];
+    bool in_range = true;
 #pragma unroll
-    for (int i = 0; i < NN; ++i) nodes[i] = conn[e * NN + i] - base;
+    for (int i = 0; i < NN; ++i) {
+      nodes[i] = conn[e * NN + i] - base;
+      in_range = in_range && nodes[i] >= 0 && nodes[i] < N;
+    }
     const double Ee = Em[e], ne = num[e];
+    if (!in_range || !(Ee > 0.0) || !(ne > -1.0 && ne < 0.5)) {
+      raise_error(err, JFEM_ERR_INVALID);
+#pragma unroll
+      for (int i = 0; i < NN; ++i)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ye[(int64_t)(3 * i + c) * E + e] = 0.0;
+      continue;
+    }
     const double lam = Ee * ne / ((1.0 + ne) * (1.0 - 2.0 * ne));
     const double mu = Ee / (2.0 * (1.0 + ne));
     double y[NN][3];
@@ -199,13 +214,14 @@ __global__ void __launch_bounds__(128) k_na_elem(int64_t E, const int64_t* __res
   }
 }
 
-__global__ void k_na_gather(int64_t N, int64_t E, const int* __restrict__ ptr, const unsigned* __restrict__ adj,
+__global__ void k_na_gather(int64_t N, int64_t E, int nn, const int* __restrict__ ptr, const unsigned* __restrict__ adj,
                             const double* __restrict__ ye, double* __restrict__ y) {
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x) {
     double s0 = 0.0, s1 = 0.0, s2 = 0.0;
     for (int t = ptr[j]; t < ptr[j + 1]; ++t) {
       const int64_t e = adj[t] >> 4;
       const int a = (int)(adj[t] & 15u);
+      if (e >= E || a >= nn) continue;   // k_na_fill writes only e < E, a < nn; checked all the same
       s0 += ye[(int64_t)(3 * a) * E + e];
       s1 += ye[(int64_t)(3 * a + 1) * E + e];
       s2 += ye[(int64_t)(3 * a + 2) * E + e];
@@ -256,23 +272,37 @@ extern "C" int jfem_apply_noalloc(int elem_type, int64_t n_nodes, const double* 
   double* ye = (double*)(s + L.ye);
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t N = n_nodes, Ne = n_elem;
+  // Each launch's own status (cudaLaunchKernelEx), so an error the caller left
+  // behind on this thread is neither reported nor cleared here.
+  cudaError_t launch_err = cudaSuccess;
+  auto launch = [&](auto kernel, unsigned grid, unsigned block, auto... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.stream = st;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, args...);
+    if (launch_err == cudaSuccess) launch_err = e;
+  };
   // clear what must start at zero: the error flag, the counts and the fill cursors
-  k_na_zero<<<1, 32, 0, st>>>(err, 1);
-  k_na_zero<<<grid_for(N + 1, 256), 256, 0, st>>>(cnt, N + 1);
-  k_na_zero<<<grid_for(N, 256), 256, 0, st>>>(cursor, N);
-  k_na_count<<<grid_for(Ne * nn, 256), 256, 0, st>>>(conn, Ne, nn, N, index_base, cnt, err);
-  k_na_scan<<<1, 1024, 0, st>>>(cnt, ptr, N);
-  k_na_fill<<<grid_for(Ne * nn, 256), 256, 0, st>>>(conn, Ne, nn, N, index_base, ptr, cursor, adj);
-  k_na_sort<<<grid_for(N, 128), 128, 0, st>>>(ptr, adj, N);
+  launch(k_na_zero, 1, 32, err, (int64_t)1);
+  launch(k_na_zero, grid_for(N + 1, 256), 256, cnt, N + 1);
+  launch(k_na_zero, grid_for(N, 256), 256, cursor, N);
+  launch(k_na_count, grid_for(Ne * nn, 256), 256, conn, Ne, nn, N, index_base, cnt, err);
+  launch(k_na_scan, 1, 1024, (const int*)cnt, ptr, N);
+  launch(k_na_fill, grid_for(Ne * nn, 256), 256, conn, Ne, nn, N, index_base, (const int*)ptr, cursor, adj);
+  launch(k_na_sort, grid_for(N, 128), 128, (const int*)ptr, adj, N);
   const unsigned ge = grid_for(Ne, 128, 1LL << 30);
   switch (elem_type) {
-    case JFEM_TET4: k_na_elem<JFEM_TET4><<<ge, 128, 0, st>>>(Ne, conn, index_base, X, E, nu, v, ye, err); break;
-    case JFEM_TET10: k_na_elem<JFEM_TET10><<<ge, 128, 0, st>>>(Ne, conn, index_base, X, E, nu, v, ye, err); break;
-    default: k_na_elem<JFEM_HEX8><<<ge, 128, 0, st>>>(Ne, conn, index_base, X, E, nu, v, ye, err); break;
+    case JFEM_TET4: launch(k_na_elem<JFEM_TET4>, ge, 128, Ne, N, conn, index_base, X, E, nu, v, ye, err); break;
+    case JFEM_TET10: launch(k_na_elem<JFEM_TET10>, ge, 128, Ne, N, conn, index_base, X, E, nu, v, ye, err); break;
+    default: launch(k_na_elem<JFEM_HEX8>, ge, 128, Ne, N, conn, index_base, X, E, nu, v, ye, err); break;
   }
-  k_na_gather<<<grid_for(N, 256), 256, 0, st>>>(N, Ne, ptr, adj, ye, y);
+  launch(k_na_gather, grid_for(N, 256), 256, N, Ne, nn, (const int*)ptr, (const unsigned*)adj, (const double*)ye, y);
   int h_err = 0;
-  if (cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return JFEM_ERR_CUDA;
-  if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) return JFEM_ERR_CUDA;
+  const cudaError_t ce = launch_err == cudaSuccess
+                             ? cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st)
+                             : launch_err;
+  const cudaError_t se = cudaStreamSynchronize(st);   // the work launched above has ended either way
+  if (ce != cudaSuccess || se != cudaSuccess) return JFEM_ERR_CUDA;
   return h_err;
 }

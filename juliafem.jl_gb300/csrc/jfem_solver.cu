@@ -637,7 +637,8 @@ struct PcgSnap {
 // reached the attainable accuracy of the arithmetic: the best iterate is kept
 // and JFEM_NOT_CONVERGED returned.
 static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, double time_budget, double t_start,
-               bool reliable, bool x_zero, PcgResult* res, double drop = 1e-2, PcgSnap* snap = nullptr) {
+               bool reliable, bool x_zero, PcgResult* res, double drop = 1e-2, PcgSnap* snap = nullptr,
+               bool tol_abs = false) {
   int rc = 0;
   double rr0 = 0.0;
   const int64_t n = 3 * c->N;
@@ -650,6 +651,7 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
   } else if ((rc = true_residual(c, f, c->x, c->r, &rr0))) {
     return rc;
   }
+  if (tol_abs && rr0 > 0.0) tol /= std::sqrt(rr0);   // ‖r‖ ≤ tol as the reference's CG tests it
   if (fp32) {   // double-float state: δx, r, p; FP32 Jacobi diagonal
     k_narrow<<<gv, 256, 0, c->stream>>>(n, c->dinv, c->dinvf);
     cudaMemsetAsync(c->xd, 0, n * sizeof(float2), c->stream);   // correction δx since the last refinement
@@ -742,8 +744,22 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
       c->launches += 1;
       if ((rc = read_scalars(c))) return rc;
     }
-    if (time_budget > 0.0 && now_s() - t_start > time_budget)
+    if (time_budget > 0.0 && now_s() - t_start > time_budget) {
+      // hand back the better (true FP64 residual) of the current and the best iterate
+      if (fp32) {
+        k_df_absorb<<<gv, 256, 0, c->stream>>>(n, c->xd, c->x);
+        c->launches += 1;
+      }
+      double rr_t = 0.0;
+      if ((rc = true_residual(c, f, c->x, c->r, &rr_t))) return rc;
+      if (rr_t == rr_t && rr_t < rr_best) rr_best = rr_t;
+      else cudaMemcpyAsync(c->x, c->xbest, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+      res->iters = iters;
+      res->refinements = refinements;
+      res->relres = std::sqrt(rr_best / bb);
+      res->status = JFEM_ERR_TIMEOUT;
       return set_err(c, JFEM_ERR_TIMEOUT, "solve exceeded its time budget");
+    }
   }
 }
 
@@ -756,7 +772,7 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
 // residual norms are not monotone) the solve continues with Jacobi from the
 // best iterate (res->fallbacks = 1).
 static int fcg(Ctx* c, const double* f, bool nn, double tol, int max_iter, double time_budget, double t_start,
-               bool x_zero, PcgResult* res, double drop) {
+               bool x_zero, PcgResult* res, double drop, bool tol_abs = false) {
   int rc = 0;
   double rr0 = 0.0;
   const int64_t n = 3 * c->N;
@@ -773,6 +789,7 @@ static int fcg(Ctx* c, const double* f, bool nn, double tol, int max_iter, doubl
   } else if ((rc = true_residual(c, f, c->x, c->r, &rr0))) {
     return rc;
   }
+  if (tol_abs && rr0 > 0.0) tol /= std::sqrt(rr0);
   k_narrow<<<gv, 256, 0, c->stream>>>(n, c->dinv, c->dinvf);
   cudaMemsetAsync(c->xd, 0, n * sizeof(float2), c->stream);
   cudaMemsetAsync(c->Apf, 0, n * sizeof(float), c->stream);
@@ -859,8 +876,21 @@ static int fcg(Ctx* c, const double* f, bool nn, double tol, int max_iter, doubl
       c->launches += 3;
       if ((rc = read_scalars(c))) return rc;
     }
-    if (time_budget > 0.0 && now_s() - t_start > time_budget)
+    if (time_budget > 0.0 && now_s() - t_start > time_budget) {
+      // hand back the better (true FP64 residual) of the current and the best iterate
+      k_df_absorb<<<gv, 256, 0, c->stream>>>(n, c->xd, c->x);
+      c->launches += 1;
+      double rr_t = 0.0;
+      if ((rc = true_residual(c, f, c->x, c->r, &rr_t))) return rc;
+      if (rr_t == rr_t && rr_t < rr_best) rr_best = rr_t;
+      else cudaMemcpyAsync(c->x, c->xbest, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+      res->iters = iters;
+      res->refinements = refinements;
+      res->fallbacks = fallbacks;
+      res->relres = std::sqrt(rr_best / bb);
+      res->status = JFEM_ERR_TIMEOUT;
       return set_err(c, JFEM_ERR_TIMEOUT, "solve exceeded its time budget");
+    }
   }
 }
 
@@ -894,20 +924,24 @@ static int solve_linear(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
   const bool fp32 = o->precision == JFEM_MIXED;
   PcgResult pr;
   const double drop = o->refine_drop > 0.0 ? o->refine_drop : 0.3;
+  const bool tol_abs = o->tol_absolute != 0;
   if (o->method == JFEM_FCG_LEARNED)
-    rc = fcg(c, c->f_ext, true, o->tol, o->max_iter, o->time_budget_s, t0, c->n_fixed_nonzero == 0, &pr, drop);
+    rc = fcg(c, c->f_ext, true, o->tol, o->max_iter, o->time_budget_s, t0, c->n_fixed_nonzero == 0, &pr, drop,
+             tol_abs);
   else
     rc = pcg(c, c->f_ext, fp32, o->tol, o->max_iter, o->time_budget_s, t0, true, c->n_fixed_nonzero == 0, &pr,
-             drop);
-  if (rc) return rc;
+             drop, nullptr, tol_abs);
+  if (rc && rc != JFEM_ERR_TIMEOUT) return rc;
+  // on JFEM_ERR_TIMEOUT x holds the best iterate found before the budget ran out
+  const int rc_solve = rc;
   cudaMemcpyAsync(u_d, c->x, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   if ((rc = sync_and_check(c, "solution copy"))) return rc;
-  fill_stats(st, pr.status, 1, pr.iters, pr.refinements, pr.relres, now_s() - t0);
+  fill_stats(st, rc_solve ? rc_solve : pr.status, 1, pr.iters, pr.refinements, pr.relres, now_s() - t0);
   if (st) {
     st->history_len = 0;
     st->fallbacks = pr.fallbacks;
   }
-  return pr.status;
+  return rc_solve ? rc_solve : pr.status;
 }
 
 // FP64 Jacobi-PCG of the current system from x = prescribed values to tol,
@@ -934,10 +968,20 @@ int pcg_fp64_snapshots(Ctx* c, const double* f, double tol, int max_iter, double
   return sync_and_check(c, "snapshots");
 }
 
+// A Newton solve that ran out of its time budget hands back the last accepted
+// Newton state (u after the last completed Newton update).
+static void newton_timeout_state(Ctx* c, double* u_d, jfem_stats* st, int newton, int cg, int refin, double rel,
+                                 double t0) {
+  cudaMemcpyAsync(u_d, c->u_state, 3 * c->N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  cudaStreamSynchronize(c->stream);
+  fill_stats(st, JFEM_ERR_TIMEOUT, newton, cg, refin, rel, now_s() - t0);
+}
+
 // Inexact Newton–Krylov with load stepping.  Step s of S applies s/S of the
 // traction and of the prescribed values; the first iteration of a step carries
 // the increment of the prescribed DOFs.  Converged when ‖R_free‖ ≤
-// newton_tol·‖f_int‖ (FP64; f_int over all DOFs, reactions included).
+// newton_tol·‖f_int‖ (FP64; f_int over all DOFs, reactions included), or, with
+// opts.tol_absolute, when ‖R_free‖ ≤ newton_tol as in the reference.
 static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stats* st) {
   const double t0 = now_s();
   int rc = 0;
@@ -978,7 +1022,10 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
         c->launches += 1;
         if ((rc = read_norms(c, &dgg, nullptr))) return rc;
       }
-      if ((!first || dgg == 0.0) && rn <= o->newton_tol * scale) {
+      // relative test by default; with tol_absolute the reference's ‖R‖ < newton_tol
+      // (ext/JuliaFEMCUDAExt.jl:754,779)
+      const double newton_goal = o->tol_absolute ? o->newton_tol : o->newton_tol * scale;
+      if ((!first || dgg == 0.0) && rn <= newton_goal) {
         converged = true;
         break;
       }
@@ -1000,7 +1047,10 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
       cudaMemsetAsync(c->x, 0, n * sizeof(double), c->stream);
       if (fp32 && (rc = nh_state_prepare(c))) return rc;   // tangent point state at u for this Newton step
       PcgResult pr;
-      if ((rc = pcg(c, c->b, fp32, eta, o->max_cg_per_newton, o->time_budget_s, t0, false, true, &pr))) return rc;
+      if ((rc = pcg(c, c->b, fp32, eta, o->max_cg_per_newton, o->time_budget_s, t0, false, true, &pr))) {
+        if (rc == JFEM_ERR_TIMEOUT) newton_timeout_state(c, u_d, st, total_newton, total_cg + pr.iters, refin, last_rel, t0);
+        return rc;
+      }
       total_cg += pr.iters;
       refin += pr.refinements;
       ++total_newton;
@@ -1014,8 +1064,10 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
         st->history[3 * hist + 2] = eta;
         st->history_len = ++hist;
       }
-      if (o->time_budget_s > 0.0 && now_s() - t0 > o->time_budget_s)
+      if (o->time_budget_s > 0.0 && now_s() - t0 > o->time_budget_s) {
+        newton_timeout_state(c, u_d, st, total_newton, total_cg, refin, last_rel, t0);
         return set_err(c, JFEM_ERR_TIMEOUT, "solve exceeded its time budget");
+      }
     }
     if (!converged) status = JFEM_NOT_CONVERGED;
   }

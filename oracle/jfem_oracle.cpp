@@ -657,6 +657,36 @@ int orc_traction(int ft, i64 n_faces, const i64* fconn, const double* X, const d
   return 0;
 }
 
+// Surface pressure (problems_elasticity.jl:486-493): for each face and surface
+// integration point, n = (∂X/∂ξ₁ × ∂X/∂ξ₂)/‖·‖ and, positive pressure acting
+// towards the surface, f += w·‖∂X/∂ξ₁ × ∂X/∂ξ₂‖·(−p)·n ⊗ N.  p is one value per
+// face.  f (length 3N) is accumulated into (not zeroed).
+int orc_pressure(int ft, i64 n_faces, const i64* fconn, const double* X, const double* p, double* f) {
+  const int nf = surface_nodes_of(ft);
+  if (nf < 0) return -1;
+  const Rule rule = surface_rule(ft);
+  for (i64 s = 0; s < n_faces; ++s) {
+    double fe[18] = {0};
+    for (int q = 0; q < rule.nq; ++q) {
+      double N[6], dN[6][2];
+      surface_basis(ft, rule.xi[q], N, dN);
+      double J[2][3] = {{0}};
+      for (int i = 0; i < nf; ++i)
+        for (int a = 0; a < 2; ++a)
+          for (int b = 0; b < 3; ++b) J[a][b] += dN[i][a] * X[3 * fconn[s * nf + i] + b];
+      const double c[3] = {J[0][1] * J[1][2] - J[0][2] * J[1][1], J[0][2] * J[1][0] - J[0][0] * J[1][2],
+                           J[0][0] * J[1][1] - J[0][1] * J[1][0]};
+      const double a = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+      const double w = rule.w[q] * a;
+      for (int i = 0; i < nf; ++i)
+        for (int k = 0; k < 3; ++k) fe[3 * i + k] += w * (-p[s]) * (c[k] / a) * N[i];
+    }
+    for (int i = 0; i < nf; ++i)
+      for (int k = 0; k < 3; ++k) f[3 * fconn[s * nf + i] + k] += fe[3 * i + k];
+  }
+  return 0;
+}
+
 // y = A x for a CSC matrix (column-oriented SpMV, element_assembly_structures.jl:307-309).
 void orc_csc_spmv(i64 n, const i64* colptr, const i64* rowval, const double* nzval,
                   const double* x, double* y) {

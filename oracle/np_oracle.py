@@ -148,12 +148,15 @@ def assemble(et, X, conn, E, nu, u=None, model=0, finite=False):
     return K, fint
 
 
-def traction(ft, fconn, X, t):
-    """Consistent surface load: Σ w‖∂X/∂ξ₁×∂X/∂ξ₂‖ t Nᵢ."""
+def traction(ft, fconn, X, t, p=None):
+    """Consistent surface load: Σ w‖∂X/∂ξ₁×∂X/∂ξ₂‖ t Nᵢ, plus, when the
+    per-face pressure p is given, Σ w (∂X/∂ξ₁×∂X/∂ξ₂)(−p) Nᵢ (the normal
+    times the area element; problems_elasticity.jl:486-493)."""
     X = np.asarray(X, dtype=np.float64)
     fconn = np.asarray(fconn, dtype=np.int64)
     nf = fconn.shape[0]
     t = np.broadcast_to(np.asarray(t, dtype=np.float64), (nf, 3))
+    pf = None if p is None else np.broadcast_to(np.asarray(p, dtype=np.float64), (nf,))
     if ft == 3:
         pts, wts = np.array([[1 / 3, 1 / 3]]), np.array([0.5])
     elif ft == 6:
@@ -189,7 +192,8 @@ def traction(ft, fconn, X, t):
         Xf = X[fconn]                                    # (nf, nfn, 3)
         T = np.einsum("ak,fab->fkb", dN, Xf)             # (nf, 2, 3)
         area = np.linalg.norm(np.cross(T[:, 0], T[:, 1]), axis=1)
-        contrib = (wq * area)[:, None, None] * t[:, None, :] * N[None, :, None]
+        load = t if pf is None else t - pf[:, None] * np.cross(T[:, 0], T[:, 1]) / area[:, None]
+        contrib = (wq * area)[:, None, None] * load[:, None, :] * N[None, :, None]
         np.add.at(f, (3 * fconn[:, :, None] + np.arange(3)).ravel(), contrib.ravel())
     return f
 

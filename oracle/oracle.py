@@ -57,6 +57,7 @@ def lib():
                                            C.c_int64, _i64p, _f64p, _f64p, C.c_int, _f64p,
                                            _i64p, _i64p, _f64p, _f64p]
         L.orc_traction.argtypes = [C.c_int, C.c_int64, _i64p, _f64p, _f64p, _f64p]
+        L.orc_pressure.argtypes = [C.c_int, C.c_int64, _i64p, _f64p, _f64p, _f64p]
         L.orc_csc_spmv.argtypes = [C.c_int64, _i64p, _i64p, _f64p, _f64p, _f64p]
         L.orc_csc_spmv.restype = None
         L.orc_pcg.argtypes = [C.c_int64, _i64p, _i64p, _f64p, _f64p, _u8p, C.c_double, C.c_int,
@@ -180,6 +181,20 @@ def traction(ft, fconn, X, t, n_nodes=None):
     rc = lib().orc_traction(ft, nf, _p(fconn, _i64p), _p(X, _f64p), _p(t, _f64p), _p(f, _f64p))
     if rc != 0:
         raise RuntimeError("orc_traction failed")
+    return f
+
+
+def pressure(ft, fconn, X, p, n_nodes=None):
+    """Consistent surface-pressure load (problems_elasticity.jl:486-493); p is a
+    scalar or one value per face, positive towards the surface."""
+    X = _f(X)
+    fconn = np.ascontiguousarray(fconn, dtype=np.int64)
+    nf = fconn.shape[0]
+    p = np.ascontiguousarray(np.broadcast_to(np.asarray(p, dtype=np.float64), (nf,)))
+    f = np.zeros(3 * (X.shape[0] if n_nodes is None else n_nodes))
+    rc = lib().orc_pressure(ft, nf, _p(fconn, _i64p), _p(X, _f64p), _p(p, _f64p), _p(f, _f64p))
+    if rc != 0:
+        raise RuntimeError("orc_pressure failed")
     return f
 
 

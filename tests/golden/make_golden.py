@@ -6,7 +6,8 @@ Run from the repository root:  python tests/golden/make_golden.py
   (10 nodes, 17 C3D4, symmetry planes, unit pressure on the top face) parsed by
   the package's Abaqus reader, plus its analytic solution: a linear field
   u = (νx/E, νy/E, −z/E) that Tet4 must reproduce exactly (patch test).
-  Needs the reference tree at /root/reference; skipped when it is absent.
+  Needs a JuliaFEM.jl source tree named by the environment variable
+  JFEM_REFERENCE_ROOT; skipped when it is unset or the file is absent.
 * tet4_cantilever.npz — oracle outputs for the Tet4 40×4×4 cantilever: a
   SHA-256 of the CSC pattern, nnz, seeded samples of K, K·w for a seeded w,
   f, and u from the elimination + sparse direct solve (the oracle's stand-in
@@ -22,6 +23,7 @@ oracle/np_oracle.py before anything is written.
 from __future__ import annotations
 
 import hashlib
+import os
 import sys
 from pathlib import Path
 
@@ -35,7 +37,8 @@ import np_oracle  # noqa: E402
 import oracle  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
-REF_INP = Path("/root/reference/test/testdata/cube_tet4.inp")
+REF_INP = Path(os.environ.get("JFEM_REFERENCE_ROOT", "")) / "test" / "testdata" / "cube_tet4.inp" \
+    if os.environ.get("JFEM_REFERENCE_ROOT") else None
 
 
 def pattern_hash(colptr, rowval) -> str:
@@ -83,7 +86,7 @@ def main():
                            w3.prescribed(), n_steps=w3.n_load_steps, tol=1e-10, max_newton=25, model=1)
     np.savez_compressed(OUT / "hex8_neohookean_small.npz", u=u, newton_its=np.array(its), E=w3.E)
     # reference fixture (patch test)
-    if REF_INP.exists():
+    if REF_INP is not None and REF_INP.exists():
         ab = jfem.abaqus.read(str(REF_INP))
         et, X, conn, index, eids = ab.to_arrays()
         dofs, vals = jfem.abaqus.boundary_dofs(ab, index)

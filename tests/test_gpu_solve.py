@@ -135,3 +135,52 @@ def test_legacy_problem_assemble_and_run(jfem, orc):
     u = jfem.run_(an)
     uu = np.concatenate([u[int(n)] for n in ids])
     assert np.abs(uu - d["u_exact"]).max() <= 1e-10 * np.abs(d["u_exact"]).max()
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_time_budget_returns_best_iterate(jfem, gpu_ctx_factory, method):
+    """A solve whose time budget (1 µs) runs out after its first chunk of CG
+    iterations returns JFEM_ERR_TIMEOUT (a host-side check between graph
+    launches; no kernel waits on anything), hands back the better of the
+    current and the best FP64 iterate — finite, prescribed DOFs kept, its true
+    relative residual in the stats — and the iteration count reached, and the
+    context stays usable: the next solve converges."""
+    import ctypes as C
+    w = jfem.workloads.cantilever(10, 20, 2, 2, 10.0, 1.0, 1.0)
+    abi = jfem._abi
+    with gpu_ctx_factory(w) as ctx:
+        if method == 1:
+            ctx.mpnn_init(3)
+        o = jfem.default_opts(method=abi.FCG_LEARNED if method else abi.PCG_JACOBI, precision=abi.MIXED,
+                              tol=1e-10, max_iter=100000)
+        o.time_budget_s = 1e-6
+        u = np.full(w.mesh.n_dofs, np.nan)
+        st = abi.Stats()
+        rc = ctx._lib.jfem_solve(ctx._h, C.byref(o), u.ctypes.data_as(C.POINTER(C.c_double)), C.byref(st))
+        assert rc == abi.ERR_TIMEOUT and st.status == abi.ERR_TIMEOUT
+        assert "time budget" in ctx._lib.jfem_last_error(ctx._h).decode()
+        assert np.all(np.isfinite(u)) and np.all(u[w.fixed_dofs] == 0.0)
+        assert 0 < st.cg_iterations < 1000 and 0.0 < st.residual <= 1.0
+        o.time_budget_s = 0.0
+        u2, st2, rc2 = ctx.solve(o)
+        assert rc2 in (0, abi.STALL) and st2.residual <= 1e-10
+
+
+def test_absolute_tolerance_mode(jfem, gpu_ctx_factory):
+    """tol_absolute = 1 stops CG on ‖f − K u‖ ≤ tol, the reference's absolute
+    test (src/backend/cpu.jl:230,244): with tol = 1e-9·‖f‖ it converges to the
+    same relative level as the default mode with tol = 1e-9, and a tighter
+    absolute tol reaches a smaller relative residual."""
+    w = jfem.workloads.cantilever(4, 20, 4, 4, 10.0, 1.0, 1.0)
+    abi = jfem._abi
+    with gpu_ctx_factory(w) as ctx:
+        _, _, _, f = ctx.assemble_csc(0)
+        fn = float(np.linalg.norm(f[~w.fixed_mask().astype(bool)]))
+        _, st_rel, rc1 = ctx.solve(method=abi.PCG_JACOBI, precision=abi.MIXED, tol=1e-9, max_iter=100000)
+        _, st_abs, rc2 = ctx.solve(method=abi.PCG_JACOBI, precision=abi.MIXED, tol=1e-9 * fn, max_iter=100000,
+                                   tol_absolute=1)
+        _, st_abs2, rc3 = ctx.solve(method=abi.PCG_JACOBI, precision=abi.MIXED, tol=1e-10 * fn,
+                                    max_iter=100000, tol_absolute=1)
+    assert rc1 == rc2 == rc3 == 0
+    assert st_rel.residual <= 1e-9 and st_abs.residual * fn <= 1e-9 * fn
+    assert st_abs2.residual <= 1e-10 and st_abs2.cg_iterations >= st_abs.cg_iterations

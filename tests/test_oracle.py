@@ -149,3 +149,44 @@ def test_lsq_fit_reproduces_a_uniform_field(jfem, npo, et):
         x = npo.lsq_fit(et, m.X, m.conn, 210e3, 0.3, u, field)
         ref = np.array([t[0, 0], t[1, 1], t[2, 2], t[0, 1], t[1, 2], t[0, 2]])
         assert np.abs(x - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+def _box_surface(jfem, et, dims, seed, amp=0.03):
+    """All six faces of a distorted box mesh (curved Tri6 / warped Quad4)."""
+    m = jfem.mesh.box_mesh(et, *dims, 1.4, 1.0, 0.8)
+    X = m.X + amp * np.random.default_rng(seed).standard_normal(m.X.shape)
+    flip = {3: [0, 2, 1], 6: [0, 2, 1, 5, 4, 3], 4: [0, 3, 2, 1]}   # reversed orientation, same face
+    ft, faces = None, []
+    for axis in range(3):
+        for side in range(2):
+            ft, fc = m.face(axis, side)
+            P = m.X[fc]                                  # orient every side outward
+            nrm = np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0]).sum(0)
+            if (nrm[axis] > 0) != (side == 1):
+                fc = fc[:, flip[ft]]
+            faces.append(fc)
+    return m, X, ft, np.concatenate(faces)
+
+
+@pytest.mark.parametrize("et", [4, 10, 8])
+def test_surface_loads_cpp_matches_numpy(jfem, orc, npo, et):
+    """Consistent traction and pressure (problems_elasticity.jl:454-502) for
+    Tri3, Tri6 and Quad4 faces: the C++ oracle against the numpy restatement on
+    non-planar faces with per-face values; a uniform pressure on the closed
+    surface of a box has zero resultant; on one flat face it gives −p·A·n."""
+    m, X, ft, faces = _box_surface(jfem, et, (3, 2, 2), seed=et)
+    g = np.random.default_rng(10 + et)
+    t = g.standard_normal((faces.shape[0], 3))
+    p = g.uniform(0.5, 2.0, faces.shape[0])
+    assert rel_err(orc.traction(ft, faces, X, t), npo.traction(ft, faces, X, t)) <= 1e-13
+    assert rel_err(orc.pressure(ft, faces, X, p), npo.traction(ft, faces, X, np.zeros(3), p=p)) <= 1e-13
+    # a closed (distorted) surface under uniform pressure: no net force
+    fp = orc.pressure(ft, faces, X, 1.0)
+    assert np.abs(fp.reshape(-1, 3).sum(0)).max() <= 1e-12 * np.abs(fp).max()
+    # flat x = 1.4 face of the undistorted box: resultant −p·A·n (A = 1.0·0.8,
+    # n = ±e_x by the face's orientation)
+    ft1, f1 = m.face(0, 1)
+    P = m.X[f1]
+    n = np.sign(np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0]).sum(0)[0])
+    r = orc.pressure(ft1, f1, m.X, 2.5).reshape(-1, 3).sum(0)
+    assert np.allclose(r, [-2.5 * 0.8 * n, 0.0, 0.0], rtol=0, atol=1e-12)
