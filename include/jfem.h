@@ -54,6 +54,7 @@ extern "C" {
 #define JFEM_PCG_JACOBI   0
 #define JFEM_FCG_LEARNED  1
 #define JFEM_NEWTON       2
+#define JFEM_FCG_TWO_LEVEL 3  /* flexible CG, Jacobi + the coarse space of jfem_set_coarse_space */
 #define JFEM_FP64         0   /* FP64 apply throughout */
 #define JFEM_MIXED        1   /* FP32 apply, FP64 vectors/dots/residual + refinement */
 
@@ -237,6 +238,39 @@ int jfem_mpnn_loss_grad(jfem_ctx* ctx, const double* r, const double* e, double*
 /* z = D^{-1/2}(y + NᵀN y), y = mask ⊙ D^{-1/2} r, for a host residual r
  * (3 n_nodes), through the inference kernels. */
 int jfem_mpnn_precondition(jfem_ctx* ctx, const double* r, double* z);
+
+/* ------------------------------------------------------------------------
+ * Two-level preconditioner (methods JFEM_FCG_TWO_LEVEL and JFEM_FCG_LEARNED):
+ *   z = S r + P A_c⁻¹ Pᵀ r,   A_c = Pᵀ K P,
+ * S the smoother (D⁻¹, or the learned network above), P the rigid-body modes
+ * (3 translations, 3 rotations about the centroid) of node aggregates — the
+ * nodes binned into a structured grid of equal boxes over the bounding box —
+ * zero on prescribed DOFs.  A_c is assembled in FP64 on the device from the
+ * elements that straddle aggregates or hold prescribed DOFs, inverted in FP64
+ * (Gauss–Jordan, a pivot below 1e-12 of its diagonal drops that mode) and
+ * applied in FP32.  No counterpart in the reference, whose GPU solver design
+ * note recommends a multigrid-type coarse correction with point smoothers
+ * (docs/src/book/design/gpu_solver_strategy_expert_validated.md:114-156) but
+ * ships unpreconditioned CG.  Linear-elastic small strain only.
+ * coarse_dofs: 0 = no coarse space (JFEM_FCG_LEARNED is then one-level),
+ * < 0 = automatic (about one coarse DOF per 2,500 DOFs, within [192, 768];
+ * the default), > 0 = about that many, at most JFEM_COARSE_MAX_DOFS (the
+ * binning never exceeds it).  Kept across jfem_set_mesh. */
+#define JFEM_COARSE_MAX_DOFS 4096
+int jfem_set_coarse_space(jfem_ctx* ctx, int coarse_dofs);
+/* Builds the coarse space for the current mesh, mask and material if needed
+ * and reports its size: aggregates, coarse DOFs (6 per aggregate), elements
+ * evaluated for A_c, and the device time of the last A_c set-up (assembly and
+ * inversion, ms).  Each output may be NULL. */
+int jfem_coarse_info(jfem_ctx* ctx, int* n_aggregates, int* n_coarse_dofs, int64_t* n_elements,
+                     double* setup_ms);
+/* A_c (n_coarse_dofs², row-major, rows 6a..6a+5 = aggregate a: x, y, z
+ * translation, rotation about x, y, z) and the aggregate of each node
+ * (n_nodes); either may be NULL.  For parity tests. */
+int jfem_coarse_matrix(jfem_ctx* ctx, double* Ac, int* node_aggregate);
+/* z = D⁻¹ r + P A_c⁻¹ Pᵀ r for a host residual r (3 n_nodes): the two-level
+ * preconditioner with the Jacobi smoother, through the solver's kernels. */
+int jfem_coarse_precondition(jfem_ctx* ctx, const double* r, double* z);
 
 /* ------------------------------------------------------------------------
  * Batched solves: many small independent linear-elastic Tet4 problems solved

@@ -20,7 +20,7 @@ NOALLOC_SCRATCH_BYTES = 64 << 20
 TET4, TET10, HEX8 = 4, 10, 8
 TRI3, TRI6, QUAD4 = 3, 6, 4
 LINEAR_ELASTIC, NEO_HOOKEAN = 0, 1
-PCG_JACOBI, FCG_LEARNED, NEWTON = 0, 1, 2
+PCG_JACOBI, FCG_LEARNED, NEWTON, FCG_TWO_LEVEL = 0, 1, 2, 3
 FP64, MIXED = 0, 1
 APPLY_FP32, APPLY_MASKED = 1, 2
 HISTORY_MAX = 256
@@ -97,6 +97,11 @@ SIGNATURES = {
     "jfem_mpnn_train": (C.c_int, [_P, C.c_int, C.c_int, C.c_double, C.c_uint64, _f64p]),
     "jfem_mpnn_loss_grad": (C.c_int, [_P, _f64p, _f64p, _f64p, _f32p]),
     "jfem_mpnn_precondition": (C.c_int, [_P, _f64p, _f64p]),
+    "jfem_set_coarse_space": (C.c_int, [_P, C.c_int]),
+    "jfem_coarse_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64),
+                                   C.POINTER(C.c_double)]),
+    "jfem_coarse_matrix": (C.c_int, [_P, _f64p, C.POINTER(C.c_int)]),
+    "jfem_coarse_precondition": (C.c_int, [_P, _f64p, _f64p]),
     "jfem_batch_create": (C.c_int, [C.POINTER(_P), C.c_int]),
     "jfem_batch_destroy": (C.c_int, [_P]),
     "jfem_batch_last_error": (C.c_char_p, [_P]),
@@ -332,6 +337,32 @@ class Context:
         r = np.ascontiguousarray(r, dtype=np.float64)
         z = np.empty_like(r)
         self._check(self._lib.jfem_mpnn_precondition(self._h, _ptr(r, _f64p), _ptr(z, _f64p)))
+        return z
+
+    # -- two-level preconditioner ------------------------------------------------
+    def set_coarse_space(self, coarse_dofs: int = -1):
+        """0: no coarse space; < 0: automatic size; > 0: about that many coarse DOFs."""
+        self._check(self._lib.jfem_set_coarse_space(self._h, int(coarse_dofs)))
+
+    def coarse_info(self):
+        """(aggregates, coarse DOFs, elements evaluated for A_c, set-up ms)."""
+        a, n, ms = C.c_int(0), C.c_int(0), C.c_double(0)
+        e = C.c_int64(0)
+        self._check(self._lib.jfem_coarse_info(self._h, C.byref(a), C.byref(n), C.byref(e), C.byref(ms)))
+        return a.value, n.value, e.value, ms.value
+
+    def coarse_matrix(self):
+        """(A_c [nc, nc], aggregate of each node)."""
+        _, nc, _, _ = self.coarse_info()
+        Ac = np.empty((nc, nc))
+        agg = np.empty(self.n_nodes, dtype=np.int32)
+        self._check(self._lib.jfem_coarse_matrix(self._h, _ptr(Ac, _f64p), agg.ctypes.data_as(C.POINTER(C.c_int))))
+        return Ac, agg
+
+    def coarse_precondition(self, r):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = np.empty_like(r)
+        self._check(self._lib.jfem_coarse_precondition(self._h, _ptr(r, _f64p), _ptr(z, _f64p)))
         return z
 
     def time_apply(self, reps: int = 20, fp32: bool = True, masked: bool = True):

@@ -55,6 +55,9 @@ void free_mesh(Ctx* c) {
   fresh.sc_host = c->sc_host;
   fresh.norms_host = c->norms_host;
   fresh.mp = c->mp;
+  fresh.coarse_target = c->coarse_target;
+  fresh.geo_gen = c->geo_gen + 1;
+  fresh.mask_gen = c->mask_gen + 1;
   fresh.launches = c->launches;
   fresh.err = c->err;
   *c = fresh;
@@ -237,6 +240,7 @@ int jfem_set_dirichlet(jfem_ctx* h, int64_t n, const int64_t* dofs, const double
   cudaMemcpyAsync(c->gvals, g.data(), 3 * c->N * sizeof(double), cudaMemcpyHostToDevice, c->stream);
   c->n_fixed = n;
   c->n_fixed_nonzero = nz;
+  ++c->mask_gen;
   return jfem::sync_and_check(c, "Dirichlet upload");
 }
 
@@ -398,6 +402,36 @@ int jfem_recover_field(jfem_ctx* h, const double* u, int field, double tol, int 
   return jfem::recover_field(c, u, field, tol, max_iter, nodal, iterations);
 }
 
+int jfem_set_coarse_space(jfem_ctx* h, int coarse_dofs) {
+  ENTER(h);
+  if (coarse_dofs > JFEM_COARSE_MAX_DOFS)
+    return jfem::set_err(&h->c, JFEM_ERR_INVALID, "coarse_dofs above JFEM_COARSE_MAX_DOFS");
+  h->c.coarse_target = coarse_dofs < 0 ? -1 : coarse_dofs;
+  return JFEM_OK;
+}
+
+int jfem_coarse_info(jfem_ctx* h, int* n_aggregates, int* n_coarse_dofs, int64_t* n_elements, double* setup_ms) {
+  ENTER(h);
+  Ctx* c = &h->c;
+  if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
+  return jfem::coarse_info(c, n_aggregates, n_coarse_dofs, n_elements, setup_ms);
+}
+
+int jfem_coarse_matrix(jfem_ctx* h, double* Ac, int* node_aggregate) {
+  ENTER(h);
+  Ctx* c = &h->c;
+  if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
+  return jfem::coarse_matrix(c, Ac, node_aggregate);
+}
+
+int jfem_coarse_precondition(jfem_ctx* h, const double* r, double* z) {
+  ENTER(h);
+  Ctx* c = &h->c;
+  if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
+  if (!r || !z) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL array");
+  return jfem::coarse_precondition(c, r, z);
+}
+
 int jfem_mpnn_init(jfem_ctx* h, uint64_t seed) {
   ENTER(h);
   return jfem::mpnn_init(&h->c, seed);
@@ -426,6 +460,7 @@ int jfem_mpnn_collect(jfem_ctx* h, int max_pairs, double tol) {
 int jfem_mpnn_clear(jfem_ctx* h) {
   ENTER(h);
   h->c.mp_pairs = 0;
+  h->c.mp_coarse = -1;
   return JFEM_OK;
 }
 

@@ -341,6 +341,7 @@ int geometry_invalidate(Ctx* c) {
   if (c->geoT32) { dfree(c, c->geoT32); c->geoT32 = nullptr; }
   c->geo_ready = false;
   ++c->state_version;
+  ++c->geo_gen;
   return 0;
 }
 

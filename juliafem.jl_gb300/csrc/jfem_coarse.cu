@@ -1,0 +1,696 @@
+// jfem_coarse.cu — the coarse level of the two-level preconditioner used by
+// flexible CG (methods JFEM_FCG_TWO_LEVEL and JFEM_FCG_LEARNED):
+//
+//   z = S r + P A_c⁻¹ Pᵀ r,      A_c = Pᵀ K P,
+//
+// S the fine-level smoother (Jacobi D⁻¹, or the learned SPD network), P the
+// rigid-body modes of node aggregates: the nodes are binned into a structured
+// grid of boxes over the mesh's bounding box, and each aggregate a contributes
+// six columns — three translations and three rotations about its centroid c_a,
+// (P_a)_i = m_i ⊙ (t + ω × (X_i − c_a)), m_i zero on prescribed DOFs.  Both terms
+// are symmetric positive (semi)definite, so z = M r with M SPD and flexible CG
+// keeps PCG's convergence.  The reference ships only unpreconditioned CG
+// (src/backend/cpu.jl:221-254, ext/JuliaFEMCUDAExt.jl:531-577); its GPU solver
+// design note names a multigrid-type coarse correction with GPU-friendly
+// point smoothers as the preconditioner to build
+// (docs/src/book/design/gpu_solver_strategy_expert_validated.md:114-156).  An
+// aggregation coarse space of rigid-body modes is that coarse level in its
+// algebraic form: it needs no mesh hierarchy and removes the low-energy
+// bending modes that set Jacobi-PCG's iteration count on slender parts.
+//
+// Set-up, per (mesh, Dirichlet mask) on the host: the aggregation, node
+// offsets X_i − c_a, and the list of elements whose A_c contribution is not
+// zero — an element whose nodes all lie in one aggregate with no prescribed DOF
+// moves rigidly under every mode of that aggregate, so K_e P_e = 0 there.
+// Per geometry generation (material, coordinates) on the device, FP64:
+//   k_coarse_elem    one warp per listed element: the strain of each mode at
+//                    each integration point and the 6×6 blocks
+//                    Σ_q w_q (λ tr ε_a tr ε_b + 2μ ε_a : ε_b) for every pair
+//                    of the element's aggregates;
+//   k_coarse_reduce  each A_c block summed over its elements in ascending
+//                    element order (deterministic, no atomics);
+//   k_gj_*           blocked Gauss–Jordan inversion of the dense SPD A_c
+//                    (diagonal pivots, 32×32 blocks; a pivot below 1e-12 of
+//                    its original diagonal drops that mode);
+// the inverse is rounded to FP32 for the per-iteration coarse solve.
+// Per CG iteration: k_coarse_restrict (one CTA per aggregate: force and moment
+// resultants of r about c_a), k_coarse_gemv (Ec = A_c⁻¹ Rc, one warp per row);
+// the prolongation P Ec is fused into the kernel that forms z.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "jfem_common.cuh"
+
+namespace jfem {
+
+#define CG_MAXN 10   // node slots per element in celem_aggs (Tet10 has the most nodes)
+
+// ---------------------------------------------------------------------------
+// A_c contributions (FP64)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mode_vector(int k, double dx, double dy, double dz, double v[3]) {
+  switch (k) {
+    case 0: v[0] = 1.0; v[1] = 0.0; v[2] = 0.0; break;
+    case 1: v[0] = 0.0; v[1] = 1.0; v[2] = 0.0; break;
+    case 2: v[0] = 0.0; v[1] = 0.0; v[2] = 1.0; break;
+    case 3: v[0] = 0.0; v[1] = -dz; v[2] = dy; break;    // e_x × d
+    case 4: v[0] = dz; v[1] = 0.0; v[2] = -dx; break;    // e_y × d
+    default: v[0] = -dy; v[1] = dx; v[2] = 0.0; break;   // e_z × d
+  }
+}
+
+template <int ET>
+__global__ void __launch_bounds__(64) k_coarse_elem(int64_t n_celem, const int* __restrict__ celem,
+                                                    const int* __restrict__ celem_aggs,
+                                                    const int64_t* __restrict__ celem_off, int64_t E,
+                                                    const int* __restrict__ conn, const uint8_t* __restrict__ mask,
+                                                    const int* __restrict__ node_agg,
+                                                    const double* __restrict__ node_d,
+                                                    const double* __restrict__ geo, int affine,
+                                                    double* __restrict__ contrib) {
+  constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ, NC = 6 * NN;
+  __shared__ double s_d[2][NN][3];
+  __shared__ int s_al[2][NN];
+  __shared__ unsigned s_m[2][NN];
+  __shared__ double s_gN[2][NQ][NN][3];
+  __shared__ double s_S[2][NQ][NC][6];
+  __shared__ double s_lw[2][NQ], s_mw[2][NQ];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int64_t k = (int64_t)blockIdx.x * 2 + w; k < n_celem; k += (int64_t)gridDim.x * 2) {
+    const int64_t e = celem[k];
+    const int* al = celem_aggs + k * CG_MAXN;
+    int A = 0;
+    while (A < NN && al[A] >= 0) ++A;
+    if (lane < NN) {
+      const int n = conn[(int64_t)lane * E + e];
+      const int a = node_agg[n];
+      int la = 0;
+      while (la < A - 1 && al[la] != a) ++la;
+      s_al[w][lane] = la;
+      s_m[w][lane] = mask[n];
+#pragma unroll
+      for (int b = 0; b < 3; ++b) s_d[w][lane][b] = node_d[3 * (int64_t)n + b];
+    }
+    // physical gradients ∇N_i(q) = J⁻ᵀ dN_i(q) and the weights w_q λ detJ, w_q μ detJ
+    for (int t = lane; t < NQ * NN; t += 32) {
+      const int q = t / NN, i = t % NN;
+      const int64_t base = affine ? 0 : 10 * q;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        double s = 0.0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) s += geo[(base + 3 * d + a) * E + e] * dshape(ET, q, i, a);
+        s_gN[w][q][i][d] = s;
+      }
+    }
+    if (lane < NQ) {
+      const int q = lane;
+      const double wq = qp_weight(ET, q);
+      if (affine) {
+        s_lw[w][q] = wq * geo[9 * E + e];
+        s_mw[w][q] = wq * geo[10 * E + e];
+      } else {
+        const double det = geo[(int64_t)(10 * q + 9) * E + e];
+        s_lw[w][q] = wq * det * geo[(int64_t)(10 * NQ) * E + e];
+        s_mw[w][q] = wq * det * geo[(int64_t)(10 * NQ + 1) * E + e];
+      }
+    }
+    __syncwarp();
+    // strain (xx, yy, zz, xy, yz, xz) of every mode column (aggregate α, mode k) at every q
+    const int ncol = 6 * A;
+    for (int t = lane; t < NQ * ncol; t += 32) {
+      const int q = t / ncol, col = t % ncol, alpha = col / 6, km = col % 6;
+      double G[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+      for (int i = 0; i < NN; ++i) {
+        if (s_al[w][i] != alpha) continue;
+        double v[3];
+        mode_vector(km, s_d[w][i][0], s_d[w][i][1], s_d[w][i][2], v);
+        const unsigned m = s_m[w][i];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const double vc = ((m >> c) & 1u) ? 0.0 : v[c];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) G[c][d] += vc * s_gN[w][q][i][d];
+        }
+      }
+      double* S = s_S[w][q][col];
+      S[0] = G[0][0];
+      S[1] = G[1][1];
+      S[2] = G[2][2];
+      S[3] = 0.5 * (G[0][1] + G[1][0]);
+      S[4] = 0.5 * (G[1][2] + G[2][1]);
+      S[5] = 0.5 * (G[0][2] + G[2][0]);
+    }
+    __syncwarp();
+    // blocks (α, β): entry (k, l) = Σ_q λ_q tr ε_αk tr ε_βl + 2 μ_q ε_αk : ε_βl.  The expression
+    // is symmetric in its two operands, so block (β, α) is exactly the transpose of (α, β).
+    const int64_t off = celem_off[k];
+    for (int t = lane; t < ncol * ncol; t += 32) {
+      const int ca = t / ncol, cb = t % ncol;
+      double s = 0.0;
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const double* a = s_S[w][q][ca];
+        const double* b = s_S[w][q][cb];
+        const double tra = a[0] + a[1] + a[2], trb = b[0] + b[1] + b[2];
+        const double dd = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+        const double od = a[3] * b[3] + a[4] * b[4] + a[5] * b[5];
+        s += s_lw[w][q] * (tra * trb) + 2.0 * s_mw[w][q] * (dd + 2.0 * od);
+      }
+      const int alpha = ca / 6, beta = cb / 6;
+      contrib[(off + alpha * A + beta) * 36 + 6 * (ca % 6) + (cb % 6)] = s;
+    }
+    __syncwarp();
+  }
+}
+
+// A_c block (a, b) = Σ of its element blocks, ascending element order
+__global__ void k_coarse_reduce(int64_t n_cblk, const int* __restrict__ cblk_ab, const int* __restrict__ cblk_ptr,
+                                const int64_t* __restrict__ cblk_src, const double* __restrict__ contrib, int ld,
+                                double* __restrict__ Ac) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n_cblk * 36;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / 36;
+    const int ent = (int)(t % 36);
+    double s = 0.0;
+    for (int p = cblk_ptr[b]; p < cblk_ptr[b + 1]; ++p) s += contrib[cblk_src[p] * 36 + ent];
+    const int ra = cblk_ab[2 * b], cb = cblk_ab[2 * b + 1];
+    Ac[(int64_t)(6 * ra + ent / 6) * ld + 6 * cb + ent % 6] = s;
+  }
+}
+
+__global__ void k_diag_copy(int n, int ld, const double* __restrict__ A, double* __restrict__ d) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) d[i] = A[(int64_t)i * ld + i];
+}
+
+__global__ void k_round_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// ---------------------------------------------------------------------------
+// blocked Gauss–Jordan inversion (FP64, in place; A symmetric positive definite)
+// Per pivot block K with P = A_KK⁻¹:  A_IJ −= A_IK P A_KJ,  A_KJ ← P A_KJ,
+// A_IK ← −A_IK P,  A_KK ← P  (I, J ≠ K).  After the last block A holds A⁻¹.
+// ---------------------------------------------------------------------------
+#define GJ_B 32
+
+__global__ void __launch_bounds__(1024) k_gj_pivot(const double* __restrict__ A, int ld, int K0,
+                                                   const double* __restrict__ diag0, double* __restrict__ P) {
+  __shared__ double B[GJ_B][GJ_B + 1];
+  __shared__ double prow[GJ_B], pcol[GJ_B];
+  __shared__ double pinv;
+  const int i = threadIdx.y, j = threadIdx.x;
+  B[i][j] = A[(int64_t)(K0 + i) * ld + K0 + j];
+  __syncthreads();
+  for (int k = 0; k < GJ_B; ++k) {
+    if (i == 0 && j == 0) {
+      const double piv = B[k][k], d0 = diag0[K0 + k];
+      pinv = (d0 > 0.0 && piv > 1e-12 * d0) ? 1.0 / piv : 0.0;   // else: drop this mode
+    }
+    if (i == 0) prow[j] = B[k][j];
+    if (j == 0) pcol[i] = B[i][k];
+    __syncthreads();
+    const double p = pinv;
+    double v = B[i][j];
+    if (i != k && j != k) v -= pcol[i] * prow[j] * p;
+    else if (i == k && j != k) v = prow[j] * p;
+    else if (i != k) v = -pcol[i] * p;
+    else v = p;
+    B[i][j] = v;
+    __syncthreads();
+  }
+  P[i * GJ_B + j] = B[i][j];
+}
+
+// row panel Brow[:, J] = P A_KJ and a copy of the old column panel Ccol[J, :] = A_JK
+__global__ void __launch_bounds__(256) k_gj_panel(const double* __restrict__ A, int ld, int Kb,
+                                                  const double* __restrict__ P, double* __restrict__ Brow,
+                                                  double* __restrict__ Ccol) {
+  __shared__ double sP[GJ_B][GJ_B + 1], sA[GJ_B][GJ_B + 1];
+  const int J = blockIdx.x;
+  if (J == Kb) return;
+  const int K0 = Kb * GJ_B, J0 = J * GJ_B;
+  for (int t = threadIdx.x; t < GJ_B * GJ_B; t += blockDim.x) {
+    const int r = t / GJ_B, q = t % GJ_B;
+    sP[r][q] = P[t];
+    sA[r][q] = A[(int64_t)(K0 + r) * ld + J0 + q];
+    Ccol[(int64_t)(J0 + r) * GJ_B + q] = A[(int64_t)(J0 + r) * ld + K0 + q];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < GJ_B * GJ_B; t += blockDim.x) {
+    const int r = t / GJ_B, q = t % GJ_B;
+    double s = 0.0;
+#pragma unroll 8
+    for (int k = 0; k < GJ_B; ++k) s += sP[r][k] * sA[k][q];
+    Brow[(int64_t)r * ld + J0 + q] = s;
+  }
+}
+
+// every block of A; each CTA writes only its own block and reads only the panels
+__global__ void __launch_bounds__(256) k_gj_update(double* __restrict__ A, int ld, int Kb,
+                                                   const double* __restrict__ P, const double* __restrict__ Brow,
+                                                   const double* __restrict__ Ccol) {
+  __shared__ double sC[GJ_B][GJ_B + 1], sB[GJ_B][GJ_B + 1];
+  const int I = blockIdx.y, J = blockIdx.x;
+  const int I0 = I * GJ_B, J0 = J * GJ_B;
+  if (I == Kb && J == Kb) {
+    for (int t = threadIdx.x; t < GJ_B * GJ_B; t += blockDim.x)
+      A[(int64_t)(I0 + t / GJ_B) * ld + J0 + t % GJ_B] = P[t];
+    return;
+  }
+  if (I == Kb) {
+    for (int t = threadIdx.x; t < GJ_B * GJ_B; t += blockDim.x)
+      A[(int64_t)(I0 + t / GJ_B) * ld + J0 + t % GJ_B] = Brow[(int64_t)(t / GJ_B) * ld + J0 + t % GJ_B];
+    return;
+  }
+  for (int t = threadIdx.x; t < GJ_B * GJ_B; t += blockDim.x) {
+    const int r = t / GJ_B, q = t % GJ_B;
+    sC[r][q] = Ccol[(int64_t)(I0 + r) * GJ_B + q];
+    sB[r][q] = (J == Kb) ? P[t] : Brow[(int64_t)r * ld + J0 + q];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < GJ_B * GJ_B; t += blockDim.x) {
+    const int r = t / GJ_B, q = t % GJ_B;
+    double s = 0.0;
+#pragma unroll 8
+    for (int k = 0; k < GJ_B; ++k) s += sC[r][k] * sB[k][q];
+    double* a = A + (int64_t)(I0 + r) * ld + J0 + q;
+    *a = (J == Kb) ? -s : *a - s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per-iteration kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Rc[6a + k] = Σ_{i ∈ a} φ_k(d_i) · r_i: force (k < 3) and moment (k ≥ 3) resultants
+// of r about the centroid.  r is zero on prescribed DOFs.  FP32 per thread, FP64
+// across threads, fixed order.
+__global__ void __launch_bounds__(256) k_coarse_restrict(int nagg, const int* __restrict__ agg_ptr,
+                                                         const int* __restrict__ agg_nodes,
+                                                         const float4* __restrict__ d32,
+                                                         const float2* __restrict__ r, const int* __restrict__ stop,
+                                                         float* __restrict__ Rc) {
+  __shared__ double sh[8][6];
+  if (stop && *stop) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int a = blockIdx.x; a < nagg; a += gridDim.x) {
+    float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int t = agg_ptr[a] + threadIdx.x; t < agg_ptr[a + 1]; t += blockDim.x) {
+      const int64_t i = agg_nodes[t];
+      const float2 r0 = r[3 * i], r1 = r[3 * i + 1], r2 = r[3 * i + 2];
+      const float rx = r0.x + r0.y, ry = r1.x + r1.y, rz = r2.x + r2.y;
+      const float4 d = d32[i];
+      s[0] += rx;
+      s[1] += ry;
+      s[2] += rz;
+      s[3] = fmaf(d.y, rz, fmaf(-d.z, ry, s[3]));
+      s[4] = fmaf(d.z, rx, fmaf(-d.x, rz, s[4]));
+      s[5] = fmaf(d.x, ry, fmaf(-d.y, rx, s[5]));
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const double v = warp_sum_d((double)s[k]);
+      if (lane == 0) sh[wid][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+      double v = 0.0;
+      for (int q = 0; q < nw; ++q) v += sh[q][threadIdx.x];
+      Rc[6 * a + threadIdx.x] = (float)v;
+    }
+    __syncthreads();
+  }
+}
+
+// Ec = A_c⁻¹ Rc (FP32, one warp per row, rows 16-byte aligned: ld is a multiple of 32)
+__global__ void __launch_bounds__(256) k_coarse_gemv(int nc, int ld, const float* __restrict__ Ainv,
+                                                     const float* __restrict__ Rc, const int* __restrict__ stop,
+                                                     float* __restrict__ Ec) {
+  if (stop && *stop) return;
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= nc) return;
+  const float4* a = reinterpret_cast<const float4*>(Ainv + (int64_t)row * ld);
+  const float4* x = reinterpret_cast<const float4*>(Rc);
+  float s = 0.f;
+  for (int j = lane; j < ld / 4; j += 32) {
+    const float4 av = a[j], xv = x[j];
+    s = fmaf(av.x, xv.x, s);
+    s = fmaf(av.y, xv.y, s);
+    s = fmaf(av.z, xv.z, s);
+    s = fmaf(av.w, xv.w, s);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) Ec[row] = s;
+}
+
+// z = D⁻¹ r + P Ec (FP64 out): the two-level preconditioner with the Jacobi smoother
+// for a host-given residual (jfem_coarse_precondition)
+__global__ void k_coarse_jacobi_out(int64_t N, const double* __restrict__ r, const double* __restrict__ dinv,
+                                    const uint8_t* __restrict__ mask, const int* __restrict__ node_agg,
+                                    const float4* __restrict__ d32, const float* __restrict__ Ec,
+                                    double* __restrict__ z) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * N; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = q / 3;
+    const int c = (int)(q % 3);
+    if ((mask[i] >> c) & 1) {
+      z[q] = 0.0;
+      continue;
+    }
+    z[q] = dinv[q] * r[q] + (double)coarse_prolong(node_agg, d32, Ec, i, c);
+  }
+}
+
+__global__ void k_to_df(int64_t n, const double* __restrict__ a, float2* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float hi = (float)a[i];
+    b[i] = make_float2(hi, (float)(a[i] - (double)hi));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host: structure (aggregation, element lists, block pattern)
+// ---------------------------------------------------------------------------
+// Coarse DOFs when none are requested: about one per 2,500 fine DOFs, within
+// [192, 768] — enough aggregates to carry the bending modes of slender parts,
+// few enough that the FP64 inversion stays a small share of a solve.
+static int auto_coarse_dofs(int64_t n_dofs) {
+  const int64_t v = n_dofs / 2500;
+  return (int)std::min<int64_t>(768, std::max<int64_t>(192, v));
+}
+
+static int coarse_build(Ctx* c, int target_nc) {
+  const int64_t N = c->N, E = c->E;
+  const int nn = c->nn;
+  std::vector<double> X((size_t)(3 * N));
+  std::vector<int> conn((size_t)(nn * E));
+  std::vector<uint8_t> mask((size_t)N);
+  cudaMemcpyAsync(X.data(), c->X64, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(conn.data(), c->conn, (size_t)nn * E * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(mask.data(), c->mask, N, cudaMemcpyDeviceToHost, c->stream);
+  int rc = sync_and_check(c, "coarse set-up download");
+  if (rc) return rc;
+  // bins over the bounding box: about target_nc / 6 boxes of equal edge H
+  double lo[3], hi[3], ext[3];
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = hi[d] = X[d];
+  }
+  for (int64_t i = 0; i < N; ++i)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(lo[d], X[3 * i + d]);
+      hi[d] = std::max(hi[d], X[3 * i + d]);
+    }
+  const double emax = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+  if (!(emax > 0.0)) return set_err(c, JFEM_ERR_INVALID, "coarse space: the mesh has no extent");
+  for (int d = 0; d < 3; ++d) ext[d] = std::max(hi[d] - lo[d], 1e-9 * emax);
+  const int n_target = std::max(1, target_nc / 6);
+  double H = std::cbrt(ext[0] * ext[1] * ext[2] / n_target);
+  int nb[3];
+  for (;;) {   // rounding each axis can overshoot the target; stay within JFEM_COARSE_MAX_DOFS
+    for (int d = 0; d < 3; ++d) nb[d] = (int)std::max<long>(1, std::lround(ext[d] / H));
+    if (6LL * nb[0] * nb[1] * nb[2] <= JFEM_COARSE_MAX_DOFS) break;
+    H *= 1.05;
+  }
+  const int64_t ncell = (int64_t)nb[0] * nb[1] * nb[2];
+  std::vector<int64_t> cell((size_t)N);
+  std::vector<int> cell_id((size_t)ncell, -1);
+  for (int64_t i = 0; i < N; ++i) {
+    int64_t cidx = 0;
+    for (int d = 2; d >= 0; --d) {
+      const int64_t b = std::min<int64_t>(nb[d] - 1, (int64_t)std::floor((X[3 * i + d] - lo[d]) / ext[d] * nb[d]));
+      cidx = cidx * nb[d] + std::max<int64_t>(0, b);
+    }
+    cell[(size_t)i] = cidx;
+    cell_id[(size_t)cidx] = 0;
+  }
+  int nagg = 0;
+  for (int64_t k = 0; k < ncell; ++k)
+    if (cell_id[(size_t)k] == 0) cell_id[(size_t)k] = nagg++;
+  const int nc = 6 * nagg, nc_pad = (nc + GJ_B - 1) / GJ_B * GJ_B;
+  std::vector<int> node_agg((size_t)N), agg_ptr((size_t)nagg + 1, 0), agg_nodes((size_t)N);
+  for (int64_t i = 0; i < N; ++i) {
+    node_agg[(size_t)i] = cell_id[(size_t)cell[(size_t)i]];
+    ++agg_ptr[(size_t)node_agg[(size_t)i] + 1];
+  }
+  for (int a = 0; a < nagg; ++a) agg_ptr[(size_t)a + 1] += agg_ptr[(size_t)a];
+  {
+    std::vector<int> cur(agg_ptr.begin(), agg_ptr.end() - 1);
+    for (int64_t i = 0; i < N; ++i) agg_nodes[(size_t)cur[(size_t)node_agg[(size_t)i]]++] = (int)i;
+  }
+  std::vector<double> cen((size_t)3 * nagg, 0.0);
+  for (int a = 0; a < nagg; ++a) {
+    double s[3] = {0, 0, 0};
+    for (int t = agg_ptr[(size_t)a]; t < agg_ptr[(size_t)a + 1]; ++t)
+      for (int d = 0; d < 3; ++d) s[d] += X[3 * (size_t)agg_nodes[(size_t)t] + d];
+    const double cnt = (double)(agg_ptr[(size_t)a + 1] - agg_ptr[(size_t)a]);
+    for (int d = 0; d < 3; ++d) cen[3 * (size_t)a + d] = s[d] / cnt;
+  }
+  std::vector<double> d64((size_t)(3 * N));
+  std::vector<float4> d32((size_t)N);
+  for (int64_t i = 0; i < N; ++i) {
+    const int a = node_agg[(size_t)i];
+    for (int d = 0; d < 3; ++d) d64[3 * (size_t)i + d] = X[3 * (size_t)i + d] - cen[3 * (size_t)a + d];
+    d32[(size_t)i] = make_float4((float)d64[3 * (size_t)i], (float)d64[3 * (size_t)i + 1],
+                                 (float)d64[3 * (size_t)i + 2], 0.f);
+  }
+  // elements with a nonzero contribution, their aggregates and contribution blocks
+  std::vector<int> celem, celem_aggs;
+  std::vector<int64_t> celem_off;
+  int64_t n_contrib = 0;
+  for (int64_t e = 0; e < E; ++e) {
+    int ag[CG_MAXN];
+    int A = 0;
+    bool masked = false;
+    for (int i = 0; i < nn; ++i) {
+      const int n = conn[(size_t)i * E + e];
+      masked = masked || mask[(size_t)n] != 0;
+      const int a = node_agg[(size_t)n];
+      bool seen = false;
+      for (int q = 0; q < A; ++q) seen = seen || ag[q] == a;
+      if (!seen) ag[A++] = a;
+    }
+    if (A < 2 && !masked) continue;
+    std::sort(ag, ag + A);
+    celem.push_back((int)e);
+    for (int q = 0; q < CG_MAXN; ++q) celem_aggs.push_back(q < A ? ag[q] : -1);
+    celem_off.push_back(n_contrib);
+    n_contrib += (int64_t)A * A;
+  }
+  const int64_t n_celem = (int64_t)celem.size();
+  if (n_contrib >= (1LL << 31)) return set_err(c, JFEM_ERR_TOO_LARGE, "coarse space: too many element blocks");
+  // A_c block pattern: (a, b) keys; sources in ascending element order
+  std::vector<int> cnt((size_t)nagg * nagg, 0);
+  for (int64_t k = 0; k < n_celem; ++k) {
+    const int* ag = &celem_aggs[(size_t)k * CG_MAXN];
+    for (int x = 0; x < CG_MAXN && ag[x] >= 0; ++x)
+      for (int y = 0; y < CG_MAXN && ag[y] >= 0; ++y) ++cnt[(size_t)ag[x] * nagg + ag[y]];
+  }
+  std::vector<int> key_blk((size_t)nagg * nagg, -1), cblk_ab, cblk_ptr(1, 0);
+  for (int64_t key = 0; key < (int64_t)nagg * nagg; ++key)
+    if (cnt[(size_t)key]) {
+      key_blk[(size_t)key] = (int)(cblk_ab.size() / 2);
+      cblk_ab.push_back((int)(key / nagg));
+      cblk_ab.push_back((int)(key % nagg));
+      cblk_ptr.push_back(cblk_ptr.back() + cnt[(size_t)key]);
+    }
+  const int64_t n_cblk = (int64_t)cblk_ab.size() / 2;
+  std::vector<int64_t> cblk_src((size_t)cblk_ptr.back());
+  {
+    std::vector<int> cur(cblk_ptr.begin(), cblk_ptr.end() - 1);
+    for (int64_t k = 0; k < n_celem; ++k) {
+      const int* ag = &celem_aggs[(size_t)k * CG_MAXN];
+      int A = 0;
+      while (A < CG_MAXN && ag[A] >= 0) ++A;
+      for (int x = 0; x < A; ++x)
+        for (int y = 0; y < A; ++y) {
+          const int b = key_blk[(size_t)ag[x] * nagg + ag[y]];
+          cblk_src[(size_t)cur[(size_t)b]++] = celem_off[(size_t)k] + (int64_t)x * A + y;
+        }
+    }
+  }
+  // device arrays (owned by the mesh; any previous set is released first)
+  if (c->pcg_graph) {   // captured launches hold the old coarse pointers
+    cudaGraphExecDestroy(c->pcg_graph);
+    c->pcg_graph = nullptr;
+    c->pcg_graph_key = -1;
+  }
+  void* old[] = {c->agg_ptr, c->agg_nodes, c->node_agg, c->node_d32, c->node_d64, c->celem, c->celem_aggs,
+                 c->celem_off, c->contrib, c->cblk_ab, c->cblk_ptr, c->cblk_src, c->Ac, c->Ac_diag, c->gj_buf,
+                 c->Ainv32, c->Rc, c->Ec};
+  for (void* p : old) dfree(c, p);
+  c->nagg = nagg;
+  c->nc = nc;
+  c->nc_pad = nc_pad;
+  for (int d = 0; d < 3; ++d) c->nb_bins[d] = nb[d];
+  c->n_celem = n_celem;
+  c->n_contrib = n_contrib;
+  c->n_cblk = n_cblk;
+  if ((rc = dalloc(c, &c->agg_ptr, (size_t)nagg + 1)) || (rc = dalloc(c, &c->agg_nodes, (size_t)N)) ||
+      (rc = dalloc(c, &c->node_agg, (size_t)N)) || (rc = dalloc(c, &c->node_d32, (size_t)N)) ||
+      (rc = dalloc(c, &c->node_d64, (size_t)(3 * N))) || (rc = dalloc(c, &c->celem, (size_t)n_celem)) ||
+      (rc = dalloc(c, &c->celem_aggs, (size_t)n_celem * CG_MAXN)) ||
+      (rc = dalloc(c, &c->celem_off, (size_t)n_celem)) || (rc = dalloc(c, &c->contrib, (size_t)n_contrib * 36)) ||
+      (rc = dalloc(c, &c->cblk_ab, (size_t)(2 * n_cblk))) || (rc = dalloc(c, &c->cblk_ptr, (size_t)n_cblk + 1)) ||
+      (rc = dalloc(c, &c->cblk_src, cblk_src.size())) || (rc = dalloc(c, &c->Ac, (size_t)nc_pad * nc_pad)) ||
+      (rc = dalloc(c, &c->Ac_diag, (size_t)nc_pad)) ||
+      (rc = dalloc(c, &c->gj_buf, (size_t)GJ_B * GJ_B + 2 * (size_t)GJ_B * nc_pad)) ||
+      (rc = dalloc(c, &c->Ainv32, (size_t)nc_pad * nc_pad)) || (rc = dalloc(c, &c->Rc, (size_t)nc_pad)) ||
+      (rc = dalloc(c, &c->Ec, (size_t)nc_pad)))
+    return rc;
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+  };
+  up(c->agg_ptr, agg_ptr.data(), agg_ptr.size() * sizeof(int));
+  up(c->agg_nodes, agg_nodes.data(), agg_nodes.size() * sizeof(int));
+  up(c->node_agg, node_agg.data(), node_agg.size() * sizeof(int));
+  up(c->node_d32, d32.data(), d32.size() * sizeof(float4));
+  up(c->node_d64, d64.data(), d64.size() * sizeof(double));
+  up(c->celem, celem.data(), celem.size() * sizeof(int));
+  up(c->celem_aggs, celem_aggs.data(), celem_aggs.size() * sizeof(int));
+  up(c->celem_off, celem_off.data(), celem_off.size() * sizeof(int64_t));
+  up(c->cblk_ab, cblk_ab.data(), cblk_ab.size() * sizeof(int));
+  up(c->cblk_ptr, cblk_ptr.data(), cblk_ptr.size() * sizeof(int));
+  up(c->cblk_src, cblk_src.data(), cblk_src.size() * sizeof(int64_t));
+  cudaMemsetAsync(c->Rc, 0, (size_t)nc_pad * sizeof(float), c->stream);   // padding stays zero
+  cudaMemsetAsync(c->Ec, 0, (size_t)nc_pad * sizeof(float), c->stream);
+  if ((rc = sync_and_check(c, "coarse set-up upload"))) return rc;
+  c->coarse_mask_gen = c->mask_gen;
+  c->coarse_built_target = target_nc;
+  c->coarse_geo_gen = 0;   // values follow
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// host: values (A_c and its inverse)
+// ---------------------------------------------------------------------------
+template <int ET>
+static void launch_coarse_elem(Ctx* c) {
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((c->n_celem + 1) / 2, 152LL * 64));
+  k_coarse_elem<ET><<<g, 64, 0, c->stream>>>(c->n_celem, c->celem, c->celem_aggs, c->celem_off, c->E, c->conn,
+                                             c->mask, c->node_agg, c->node_d64, c->geo64, c->geo_affine ? 1 : 0,
+                                             c->contrib);
+}
+
+// A_c (not inverted) into c->Ac
+static int coarse_assemble(Ctx* c) {
+  if (c->n_celem > 0) {
+    switch (c->et) {
+      case JFEM_TET4: launch_coarse_elem<JFEM_TET4>(c); break;
+      case JFEM_TET10: launch_coarse_elem<JFEM_TET10>(c); break;
+      default: launch_coarse_elem<JFEM_HEX8>(c); break;
+    }
+    c->launches += 1;
+  }
+  cudaMemsetAsync(c->Ac, 0, (size_t)c->nc_pad * c->nc_pad * sizeof(double), c->stream);
+  if (c->n_cblk > 0) {
+    k_coarse_reduce<<<grid_for(c->n_cblk * 36, 256), 256, 0, c->stream>>>(c->n_cblk, c->cblk_ab, c->cblk_ptr,
+                                                                          c->cblk_src, c->contrib, c->nc_pad, c->Ac);
+    c->launches += 1;
+  }
+  return 0;
+}
+
+static int coarse_values(Ctx* c) {
+  int rc = geometry_prepare(c);
+  if (rc) return rc;
+  if (c->model != JFEM_LINEAR_ELASTIC || c->finite)
+    return set_err(c, JFEM_ERR_INVALID, "the coarse space is built for the linear-elastic small-strain operator");
+  cudaEventRecord(c->ev0, c->stream);
+  coarse_assemble(c);
+  const int n = c->nc_pad, nbk = n / GJ_B;
+  k_diag_copy<<<grid_for(n, 256), 256, 0, c->stream>>>(n, n, c->Ac, c->Ac_diag);
+  c->launches += 1;
+  double* P = c->gj_buf;
+  double* Brow = P + GJ_B * GJ_B;
+  double* Ccol = Brow + (size_t)GJ_B * n;
+  for (int kb = 0; kb < nbk; ++kb) {
+    k_gj_pivot<<<1, dim3(GJ_B, GJ_B), 0, c->stream>>>(c->Ac, n, kb * GJ_B, c->Ac_diag, P);
+    k_gj_panel<<<nbk, 256, 0, c->stream>>>(c->Ac, n, kb, P, Brow, Ccol);
+    k_gj_update<<<dim3(nbk, nbk), 256, 0, c->stream>>>(c->Ac, n, kb, P, Brow, Ccol);
+    c->launches += 3;
+  }
+  k_round_f32<<<grid_for((int64_t)n * n, 256), 256, 0, c->stream>>>((int64_t)n * n, c->Ac, c->Ainv32);
+  c->launches += 1;
+  cudaEventRecord(c->ev1, c->stream);
+  if ((rc = sync_and_check(c, "coarse matrix"))) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->coarse_setup_ms = ms;
+  c->coarse_geo_gen = c->geo_gen;
+  return 0;
+}
+
+static int coarse_target_dofs(const Ctx* c) {
+  return c->coarse_target > 0 ? c->coarse_target : auto_coarse_dofs(3 * c->N);
+}
+
+int coarse_prepare(Ctx* c) {
+  if (c->N == 0) return set_err(c, JFEM_ERR_INVALID, "jfem_set_mesh must come first");
+  int rc = geometry_prepare(c);
+  if (rc) return rc;
+  const int target = coarse_target_dofs(c);
+  if (!c->node_agg || c->coarse_mask_gen != c->mask_gen || c->coarse_built_target != target) {
+    if ((rc = coarse_build(c, target))) return rc;
+  }
+  if (c->coarse_geo_gen != c->geo_gen) {
+    if ((rc = coarse_values(c))) return rc;
+  }
+  return 0;
+}
+
+void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop) {
+  k_coarse_restrict<<<std::min(c->nagg, 152 * 8), 256, 0, c->stream>>>(c->nagg, c->agg_ptr, c->agg_nodes,
+                                                                      c->node_d32, r, stop, c->Rc);
+  k_coarse_gemv<<<(c->nc + 7) / 8, 256, 0, c->stream>>>(c->nc, c->nc_pad, c->Ainv32, c->Rc, stop, c->Ec);
+  c->launches += 2;
+}
+
+int coarse_info(Ctx* c, int* n_agg, int* n_coarse, int64_t* n_elem_listed, double* setup_ms) {
+  int rc = coarse_prepare(c);
+  if (rc) return rc;
+  if (n_agg) *n_agg = c->nagg;
+  if (n_coarse) *n_coarse = c->nc;
+  if (n_elem_listed) *n_elem_listed = c->n_celem;
+  if (setup_ms) *setup_ms = c->coarse_setup_ms;
+  return 0;
+}
+
+int coarse_matrix(Ctx* c, double* Ac_h, int* node_agg_h) {
+  int rc = coarse_prepare(c);
+  if (rc) return rc;
+  if (node_agg_h) cudaMemcpyAsync(node_agg_h, c->node_agg, c->N * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (Ac_h) {
+    coarse_assemble(c);   // overwrites the inverse: recomputed by the next coarse_prepare
+    c->coarse_geo_gen = 0;
+    cudaMemcpy2DAsync(Ac_h, (size_t)c->nc * sizeof(double), c->Ac, (size_t)c->nc_pad * sizeof(double),
+                      (size_t)c->nc * sizeof(double), (size_t)c->nc, cudaMemcpyDeviceToHost, c->stream);
+  }
+  return sync_and_check(c, "coarse matrix download");
+}
+
+int coarse_precondition(Ctx* c, const double* r_h, double* z_h) {
+  int rc = coarse_prepare(c);
+  if (rc) return rc;
+  if ((rc = jacobi_diag_device(c, c->dinv))) return rc;
+  const int64_t n3 = 3 * c->N;
+  cudaMemcpyAsync(c->tmp, r_h, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  k_to_df<<<grid_for(n3, 256), 256, 0, c->stream>>>(n3, c->tmp, c->rd);
+  enqueue_coarse_restrict_solve(c, c->rd, nullptr);
+  k_coarse_jacobi_out<<<grid_for(n3, 256), 256, 0, c->stream>>>(c->N, c->tmp, c->dinv, c->mask, c->node_agg,
+                                                                 c->node_d32, c->Ec, c->tmp2);
+  c->launches += 2;
+  cudaMemcpyAsync(z_h, c->tmp2, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  return sync_and_check(c, "two-level preconditioner");
+}
+
+}  // namespace jfem

@@ -197,6 +197,17 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
   return false;
 }
 
+// Prolongation of the two-level preconditioner at DOF (i, c): (P Ec)_ic =
+// t_a + (ω_a × d_i)_c with (t_a, ω_a) = Ec[6a .. 6a+5], a the aggregate of node
+// i and d_i = X_i − c_a (jfem_coarse.cu).  The caller applies the Dirichlet mask.
+__device__ __forceinline__ float coarse_prolong(const int* __restrict__ node_agg, const float4* __restrict__ d32,
+                                                const float* __restrict__ Ec, int64_t i, int c) {
+  const int a = node_agg[i];
+  const float4 d = d32[i];
+  const float* e = Ec + 6 * a;
+  return c == 0 ? e[0] + e[4] * d.z - e[5] * d.y : c == 1 ? e[1] + e[5] * d.x - e[3] * d.z : e[2] + e[3] * d.y - e[4] * d.x;
+}
+
 // ---------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------
@@ -359,6 +370,8 @@ struct Ctx {
   // training pairs [pairs][N][3] (x, t, d), activations for B samples, FCG z
   MpnnState* mp = nullptr;
   float *mp_x = nullptr, *mp_t = nullptr, *mp_d = nullptr, *mp_den = nullptr;
+  float* mp_c = nullptr;      // [pairs][N][3] coarse term Q r̃ of each pair (pairs collected two-level)
+  int mp_coarse = -1;         // pairs collected with (1) or without (0) the coarse space; −1 none held
   int64_t mp_pairs = 0, mp_cap = 0;
   MpBufs mb;                  // activations and scratch for m_actB samples (one arena)
   float* marena = nullptr;
@@ -368,6 +381,39 @@ struct Ctx {
   int64_t m_actB = 0, m_gpart_cap = 0;
   float* zf = nullptr;        // FCG: preconditioned residual (FP32)
   float* invdeg = nullptr;    // 1 / (neighbours of each node), the mean-aggregation weights
+
+  // two-level preconditioner: Galerkin coarse space of rigid-body modes on node
+  // aggregates (jfem_coarse.cu).  Structure per (mesh, Dirichlet mask); values
+  // per geometry generation (material and coordinates).
+  int coarse_target = -1;       // requested coarse DOFs: 0 off, < 0 automatic (kept across meshes)
+  uint64_t geo_gen = 1;         // bumped by every geometry invalidation
+  uint64_t mask_gen = 1;        // bumped by every jfem_set_dirichlet
+  uint64_t coarse_geo_gen = 0, coarse_mask_gen = 0;   // generations the coarse data was built for
+  int coarse_built_target = 0;
+  int nagg = 0, nc = 0, nc_pad = 0;   // aggregates, coarse DOFs (6 per aggregate), padded to 32
+  int nb_bins[3] = {0, 0, 0};
+  int* agg_ptr = nullptr;       // [nagg+1] nodes of each aggregate (CSR, ascending node)
+  int* agg_nodes = nullptr;     // [N]
+  int* node_agg = nullptr;      // [N] aggregate of each node
+  float4* node_d32 = nullptr;   // [N] X_i − centroid of its aggregate (FP32; w unused)
+  double* node_d64 = nullptr;   // [N][3] the same in FP64 (coarse matrix)
+  int64_t n_celem = 0;          // elements whose A_c contribution is not zero
+  int* celem = nullptr;         // [n_celem] element ids, ascending
+  int* celem_aggs = nullptr;    // [n_celem][10] distinct aggregates of the element, ascending, −1 padded
+  int64_t* celem_off = nullptr; // [n_celem] first contribution block of the element (A_e² blocks)
+  int64_t n_contrib = 0;
+  double* contrib = nullptr;    // [n_contrib][36] 6×6 element blocks of A_c (FP64)
+  int64_t n_cblk = 0;           // nonzero 6×6 blocks of A_c
+  int* cblk_ab = nullptr;       // [n_cblk][2] (row aggregate, column aggregate)
+  int* cblk_ptr = nullptr;      // [n_cblk+1] into cblk_src
+  int64_t* cblk_src = nullptr;  // contribution blocks of each A_c block, ascending element
+  double* Ac = nullptr;         // [nc_pad][nc_pad] A_c, inverted in place (FP64)
+  double* Ac_diag = nullptr;    // [nc_pad] diagonal of A_c before the inversion
+  double* gj_buf = nullptr;     // Gauss–Jordan panels: P (32×32), row panel, old column panel
+  float* Ainv32 = nullptr;      // [nc_pad][nc_pad] A_c⁻¹ rounded to FP32 (the per-iteration coarse solve)
+  float* Rc = nullptr;          // [nc_pad] restricted residual Pᵀ r
+  float* Ec = nullptr;          // [nc_pad] coarse correction A_c⁻¹ Pᵀ r
+  double coarse_setup_ms = 0.0; // last coarse value setup (CUDA events)
 
   std::vector<void*> owned;   // everything cudaMalloc'ed for this mesh
 };
@@ -444,6 +490,12 @@ int mpnn_precondition(Ctx* c, const double* r, double* z);
 int mpnn_ensure_act(Ctx* c, int64_t B);
 int mpnn_refresh_poly(Ctx* c);
 void enqueue_mpnn_spd(Ctx* c, const float* y, float* v);   // v = NᵀN y for one sample (y, v: [N][3])
+// jfem_coarse.cu
+int coarse_prepare(Ctx* c);   // structure and values for the current mesh, mask and geometry
+int coarse_info(Ctx* c, int* n_agg, int* n_coarse, int64_t* n_elem_listed, double* setup_ms);
+int coarse_matrix(Ctx* c, double* Ac_h, int* node_agg_h);
+int coarse_precondition(Ctx* c, const double* r_h, double* z_h);
+void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop);   // Ec = A_c⁻¹ Pᵀ r
 // jfem_recovery.cu
 int recover_field(Ctx* c, const double* u_h, int field, double tol, int max_iter, double* nodal_h, int* iters_out);
 // jfem_solver.cu

@@ -330,29 +330,33 @@ __global__ void k_mp_to_bf16(int n, float* __restrict__ w, __nv_bfloat16* __rest
 // ---------------------------------------------------------------------------
 // loss (energy-norm cosine) and its gradient with respect to z
 // ---------------------------------------------------------------------------
-// z = mask ⊙ (y + v) / sq of one pair as the double-float input of the tiled apply
+// z = mask ⊙ (y + v) / sq (+ cq, the pair's coarse term, when given) of one pair
+// as the double-float input of the tiled apply
 __global__ void k_mp_zsplit(int64_t n3, const float* __restrict__ y, const float* __restrict__ v,
-                            const float* __restrict__ sq, float2* __restrict__ p2) {
+                            const float* __restrict__ sq, const float* __restrict__ cq, float2* __restrict__ p2) {
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n3; q += (int64_t)gridDim.x * blockDim.x)
-    p2[q] = make_float2(sq[q] > 0.f ? (y[q] + v[q]) / sq[q] : 0.f, 0.f);
+    p2[q] = make_float2(sq[q] > 0.f ? (y[q] + v[q]) / sq[q] + (cq ? cq[q] : 0.f) : 0.f, 0.f);
 }
 
-// per pair b = blockIdx.y: partials of a_b = zᵀr̃ = Σ (y + v) y and q_b = zᵀKz
-// into dots[(b·gridDim.x + blockIdx.x)·2 + {0, 1}]
+// per pair b = blockIdx.y: partials of a_b = zᵀr̃ = Σ (y + v) y (+ Σ cq sq y) and
+// q_b = zᵀKz into dots[(b·gridDim.x + blockIdx.x)·2 + {0, 1}]
 __global__ void __launch_bounds__(256) k_mp_cos_dots(int64_t n3, const float* __restrict__ y,
                                                      const float* __restrict__ v, const float* __restrict__ sq,
-                                                     const float* __restrict__ kz, double* __restrict__ dots) {
+                                                     const float* __restrict__ cq, const float* __restrict__ kz,
+                                                     double* __restrict__ dots) {
   __shared__ double sh[32];
   const int64_t b = blockIdx.y;
   const float* yb = y + b * n3;
   const float* vb = v + b * n3;
   const float* sb = sq + b * n3;
+  const float* cb = cq ? cq + b * n3 : nullptr;
   const float* kb = kz + b * n3;
   double a = 0.0, q = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x) {
     const double yv = (double)yb[i] + (double)vb[i];
-    a += yv * (double)yb[i];
-    q += (sb[i] > 0.f ? (double)((yb[i] + vb[i]) / sb[i]) : 0.0) * (double)kb[i];
+    const double ci = (cb && sb[i] > 0.f) ? (double)cb[i] : 0.0;
+    a += yv * (double)yb[i] + ci * (double)sb[i] * (double)yb[i];
+    q += (sb[i] > 0.f ? (double)((yb[i] + vb[i]) / sb[i]) + ci : 0.0) * (double)kb[i];
   }
   a = block_sum(a, sh);
   q = block_sum(q, sh);
@@ -836,8 +840,8 @@ void enqueue_mpnn_spd(Ctx* c, const float* y, float* v) {
 
 // forward, loss and gradient for B pairs (y, sq [B][N][3], den [B]); the
 // gradient of scale·Σ_b ℓ_b lands in mp->g, the loss in *loss_out (if set).
-static int train_step(Ctx* c, int64_t B, const float* y, const float* sq, const float* den, float scale,
-                      double* loss_out) {
+static int train_step(Ctx* c, int64_t B, const float* y, const float* sq, const float* cq, const float* den,
+                      float scale, double* loss_out) {
   const int64_t N = c->N, rows = B * N, n3 = 3 * N;
   const int64_t nblk = (rows + MP_THREADS - 1) / MP_THREADS;
   int rc = ensure_gpart(c, nblk);
@@ -850,12 +854,13 @@ static int train_step(Ctx* c, int64_t B, const float* y, const float* sq, const 
   enqueue_backward(c, B, b.u, 0, y, false, false, b.v);
   // K z per pair, z = (y + v)/sq (FP32 tiled apply)
   for (int64_t k = 0; k < B; ++k) {
-    k_mp_zsplit<<<grid_for(n3, 256), 256, 0, c->stream>>>(n3, y + k * n3, b.v + k * n3, sq + k * n3, c->p2);
+    k_mp_zsplit<<<grid_for(n3, 256), 256, 0, c->stream>>>(n3, y + k * n3, b.v + k * n3, sq + k * n3,
+                                                          cq ? cq + k * n3 : nullptr, c->p2);
     enqueue_apply_tiled(c, c->p2, c->Apf, true, nullptr, nullptr, nullptr);
     cudaMemcpyAsync(b.kz + k * n3, c->Apf, n3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream);
     c->launches += 1;
   }
-  k_mp_cos_dots<<<dim3(MP_DOT_BLOCKS, (unsigned)B), 256, 0, c->stream>>>(n3, y, b.v, sq, b.kz, c->mdots);
+  k_mp_cos_dots<<<dim3(MP_DOT_BLOCKS, (unsigned)B), 256, 0, c->stream>>>(n3, y, b.v, sq, cq, b.kz, c->mdots);
   k_mp_cos_coef<<<1, 32, 0, c->stream>>>((int)B, MP_DOT_BLOCKS, c->mdots, den, scale, c->mcoef);
   k_mp_cos_ghat<<<gs, MP_THREADS, 0, c->stream>>>(rows, N, y, sq, b.kz, c->mcoef, c->mask, b.ghat);
   c->launches += 3;
@@ -881,22 +886,48 @@ static double sum_partials_host(Ctx* c, int n) {
   return s;
 }
 
-// Append (y, t, sq, den) for one pair (r, e) (device, FP64).
+// coarse term of a training pair: cq = mask ⊙ P Ec (Ec = A_c⁻¹ Pᵀ r̃ for the
+// pair's scaled residual r̃)
+__global__ void k_mp_coarse_term(int64_t N, const int* __restrict__ node_agg, const float4* __restrict__ d32,
+                                 const float* __restrict__ Ec, const uint8_t* __restrict__ mask,
+                                 const double* __restrict__ dinv, float* __restrict__ cq) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * N; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = q / 3;
+    const int k = (int)(q % 3);
+    cq[q] = (dof_free(mask, i, k) && dinv[q] > 0.0) ? coarse_prolong(node_agg, d32, Ec, i, k) : 0.f;
+  }
+}
+
+// r̃ = r / s as double-float (the restriction's input)
+__global__ void k_mp_scaled_df(int64_t n, const double* __restrict__ r, double inv_s, float2* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = r[i] * inv_s;
+    const float hi = (float)v;
+    out[i] = make_float2(hi, (float)(v - (double)hi));
+  }
+}
+
+// Append (y, t, sq, den) — and, for a two-level context, the coarse term cq —
+// for one pair (r, e) (device, FP64).
 static int append_pair(Ctx* c, const double* r, const double* e) {
   const int64_t n3 = 3 * c->N;
-  if (c->mp_pairs >= c->mp_cap) {   // grow geometrically
-    const int64_t cap = std::max<int64_t>(16, 2 * c->mp_cap);
-    float *x = nullptr, *t = nullptr, *d = nullptr, *den = nullptr;
+  const bool coarse = c->mp_coarse == 1;
+  if (c->mp_pairs >= c->mp_cap || (coarse && !c->mp_c)) {   // grow geometrically
+    const int64_t cap = std::max<int64_t>(16, c->mp_pairs >= c->mp_cap ? 2 * c->mp_cap : c->mp_cap);
+    float *x = nullptr, *t = nullptr, *d = nullptr, *den = nullptr, *cc = nullptr;
     int rc = dalloc(c, &x, (size_t)cap * n3);
     if (!rc) rc = dalloc(c, &t, (size_t)cap * n3);
     if (!rc) rc = dalloc(c, &d, (size_t)cap * n3);
     if (!rc) rc = dalloc(c, &den, (size_t)cap);
+    if (!rc && coarse) rc = dalloc(c, &cc, (size_t)cap * n3);
     if (rc) return rc;
     if (c->mp_pairs) {
       cudaMemcpyAsync(x, c->mp_x, c->mp_pairs * n3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream);
       cudaMemcpyAsync(t, c->mp_t, c->mp_pairs * n3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream);
       cudaMemcpyAsync(d, c->mp_d, c->mp_pairs * n3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream);
       cudaMemcpyAsync(den, c->mp_den, c->mp_pairs * sizeof(float), cudaMemcpyDeviceToDevice, c->stream);
+      if (coarse && c->mp_c)
+        cudaMemcpyAsync(cc, c->mp_c, c->mp_pairs * n3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream);
       cudaStreamSynchronize(c->stream);
     }
     if (c->mp_x) {
@@ -905,10 +936,12 @@ static int append_pair(Ctx* c, const double* r, const double* e) {
       dfree(c, c->mp_d);
       dfree(c, c->mp_den);
     }
+    if (c->mp_c) dfree(c, c->mp_c);
     c->mp_x = x;
     c->mp_t = t;
     c->mp_d = d;
     c->mp_den = den;
+    c->mp_c = cc;
     c->mp_cap = cap;
   }
   k_mp_sample_norm<<<JFEM_RED_BLOCKS, 256, 0, c->stream>>>(c->N, r, c->dinv, c->mask, c->part);
@@ -923,6 +956,13 @@ static int append_pair(Ctx* c, const double* r, const double* e) {
   c->launches += 1;
   const double den = sum_partials_host(c, JFEM_RED_BLOCKS);
   if (!(den > 0.0)) return 0;
+  if (coarse) {   // cq = Q r̃ with the current system's coarse operator
+    k_mp_scaled_df<<<grid_for(n3, 256), 256, 0, c->stream>>>(n3, r, 1.0 / s, c->rd);
+    enqueue_coarse_restrict_solve(c, c->rd, nullptr);
+    k_mp_coarse_term<<<grid_for(n3, 256), 256, 0, c->stream>>>(c->N, c->node_agg, c->node_d32, c->Ec, c->mask,
+                                                                c->dinv, c->mp_c + k * n3);
+    c->launches += 2;
+  }
   const float denf = (float)den;
   cudaMemcpyAsync(c->mp_den + k, &denf, sizeof(float), cudaMemcpyHostToDevice, c->stream);
   int rc = sync_and_check(c, "training pair");
@@ -931,10 +971,23 @@ static int append_pair(Ctx* c, const double* r, const double* e) {
   return 0;
 }
 
+// Pairs carry the coarse term when the context's coarse space is on; pairs of
+// both kinds are never mixed.
+static int pairs_coarse_state(Ctx* c) {
+  const int want = c->coarse_target != 0 ? 1 : 0;
+  if (c->mp_pairs > 0 && c->mp_coarse != want)
+    return set_err(c, JFEM_ERR_INVALID,
+                   "training pairs were collected with another coarse-space setting (jfem_mpnn_clear first)");
+  c->mp_coarse = want;
+  if (want) return coarse_prepare(c);
+  return 0;
+}
+
 int mpnn_collect(Ctx* c, int max_pairs, double tol) {
   if (max_pairs <= 0) return set_err(c, JFEM_ERR_INVALID, "max_pairs must be positive");
   int rc = geometry_prepare(c);
   if (rc) return rc;
+  if ((rc = pairs_coarse_state(c))) return rc;
   const int64_t n3 = 3 * c->N;
   const int max_snaps = max_pairs - 1;   // plus the x = 0 pair
   std::vector<int> snap_iters((size_t)std::max(1, max_snaps));
@@ -980,7 +1033,8 @@ int mpnn_train(Ctx* c, int epochs, int batch, double lr, uint64_t seed, double* 
       const int64_t Bq = std::min<int64_t>(B, c->mp_pairs - s0);
       const int64_t off = s0 * 3 * c->N;
       double lq = 0.0;
-      rc = train_step(c, Bq, c->mp_x + off, c->mp_d + off, c->mp_den + s0, 1.f / (float)Bq, losses ? &lq : nullptr);
+      rc = train_step(c, Bq, c->mp_x + off, c->mp_d + off, c->mp_coarse == 1 ? c->mp_c + off : nullptr, c->mp_den + s0,
+                      1.f / (float)Bq, losses ? &lq : nullptr);
       if (rc) return rc;
       m->step += 1;
       const float c1 = 1.f - std::pow(0.9f, (float)m->step), c2 = 1.f - std::pow(0.999f, (float)m->step);
@@ -1005,12 +1059,16 @@ int mpnn_loss_grad(Ctx* c, const double* r_h, const double* e_h, double* loss, f
   cudaMemcpyAsync(c->tmp, r_h, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(c->b, e_h, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
   const int64_t keep = c->mp_pairs;   // the pair goes to slot `keep` and is dropped again below
+  const int keep_state = c->mp_coarse;
+  if ((rc = pairs_coarse_state(c))) return rc;
   if ((rc = append_pair(c, c->tmp, c->b))) return rc;
   if (c->mp_pairs == keep) return set_err(c, JFEM_ERR_INVALID, "zero residual or error");
   const int64_t off = keep * n3;
   double L = 0.0;
-  rc = train_step(c, 1, c->mp_x + off, c->mp_d + off, c->mp_den + keep, 1.f, &L);
+  rc = train_step(c, 1, c->mp_x + off, c->mp_d + off, c->mp_coarse == 1 ? c->mp_c + off : nullptr, c->mp_den + keep, 1.f,
+                  &L);
   c->mp_pairs = keep;
+  if (keep == 0) c->mp_coarse = keep_state;
   if (rc) return rc;
   cudaMemcpyAsync(grad, c->mp->g, MP_P * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
   if ((rc = sync_and_check(c, "gradient"))) return rc;

@@ -376,29 +376,37 @@ __global__ void __launch_bounds__(256) k_fcg_input(int64_t N, const float2* __re
   }
 }
 
-// z = D^{-1/2}(y + NᵀN y) (NN; y, v = NᵀN y given) or z = D⁻¹r (Jacobi); z·q_old
-// partials → the last block forms β = z·q_old / p_old·q_old (0 on restart)
-template <bool NN>
+// z = D^{-1/2}(y + NᵀN y) (NN; y, v = NᵀN y given) or z = D⁻¹r (Jacobi), plus
+// the coarse correction P Ec when COARSE (two-level); z·q_old partials → the
+// last block forms β = z·q_old / p_old·q_old (0 on restart)
+template <bool NN, bool COARSE>
 __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_z(int64_t n, const float* __restrict__ y,
                                                             const float* __restrict__ v,
                                                             const float2* __restrict__ r,
                                                             const float* __restrict__ dinv,
                                                             const uint8_t* __restrict__ mask,
                                                             const float* __restrict__ qold,
+                                                            const int* __restrict__ node_agg,
+                                                            const float4* __restrict__ d32,
+                                                            const float* __restrict__ Ec,
                                                             SolverScalars* __restrict__ sc, float* __restrict__ z,
                                                             double* __restrict__ part) {
   __shared__ double sh[32];
   if (sc->done[0]) return;
   float2 dot = make_float2(0.f, 0.f);
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-    const bool fr = !((mask[q / 3] >> (int)(q % 3)) & 1);
+    const int64_t i = q / 3;
+    const int cc = (int)(q % 3);
+    const bool fr = !((mask[i] >> cc) & 1);
     float zq;
     if (NN) {
-      zq = fr ? sqrtf(dinv[q]) * (y[q] + v[q]) : 0.f;
+      zq = sqrtf(dinv[q]) * (y[q] + v[q]);
     } else {
       const float2 rq = r[q];
-      zq = fr ? dinv[q] * (rq.x + rq.y) : 0.f;
+      zq = dinv[q] * (rq.x + rq.y);
     }
+    if (COARSE) zq += coarse_prolong(node_agg, d32, Ec, i, cc);
+    zq = fr ? zq : 0.f;
     z[q] = zq;
     dot = df_add(dot, df_two_prod(zq, qold[q]));
   }
@@ -537,17 +545,29 @@ static int true_residual(Ctx* c, const double* f, const double* xv, double* r, d
   return read_norms(c, rr_out, drift2);
 }
 
-static void enqueue_fcg_iteration(Ctx* c, bool nn) {
+static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
   const int64_t n = 3 * c->N;
+  if (coarse) enqueue_coarse_restrict_solve(c, c->rd, &c->sc->done[0]);
+  const int* na = coarse ? c->node_agg : nullptr;
+  const float4* d32 = coarse ? c->node_d32 : nullptr;
+  const float* Ec = coarse ? c->Ec : nullptr;
   if (nn) {
     k_fcg_input<<<grid_for(n, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, c->mb.y);
     enqueue_mpnn_spd(c, c->mb.y, c->mb.v);
-    k_fcg_z<true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->mb.y, c->mb.v, c->rd, c->dinvf, c->mask, c->Apf,
-                                                           c->sc, c->zf, c->part);
+    if (coarse)
+      k_fcg_z<true, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->mb.y, c->mb.v, c->rd, c->dinvf, c->mask,
+                                                                  c->Apf, na, d32, Ec, c->sc, c->zf, c->part);
+    else
+      k_fcg_z<true, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->mb.y, c->mb.v, c->rd, c->dinvf, c->mask,
+                                                                   c->Apf, na, d32, Ec, c->sc, c->zf, c->part);
     c->launches += 2;
   } else {
-    k_fcg_z<false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, nullptr, nullptr, c->rd, c->dinvf, c->mask, c->Apf,
-                                                            c->sc, c->zf, c->part);
+    if (coarse)
+      k_fcg_z<false, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, nullptr, nullptr, c->rd, c->dinvf, c->mask,
+                                                                   c->Apf, na, d32, Ec, c->sc, c->zf, c->part);
+    else
+      k_fcg_z<false, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, nullptr, nullptr, c->rd, c->dinvf, c->mask,
+                                                                    c->Apf, na, d32, Ec, c->sc, c->zf, c->part);
     c->launches += 1;
   }
   k_fcg_p<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->zf, c->p2, c->rd, c->sc, c->part);
@@ -573,10 +593,11 @@ static void enqueue_iteration(Ctx* c, bool fp32, int slot) {
   c->launches += 2;
 }
 
-// kind: 0 FP64 PCG, 1 mixed PCG, 2 FCG Jacobi, 3 FCG learned
+// kind: 0 FP64 PCG, 1 mixed PCG, 2 FCG Jacobi, 3 FCG learned, 4 FCG Jacobi + coarse,
+// 5 FCG learned + coarse
 static int graph_key(Ctx* c, int kind) {
-  return kind | (c->finite << 2) | (c->model << 3) | (c->geom << 4) | ((c->geo_affine ? 1 : 0) << 5) |
-         (c->et << 6) | ((c->geoT32 ? 1 : 0) << 11) | ((nh_cache_ready(c) ? 1 : 0) << 12);
+  return kind | (c->finite << 3) | (c->model << 4) | (c->geom << 5) | ((c->geo_affine ? 1 : 0) << 6) |
+         (c->et << 7) | ((c->geoT32 ? 1 : 0) << 12) | ((nh_cache_ready(c) ? 1 : 0) << 13);
 }
 
 static int build_graph(Ctx* c, int kind) {
@@ -591,7 +612,7 @@ static int build_graph(Ctx* c, int kind) {
   cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_check(c, e, "begin capture");
   for (int k = 0; k < PCG_CHUNK; ++k) {
-    if (kind >= 2) enqueue_fcg_iteration(c, kind == 3);
+    if (kind >= 2) enqueue_fcg_iteration(c, kind == 3 || kind == 5, kind >= 4);
     else enqueue_iteration(c, kind == 1, kind == 1 ? 0 : (k & 1));
   }
   e = cudaStreamEndCapture(c->stream, &g);
@@ -771,8 +792,8 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
 // the recursive residual norm over `window` iterations — generous, since CG
 // residual norms are not monotone) the solve continues with Jacobi from the
 // best iterate (res->fallbacks = 1).
-static int fcg(Ctx* c, const double* f, bool nn, double tol, int max_iter, double time_budget, double t_start,
-               bool x_zero, PcgResult* res, double drop, bool tol_abs = false) {
+static int fcg(Ctx* c, const double* f, bool nn, bool coarse, double tol, int max_iter, double time_budget,
+               double t_start, bool x_zero, PcgResult* res, double drop, bool tol_abs = false) {
   int rc = 0;
   double rr0 = 0.0;
   const int64_t n = 3 * c->N;
@@ -781,6 +802,8 @@ static int fcg(Ctx* c, const double* f, bool nn, double tol, int max_iter, doubl
   if (nn && (!c->mp || !c->mp->ready)) return set_err(c, JFEM_ERR_INVALID, "no network weights (jfem_mpnn_init)");
   if (nn && (rc = mpnn_ensure_act(c, 1))) return rc;
   if (nn && (rc = mpnn_refresh_poly(c))) return rc;
+  if (coarse && (rc = coarse_prepare(c))) return rc;
+  const auto kind_of = [&]() { return (nn ? 3 : 2) + (coarse ? 2 : 0); };
   if (!c->zf && (rc = dalloc(c, &c->zf, (size_t)n))) return rc;
   if (x_zero) {
     k_residual<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, f, 1.0, nullptr, c->mask, c->r, 0, c->part);
@@ -801,7 +824,7 @@ static int fcg(Ctx* c, const double* f, bool nn, double tol, int max_iter, doubl
   const double bb = c->sc_host->bb;
   *res = PcgResult();
   if (!(bb > 0.0)) return 0;
-  if ((rc = build_graph(c, nn ? 3 : 2))) return rc;
+  if ((rc = build_graph(c, kind_of()))) return rc;
   const double ru = drop * drop;
   const double goal = tol * tol * bb;
   const int window = 4096;
@@ -843,8 +866,9 @@ static int fcg(Ctx* c, const double* f, bool nn, double tol, int max_iter, doubl
       const bool converged = finite && rr_t <= goal;
       bool switch_jacobi = false;
       if (!converged && !at_cap && (stalls >= 2 || !finite) && nn) {   // learned preconditioner stalled
-        switch_jacobi = true;
+        switch_jacobi = true;   // continue as plain Jacobi-PCG
         nn = false;
+        coarse = false;
         fallbacks = 1;
         stalls = 0;
       }
@@ -866,7 +890,7 @@ static int fcg(Ctx* c, const double* f, bool nn, double tol, int max_iter, doubl
         if ((rc = true_residual(c, f, c->x, c->r, &rr_t))) return rc;
         rr_true_last = rr_t;
       }
-      if (switch_jacobi && (rc = build_graph(c, 2))) return rc;
+      if (switch_jacobi && (rc = build_graph(c, kind_of()))) return rc;
       rr_rec_best = rr_t;
       rec_best_it = iters;
       const int restart = (!finite || switch_jacobi || !(drift2 < 0.01 * rr_t)) ? 1 : 0;
@@ -925,10 +949,12 @@ static int solve_linear(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
   PcgResult pr;
   const double drop = o->refine_drop > 0.0 ? o->refine_drop : 0.3;
   const bool tol_abs = o->tol_absolute != 0;
-  if (o->method == JFEM_FCG_LEARNED)
-    rc = fcg(c, c->f_ext, true, o->tol, o->max_iter, o->time_budget_s, t0, c->n_fixed_nonzero == 0, &pr, drop,
-             tol_abs);
-  else
+  if (o->method == JFEM_FCG_LEARNED || o->method == JFEM_FCG_TWO_LEVEL) {
+    const bool nn = o->method == JFEM_FCG_LEARNED;
+    const bool coarse = !nn || c->coarse_target != 0;
+    rc = fcg(c, c->f_ext, nn, coarse, o->tol, o->max_iter, o->time_budget_s, t0, c->n_fixed_nonzero == 0, &pr,
+             drop, tol_abs);
+  } else
     rc = pcg(c, c->f_ext, fp32, o->tol, o->max_iter, o->time_budget_s, t0, true, c->n_fixed_nonzero == 0, &pr,
              drop, nullptr, tol_abs);
   if (rc && rc != JFEM_ERR_TIMEOUT) return rc;
@@ -1086,7 +1112,8 @@ int solve_device(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stats* st) 
     return set_err(c, JFEM_ERR_INVALID, "Newton options must be positive");
   switch (o->method) {
     case JFEM_PCG_JACOBI:
-    case JFEM_FCG_LEARNED: return solve_linear(c, o, u_d, st);
+    case JFEM_FCG_LEARNED:
+    case JFEM_FCG_TWO_LEVEL: return solve_linear(c, o, u_d, st);
     case JFEM_NEWTON: return solve_newton(c, o, u_d, st);
     default: return set_err(c, JFEM_ERR_INVALID, "unknown solve method");
   }

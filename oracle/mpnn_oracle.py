@@ -141,21 +141,30 @@ def apply_scaled(params, y, sq, graph, mask3):
     return (y + v) * mask3 / np.where(sq > 0, sq, 1.0)
 
 
-def loss(params, y, t, sq, graph, mask3, kmul):
-    """kmul(v [N,3]) → K v with prescribed rows and columns removed."""
+def loss(params, y, t, sq, graph, mask3, kmul, c=None):
+    """kmul(v [N,3]) → K v with prescribed rows and columns removed.  c (same
+    shape as y, may be None): a term added to z that does not depend on the
+    weights — the coarse correction P A_c⁻¹ Pᵀ r̃ of the two-level
+    preconditioner, in the same scaled units."""
     z = apply_scaled(params, y, sq, graph, mask3)
+    if c is not None:
+        z = z + c * mask3
     rt = sq * y
     a = float(np.sum(z * rt))
     q = float(np.sum(z * kmul(z)))
     return 1.0 - a * a / (q * float(np.sum(t * rt)))
 
 
-def loss_and_grad(params, y, t, sq, graph, mask3, kmul):
-    """Loss and its gradient with respect to the (BF16-valued) parameters."""
+def loss_and_grad(params, y, t, sq, graph, mask3, kmul, c=None):
+    """Loss and its gradient with respect to the (BF16-valued) parameters; c as
+    in loss() (it shifts z, so ∂ℓ/∂z changes through a, q and Kz, while
+    ∂z/∂(NᵀN y) = D^{-1/2} stays as without it)."""
     u, cache_y = forward(params, y, graph, mask3)
     v = adjoint(params, u, graph, mask3)
     isq = np.where(sq > 0, 1.0 / np.where(sq > 0, sq, 1.0), 0.0)
     z = (y + v) * mask3 * isq
+    if c is not None:
+        z = z + c * mask3
     rt = sq * y
     kz = kmul(z)
     a = float(np.sum(z * rt))

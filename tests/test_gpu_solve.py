@@ -160,7 +160,7 @@ def test_time_budget_returns_best_iterate(jfem, gpu_ctx_factory, method):
         assert rc == abi.ERR_TIMEOUT and st.status == abi.ERR_TIMEOUT
         assert "time budget" in ctx._lib.jfem_last_error(ctx._h).decode()
         assert np.all(np.isfinite(u)) and np.all(u[w.fixed_dofs] == 0.0)
-        assert 0 < st.cg_iterations < 1000 and 0.0 < st.residual <= 1.0
+        assert 0 < st.cg_iterations < 1000 and 0.0 < st.residual <= 1.0 + 1e-12   # never worse than x0
         o.time_budget_s = 0.0
         u2, st2, rc2 = ctx.solve(o)
         assert rc2 in (0, abi.STALL) and st2.residual <= 1e-10
