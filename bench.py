@@ -34,7 +34,7 @@ sys.path.insert(0, str(ROOT))
 
 import numpy as np  # noqa: E402
 
-METRIC = "time-to-1e-8 residual, 2M-DOF Tet10 cantilever (Jacobi-PCG, FP32 apply + FP64 refinement)"
+METRIC = "time-to-1e-8 residual, 2M-DOF Tet10 cantilever (learned two-level FCG; Jacobi-PCG beside)"
 UNIT = "s"
 TOL = 1e-8
 # Jacobi-PCG iterations the 200×20×20 Tet10 cantilever needs to reach 1e-8 (FP64
@@ -62,7 +62,7 @@ def parse():
     p.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner leg")
     p.add_argument("--learned-train", type=int, default=512, help="training systems of the Tet10 family")
     p.add_argument("--learned-eval", type=int, default=64, help="unseen evaluation systems")
-    p.add_argument("--learned-epochs", type=int, default=60)
+    p.add_argument("--learned-epochs", type=int, default=15, help="epochs per phase (two phases)")
     p.add_argument("--no-batch", action="store_true", help="skip the batched-solves leg")
     p.add_argument("--no-newton", action="store_true", help="skip the Newton–Krylov leg")
     p.add_argument("--newton-n", type=int, default=128, help="Hex8 cells per side of the Newton cube")
@@ -242,7 +242,7 @@ def run_reference(args):
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": workload_config(args.size),
+            "config": workload_config(args.size), "solver": SOLVER_REF,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": "port",
                              "sample": last["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -253,9 +253,14 @@ def run_reference(args):
 def workload_config(size):
     nx, ny, nz = size
     return {"workload": f"tet10_cantilever_{nx}x{ny}x{nz}", "elements": 6 * nx * ny * nz,
-            "dofs": 3 * (2 * nx + 1) * (2 * ny + 1) * (2 * nz + 1), "solver": "Jacobi-PCG",
-            "tol": TOL, "apply": "matrix-free FP32, FP64 vectors/dots/residual",
+            "dofs": 3 * (2 * nx + 1) * (2 * ny + 1) * (2 * nz + 1), "tol": TOL,
             "l2": "flushed before every step (256 MiB write)"}
+
+
+SOLVER_GPU = ("learned two-level flexible CG: z = D^-1/2(y + N^T N y) + P A_c^-1 P^T r (3-layer width-32 "
+              "message-passing network, BF16 weights; rigid-body modes of node aggregates), FP32 matrix-free "
+              "apply, double-float vectors, FP64 true-residual judge")
+SOLVER_REF = "Jacobi-PCG on the assembled FP64 CSC matrix (C++ restatement of the reference's assembly and CG)"
 
 
 # ---------------------------------------------------------------------------
@@ -271,15 +276,40 @@ def _set_system(ctx, w, mesh=True):
     ctx.set_traction(w.face_type, w.faces, w.traction)
 
 
-def learned_leg(jfem, args, device, big_workload):
-    """Train the network on solver-generated pairs of the Tet10 family (40×4×4
-    cubes on [0,10]×[0,1]², lognormal E with σ_log 0.5, random surface-patch
-    tractions), then time Jacobi-PCG and learned flexible CG to the FP64
-    relative residual 1e-8 on unseen seeds of the family and on the 2M-DOF
-    cantilever.  Times are host wall clock around a synchronous solve (second
-    of two runs)."""
-    abi = jfem._abi
+def train_network(jfem, args, device):
+    """Train the network on pairs the solver generates for the Tet10 family
+    (40×4×4 cubes on [0,10]×[0,1]², lognormal E with σ_log 0.5, random
+    surface-patch tractions; args.learned_train systems, 8 pairs each), with the
+    coarse space on: each pair carries its coarse term, so the network learns
+    the fine-level correction the coarse level leaves.  Returns the weights and
+    the training record."""
     fam = jfem.workloads.learned_family(args.learned_train, seed_item=40)
+    with jfem.Context(device) as ctx:
+        _set_system(ctx, fam[0])
+        ctx.set_coarse_space(-1)
+        ctx.mpnn_init(3)
+        t0 = time.perf_counter()
+        pairs = 0
+        for w in fam:
+            _set_system(ctx, w, mesh=False)
+            pairs = ctx.mpnn_collect(8, 1e-10)
+        t1 = time.perf_counter()
+        l1 = ctx.mpnn_train(args.learned_epochs, 32, 3e-3, seed=1)
+        l2 = ctx.mpnn_train(args.learned_epochs, 32, 1e-3, seed=2)
+        t2 = time.perf_counter()
+        W = ctx.mpnn_get_weights()
+    return W, {"family": "tet10_cantilever_40x4x4 (19,683 DOFs), lognormal E (sigma_log 0.5), patch tractions",
+               "train_systems": len(fam), "pairs": int(pairs), "epochs": 2 * args.learned_epochs,
+               "collect_s": t1 - t0, "train_s": t2 - t1, "loss_first": float(l1[0]), "loss_last": float(l2[-1])}
+
+
+def family_eval(jfem, args, device, W):
+    """args.learned_eval unseen systems of the family: Jacobi-PCG, the two-level
+    method with the network zeroed (JFEM_FCG_TWO_LEVEL) and the learned
+    two-level FCG, each to the FP64 relative residual 1e-8; host wall clock
+    around a synchronous solve (second of two runs: the coarse level and the
+    captured graphs are built by the first)."""
+    abi = jfem._abi
     ev = jfem.workloads.learned_family(args.learned_eval, seed_item=40 + 100000)
 
     def timed(ctx, method):
@@ -292,40 +322,25 @@ def learned_leg(jfem, args, device, big_workload):
             raise RuntimeError(f"solve did not converge: status {rc}")
         return st.cg_iterations, dt, st.fallbacks
 
-    out = {}
+    rows = []
     with jfem.Context(device) as ctx:
-        _set_system(ctx, fam[0])
-        ctx.mpnn_init(3)
-        t0 = time.perf_counter()
-        for w in fam:
-            _set_system(ctx, w, mesh=False)
-            pairs = ctx.mpnn_collect(8, 1e-10)
-        t1 = time.perf_counter()
-        l1 = ctx.mpnn_train(args.learned_epochs, 32, 3e-3, seed=1)
-        l2 = ctx.mpnn_train(args.learned_epochs, 32, 1e-3, seed=2)
-        t2 = time.perf_counter()
-        trained = ctx.mpnn_get_weights()
-        rows = []
+        _set_system(ctx, ev[0])
+        ctx.set_coarse_space(-1)
+        ctx.mpnn_set_weights(W)
         for w in ev:
             _set_system(ctx, w, mesh=False)
-            rows.append(timed(ctx, abi.PCG_JACOBI) + timed(ctx, abi.FCG_LEARNED))
-        r = np.array(rows, dtype=np.float64)
-        out["family"] = {"workload": "tet10_cantilever_40x4x4 family (19,683 DOFs)", "train_systems": len(fam),
-                         "pairs": int(pairs), "epochs": 2 * args.learned_epochs, "collect_s": t1 - t0,
-                         "train_s": t2 - t1, "loss_first": float(l1[0]), "loss_last": float(l2[-1]),
-                         "eval_systems": len(ev),
-                         "jacobi_pcg": {"iterations": float(r[:, 0].mean()), "s": float(r[:, 1].mean())},
-                         "learned_fcg": {"iterations": float(r[:, 3].mean()), "s": float(r[:, 4].mean()),
-                                         "fallbacks": int(r[:, 5].sum())},
-                         "iteration_ratio": float(r[:, 0].mean() / r[:, 3].mean()),
-                         "wall_time_ratio": float(r[:, 1].mean() / r[:, 4].mean())}
-        _set_system(ctx, big_workload)
-        ctx.mpnn_set_weights(trained)
-        pj = timed(ctx, abi.PCG_JACOBI)
-        pl = timed(ctx, abi.FCG_LEARNED)
-        out["tet10_2M"] = {"jacobi_pcg": {"iterations": pj[0], "s": pj[1]},
-                           "learned_fcg": {"iterations": pl[0], "s": pl[1], "fallbacks": pl[2]},
-                           "wall_time_ratio": pj[1] / pl[1]}
+            rows.append(timed(ctx, abi.PCG_JACOBI) + timed(ctx, abi.FCG_TWO_LEVEL) + timed(ctx, abi.FCG_LEARNED))
+    r = np.array(rows, dtype=np.float64)
+    res = lambda k: {"iterations": float(r[:, 3 * k].mean()), "s": float(r[:, 3 * k + 1].mean())}
+    out = {"workload": "tet10_cantilever_40x4x4 family, unseen seeds", "eval_systems": len(ev),
+           "jacobi_pcg": res(0), "two_level_network_zeroed": res(1), "learned_two_level": res(2)}
+    out["learned_two_level"]["fallbacks"] = int(r[:, 8].sum())
+    out["iteration_ratio_vs_jacobi"] = out["jacobi_pcg"]["iterations"] / out["learned_two_level"]["iterations"]
+    out["wall_time_ratio_vs_jacobi"] = out["jacobi_pcg"]["s"] / out["learned_two_level"]["s"]
+    out["iteration_ratio_vs_network_zeroed"] = (out["two_level_network_zeroed"]["iterations"] /
+                                                out["learned_two_level"]["iterations"])
+    out["wall_time_ratio_vs_network_zeroed"] = (out["two_level_network_zeroed"]["s"] /
+                                                out["learned_two_level"]["s"])
     return out
 
 
@@ -392,6 +407,15 @@ def batch_leg(jfem, args, device):
             times.append(t)
             lats.append(lat)
             ok = ok and bool(np.all(st == 0)) and bool(np.all(res <= TOL))
+    # a second batch object of the same shape takes the cached configuration
+    with jfem.Batch(device) as b2:
+        for w in ws:
+            b2.add_workload(w)
+        t0 = time.perf_counter()
+        b2.solve(tol=TOL, max_iter=200000, block_size=0)
+        t_second = time.perf_counter() - t0
+        second_source = b2.tune_source
+        t_second_solve = b2.solve(tol=TOL, max_iter=200000, block_size=0)[5]
     t = statistics.mean(times)
     lat = np.concatenate(lats)
     dofs = [w.mesh.n_dofs for w in ws]
@@ -399,7 +423,9 @@ def batch_leg(jfem, args, device):
             "solves_per_s": len(ws) / t, "launch_ms": t * 1e3, "p50_latency_ms": float(np.percentile(lat, 50)) * 1e3,
             "p99_latency_ms": float(np.percentile(lat, 99)) * 1e3, "block_size": bs, "grid": grid,
             "cluster_size": cluster, "clustered_instances": n_clustered, "cluster_block_size": bs_c,
-            "autotune_s": t_tune, "iterations_mean": float(np.mean(its)), "all_converged": ok}
+            "autotune_s": t_tune, "iterations_mean": float(np.mean(its)), "all_converged": ok,
+            "second_batch_object": {"tune_source": "cache" if second_source == 2 else "autotuned",
+                                    "first_solve_s": t_second, "solve_ms": t_second_solve * 1e3}}
 
 
 # ---------------------------------------------------------------------------
@@ -472,6 +498,28 @@ def setup_ctx(jfem, w, device, pinned=None):
     return ctx
 
 
+def timed_steps(ctx, u, opts, steps, stream, flush, torch):
+    """`steps` solves on the device, each bracketed by CUDA events on the
+    context stream, L2 flushed before each (256 MiB write)."""
+    times, iters, refin, res = [], [], [], []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st, rc = ctx.solve_device(u.data_ptr(), opts)
+        e1.record(stream)
+        e1.synchronize()
+        if rc != 0:
+            raise RuntimeError(f"solve did not converge: status {rc}, residual {st.residual}")
+        times.append(e0.elapsed_time(e1) / 1e3)
+        iters.append(st.cg_iterations)
+        refin.append(st.refinements)
+        res.append(st.residual)
+    return times, iters, refin, res
+
+
 def run_gpu(args):
     ws, rank, local = dist_setup("nccl")
     import torch
@@ -481,14 +529,19 @@ def run_gpu(args):
     jfem = jfem_loader.load_package()
     from jfem_gb300 import build as _b
     _b.build()
+    abi = jfem._abi
     nx, ny, nz = args.size
     w = jfem.workloads.cfg_tet10_cantilever(nx, ny, nz)
     m = w.mesh
     n = m.n_dofs
+    # the network is trained first, off the clock (a model trained once, used for many solves)
+    W, train_info = train_network(jfem, args, local)
     t_setup0 = time.perf_counter()
     ctx = setup_ctx(jfem, w, local)
+    ctx.set_coarse_space(-1)
+    ctx.mpnn_set_weights(W)
     t_setup = time.perf_counter() - t_setup0
-    opts = jfem.default_opts(method=jfem._abi.PCG_JACOBI, precision=jfem._abi.MIXED, tol=TOL, max_iter=500000)
+    opts = jfem.default_opts(method=abi.FCG_LEARNED, precision=abi.MIXED, tol=TOL, max_iter=500000)
     u = torch.empty(n, dtype=torch.float64, device=dev)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -500,24 +553,9 @@ def run_gpu(args):
     clocks = ClockSampler(local)
     clocks.start()
     launches0 = ctx.kernel_launches
-    times, iters, refin, res = [], [], [], []
     torch.cuda.synchronize()
     barrier(ws)
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        st, rc = ctx.solve_device(u.data_ptr(), opts)
-        e1.record(stream)
-        e1.synchronize()
-        times.append(e0.elapsed_time(e1) / 1e3)
-        iters.append(st.cg_iterations)
-        refin.append(st.refinements)
-        res.append(st.residual)
-        if rc != 0:
-            raise RuntimeError(f"solve did not converge: status {rc}, residual {st.residual}")
+    times, iters, refin, res = timed_steps(ctx, u, opts, args.steps, stream, flush, torch)
     torch.cuda.synchronize()
     barrier(ws)
     launches = ctx.kernel_launches - launches0
@@ -525,12 +563,26 @@ def run_gpu(args):
     u_headline = u.cpu().numpy()
     t_step = statistics.mean(times)
     t_step = max_over_ranks(ws, t_step, dev)
+    n_agg, n_coarse, n_celem, coarse_ms = ctx.coarse_info()
+
+    # the same GPU's Jacobi-PCG and the two-level method with the network zeroed, same timing
+    cmp_steps = max(1, min(args.steps, 3))
+    other = {}
+    for name, method in (("jacobi_pcg", abi.PCG_JACOBI), ("two_level_network_zeroed", abi.FCG_TWO_LEVEL)):
+        o = jfem.default_opts(method=method, precision=abi.MIXED, tol=TOL, max_iter=500000)
+        ctx.solve_device(u.data_ptr(), o)
+        tt, it, rf, rs = timed_steps(ctx, u, o, cmp_steps, stream, flush, torch)
+        other[name] = {"s": statistics.mean(tt), "iterations": int(statistics.median(it)),
+                       "refinements": int(statistics.median(rf)), "final_relative_residual": max(rs)}
 
     # matrix-free apply: per-kernel CUDA-event timing on the context stream
     ms_el, ms_ga = ctx.time_apply(reps=50, fp32=True, masked=True)
     t_apply = (ms_el + ms_ga) / 1e3
     nn = 10
-    alg_bytes = m.n_elem * (4 * nn + 44) + 16 * n      # conn + geometry records + v read + y write
+    # algorithmic bytes of one FP32 apply (precomputed-geometry representation):
+    # connectivity (4 B per element node) + affine records (11 floats per element)
+    # + the input direction (4 B per DOF) + the output (4 B per DOF)
+    alg_bytes = m.n_elem * (4 * nn + 44) + 8 * n
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / t_apply / 1e9
     # FP64 apply for the residual path, for reference
@@ -553,7 +605,8 @@ def run_gpu(args):
                 "written_bytes": int(written), "fp64_gflops": asm_flops / t_asm / 1e9,
                 "fp64_nominal_peak_gflops": 1250.0, "bound": "fp64 pipe", "precision": "FP64"}
 
-    # end to end through the C ABI from pinned host buffers
+    # end to end through the C ABI from pinned host buffers: a new context per
+    # step (mesh, material, loads, network weights uploaded; coarse level built)
     Xp = torch.from_numpy(np.ascontiguousarray(m.X)).pin_memory()
     Cp = torch.from_numpy(np.ascontiguousarray(m.conn)).pin_memory()
     e2e_times = []
@@ -563,14 +616,18 @@ def run_gpu(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         c2 = setup_ctx(jfem, w, local, pinned=(Xp.numpy(), Cp.numpy()))
+        c2.set_coarse_space(-1)
+        c2.mpnn_set_weights(W)
         uh, st2, rc2 = c2.solve(opts)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         c2.close()
+        if rc2 != 0:
+            raise RuntimeError(f"end-to-end solve did not converge: status {rc2}")
         if k > 0:                      # first round is a warm-up
             e2e_times.append(t1 - t0)
     h2d = m.X.nbytes + m.conn.nbytes + 16 + w.fixed_dofs.nbytes + w.fixed_values.nbytes + \
-        w.faces.nbytes + w.traction.nbytes
+        w.faces.nbytes + w.traction.nbytes + 4 * len(W)
     d2h = 8 * n
     e2e = max_over_ranks(ws, statistics.mean(e2e_times), dev)
 
@@ -578,9 +635,14 @@ def run_gpu(args):
         line = {"metric": METRIC, "value": t_step, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32-apply/f64-residual", "data": "synthetic",
-                "config": workload_config(args.size),
+                "config": workload_config(args.size), "solver": SOLVER_GPU,
                 "pcg_iterations": int(statistics.median(iters)), "refinements": int(statistics.median(refin)),
                 "final_relative_residual": max(res),
+                "coarse": {"aggregates": n_agg, "coarse_dofs": n_coarse, "elements_in_A_c": n_celem,
+                           "value_setup_ms": coarse_ms},
+                "same_gpu": other,
+                "speedup_vs_same_gpu_jacobi_pcg": other["jacobi_pcg"]["s"] / t_step,
+                "network_training": train_info,
                 "kxu_gdofs": n / t_apply / 1e9,
                 "apply_ms": {"element": ms_el, "gather": ms_ga, "fp64_element": ms_el64, "fp64_gather": ms_ga64},
                 "assembly": assembly,
@@ -597,7 +659,7 @@ def run_gpu(args):
         if ws == 1 and not args.no_batch:
             line["batched"] = batch_leg(jfem, args, local)
         if ws == 1 and not args.no_learned:
-            line["learned_preconditioner"] = learned_leg(jfem, args, local, w)
+            line["learned_preconditioner_family"] = family_eval(jfem, args, local, W)
         if ws == 1 and not args.no_oracle_full:
             line["oracle_full"] = oracle_full_leg(jfem, w, u_headline, local)
         if ws == 1 and not args.no_cpu_baseline:

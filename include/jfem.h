@@ -88,7 +88,8 @@ typedef struct jfem_solve_opts {
                              CG iterations); u then receives the best iterate found so far
                              (the last accepted Newton state for JFEM_NEWTON) and stats the
                              counts up to that point */
-  double refine_drop;     /* JFEM_MIXED: FP64 residual each time ‖r‖ drops by this factor (0 → 0.3) */
+  double refine_drop;     /* JFEM_MIXED: FP64 residual each time ‖r‖ drops by this factor (0 → 0.3
+                             for JFEM_PCG_JACOBI, 0.01 for the flexible-CG methods) */
   int tol_absolute;       /* 0: relative tests (default); 1: the reference's absolute ‖r‖ and ‖R‖ */
 } jfem_solve_opts;
 
@@ -303,6 +304,13 @@ int jfem_batch_solve(jfem_batch* batch, double tol, int max_iter, int block_size
  * the single-CTA launch, and the cluster launch of the largest instances
  * (cluster_size 1 and n_clustered 0 when there is none). */
 int jfem_batch_config(const jfem_batch* batch, int* block_size, int* grid);
+/* Where the autotuned configuration of the last block_size-0 solve came from:
+ * 0 none yet, 1 timed by this batch object, 2 the autotuner cache.  The cache
+ * is keyed by GPU name, element type and the batch shape (instance count,
+ * largest and mean instance DOFs, each rounded up to a power of two); it lives
+ * for the process and, when the environment variable JFEM_AUTOTUNE_CACHE names
+ * a file, is read from and written to that file (JSON, one entry per line). */
+int jfem_batch_tune_source(const jfem_batch* batch);
 int jfem_batch_cluster_config(const jfem_batch* batch, int* cluster_size, int* n_clustered, int* cluster_block);
 /* Fix the configuration jfem_batch_solve uses when its block_size is 0 (instead
  * of the autotuner): single-CTA block size, cluster size (1, 2, 4, 8), the

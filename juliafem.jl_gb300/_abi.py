@@ -110,6 +110,7 @@ SIGNATURES = {
     "jfem_batch_solve": (C.c_int, [_P, C.c_double, C.c_int, C.c_int, _f64p, C.POINTER(C.c_int),
                                    C.POINTER(C.c_int), _f64p, _f64p, _f64p]),
     "jfem_batch_config": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "jfem_batch_tune_source": (C.c_int, [_P]),
     "jfem_batch_cluster_config": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "jfem_batch_set_config": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int]),
     "jfem_rcm": (C.c_int, [_i64, _i64, C.c_int, _i64p, C.c_int, _i64, _i64p, _i64p, _i64p]),
@@ -446,6 +447,11 @@ class Batch:
         offs = np.concatenate([[0], np.cumsum(3 * np.asarray(self.node_counts))])
         us = [u[offs[k]:offs[k + 1]] for k in range(n)]
         return us, it, stv, res, lat, t.value
+
+    @property
+    def tune_source(self) -> int:
+        """0 none yet, 1 autotuned by this object, 2 taken from the autotuner cache."""
+        return int(self._lib.jfem_batch_tune_source(self._h))
 
     def config(self):
         bs, g = C.c_int(0), C.c_int(0)

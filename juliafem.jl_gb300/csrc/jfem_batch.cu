@@ -26,9 +26,14 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
-#include <numeric>
+#include <map>
+#include <mutex>
 #include <new>
+#include <numeric>
+#include <string>
 #include <vector>
 
 #include "jfem_apply_kernels.cuh"
@@ -437,6 +442,7 @@ struct BatchHost {
     int bs = 0, grid = 0;        // single-CTA launch over order[n_large..n_inst)
     int cluster = 1, bs_c = 0;   // cluster launch over order[0..n_large), C CTAs per instance
     int grid_c = 0, n_large = 0;
+    int per_sm = 1, frac = 0, per_sm_c = 1;   // how grid, n_large, grid_c were derived (autotuner cache)
     bool operator==(const Config& o) const {
       return bs == o.bs && grid == o.grid && cluster == o.cluster && bs_c == o.bs_c && grid_c == o.grid_c &&
              n_large == o.n_large;
@@ -445,6 +451,7 @@ struct BatchHost {
   Config graph_cfg, tuned;
   Config forced;                 // set by jfem_batch_set_config (bs 0: none)
   double tuned_ms = 0.0;
+  int tune_source = 0;           // 0 none, 1 autotuned in this object, 2 from the autotuner cache
   int64_t launches = 0;
 };
 
@@ -714,16 +721,124 @@ static int sm_count(int device) {
   return n > 0 ? n : 1;
 }
 
+// ---------------------------------------------------------------------------
+// autotuner cache: the configuration chosen for a (GPU, element type, batch
+// shape) is kept for the process and, when JFEM_AUTOTUNE_CACHE names a file,
+// in that file (JSON object, one entry per line) for later processes.  The
+// batch shape is bucketed to powers of two: instance count, largest and mean
+// instance DOFs.  Entries hold the configuration in relative form (CTAs per SM,
+// fraction on clusters), re-derived for the batch at hand.
+// ---------------------------------------------------------------------------
+struct TuneEntry {
+  int bs, per_sm, cluster, bs_c, frac, per_sm_c;
+  double ms;
+};
+static std::mutex g_tune_mu;
+static std::map<std::string, TuneEntry> g_tune;
+static bool g_tune_loaded = false;
+
+static int pow2_bucket(int64_t v) {
+  int k = 0;
+  while ((1LL << k) < v && k < 62) ++k;
+  return k;
+}
+
+static std::string tune_key(const BatchHost* b) {
+  cudaDeviceProp prop;
+  std::string name = cudaGetDeviceProperties(&prop, b->device) == cudaSuccess ? prop.name : "unknown";
+  for (char& ch : name)
+    if (ch == '"' || ch == '\\' || ch == '\n') ch = '_';
+  const int n = b->d.n_inst;
+  int64_t mx = 0, tot = 0;
+  for (int k = 0; k < n; ++k) {
+    const int64_t dofs = 3 * (b->node_off[(size_t)k + 1] - b->node_off[(size_t)k]);
+    mx = std::max(mx, dofs);
+    tot += dofs;
+  }
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "%s|tet4|n%d|max%d|mean%d", name.c_str(), pow2_bucket(n), pow2_bucket(mx),
+                pow2_bucket(n ? tot / n : 0));
+  return buf;
+}
+
+static void tune_cache_load_locked() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char* path = std::getenv("JFEM_AUTOTUNE_CACHE");
+  if (!path || !*path) return;
+  FILE* fp = std::fopen(path, "r");
+  if (!fp) return;
+  char line[1024];
+  while (std::fgets(line, sizeof line, fp)) {
+    char key[512];
+    TuneEntry e;
+    if (std::sscanf(line, " \"%511[^\"]\": {\"bs\": %d, \"per_sm\": %d, \"cluster\": %d, \"bs_c\": %d, "
+                          "\"frac\": %d, \"per_sm_c\": %d, \"ms\": %lf}",
+                    key, &e.bs, &e.per_sm, &e.cluster, &e.bs_c, &e.frac, &e.per_sm_c, &e.ms) == 8)
+      g_tune[key] = e;
+  }
+  std::fclose(fp);
+}
+
+static void tune_cache_store_locked() {
+  const char* path = std::getenv("JFEM_AUTOTUNE_CACHE");
+  if (!path || !*path) return;
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* fp = std::fopen(tmp.c_str(), "w");
+  if (!fp) return;
+  std::fprintf(fp, "{\n");
+  size_t k = 0;
+  for (const auto& kv : g_tune) {
+    const TuneEntry& e = kv.second;
+    std::fprintf(fp, "  \"%s\": {\"bs\": %d, \"per_sm\": %d, \"cluster\": %d, \"bs_c\": %d, \"frac\": %d, "
+                     "\"per_sm_c\": %d, \"ms\": %.6f}%s\n",
+                 kv.first.c_str(), e.bs, e.per_sm, e.cluster, e.bs_c, e.frac, e.per_sm_c, e.ms,
+                 ++k < g_tune.size() ? "," : "");
+  }
+  std::fprintf(fp, "}\n");
+  std::fclose(fp);
+  std::rename(tmp.c_str(), path);
+}
+
 // Times the whole batch for every candidate configuration and keeps the
 // fastest (ties to the earlier, simpler one): single-CTA teams for all
 // instances at block sizes 128–1024 and 1/2/4 CTAs per SM; then the largest
 // 1/8, 1/4 or 1/2 of the instances on clusters of 2, 4 or 8 CTAs (block 256 or
 // 512, one or two cluster CTAs per SM) running beside the rest on single CTAs
-// of the best size above.
+// of the best size above.  A configuration cached for the same GPU and batch
+// shape is taken instead when its cluster shape can be scheduled here.
 static int batch_autotune(BatchHost* b) {
   if (b->tuned.bs) return 0;
   const int sms = sm_count(b->device);
   const int n = b->d.n_inst;
+  const std::string key = tune_key(b);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_cache_load_locked();
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      const TuneEntry& e = it->second;
+      BatchHost::Config cf;
+      cf.bs = e.bs;
+      cf.per_sm = e.per_sm;
+      cf.grid = std::min(n, sms * e.per_sm);
+      const int nl = e.frac > 0 ? n / e.frac : 0;
+      if (e.cluster > 1 && nl >= 1) {
+        cf.cluster = e.cluster;
+        cf.bs_c = e.bs_c;
+        cf.frac = e.frac;
+        cf.per_sm_c = e.per_sm_c;
+        cf.n_large = nl;
+        cf.grid_c = std::min(nl, e.per_sm_c * sms / e.cluster) * e.cluster;
+      }
+      if (cf.bs && (cf.n_large == 0 || max_clusters_for(b, cf.bs_c, cf.cluster, cf.grid_c) >= 1)) {
+        b->tuned = cf;
+        b->tuned_ms = e.ms;
+        b->tune_source = 2;
+        return 0;
+      }
+    }
+  }
   float best = 1e30f;
   auto try_cfg = [&](const BatchHost::Config& cf) -> int {
     float ms = 0.f;
@@ -740,6 +855,7 @@ static int batch_autotune(BatchHost* b) {
       if (bs * k > 2048) continue;
       BatchHost::Config cf;
       cf.bs = bs;
+      cf.per_sm = k;
       cf.grid = std::min(n, sms * k);
       if (int rc = try_cfg(cf)) return rc;
     }
@@ -754,6 +870,8 @@ static int batch_autotune(BatchHost* b) {
           cf.cluster = C;
           cf.bs_c = bs_c;
           cf.n_large = nl;
+          cf.frac = frac;
+          cf.per_sm_c = per_sm;
           cf.grid_c = std::min(nl, per_sm * sms / C) * C;
           if (max_clusters_for(b, bs_c, C, cf.grid_c) < 1) continue;   // shape not schedulable here
           if (try_cfg(cf)) {   // a cluster shape the launch refused: keep the configurations that ran
@@ -762,6 +880,14 @@ static int batch_autotune(BatchHost* b) {
           }
         }
   b->tuned_ms = best;
+  b->tune_source = 1;
+  {
+    const BatchHost::Config& t = b->tuned;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = TuneEntry{t.bs, t.per_sm, t.n_large > 0 ? t.cluster : 1, t.n_large > 0 ? t.bs_c : 0,
+                            t.n_large > 0 ? t.frac : 0, t.n_large > 0 ? t.per_sm_c : 1, (double)best};
+    tune_cache_store_locked();
+  }
   return 0;
 }
 
@@ -933,6 +1059,8 @@ int jfem_batch_solve(jfem_batch* h, double tol, int max_iter, int block_size, do
   if (solve_s) *solve_s = ms * 1e-3;
   return JFEM_OK;
 }
+
+int jfem_batch_tune_source(const jfem_batch* h) { return h ? h->b.tune_source : JFEM_ERR_INVALID; }
 
 int jfem_batch_config(const jfem_batch* h, int* block_size, int* grid) {
   if (!h) return JFEM_ERR_INVALID;

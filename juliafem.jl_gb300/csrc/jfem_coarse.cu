@@ -42,6 +42,7 @@
 #include <vector>
 
 #include "jfem_common.cuh"
+#include "jfem_df.cuh"
 
 namespace jfem {
 
@@ -292,43 +293,54 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 // Rc[6a + k] = Σ_{i ∈ a} φ_k(d_i) · r_i: force (k < 3) and moment (k ≥ 3) resultants
-// of r about the centroid.  r is zero on prescribed DOFs.  FP32 per thread, FP64
-// across threads, fixed order.
-__global__ void __launch_bounds__(256) k_coarse_restrict(int nagg, const int* __restrict__ agg_ptr,
+// of r about the centroid.  r is zero on prescribed DOFs.  Each aggregate's node
+// list is cut into chunks of at most CR_CHUNK nodes, one CTA per chunk (FP32 per
+// thread, FP64 across the CTA); the last CTA to finish sums each aggregate's
+// chunk partials in chunk order (deterministic) and re-arms the counter.
+#define CR_CHUNK 1024
+__global__ void __launch_bounds__(256) k_coarse_restrict(int n_chunks, const int* __restrict__ chunk_begin,
                                                          const int* __restrict__ agg_nodes,
                                                          const float4* __restrict__ d32,
-                                                         const float2* __restrict__ r, const int* __restrict__ stop,
-                                                         float* __restrict__ Rc) {
+                                                         const float2* __restrict__ r, int nagg,
+                                                         const int* __restrict__ agg_chunk_ptr,
+                                                         const int* __restrict__ stop, double* __restrict__ cpart,
+                                                         unsigned* __restrict__ counter, float* __restrict__ Rc) {
   __shared__ double sh[8][6];
   if (stop && *stop) return;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int a = blockIdx.x; a < nagg; a += gridDim.x) {
-    float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int t = agg_ptr[a] + threadIdx.x; t < agg_ptr[a + 1]; t += blockDim.x) {
-      const int64_t i = agg_nodes[t];
-      const float2 r0 = r[3 * i], r1 = r[3 * i + 1], r2 = r[3 * i + 2];
-      const float rx = r0.x + r0.y, ry = r1.x + r1.y, rz = r2.x + r2.y;
-      const float4 d = d32[i];
-      s[0] += rx;
-      s[1] += ry;
-      s[2] += rz;
-      s[3] = fmaf(d.y, rz, fmaf(-d.z, ry, s[3]));
-      s[4] = fmaf(d.z, rx, fmaf(-d.x, rz, s[4]));
-      s[5] = fmaf(d.x, ry, fmaf(-d.y, rx, s[5]));
-    }
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      const double v = warp_sum_d((double)s[k]);
-      if (lane == 0) sh[wid][k] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < 6) {
-      double v = 0.0;
-      for (int q = 0; q < nw; ++q) v += sh[q][threadIdx.x];
-      Rc[6 * a + threadIdx.x] = (float)v;
-    }
-    __syncthreads();
+  const int ch = blockIdx.x;
+  float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int t = chunk_begin[ch] + threadIdx.x; t < chunk_begin[ch + 1]; t += blockDim.x) {
+    const int64_t i = agg_nodes[t];
+    const float2 r0 = r[3 * i], r1 = r[3 * i + 1], r2 = r[3 * i + 2];
+    const float rx = r0.x + r0.y, ry = r1.x + r1.y, rz = r2.x + r2.y;
+    const float4 d = d32[i];
+    s[0] += rx;
+    s[1] += ry;
+    s[2] += rz;
+    s[3] = fmaf(d.y, rz, fmaf(-d.z, ry, s[3]));
+    s[4] = fmaf(d.z, rx, fmaf(-d.x, rz, s[4]));
+    s[5] = fmaf(d.x, ry, fmaf(-d.y, rx, s[5]));
   }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const double v = warp_sum_d((double)s[k]);
+    if (lane == 0) sh[wid][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = 0.0;
+    for (int q = 0; q < nw; ++q) v += sh[q][threadIdx.x];
+    cpart[6 * (int64_t)ch + threadIdx.x] = v;
+  }
+  if (!arrive_last(counter)) return;
+  for (int t = threadIdx.x; t < 6 * nagg; t += blockDim.x) {
+    const int a = t / 6, k = t % 6;
+    double v = 0.0;
+    for (int q = agg_chunk_ptr[a]; q < agg_chunk_ptr[a + 1]; ++q) v += __ldcg(cpart + 6 * (int64_t)q + k);
+    Rc[t] = (float)v;
+  }
+  if (threadIdx.x == 0) *counter = 0u;
 }
 
 // Ec = A_c⁻¹ Rc (FP32, one warp per row, rows 16-byte aligned: ld is a multiple of 32)
@@ -447,6 +459,14 @@ static int coarse_build(Ctx* c, int target_nc) {
     std::vector<int> cur(agg_ptr.begin(), agg_ptr.end() - 1);
     for (int64_t i = 0; i < N; ++i) agg_nodes[(size_t)cur[(size_t)node_agg[(size_t)i]]++] = (int)i;
   }
+  // restriction chunks: each aggregate's node list cut into pieces of ≤ CR_CHUNK
+  std::vector<int> chunk_begin, agg_chunk_ptr(1, 0);
+  for (int a = 0; a < nagg; ++a) {
+    for (int t = agg_ptr[(size_t)a]; t < agg_ptr[(size_t)a + 1]; t += CR_CHUNK) chunk_begin.push_back(t);
+    agg_chunk_ptr.push_back((int)chunk_begin.size());
+  }
+  const int n_chunks = (int)chunk_begin.size();
+  chunk_begin.push_back((int)N);
   std::vector<double> cen((size_t)3 * nagg, 0.0);
   for (int a = 0; a < nagg; ++a) {
     double s[3] = {0, 0, 0};
@@ -526,7 +546,7 @@ static int coarse_build(Ctx* c, int target_nc) {
   }
   void* old[] = {c->agg_ptr, c->agg_nodes, c->node_agg, c->node_d32, c->node_d64, c->celem, c->celem_aggs,
                  c->celem_off, c->contrib, c->cblk_ab, c->cblk_ptr, c->cblk_src, c->Ac, c->Ac_diag, c->gj_buf,
-                 c->Ainv32, c->Rc, c->Ec};
+                 c->Ainv32, c->Rc, c->Ec, c->chunk_begin, c->agg_chunk_ptr, c->cpart, c->ccounter};
   for (void* p : old) dfree(c, p);
   c->nagg = nagg;
   c->nc = nc;
@@ -535,6 +555,7 @@ static int coarse_build(Ctx* c, int target_nc) {
   c->n_celem = n_celem;
   c->n_contrib = n_contrib;
   c->n_cblk = n_cblk;
+  c->n_chunks = n_chunks;
   if ((rc = dalloc(c, &c->agg_ptr, (size_t)nagg + 1)) || (rc = dalloc(c, &c->agg_nodes, (size_t)N)) ||
       (rc = dalloc(c, &c->node_agg, (size_t)N)) || (rc = dalloc(c, &c->node_d32, (size_t)N)) ||
       (rc = dalloc(c, &c->node_d64, (size_t)(3 * N))) || (rc = dalloc(c, &c->celem, (size_t)n_celem)) ||
@@ -542,7 +563,9 @@ static int coarse_build(Ctx* c, int target_nc) {
       (rc = dalloc(c, &c->celem_off, (size_t)n_celem)) || (rc = dalloc(c, &c->contrib, (size_t)n_contrib * 36)) ||
       (rc = dalloc(c, &c->cblk_ab, (size_t)(2 * n_cblk))) || (rc = dalloc(c, &c->cblk_ptr, (size_t)n_cblk + 1)) ||
       (rc = dalloc(c, &c->cblk_src, cblk_src.size())) || (rc = dalloc(c, &c->Ac, (size_t)nc_pad * nc_pad)) ||
-      (rc = dalloc(c, &c->Ac_diag, (size_t)nc_pad)) ||
+      (rc = dalloc(c, &c->Ac_diag, (size_t)nc_pad)) || (rc = dalloc(c, &c->chunk_begin, (size_t)n_chunks + 1)) ||
+      (rc = dalloc(c, &c->agg_chunk_ptr, (size_t)nagg + 1)) || (rc = dalloc(c, &c->cpart, (size_t)6 * n_chunks)) ||
+      (rc = dalloc(c, &c->ccounter, 1)) ||
       (rc = dalloc(c, &c->gj_buf, (size_t)GJ_B * GJ_B + 2 * (size_t)GJ_B * nc_pad)) ||
       (rc = dalloc(c, &c->Ainv32, (size_t)nc_pad * nc_pad)) || (rc = dalloc(c, &c->Rc, (size_t)nc_pad)) ||
       (rc = dalloc(c, &c->Ec, (size_t)nc_pad)))
@@ -561,6 +584,9 @@ static int coarse_build(Ctx* c, int target_nc) {
   up(c->cblk_ab, cblk_ab.data(), cblk_ab.size() * sizeof(int));
   up(c->cblk_ptr, cblk_ptr.data(), cblk_ptr.size() * sizeof(int));
   up(c->cblk_src, cblk_src.data(), cblk_src.size() * sizeof(int64_t));
+  up(c->chunk_begin, chunk_begin.data(), chunk_begin.size() * sizeof(int));
+  up(c->agg_chunk_ptr, agg_chunk_ptr.data(), agg_chunk_ptr.size() * sizeof(int));
+  cudaMemsetAsync(c->ccounter, 0, sizeof(unsigned), c->stream);
   cudaMemsetAsync(c->Rc, 0, (size_t)nc_pad * sizeof(float), c->stream);   // padding stays zero
   cudaMemsetAsync(c->Ec, 0, (size_t)nc_pad * sizeof(float), c->stream);
   if ((rc = sync_and_check(c, "coarse set-up upload"))) return rc;
@@ -649,8 +675,9 @@ int coarse_prepare(Ctx* c) {
 }
 
 void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop) {
-  k_coarse_restrict<<<std::min(c->nagg, 152 * 8), 256, 0, c->stream>>>(c->nagg, c->agg_ptr, c->agg_nodes,
-                                                                      c->node_d32, r, stop, c->Rc);
+  k_coarse_restrict<<<c->n_chunks, 256, 0, c->stream>>>(c->n_chunks, c->chunk_begin, c->agg_nodes, c->node_d32, r,
+                                                        c->nagg, c->agg_chunk_ptr, stop, c->cpart, c->ccounter,
+                                                        c->Rc);
   k_coarse_gemv<<<(c->nc + 7) / 8, 256, 0, c->stream>>>(c->nc, c->nc_pad, c->Ainv32, c->Rc, stop, c->Ec);
   c->launches += 2;
 }

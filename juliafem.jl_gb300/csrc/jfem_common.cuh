@@ -411,6 +411,11 @@ struct Ctx {
   double* Ac_diag = nullptr;    // [nc_pad] diagonal of A_c before the inversion
   double* gj_buf = nullptr;     // Gauss–Jordan panels: P (32×32), row panel, old column panel
   float* Ainv32 = nullptr;      // [nc_pad][nc_pad] A_c⁻¹ rounded to FP32 (the per-iteration coarse solve)
+  int n_chunks = 0;             // restriction chunks (≤ 1,024 nodes of one aggregate each)
+  int* chunk_begin = nullptr;   // [n_chunks+1] into agg_nodes
+  int* agg_chunk_ptr = nullptr; // [nagg+1] chunks of each aggregate
+  double* cpart = nullptr;      // [n_chunks][6] chunk partial resultants
+  unsigned* ccounter = nullptr; // last-block counter of the restriction (returns to 0)
   float* Rc = nullptr;          // [nc_pad] restricted residual Pᵀ r
   float* Ec = nullptr;          // [nc_pad] coarse correction A_c⁻¹ Pᵀ r
   double coarse_setup_ms = 0.0; // last coarse value setup (CUDA events)

@@ -488,8 +488,39 @@ __device__ __forceinline__ void mat3_acc(const float* __restrict__ C, bool trans
     for (int b = 0; b < 3; ++b) y[a] = fmaf(transpose ? C[3 * b + a] : C[3 * a + b], x[b], y[a]);
 }
 
-// out = A in  (FORWARD_LAST = false), or, for the last forward step,
-// u = mask ⊙ (C0 y + C1 a1 + C2 a2 + C3 A a2) and h = C3ᵀ u
+// The neighbour sums of the inference kernels: an 8-lane group per node strides
+// over the node's row of the graph (coalesced index reads, 3-channel gathers
+// that mostly hit L2) and reduces by a fixed xor-shuffle tree, so every run
+// gives the same bits.  The group's lanes share the node, so the group mask is
+// uniform wherever the loop condition is.
+#define MP_GL 8
+__device__ __forceinline__ unsigned group_mask() { return 0xffu << (threadIdx.x & 24); }
+
+template <bool WEIGHTED>
+__device__ __forceinline__ void group_neighbour_sum(const int* __restrict__ nb_ptr, const int* __restrict__ nbr,
+                                                    const float* __restrict__ invdeg, const float* __restrict__ in,
+                                                    int64_t i, int g, float s[3]) {
+  s[0] = s[1] = s[2] = 0.f;
+  const int j0 = __ldg(nb_ptr + i), j1 = __ldg(nb_ptr + i + 1);
+  for (int jj = j0 + g; jj < j1; jj += MP_GL) {
+    const int64_t j = __ldg(nbr + jj);
+    if (j == i) continue;
+    const float w = WEIGHTED ? __ldg(invdeg + j) : 1.f;
+    s[0] = fmaf(w, __ldg(in + 3 * j), s[0]);
+    s[1] = fmaf(w, __ldg(in + 3 * j + 1), s[1]);
+    s[2] = fmaf(w, __ldg(in + 3 * j + 2), s[2]);
+  }
+  const unsigned gm = group_mask();
+#pragma unroll
+  for (int o = MP_GL / 2; o > 0; o >>= 1) {
+    s[0] += __shfl_xor_sync(gm, s[0], o, MP_GL);
+    s[1] += __shfl_xor_sync(gm, s[1], o, MP_GL);
+    s[2] += __shfl_xor_sync(gm, s[2], o, MP_GL);
+  }
+}
+
+// a = A in (neighbour mean); LAST: also u = mask ⊙ Σ_k C_k A^k y (with y, a1 = A y,
+// in = A² y, a = A³ y) and h = C_3ᵀ u, the first Horner term of the adjoint
 template <bool LAST>
 __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __restrict__ nb_ptr,
                                                      const int* __restrict__ nbr, const float* __restrict__ invdeg,
@@ -500,16 +531,13 @@ __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __res
   __shared__ float C[36];
   if (threadIdx.x < 36) C[threadIdx.x] = poly[threadIdx.x];
   __syncthreads();
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-    float s[3] = {0.f, 0.f, 0.f};
-    const int j0 = __ldg(nb_ptr + i), j1 = __ldg(nb_ptr + i + 1);
-    for (int jj = j0; jj < j1; ++jj) {
-      const int64_t j = __ldg(nbr + jj);
-      if (j == i) continue;
-      s[0] += __ldg(in + 3 * j);
-      s[1] += __ldg(in + 3 * j + 1);
-      s[2] += __ldg(in + 3 * j + 2);
-    }
+  const int g = threadIdx.x & (MP_GL - 1);
+  const int64_t g0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / MP_GL;
+  const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
+  for (int64_t i = g0; i < N; i += gs) {
+    float s[3];
+    group_neighbour_sum<false>(nb_ptr, nbr, invdeg, in, i, g, s);
+    if (g != 0) continue;
     const float id = __ldg(invdeg + i);
     float a[3] = {s[0] * id, s[1] * id, s[2] * id};
     if (!LAST) {
@@ -547,17 +575,13 @@ __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __res
   __shared__ float C[9];
   if (threadIdx.x < 9) C[threadIdx.x] = poly[9 * k + threadIdx.x];
   __syncthreads();
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-    float s[3] = {0.f, 0.f, 0.f};
-    const int j0 = __ldg(nb_ptr + i), j1 = __ldg(nb_ptr + i + 1);
-    for (int jj = j0; jj < j1; ++jj) {
-      const int64_t j = __ldg(nbr + jj);
-      if (j == i) continue;
-      const float w = __ldg(invdeg + j);
-      s[0] = fmaf(w, __ldg(g + 3 * j), s[0]);
-      s[1] = fmaf(w, __ldg(g + 3 * j + 1), s[1]);
-      s[2] = fmaf(w, __ldg(g + 3 * j + 2), s[2]);
-    }
+  const int gl = threadIdx.x & (MP_GL - 1);
+  const int64_t g0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / MP_GL;
+  const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
+  for (int64_t i = g0; i < N; i += gs) {
+    float s[3];
+    group_neighbour_sum<true>(nb_ptr, nbr, invdeg, g, i, gl, s);
+    if (gl != 0) continue;
     const float uv[3] = {u[3 * i], u[3 * i + 1], u[3 * i + 2]};
     mat3_acc(C, true, uv, s);
     out[3 * i] = s[0];
@@ -824,7 +848,7 @@ int mpnn_refresh_poly(Ctx* c) {
 void enqueue_mpnn_spd(Ctx* c, const float* y, float* v) {
   const MpBufs& b = c->mb;
   const float* P = c->mp->poly;
-  const unsigned g = grid_for(c->N, 256);
+  const unsigned g = grid_for(c->N * MP_GL, 256);
   float *a1 = b.t3a, *a2 = b.t3b, *u = b.u, *h = b.w, *g2 = b.ghat;
   k_mp_poly_fwd<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, y, nullptr, nullptr, P, c->mask,
                                                   a1, nullptr);

@@ -16,6 +16,13 @@ Run from the repository root:  python tests/golden/make_golden.py
   [0,4]×[0,0.4]² (19,683 DOFs).
 * hex8_neohookean_small.npz — load-stepped Newton (oracle, FP64, direct
   solves) on a 4×4×4 Hex8 Neo-Hookean cube, top u_z = −0.1 over 5 steps.
+* hex8_neohookean_16.npz — the Newton–Krylov configuration at a
+  representative size: 16³ Hex8 Neo-Hookean cube, per-element lognormal E
+  (σ_log 0.2), top u_z = −0.1 over 10 load steps, oracle Newton to 1e-11
+  (about a minute of direct solves, hence a fixture rather than a test-time
+  oracle run).
+
+`python tests/golden/make_golden.py hex8_16` writes only the last one.
 
 The oracle is the restatement in oracle/jfem_oracle.cpp, cross-checked against
 oracle/np_oracle.py before anything is written.
@@ -69,10 +76,23 @@ def linear_case(w, samples=4096):
                 pcg_iters_1e12=it)
 
 
+def newton_16(jfem):
+    w = jfem.workloads.cube_compression(n=16, steps=10, top_uz=-0.1)
+    m = w.mesh
+    u, its = oracle.newton(m.elem_type, m.X, m.conn, w.E, w.nu, w.fixed_mask().astype(bool), w.prescribed(),
+                           n_steps=10, tol=1e-11, max_newton=25, model=1)
+    np.savez_compressed(OUT / "hex8_neohookean_16.npz", u=u, newton_its=np.array(its), E=w.E)
+
+
 def main():
     jfem = jfem_loader.load_package()
     wl = jfem.workloads
     oracle.build()
+    if sys.argv[1:] == ["hex8_16"]:
+        newton_16(jfem)
+        print("golden fixture written to", OUT)
+        return
+    newton_16(jfem)
     # Tet4 cantilever
     w1 = wl.cfg_tet4_cantilever()
     np.savez_compressed(OUT / "tet4_cantilever.npz", **linear_case(w1))

@@ -90,3 +90,44 @@ def test_batch_rejects_invalid_instances(jfem):
             b.add(m.X, m.conn, -1.0, w.nu, w.fixed_dofs, w.faces, w.traction)
         with pytest.raises(jfem.JFEMError):
             b.solve()                    # nothing added
+
+
+def test_cluster_teams_large_instances_against_oracle(jfem, orc):
+    """The largest instances of the batched configuration (28..32 cubes along
+    x, up to 8,019 DOFs), the half that the autotuner puts on thread-block
+    clusters, solved on 4-CTA clusters to 1e-10: every displacement within 1e-8
+    of the oracle's direct solve (not only of the single-CTA teams)."""
+    ws = jfem.workloads.batch_instances(count=6, nmin=28, nmax=32, seed_item=81)
+    with jfem.Batch(0) as b:
+        for w in ws:
+            b.add_workload(w)
+        b.set_config(256, 4, 3, 256)
+        us, it, st, res, lat, t = b.solve(tol=1e-10, max_iter=100000)
+        assert b.cluster_config() == (4, 3, 256)
+    assert np.all(st == 0) and np.all(res <= 1e-10)
+    for w, u in zip(ws, us):
+        assert rel_err(u, _oracle_u(orc, w)) <= 1e-8
+
+
+def test_autotuner_cache_reused_by_a_new_batch(jfem, tmp_path, monkeypatch):
+    """The autotuned configuration is cached by (GPU, element type, batch
+    shape): a second batch object of the same shape takes it without timing
+    candidates (tune source 2, same configuration, same bits), and the cache
+    file named by JFEM_AUTOTUNE_CACHE holds the entry as JSON."""
+    import json
+    cache = tmp_path / "autotune.json"
+    monkeypatch.setenv("JFEM_AUTOTUNE_CACHE", str(cache))
+    ws = jfem.workloads.batch_instances(count=9, nmin=8, nmax=11, seed_item=82)
+    runs = []
+    for _ in range(2):
+        with jfem.Batch(0) as b:
+            for w in ws:
+                b.add_workload(w)
+            us, it, st, *_ = b.solve(tol=1e-9, max_iter=50000, block_size=0)
+            runs.append((b.tune_source, b.config(), b.cluster_config(), us, it))
+    assert runs[0][0] in (1, 2) and runs[1][0] == 2
+    assert runs[0][1:3] == runs[1][1:3]
+    assert all(np.array_equal(a, c) for a, c in zip(runs[0][3], runs[1][3]))
+    if runs[0][0] == 1:
+        entries = json.loads(cache.read_text())
+        assert len(entries) >= 1 and all("bs" in e and "ms" in e for e in entries.values())

@@ -184,3 +184,22 @@ def test_absolute_tolerance_mode(jfem, gpu_ctx_factory):
     assert rc1 == rc2 == rc3 == 0
     assert st_rel.residual <= 1e-9 and st_abs.residual * fn <= 1e-9 * fn
     assert st_abs2.residual <= 1e-10 and st_abs2.cg_iterations >= st_abs.cg_iterations
+
+
+def test_newton_neo_hookean_cube_16_against_oracle(jfem, orc, gpu_ctx_factory):
+    """The Newton–Krylov configuration at a representative size: Hex8
+    Neo-Hookean unit cube of 16³ cells (14,739 DOFs), per-element lognormal E
+    (σ_log 0.2, seeded), ν = 0.3, bottom clamped, top u_z ramped to −0.1 over
+    10 load steps.  The GPU's mixed-precision Newton–Krylov (FP32 tangent
+    apply, FP64 residuals) against the oracle's FP64 Newton with consistent
+    tangents and direct solves (src/solvers.jl:575-620), stored in
+    tests/golden/hex8_neohookean_16.npz by tests/golden/make_golden.py:
+    u within 1e-8."""
+    w = jfem.workloads.cube_compression(n=16, steps=10, top_uz=-0.1)
+    d = np.load(GOLDEN / "hex8_neohookean_16.npz")
+    assert np.array_equal(d["E"], w.E)
+    with gpu_ctx_factory(w) as ctx:
+        u, st, rc = ctx.solve(method=2, precision=1, tol=1e-10, newton_tol=1e-10, max_newton=30,
+                              max_cg_per_newton=20000, n_load_steps=10, max_iter=200000)
+    assert rc == 0 and st.newton_iterations >= 10
+    assert rel_err(u, d["u"]) <= 1e-8
