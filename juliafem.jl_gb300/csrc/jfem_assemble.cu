@@ -692,7 +692,13 @@ __global__ void k_invert_diag(int64_t N, const uint8_t* __restrict__ mask, doubl
   }
 }
 
+// D⁻¹ of the (masked) operator at the current state.  Into c->dinv it is kept
+// until the state generation (geometry, material, formulation, u) or the
+// Dirichlet mask changes: a linear solve then reuses it instead of repeating the
+// FP64 element pass.
 int jacobi_diag_device(Ctx* c, double* dinv_d) {
+  const bool cached = dinv_d == c->dinv;
+  if (cached && c->diag_state_version == c->state_version && c->diag_mask_gen == c->mask_gen) return 0;
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
   const int use_u = c->have_state ? 1 : 0;
   const unsigned g = grid_for(c->E, 128);
@@ -718,6 +724,10 @@ int jacobi_diag_device(Ctx* c, double* dinv_d) {
   if (rc) return rc;
   if (h_err == JFEM_ERR_NEG_JACOBIAN) return set_err(c, h_err, "element with non-positive Jacobian determinant");
   if (h_err) return set_err(c, h_err, "non-positive or non-finite diagonal entry (unconstrained or degenerate DOF)");
+  if (cached) {
+    c->diag_state_version = c->state_version;
+    c->diag_mask_gen = c->mask_gen;
+  }
   return 0;
 }
 

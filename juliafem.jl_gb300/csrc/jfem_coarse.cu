@@ -33,16 +33,16 @@
 //                    (diagonal pivots, 32×32 blocks; a pivot below 1e-12 of
 //                    its original diagonal drops that mode);
 // the inverse is rounded to FP32 for the per-iteration coarse solve.
-// Per CG iteration: k_coarse_restrict (one CTA per aggregate: force and moment
-// resultants of r about c_a), k_coarse_gemv (Ec = A_c⁻¹ Rc, one warp per row);
-// the prolongation P Ec is fused into the kernel that forms z.
+// Per CG iteration: k_coarse_restrict (one CTA per chunk of an aggregate's
+// nodes: partial force and moment resultants of r about c_a), k_coarse_gemv
+// (Ec = A_c⁻¹ Pᵀ r from the chunk partials, one warp per row); the
+// prolongation P Ec is fused into the kernel that forms z.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "jfem_common.cuh"
-#include "jfem_df.cuh"
 
 namespace jfem {
 
@@ -292,19 +292,17 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
-// Rc[6a + k] = Σ_{i ∈ a} φ_k(d_i) · r_i: force (k < 3) and moment (k ≥ 3) resultants
-// of r about the centroid.  r is zero on prescribed DOFs.  Each aggregate's node
-// list is cut into chunks of at most CR_CHUNK nodes, one CTA per chunk (FP32 per
-// thread, FP64 across the CTA); the last CTA to finish sums each aggregate's
-// chunk partials in chunk order (deterministic) and re-arms the counter.
+// Restriction Pᵀ r: for aggregate a, Σ_{i ∈ a} φ_k(d_i) · r_i — force (k < 3) and
+// moment (k ≥ 3) resultants of r about the centroid (r is zero on prescribed
+// DOFs).  Each aggregate's node list is cut into chunks of at most CR_CHUNK
+// nodes, one CTA per chunk (FP32 per thread, FP64 across the CTA, fixed order);
+// the chunk partials go to cpart[chunk][6] and the coarse solve sums them.
 #define CR_CHUNK 1024
 __global__ void __launch_bounds__(256) k_coarse_restrict(int n_chunks, const int* __restrict__ chunk_begin,
                                                          const int* __restrict__ agg_nodes,
                                                          const float4* __restrict__ d32,
-                                                         const float2* __restrict__ r, int nagg,
-                                                         const int* __restrict__ agg_chunk_ptr,
-                                                         const int* __restrict__ stop, double* __restrict__ cpart,
-                                                         unsigned* __restrict__ counter, float* __restrict__ Rc) {
+                                                         const float2* __restrict__ r, const int* __restrict__ stop,
+                                                         float* __restrict__ cpart) {
   __shared__ double sh[8][6];
   if (stop && *stop) return;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -331,35 +329,29 @@ __global__ void __launch_bounds__(256) k_coarse_restrict(int n_chunks, const int
   if (threadIdx.x < 6) {
     double v = 0.0;
     for (int q = 0; q < nw; ++q) v += sh[q][threadIdx.x];
-    cpart[6 * (int64_t)ch + threadIdx.x] = v;
+    cpart[6 * ch + threadIdx.x] = (float)v;
   }
-  if (!arrive_last(counter)) return;
-  for (int t = threadIdx.x; t < 6 * nagg; t += blockDim.x) {
-    const int a = t / 6, k = t % 6;
-    double v = 0.0;
-    for (int q = agg_chunk_ptr[a]; q < agg_chunk_ptr[a + 1]; ++q) v += __ldcg(cpart + 6 * (int64_t)q + k);
-    Rc[t] = (float)v;
-  }
-  if (threadIdx.x == 0) *counter = 0u;
 }
 
-// Ec = A_c⁻¹ Rc (FP32, one warp per row, rows 16-byte aligned: ld is a multiple of 32)
+// Ec = A_c⁻¹ Pᵀ r = Σ_chunks A_c⁻¹[:, 6·agg(chunk) + k] · cpart[chunk][k]: the coarse
+// solve reads the chunk partials directly (A_c⁻¹ with its columns repeated per
+// chunk), so no kernel has to wait for a serial sum.  FP32, one warp per row,
+// lanes over chunks, fixed shuffle tree.
 __global__ void __launch_bounds__(256) k_coarse_gemv(int nc, int ld, const float* __restrict__ Ainv,
-                                                     const float* __restrict__ Rc, const int* __restrict__ stop,
+                                                     int n_chunks, const int* __restrict__ chunk_agg,
+                                                     const float* __restrict__ cpart, const int* __restrict__ stop,
                                                      float* __restrict__ Ec) {
   if (stop && *stop) return;
   const int lane = threadIdx.x & 31;
   const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (row >= nc) return;
-  const float4* a = reinterpret_cast<const float4*>(Ainv + (int64_t)row * ld);
-  const float4* x = reinterpret_cast<const float4*>(Rc);
+  const float* a = Ainv + (int64_t)row * ld;
   float s = 0.f;
-  for (int j = lane; j < ld / 4; j += 32) {
-    const float4 av = a[j], xv = x[j];
-    s = fmaf(av.x, xv.x, s);
-    s = fmaf(av.y, xv.y, s);
-    s = fmaf(av.z, xv.z, s);
-    s = fmaf(av.w, xv.w, s);
+  for (int ch = lane; ch < n_chunks; ch += 32) {
+    const float* ac = a + 6 * chunk_agg[ch];
+    const float* pc = cpart + 6 * ch;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s = fmaf(ac[k], pc[k], s);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -460,11 +452,12 @@ static int coarse_build(Ctx* c, int target_nc) {
     for (int64_t i = 0; i < N; ++i) agg_nodes[(size_t)cur[(size_t)node_agg[(size_t)i]]++] = (int)i;
   }
   // restriction chunks: each aggregate's node list cut into pieces of ≤ CR_CHUNK
-  std::vector<int> chunk_begin, agg_chunk_ptr(1, 0);
-  for (int a = 0; a < nagg; ++a) {
-    for (int t = agg_ptr[(size_t)a]; t < agg_ptr[(size_t)a + 1]; t += CR_CHUNK) chunk_begin.push_back(t);
-    agg_chunk_ptr.push_back((int)chunk_begin.size());
-  }
+  std::vector<int> chunk_begin, chunk_agg;
+  for (int a = 0; a < nagg; ++a)
+    for (int t = agg_ptr[(size_t)a]; t < agg_ptr[(size_t)a + 1]; t += CR_CHUNK) {
+      chunk_begin.push_back(t);
+      chunk_agg.push_back(a);
+    }
   const int n_chunks = (int)chunk_begin.size();
   chunk_begin.push_back((int)N);
   std::vector<double> cen((size_t)3 * nagg, 0.0);
@@ -546,7 +539,7 @@ static int coarse_build(Ctx* c, int target_nc) {
   }
   void* old[] = {c->agg_ptr, c->agg_nodes, c->node_agg, c->node_d32, c->node_d64, c->celem, c->celem_aggs,
                  c->celem_off, c->contrib, c->cblk_ab, c->cblk_ptr, c->cblk_src, c->Ac, c->Ac_diag, c->gj_buf,
-                 c->Ainv32, c->Rc, c->Ec, c->chunk_begin, c->agg_chunk_ptr, c->cpart, c->ccounter};
+                 c->Ainv32, c->Ec, c->chunk_begin, c->chunk_agg, c->cpart};
   for (void* p : old) dfree(c, p);
   c->nagg = nagg;
   c->nc = nc;
@@ -564,11 +557,9 @@ static int coarse_build(Ctx* c, int target_nc) {
       (rc = dalloc(c, &c->cblk_ab, (size_t)(2 * n_cblk))) || (rc = dalloc(c, &c->cblk_ptr, (size_t)n_cblk + 1)) ||
       (rc = dalloc(c, &c->cblk_src, cblk_src.size())) || (rc = dalloc(c, &c->Ac, (size_t)nc_pad * nc_pad)) ||
       (rc = dalloc(c, &c->Ac_diag, (size_t)nc_pad)) || (rc = dalloc(c, &c->chunk_begin, (size_t)n_chunks + 1)) ||
-      (rc = dalloc(c, &c->agg_chunk_ptr, (size_t)nagg + 1)) || (rc = dalloc(c, &c->cpart, (size_t)6 * n_chunks)) ||
-      (rc = dalloc(c, &c->ccounter, 1)) ||
+      (rc = dalloc(c, &c->chunk_agg, (size_t)n_chunks)) || (rc = dalloc(c, &c->cpart, (size_t)6 * n_chunks)) ||
       (rc = dalloc(c, &c->gj_buf, (size_t)GJ_B * GJ_B + 2 * (size_t)GJ_B * nc_pad)) ||
-      (rc = dalloc(c, &c->Ainv32, (size_t)nc_pad * nc_pad)) || (rc = dalloc(c, &c->Rc, (size_t)nc_pad)) ||
-      (rc = dalloc(c, &c->Ec, (size_t)nc_pad)))
+      (rc = dalloc(c, &c->Ainv32, (size_t)nc_pad * nc_pad)) || (rc = dalloc(c, &c->Ec, (size_t)nc_pad)))
     return rc;
   auto up = [&](void* dst, const void* src, size_t bytes) {
     if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
@@ -585,9 +576,7 @@ static int coarse_build(Ctx* c, int target_nc) {
   up(c->cblk_ptr, cblk_ptr.data(), cblk_ptr.size() * sizeof(int));
   up(c->cblk_src, cblk_src.data(), cblk_src.size() * sizeof(int64_t));
   up(c->chunk_begin, chunk_begin.data(), chunk_begin.size() * sizeof(int));
-  up(c->agg_chunk_ptr, agg_chunk_ptr.data(), agg_chunk_ptr.size() * sizeof(int));
-  cudaMemsetAsync(c->ccounter, 0, sizeof(unsigned), c->stream);
-  cudaMemsetAsync(c->Rc, 0, (size_t)nc_pad * sizeof(float), c->stream);   // padding stays zero
+  up(c->chunk_agg, chunk_agg.data(), chunk_agg.size() * sizeof(int));
   cudaMemsetAsync(c->Ec, 0, (size_t)nc_pad * sizeof(float), c->stream);
   if ((rc = sync_and_check(c, "coarse set-up upload"))) return rc;
   c->coarse_mask_gen = c->mask_gen;
@@ -676,9 +665,9 @@ int coarse_prepare(Ctx* c) {
 
 void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop) {
   k_coarse_restrict<<<c->n_chunks, 256, 0, c->stream>>>(c->n_chunks, c->chunk_begin, c->agg_nodes, c->node_d32, r,
-                                                        c->nagg, c->agg_chunk_ptr, stop, c->cpart, c->ccounter,
-                                                        c->Rc);
-  k_coarse_gemv<<<(c->nc + 7) / 8, 256, 0, c->stream>>>(c->nc, c->nc_pad, c->Ainv32, c->Rc, stop, c->Ec);
+                                                        stop, c->cpart);
+  k_coarse_gemv<<<(c->nc + 7) / 8, 256, 0, c->stream>>>(c->nc, c->nc_pad, c->Ainv32, c->n_chunks, c->chunk_agg,
+                                                        c->cpart, stop, c->Ec);
   c->launches += 2;
 }
 

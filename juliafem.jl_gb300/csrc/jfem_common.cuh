@@ -341,6 +341,7 @@ struct Ctx {
   float* geoT32 = nullptr;      // geometry records in tile order
   float* nhstate = nullptr;     // [16·n_q][Epad] Neo-Hookean point state at u_state (F, C⁻¹ sym, μ − λ ln J), tile order
   uint64_t state_version = 1;   // bumped whenever u_state, the material, the formulation or the geometry change
+  uint64_t diag_state_version = 0, diag_mask_gen = 0;   // what c->dinv was computed for (0: never)
   uint64_t nhstate_version = 0; // state_version nhstate was computed at
 
   // scratch
@@ -379,6 +380,7 @@ struct Ctx {
   double* mdots = nullptr;    // loss dot-product partials of a training batch
   float* mcoef = nullptr;     // per-pair loss-gradient coefficients
   int64_t m_actB = 0, m_gpart_cap = 0;
+  float4* mi = nullptr;       // network inference vectors, 7 × [N] float4: y, A y, A² y, u, h, g, v
   float* zf = nullptr;        // FCG: preconditioned residual (FP32)
   float* invdeg = nullptr;    // 1 / (neighbours of each node), the mean-aggregation weights
 
@@ -413,10 +415,8 @@ struct Ctx {
   float* Ainv32 = nullptr;      // [nc_pad][nc_pad] A_c⁻¹ rounded to FP32 (the per-iteration coarse solve)
   int n_chunks = 0;             // restriction chunks (≤ 1,024 nodes of one aggregate each)
   int* chunk_begin = nullptr;   // [n_chunks+1] into agg_nodes
-  int* agg_chunk_ptr = nullptr; // [nagg+1] chunks of each aggregate
-  double* cpart = nullptr;      // [n_chunks][6] chunk partial resultants
-  unsigned* ccounter = nullptr; // last-block counter of the restriction (returns to 0)
-  float* Rc = nullptr;          // [nc_pad] restricted residual Pᵀ r
+  int* chunk_agg = nullptr;     // [n_chunks] aggregate of each chunk
+  float* cpart = nullptr;       // [n_chunks][6] chunk partials of Pᵀ r
   float* Ec = nullptr;          // [nc_pad] coarse correction A_c⁻¹ Pᵀ r
   double coarse_setup_ms = 0.0; // last coarse value setup (CUDA events)
 
@@ -494,7 +494,8 @@ int mpnn_loss_grad(Ctx* c, const double* r, const double* e, double* loss, float
 int mpnn_precondition(Ctx* c, const double* r, double* z);
 int mpnn_ensure_act(Ctx* c, int64_t B);
 int mpnn_refresh_poly(Ctx* c);
-void enqueue_mpnn_spd(Ctx* c, const float* y, float* v);   // v = NᵀN y for one sample (y, v: [N][3])
+int mpnn_ensure_infer(Ctx* c);                             // the float4 inference vectors
+void enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v); // v = NᵀN y for one sample (y, v: [N] float4)
 // jfem_coarse.cu
 int coarse_prepare(Ctx* c);   // structure and values for the current mesh, mask and geometry
 int coarse_info(Ctx* c, int* n_agg, int* n_coarse, int64_t* n_elem_listed, double* setup_ms);

@@ -453,19 +453,27 @@ __global__ void k_mp_sub(int64_t n, const double* __restrict__ a, const double* 
     c[i] = a[i] - b[i];
 }
 
-// y = mask ⊙ D^{-1/2} r (FP64 r, for the host-facing preconditioner)
+// y = mask ⊙ D^{-1/2} r (FP64 r, for the host-facing preconditioner), one float4 per node
 __global__ void k_mp_input_d(int64_t N, const double* __restrict__ r, const double* __restrict__ dinv,
-                             const uint8_t* __restrict__ mask, float* __restrict__ y) {
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * N; q += (int64_t)gridDim.x * blockDim.x)
-    y[q] = dof_free(mask, q / 3, (int)(q % 3)) ? (float)(sqrt(dinv[q]) * r[q]) : 0.f;
+                             const uint8_t* __restrict__ mask, float4* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    float v[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] = dof_free(mask, i, c) ? (float)(sqrt(dinv[3 * i + c]) * r[3 * i + c]) : 0.f;
+    y[i] = make_float4(v[0], v[1], v[2], 0.f);
+  }
 }
 
 // z = D^{-1/2} (y + v) (FP64 out)
-__global__ void k_mp_precond_out(int64_t N, const float* __restrict__ y, const float* __restrict__ v,
+__global__ void k_mp_precond_out(int64_t N, const float4* __restrict__ y, const float4* __restrict__ v,
                                  const double* __restrict__ dinv, const uint8_t* __restrict__ mask,
                                  double* __restrict__ z) {
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * N; q += (int64_t)gridDim.x * blockDim.x)
-    z[q] = dof_free(mask, q / 3, (int)(q % 3)) ? sqrt(dinv[q]) * ((double)y[q] + (double)v[q]) : 0.0;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * N; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = q / 3;
+    const int c = (int)(q % 3);
+    const float yq = reinterpret_cast<const float*>(y)[4 * i + c], vq = reinterpret_cast<const float*>(v)[4 * i + c];
+    z[q] = dof_free(mask, i, c) ? sqrt(dinv[q]) * ((double)yq + (double)vq) : 0.0;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -489,26 +497,27 @@ __device__ __forceinline__ void mat3_acc(const float* __restrict__ C, bool trans
 }
 
 // The neighbour sums of the inference kernels: an 8-lane group per node strides
-// over the node's row of the graph (coalesced index reads, 3-channel gathers
-// that mostly hit L2) and reduces by a fixed xor-shuffle tree, so every run
-// gives the same bits.  The group's lanes share the node, so the group mask is
-// uniform wherever the loop condition is.
+// over the node's row of the graph (coalesced index reads; one 16-byte gather per
+// neighbour, mostly from L2) and reduces by a fixed xor-shuffle tree, so every
+// run gives the same bits.  The group's lanes share the node, so the group mask
+// is uniform wherever the loop condition is.  Vectors are one float4 per node;
+// the inputs of the adjoint steps carry the neighbour weight 1/deg_j in .w.
 #define MP_GL 8
 __device__ __forceinline__ unsigned group_mask() { return 0xffu << (threadIdx.x & 24); }
 
 template <bool WEIGHTED>
 __device__ __forceinline__ void group_neighbour_sum(const int* __restrict__ nb_ptr, const int* __restrict__ nbr,
-                                                    const float* __restrict__ invdeg, const float* __restrict__ in,
-                                                    int64_t i, int g, float s[3]) {
+                                                    const float4* __restrict__ in, int64_t i, int g, float s[3]) {
   s[0] = s[1] = s[2] = 0.f;
   const int j0 = __ldg(nb_ptr + i), j1 = __ldg(nb_ptr + i + 1);
   for (int jj = j0 + g; jj < j1; jj += MP_GL) {
     const int64_t j = __ldg(nbr + jj);
     if (j == i) continue;
-    const float w = WEIGHTED ? __ldg(invdeg + j) : 1.f;
-    s[0] = fmaf(w, __ldg(in + 3 * j), s[0]);
-    s[1] = fmaf(w, __ldg(in + 3 * j + 1), s[1]);
-    s[2] = fmaf(w, __ldg(in + 3 * j + 2), s[2]);
+    const float4 v = __ldg(in + j);
+    const float w = WEIGHTED ? v.w : 1.f;
+    s[0] = fmaf(w, v.x, s[0]);
+    s[1] = fmaf(w, v.y, s[1]);
+    s[2] = fmaf(w, v.z, s[2]);
   }
   const unsigned gm = group_mask();
 #pragma unroll
@@ -524,10 +533,10 @@ __device__ __forceinline__ void group_neighbour_sum(const int* __restrict__ nb_p
 template <bool LAST>
 __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __restrict__ nb_ptr,
                                                      const int* __restrict__ nbr, const float* __restrict__ invdeg,
-                                                     const float* __restrict__ in, const float* __restrict__ y,
-                                                     const float* __restrict__ a1, const float* __restrict__ poly,
-                                                     const uint8_t* __restrict__ mask, float* __restrict__ out,
-                                                     float* __restrict__ h) {
+                                                     const float4* __restrict__ in, const float4* __restrict__ y,
+                                                     const float4* __restrict__ a1, const float* __restrict__ poly,
+                                                     const uint8_t* __restrict__ mask, float4* __restrict__ out,
+                                                     float4* __restrict__ h) {
   __shared__ float C[36];
   if (threadIdx.x < 36) C[threadIdx.x] = poly[threadIdx.x];
   __syncthreads();
@@ -536,18 +545,17 @@ __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __res
   const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
   for (int64_t i = g0; i < N; i += gs) {
     float s[3];
-    group_neighbour_sum<false>(nb_ptr, nbr, invdeg, in, i, g, s);
+    group_neighbour_sum<false>(nb_ptr, nbr, in, i, g, s);
     if (g != 0) continue;
     const float id = __ldg(invdeg + i);
     float a[3] = {s[0] * id, s[1] * id, s[2] * id};
     if (!LAST) {
-      out[3 * i] = a[0];
-      out[3 * i + 1] = a[1];
-      out[3 * i + 2] = a[2];
+      out[i] = make_float4(a[0], a[1], a[2], 0.f);
     } else {
-      const float yv[3] = {y[3 * i], y[3 * i + 1], y[3 * i + 2]};
-      const float a1v[3] = {a1[3 * i], a1[3 * i + 1], a1[3 * i + 2]};
-      const float a2v[3] = {in[3 * i], in[3 * i + 1], in[3 * i + 2]};
+      const float4 y4 = y[i], a14 = a1[i], a24 = in[i];
+      const float yv[3] = {y4.x, y4.y, y4.z};
+      const float a1v[3] = {a14.x, a14.y, a14.z};
+      const float a2v[3] = {a24.x, a24.y, a24.z};
       float u[3] = {0.f, 0.f, 0.f};
       mat3_acc(C, false, yv, u);
       mat3_acc(C + 9, false, a1v, u);
@@ -558,20 +566,18 @@ __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __res
       for (int k = 0; k < 3; ++k) u[k] = ((m >> k) & 1) ? 0.f : u[k];
       float hv[3] = {0.f, 0.f, 0.f};
       mat3_acc(C + 27, true, u, hv);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        out[3 * i + k] = u[k];
-        h[3 * i + k] = hv[k];
-      }
+      out[i] = make_float4(u[0], u[1], u[2], 0.f);
+      h[i] = make_float4(hv[0], hv[1], hv[2], id);
     }
   }
 }
 
-// Horner step of the adjoint: out = C_kᵀ u + Aᵀ g
+// Horner step of the adjoint: out = C_kᵀ u + Aᵀ g (g.w = 1/deg); out.w = 1/deg_i
+// for the next step
 __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __restrict__ nb_ptr,
                                                      const int* __restrict__ nbr, const float* __restrict__ invdeg,
-                                                     const float* __restrict__ g, const float* __restrict__ u,
-                                                     const float* __restrict__ poly, int k, float* __restrict__ out) {
+                                                     const float4* __restrict__ g, const float4* __restrict__ u,
+                                                     const float* __restrict__ poly, int k, float4* __restrict__ out) {
   __shared__ float C[9];
   if (threadIdx.x < 9) C[threadIdx.x] = poly[9 * k + threadIdx.x];
   __syncthreads();
@@ -580,13 +586,12 @@ __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __res
   const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
   for (int64_t i = g0; i < N; i += gs) {
     float s[3];
-    group_neighbour_sum<true>(nb_ptr, nbr, invdeg, g, i, gl, s);
+    group_neighbour_sum<true>(nb_ptr, nbr, g, i, gl, s);
     if (gl != 0) continue;
-    const float uv[3] = {u[3 * i], u[3 * i + 1], u[3 * i + 2]};
+    const float4 u4 = u[i];
+    const float uv[3] = {u4.x, u4.y, u4.z};
     mat3_acc(C, true, uv, s);
-    out[3 * i] = s[0];
-    out[3 * i + 1] = s[1];
-    out[3 * i + 2] = s[2];
+    out[i] = make_float4(s[0], s[1], s[2], __ldg(invdeg + i));
   }
 }
 
@@ -844,12 +849,26 @@ int mpnn_refresh_poly(Ctx* c) {
 
 // v = NᵀN y for one sample in polynomial form (mpnn_refresh_poly first):
 // a1 = A y, a2 = A a1, u = mask ⊙ Σ C_k A^k y, then Horner for Nᵀ u.  Uses the
-// 3-channel scratch of the activation arena (B ≥ 1).
-void enqueue_mpnn_spd(Ctx* c, const float* y, float* v) {
-  const MpBufs& b = c->mb;
+// float4 inference vectors (mpnn_ensure_infer first).
+int mpnn_ensure_infer(Ctx* c) {
+  if (c->mi) return 0;
+  if (c->pcg_graph) {   // a captured solve graph may hold older buffer addresses
+    cudaStreamSynchronize(c->stream);
+    cudaGraphExecDestroy(c->pcg_graph);
+    c->pcg_graph = nullptr;
+    c->pcg_graph_key = -1;
+  }
+  int rc = dalloc(c, &c->mi, (size_t)7 * c->N);
+  if (rc) return rc;
+  cudaMemsetAsync(c->mi, 0, (size_t)7 * c->N * sizeof(float4), c->stream);
+  return 0;
+}
+
+void enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v) {
   const float* P = c->mp->poly;
   const unsigned g = grid_for(c->N * MP_GL, 256);
-  float *a1 = b.t3a, *a2 = b.t3b, *u = b.u, *h = b.w, *g2 = b.ghat;
+  float4 *a1 = c->mi + c->N, *a2 = c->mi + 2 * c->N, *u = c->mi + 3 * c->N, *h = c->mi + 4 * c->N,
+         *g2 = c->mi + 5 * c->N;
   k_mp_poly_fwd<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, y, nullptr, nullptr, P, c->mask,
                                                   a1, nullptr);
   k_mp_poly_fwd<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, a1, nullptr, nullptr, P,
@@ -1105,13 +1124,15 @@ int mpnn_precondition(Ctx* c, const double* r_h, double* z_h) {
   int rc = geometry_prepare(c);
   if (rc) return rc;
   if ((rc = jacobi_diag_device(c, c->dinv))) return rc;
-  if ((rc = mpnn_ensure_act(c, 1))) return rc;
+  if ((rc = mpnn_ensure_infer(c))) return rc;
   if ((rc = mpnn_refresh_poly(c))) return rc;
   const int64_t n3 = 3 * c->N;
+  float4* y = c->mi;
+  float4* v = c->mi + 6 * c->N;
   cudaMemcpyAsync(c->tmp, r_h, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
-  k_mp_input_d<<<grid_for(n3, 256), 256, 0, c->stream>>>(c->N, c->tmp, c->dinv, c->mask, c->mb.y);
-  enqueue_mpnn_spd(c, c->mb.y, c->mb.v);
-  k_mp_precond_out<<<grid_for(n3, 256), 256, 0, c->stream>>>(c->N, c->mb.y, c->mb.v, c->dinv, c->mask, c->tmp2);
+  k_mp_input_d<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->tmp, c->dinv, c->mask, y);
+  enqueue_mpnn_spd(c, y, v);
+  k_mp_precond_out<<<grid_for(n3, 256), 256, 0, c->stream>>>(c->N, y, v, c->dinv, c->mask, c->tmp2);
   c->launches += 2;
   cudaMemcpyAsync(z_h, c->tmp2, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
   return sync_and_check(c, "preconditioner");

@@ -364,15 +364,20 @@ void enqueue_axpy(Ctx* c, int64_t n, double a, const double* x, double* y) {
 // definite, for which FCG is PCG.  part regions: [0,G) tile p·q, [3G,4G)
 // boundary p·q, [G,2G) z·q then r·r, [2G,3G) p·r.
 // ---------------------------------------------------------------------------
-// y = mask ⊙ D^{-1/2} r (FP32), the network input
+// y = mask ⊙ D^{-1/2} r (FP32), the network input, one float4 per node
 __global__ void __launch_bounds__(256) k_fcg_input(int64_t N, const float2* __restrict__ r,
                                                    const float* __restrict__ dinv, const uint8_t* __restrict__ mask,
-                                                   const SolverScalars* __restrict__ sc, float* __restrict__ y) {
+                                                   const SolverScalars* __restrict__ sc, float4* __restrict__ y) {
   if (sc->done[0]) return;
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * N; q += (int64_t)gridDim.x * blockDim.x) {
-    const bool fr = !((mask[q / 3] >> (int)(q % 3)) & 1);
-    const float2 rq = r[q];
-    y[q] = fr ? sqrtf(dinv[q]) * (rq.x + rq.y) : 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t m = mask[i];
+    float v[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float2 rq = r[3 * i + c];
+      v[c] = ((m >> c) & 1) ? 0.f : sqrtf(dinv[3 * i + c]) * (rq.x + rq.y);
+    }
+    y[i] = make_float4(v[0], v[1], v[2], 0.f);
   }
 }
 
@@ -380,8 +385,8 @@ __global__ void __launch_bounds__(256) k_fcg_input(int64_t N, const float2* __re
 // the coarse correction P Ec when COARSE (two-level); z·q_old partials → the
 // last block forms β = z·q_old / p_old·q_old (0 on restart)
 template <bool NN, bool COARSE>
-__global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_z(int64_t n, const float* __restrict__ y,
-                                                            const float* __restrict__ v,
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_z(int64_t n, const float4* __restrict__ y,
+                                                            const float4* __restrict__ v,
                                                             const float2* __restrict__ r,
                                                             const float* __restrict__ dinv,
                                                             const uint8_t* __restrict__ mask,
@@ -400,7 +405,9 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_z(int64_t n, const flo
     const bool fr = !((mask[i] >> cc) & 1);
     float zq;
     if (NN) {
-      zq = sqrtf(dinv[q]) * (y[q] + v[q]);
+      const float* yf = reinterpret_cast<const float*>(y);
+      const float* vf = reinterpret_cast<const float*>(v);
+      zq = sqrtf(dinv[q]) * (yf[4 * i + cc] + vf[4 * i + cc]);
     } else {
       const float2 rq = r[q];
       zq = dinv[q] * (rq.x + rq.y);
@@ -552,14 +559,16 @@ static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
   const float4* d32 = coarse ? c->node_d32 : nullptr;
   const float* Ec = coarse ? c->Ec : nullptr;
   if (nn) {
-    k_fcg_input<<<grid_for(n, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, c->mb.y);
-    enqueue_mpnn_spd(c, c->mb.y, c->mb.v);
+    float4* y = c->mi;
+    float4* v = c->mi + 6 * c->N;
+    k_fcg_input<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, y);
+    enqueue_mpnn_spd(c, y, v);
     if (coarse)
-      k_fcg_z<true, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->mb.y, c->mb.v, c->rd, c->dinvf, c->mask,
-                                                                  c->Apf, na, d32, Ec, c->sc, c->zf, c->part);
+      k_fcg_z<true, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, y, v, c->rd, c->dinvf, c->mask, c->Apf, na, d32,
+                                                                  Ec, c->sc, c->zf, c->part);
     else
-      k_fcg_z<true, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->mb.y, c->mb.v, c->rd, c->dinvf, c->mask,
-                                                                   c->Apf, na, d32, Ec, c->sc, c->zf, c->part);
+      k_fcg_z<true, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, y, v, c->rd, c->dinvf, c->mask, c->Apf, na,
+                                                                   d32, Ec, c->sc, c->zf, c->part);
     c->launches += 2;
   } else {
     if (coarse)
@@ -800,7 +809,7 @@ static int fcg(Ctx* c, const double* f, bool nn, bool coarse, double tol, int ma
   const unsigned gv = grid_for(n, 256);
   if (!apply_is_tiled(c)) return set_err(c, JFEM_ERR_INVALID, "flexible CG needs the tiled apply");
   if (nn && (!c->mp || !c->mp->ready)) return set_err(c, JFEM_ERR_INVALID, "no network weights (jfem_mpnn_init)");
-  if (nn && (rc = mpnn_ensure_act(c, 1))) return rc;
+  if (nn && (rc = mpnn_ensure_infer(c))) return rc;
   if (nn && (rc = mpnn_refresh_poly(c))) return rc;
   if (coarse && (rc = coarse_prepare(c))) return rc;
   const auto kind_of = [&]() { return (nn ? 3 : 2) + (coarse ? 2 : 0); };
