@@ -35,8 +35,8 @@
 // the inverse is rounded to FP32 for the per-iteration coarse solve.
 // Per CG iteration: k_coarse_restrict (one CTA per chunk of an aggregate's
 // nodes: partial force and moment resultants of r about c_a), k_coarse_gemv
-// (Ec = A_c⁻¹ Pᵀ r from the chunk partials, one warp per row); the
-// prolongation P Ec is fused into the kernel that forms z.
+// (each block sums the chunk partials into shared memory, then Ec = A_c⁻¹ Pᵀ r
+// one warp per row); the prolongation P Ec is fused into the kernel that forms z.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -294,68 +294,133 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 
 // Restriction Pᵀ r: for aggregate a, Σ_{i ∈ a} φ_k(d_i) · r_i — force (k < 3) and
 // moment (k ≥ 3) resultants of r about the centroid (r is zero on prescribed
-// DOFs).  Each aggregate's node list is cut into chunks of at most CR_CHUNK
-// nodes, one CTA per chunk (FP32 per thread, FP64 across the CTA, fixed order);
-// the chunk partials go to cpart[chunk][6] and the coarse solve sums them.
+// DOFs) — and, when qold is given, the same for flexible CG's previous q (FP32).
+// Each aggregate's node list is cut into chunks of at most CR_CHUNK nodes, one
+// CTA per chunk (FP32 per thread, FP64 across the CTA, fixed order); the chunk
+// partials go to cpart[chunk][12] (r: 0..5, q_old: 6..11) and the coarse solve
+// sums them.
 #define CR_CHUNK 1024
+__device__ __forceinline__ void add_resultants(float s[6], float4 d, float fx, float fy, float fz) {
+  s[0] += fx;
+  s[1] += fy;
+  s[2] += fz;
+  s[3] = fmaf(d.y, fz, fmaf(-d.z, fy, s[3]));
+  s[4] = fmaf(d.z, fx, fmaf(-d.x, fz, s[4]));
+  s[5] = fmaf(d.x, fy, fmaf(-d.y, fx, s[5]));
+}
+
 __global__ void __launch_bounds__(256) k_coarse_restrict(int n_chunks, const int* __restrict__ chunk_begin,
                                                          const int* __restrict__ agg_nodes,
                                                          const float4* __restrict__ d32,
-                                                         const float2* __restrict__ r, const int* __restrict__ stop,
+                                                         const float2* __restrict__ r,
+                                                         const float* __restrict__ qold, const int* __restrict__ stop,
                                                          float* __restrict__ cpart) {
-  __shared__ double sh[8][6];
+  __shared__ double sh[8][12];
   if (stop && *stop) return;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int ch = blockIdx.x;
-  float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  for (int t = chunk_begin[ch] + threadIdx.x; t < chunk_begin[ch + 1]; t += blockDim.x) {
-    const int64_t i = agg_nodes[t];
-    const float2 r0 = r[3 * i], r1 = r[3 * i + 1], r2 = r[3 * i + 2];
-    const float rx = r0.x + r0.y, ry = r1.x + r1.y, rz = r2.x + r2.y;
-    const float4 d = d32[i];
-    s[0] += rx;
-    s[1] += ry;
-    s[2] += rz;
-    s[3] = fmaf(d.y, rz, fmaf(-d.z, ry, s[3]));
-    s[4] = fmaf(d.z, rx, fmaf(-d.x, rz, s[4]));
-    s[5] = fmaf(d.x, ry, fmaf(-d.y, rx, s[5]));
+  const int nk = qold ? 12 : 6;
+  float s[12] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  // a chunk is at most CR_CHUNK = 4 · 256 nodes: every thread issues its four node
+  // indices, then all their loads, before it adds anything (the loads overlap)
+  const int t0 = chunk_begin[ch] + threadIdx.x, t1 = chunk_begin[ch + 1];
+  int64_t idx[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) idx[u] = t0 + 256 * u < t1 ? (int64_t)agg_nodes[t0 + 256 * u] : -1;
+  float2 rv[4][3];
+  float4 dv[4];
+  float qv[4][3];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    if (idx[u] < 0) continue;
+    const int64_t i = idx[u];
+    rv[u][0] = r[3 * i];
+    rv[u][1] = r[3 * i + 1];
+    rv[u][2] = r[3 * i + 2];
+    dv[u] = d32[i];
+    if (qold) {
+      qv[u][0] = qold[3 * i];
+      qv[u][1] = qold[3 * i + 1];
+      qv[u][2] = qold[3 * i + 2];
+    }
   }
 #pragma unroll
-  for (int k = 0; k < 6; ++k) {
-    const double v = warp_sum_d((double)s[k]);
-    if (lane == 0) sh[wid][k] = v;
+  for (int u = 0; u < 4; ++u) {
+    if (idx[u] < 0) continue;
+    add_resultants(s, dv[u], rv[u][0].x + rv[u][0].y, rv[u][1].x + rv[u][1].y, rv[u][2].x + rv[u][2].y);
+    if (qold) add_resultants(s + 6, dv[u], qv[u][0], qv[u][1], qv[u][2]);
+  }
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    if (k < nk) {   // nk is the same for the whole block
+      const double v = warp_sum_d((double)s[k]);
+      if (lane == 0) sh[wid][k] = v;
+    }
   }
   __syncthreads();
-  if (threadIdx.x < 6) {
+  if (threadIdx.x < nk) {
     double v = 0.0;
     for (int q = 0; q < nw; ++q) v += sh[q][threadIdx.x];
-    cpart[6 * ch + threadIdx.x] = (float)v;
+    cpart[12 * ch + threadIdx.x] = (float)v;
   }
 }
 
-// Ec = A_c⁻¹ Pᵀ r = Σ_chunks A_c⁻¹[:, 6·agg(chunk) + k] · cpart[chunk][k]: the coarse
-// solve reads the chunk partials directly (A_c⁻¹ with its columns repeated per
-// chunk), so no kernel has to wait for a serial sum.  FP32, one warp per row,
-// lanes over chunks, fixed shuffle tree.
-__global__ void __launch_bounds__(256) k_coarse_gemv(int nc, int ld, const float* __restrict__ Ainv,
-                                                     int n_chunks, const int* __restrict__ chunk_agg,
+// Ec = A_c⁻¹ Pᵀ r.  Every block first sums the chunk partials of each aggregate
+// (chunks of an aggregate are contiguous; fixed order) into shared memory —
+// Pᵀ r, and Pᵀ q_old when t2part is given — then one warp per row forms the
+// row's dot product from contiguous float4 loads of A_c⁻¹ (FP32, fixed lane
+// order and shuffle tree).  With t2part, also the products Ec_row·(Pᵀq_old)_row,
+// summed over the block's rows in warp order, into t2part[block].
+#define CG_GEMV_MAX JFEM_COARSE_MAX_DOFS
+__global__ void __launch_bounds__(256) k_coarse_gemv(int nc, int ld, const float* __restrict__ Ainv, int nagg,
+                                                     const int* __restrict__ agg_chunk_ptr,
                                                      const float* __restrict__ cpart, const int* __restrict__ stop,
-                                                     float* __restrict__ Ec) {
+                                                     float* __restrict__ Ec, double* __restrict__ t2part) {
+  __shared__ __align__(16) float R[CG_GEMV_MAX];
+  __shared__ float Q[CG_GEMV_MAX];
+  __shared__ double sh[8];
   if (stop && *stop) return;
-  const int lane = threadIdx.x & 31;
-  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (row >= nc) return;
-  const float* a = Ainv + (int64_t)row * ld;
-  float s = 0.f;
-  for (int ch = lane; ch < n_chunks; ch += 32) {
-    const float* ac = a + 6 * chunk_agg[ch];
-    const float* pc = cpart + 6 * ch;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) s = fmaf(ac[k], pc[k], s);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int t = threadIdx.x; t < ld; t += blockDim.x) {
+    float sr = 0.f, sq = 0.f;
+    if (t < 6 * nagg) {
+      const int ag = t / 6, k = t % 6;
+#pragma unroll 4
+      for (int ch = agg_chunk_ptr[ag]; ch < agg_chunk_ptr[ag + 1]; ++ch) {
+        sr += cpart[12 * ch + k];
+        if (t2part) sq += cpart[12 * ch + 6 + k];
+      }
+    }
+    R[t] = sr;
+    Q[t] = sq;
   }
+  __syncthreads();
+  const int row = blockIdx.x * (blockDim.x >> 5) + wid;
+  double prod = 0.0;
+  if (row < nc) {
+    const float4* a = reinterpret_cast<const float4*>(Ainv + (int64_t)row * ld);
+    const float4* x = reinterpret_cast<const float4*>(R);
+    float s = 0.f;
+    for (int j = lane; j < ld / 4; j += 32) {
+      const float4 av = a[j], xv = x[j];
+      s = fmaf(av.x, xv.x, s);
+      s = fmaf(av.y, xv.y, s);
+      s = fmaf(av.z, xv.z, s);
+      s = fmaf(av.w, xv.w, s);
+    }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (lane == 0) Ec[row] = s;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) Ec[row] = s;
+    prod = (double)s * (double)Q[row];
+  }
+  if (!t2part) return;
+  if (lane == 0) sh[wid] = prod;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sh[q];
+    t2part[blockIdx.x] = t;
+  }
 }
 
 // z = D⁻¹ r + P Ec (FP64 out): the two-level preconditioner with the Jacobi smoother
@@ -385,12 +450,14 @@ __global__ void k_to_df(int64_t n, const double* __restrict__ a, float2* __restr
 // ---------------------------------------------------------------------------
 // host: structure (aggregation, element lists, block pattern)
 // ---------------------------------------------------------------------------
-// Coarse DOFs when none are requested: about one per 2,500 fine DOFs, within
-// [192, 768] — enough aggregates to carry the bending modes of slender parts,
-// few enough that the FP64 inversion stays a small share of a solve.
+// Coarse DOFs when none are requested: about one per 2,000 fine DOFs, within
+// [192, 1152] — enough aggregates to carry the bending modes of slender parts
+// (on the 2M-DOF Tet10 cantilever: 1,404 coarse DOFs after rounding the bins,
+// about 290 iterations, against 392 with 552), few enough that the FP64
+// inversion stays a small share of a solve.
 static int auto_coarse_dofs(int64_t n_dofs) {
-  const int64_t v = n_dofs / 2500;
-  return (int)std::min<int64_t>(768, std::max<int64_t>(192, v));
+  const int64_t v = n_dofs / 2000;
+  return (int)std::min<int64_t>(1152, std::max<int64_t>(192, v));
 }
 
 static int coarse_build(Ctx* c, int target_nc) {
@@ -452,12 +519,11 @@ static int coarse_build(Ctx* c, int target_nc) {
     for (int64_t i = 0; i < N; ++i) agg_nodes[(size_t)cur[(size_t)node_agg[(size_t)i]]++] = (int)i;
   }
   // restriction chunks: each aggregate's node list cut into pieces of ≤ CR_CHUNK
-  std::vector<int> chunk_begin, chunk_agg;
-  for (int a = 0; a < nagg; ++a)
-    for (int t = agg_ptr[(size_t)a]; t < agg_ptr[(size_t)a + 1]; t += CR_CHUNK) {
-      chunk_begin.push_back(t);
-      chunk_agg.push_back(a);
-    }
+  std::vector<int> chunk_begin, agg_chunk_ptr(1, 0);
+  for (int a = 0; a < nagg; ++a) {
+    for (int t = agg_ptr[(size_t)a]; t < agg_ptr[(size_t)a + 1]; t += CR_CHUNK) chunk_begin.push_back(t);
+    agg_chunk_ptr.push_back((int)chunk_begin.size());
+  }
   const int n_chunks = (int)chunk_begin.size();
   chunk_begin.push_back((int)N);
   std::vector<double> cen((size_t)3 * nagg, 0.0);
@@ -539,7 +605,7 @@ static int coarse_build(Ctx* c, int target_nc) {
   }
   void* old[] = {c->agg_ptr, c->agg_nodes, c->node_agg, c->node_d32, c->node_d64, c->celem, c->celem_aggs,
                  c->celem_off, c->contrib, c->cblk_ab, c->cblk_ptr, c->cblk_src, c->Ac, c->Ac_diag, c->gj_buf,
-                 c->Ainv32, c->Ec, c->chunk_begin, c->chunk_agg, c->cpart};
+                 c->Ainv32, c->Ec, c->chunk_begin, c->agg_chunk_ptr, c->cpart};
   for (void* p : old) dfree(c, p);
   c->nagg = nagg;
   c->nc = nc;
@@ -557,7 +623,8 @@ static int coarse_build(Ctx* c, int target_nc) {
       (rc = dalloc(c, &c->cblk_ab, (size_t)(2 * n_cblk))) || (rc = dalloc(c, &c->cblk_ptr, (size_t)n_cblk + 1)) ||
       (rc = dalloc(c, &c->cblk_src, cblk_src.size())) || (rc = dalloc(c, &c->Ac, (size_t)nc_pad * nc_pad)) ||
       (rc = dalloc(c, &c->Ac_diag, (size_t)nc_pad)) || (rc = dalloc(c, &c->chunk_begin, (size_t)n_chunks + 1)) ||
-      (rc = dalloc(c, &c->chunk_agg, (size_t)n_chunks)) || (rc = dalloc(c, &c->cpart, (size_t)6 * n_chunks)) ||
+      (rc = dalloc(c, &c->agg_chunk_ptr, (size_t)nagg + 1)) ||
+      (rc = dalloc(c, &c->cpart, (size_t)12 * n_chunks)) ||
       (rc = dalloc(c, &c->gj_buf, (size_t)GJ_B * GJ_B + 2 * (size_t)GJ_B * nc_pad)) ||
       (rc = dalloc(c, &c->Ainv32, (size_t)nc_pad * nc_pad)) || (rc = dalloc(c, &c->Ec, (size_t)nc_pad)))
     return rc;
@@ -576,7 +643,7 @@ static int coarse_build(Ctx* c, int target_nc) {
   up(c->cblk_ptr, cblk_ptr.data(), cblk_ptr.size() * sizeof(int));
   up(c->cblk_src, cblk_src.data(), cblk_src.size() * sizeof(int64_t));
   up(c->chunk_begin, chunk_begin.data(), chunk_begin.size() * sizeof(int));
-  up(c->chunk_agg, chunk_agg.data(), chunk_agg.size() * sizeof(int));
+  up(c->agg_chunk_ptr, agg_chunk_ptr.data(), agg_chunk_ptr.size() * sizeof(int));
   cudaMemsetAsync(c->Ec, 0, (size_t)nc_pad * sizeof(float), c->stream);
   if ((rc = sync_and_check(c, "coarse set-up upload"))) return rc;
   c->coarse_mask_gen = c->mask_gen;
@@ -663,11 +730,13 @@ int coarse_prepare(Ctx* c) {
   return 0;
 }
 
-void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop) {
+int coarse_gemv_blocks(const Ctx* c) { return (c->nc + 7) / 8; }
+
+void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop, const float* qold, double* t2part) {
   k_coarse_restrict<<<c->n_chunks, 256, 0, c->stream>>>(c->n_chunks, c->chunk_begin, c->agg_nodes, c->node_d32, r,
-                                                        stop, c->cpart);
-  k_coarse_gemv<<<(c->nc + 7) / 8, 256, 0, c->stream>>>(c->nc, c->nc_pad, c->Ainv32, c->n_chunks, c->chunk_agg,
-                                                        c->cpart, stop, c->Ec);
+                                                        t2part ? qold : nullptr, stop, c->cpart);
+  k_coarse_gemv<<<coarse_gemv_blocks(c), 256, 0, c->stream>>>(c->nc, c->nc_pad, c->Ainv32, c->nagg, c->agg_chunk_ptr,
+                                                              c->cpart, stop, c->Ec, t2part);
   c->launches += 2;
 }
 

@@ -25,6 +25,15 @@
 #define JFEM_MAX_NEIGHBOURS 512   // unique neighbour nodes per node (pattern build)
 #define JFEM_RED_BLOCKS 1216      // fixed reduction grid: 152 SMs x 8 → deterministic sums
 #define JFEM_RED_THREADS 256
+// Reduction partials (doubles) of the solvers: [0, 4G) the PCG/FCG dot products;
+// then the flexible-CG β terms: Σ D⁻¹r·q_old per reduction block, Σ
+// D^{-1/2}(y + v)·q_old per block of the network's last neighbour pass (its grid
+// is capped at 152·64 = 9,728 blocks), and Ec·Pᵀq_old per coarse-solve block
+// (≤ 4,096 rows / 8 per block).
+#define JFEM_PART_T1 (4 * JFEM_RED_BLOCKS)
+#define JFEM_PART_T1N (5 * JFEM_RED_BLOCKS)
+#define JFEM_PART_T2 (5 * JFEM_RED_BLOCKS + 10240)
+#define JFEM_PART_SIZE (JFEM_PART_T2 + 512)
 #define JFEM_TILE 256             // elements per tile of the shared-memory apply
 #define JFEM_TILE_CTAS 3          // resident CTAs per SM the small-strain tile kernel is compiled for
 
@@ -381,7 +390,6 @@ struct Ctx {
   float* mcoef = nullptr;     // per-pair loss-gradient coefficients
   int64_t m_actB = 0, m_gpart_cap = 0;
   float4* mi = nullptr;       // network inference vectors, 7 × [N] float4: y, A y, A² y, u, h, g, v
-  float* zf = nullptr;        // FCG: preconditioned residual (FP32)
   float* invdeg = nullptr;    // 1 / (neighbours of each node), the mean-aggregation weights
 
   // two-level preconditioner: Galerkin coarse space of rigid-body modes on node
@@ -415,8 +423,8 @@ struct Ctx {
   float* Ainv32 = nullptr;      // [nc_pad][nc_pad] A_c⁻¹ rounded to FP32 (the per-iteration coarse solve)
   int n_chunks = 0;             // restriction chunks (≤ 1,024 nodes of one aggregate each)
   int* chunk_begin = nullptr;   // [n_chunks+1] into agg_nodes
-  int* chunk_agg = nullptr;     // [n_chunks] aggregate of each chunk
-  float* cpart = nullptr;       // [n_chunks][6] chunk partials of Pᵀ r
+  int* agg_chunk_ptr = nullptr; // [nagg+1] the chunks of each aggregate (contiguous)
+  float* cpart = nullptr;       // [n_chunks][12] chunk partials of Pᵀ r and Pᵀ q_old
   float* Ec = nullptr;          // [nc_pad] coarse correction A_c⁻¹ Pᵀ r
   double coarse_setup_ms = 0.0; // last coarse value setup (CUDA events)
 
@@ -495,13 +503,20 @@ int mpnn_precondition(Ctx* c, const double* r, double* z);
 int mpnn_ensure_act(Ctx* c, int64_t B);
 int mpnn_refresh_poly(Ctx* c);
 int mpnn_ensure_infer(Ctx* c);                             // the float4 inference vectors
-void enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v); // v = NᵀN y for one sample (y, v: [N] float4)
+// v = NᵀN y for one sample (y, v: [N] float4).  With t1part, the last pass also
+// leaves block partials of Σ D^{-1/2}(y + v)·q_old (flexible CG's β) and
+// returns the number of blocks.
+int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf = nullptr, const float* qold = nullptr,
+                     double* t1part = nullptr);
 // jfem_coarse.cu
 int coarse_prepare(Ctx* c);   // structure and values for the current mesh, mask and geometry
 int coarse_info(Ctx* c, int* n_agg, int* n_coarse, int64_t* n_elem_listed, double* setup_ms);
 int coarse_matrix(Ctx* c, double* Ac_h, int* node_agg_h);
 int coarse_precondition(Ctx* c, const double* r_h, double* z_h);
-void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop);   // Ec = A_c⁻¹ Pᵀ r
+// Ec = A_c⁻¹ Pᵀ r; with qold, also the block partials of Ec·Pᵀ q_old into t2part
+void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop, const float* qold = nullptr,
+                                   double* t2part = nullptr);
+int coarse_gemv_blocks(const Ctx* c);
 // jfem_recovery.cu
 int recover_field(Ctx* c, const double* u_h, int field, double tol, int max_iter, double* nodal_h, int* iters_out);
 // jfem_solver.cu

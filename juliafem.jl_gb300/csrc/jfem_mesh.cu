@@ -384,7 +384,7 @@ int mesh_setup(Ctx* c, int et, int64_t N, const double* X, int64_t E, const int6
   if ((rc = dalloc(c, &c->rd, n))) return rc;
   if ((rc = dalloc(c, &c->Apf, n))) return rc;
   if ((rc = dalloc(c, &c->dinvf, n))) return rc;
-  if ((rc = dalloc(c, &c->part, 4 * JFEM_RED_BLOCKS))) return rc;
+  if ((rc = dalloc(c, &c->part, JFEM_PART_SIZE))) return rc;
   if ((rc = dalloc(c, &c->sc, 1))) return rc;
   if ((rc = dalloc(c, &c->norms, 2))) return rc;
   cudaMemsetAsync(c->mask, 0, N, c->stream);

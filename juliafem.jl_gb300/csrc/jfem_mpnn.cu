@@ -497,27 +497,38 @@ __device__ __forceinline__ void mat3_acc(const float* __restrict__ C, bool trans
 }
 
 // The neighbour sums of the inference kernels: an 8-lane group per node strides
-// over the node's row of the graph (coalesced index reads; one 16-byte gather per
-// neighbour, mostly from L2) and reduces by a fixed xor-shuffle tree, so every
-// run gives the same bits.  The group's lanes share the node, so the group mask
+// over the node's row of the graph, each lane taking MP_UNROLL neighbours per
+// round — their index loads first, then their 16-byte gathers (mostly L2), so the
+// loads overlap instead of forming a chain — and reduces by a fixed xor-shuffle
+// tree, so every run gives the same bits.  The group's lanes share the node, so the group mask
 // is uniform wherever the loop condition is.  Vectors are one float4 per node;
 // the inputs of the adjoint steps carry the neighbour weight 1/deg_j in .w.
 #define MP_GL 8
 __device__ __forceinline__ unsigned group_mask() { return 0xffu << (threadIdx.x & 24); }
 
+#define MP_UNROLL 4   // neighbours per lane and round: index loads, then gathers, then sums
 template <bool WEIGHTED>
 __device__ __forceinline__ void group_neighbour_sum(const int* __restrict__ nb_ptr, const int* __restrict__ nbr,
                                                     const float4* __restrict__ in, int64_t i, int g, float s[3]) {
   s[0] = s[1] = s[2] = 0.f;
   const int j0 = __ldg(nb_ptr + i), j1 = __ldg(nb_ptr + i + 1);
-  for (int jj = j0 + g; jj < j1; jj += MP_GL) {
-    const int64_t j = __ldg(nbr + jj);
-    if (j == i) continue;
-    const float4 v = __ldg(in + j);
-    const float w = WEIGHTED ? v.w : 1.f;
-    s[0] = fmaf(w, v.x, s[0]);
-    s[1] = fmaf(w, v.y, s[1]);
-    s[2] = fmaf(w, v.z, s[2]);
+  for (int base = j0 + g; base < j1; base += MP_GL * MP_UNROLL) {
+    int64_t j[MP_UNROLL];
+#pragma unroll
+    for (int u = 0; u < MP_UNROLL; ++u) {
+      const int jj = base + MP_GL * u;
+      j[u] = jj < j1 ? (int64_t)__ldg(nbr + jj) : i;   // i itself stands for "no neighbour"
+    }
+    float4 v[MP_UNROLL];
+#pragma unroll
+    for (int u = 0; u < MP_UNROLL; ++u) v[u] = j[u] != i ? __ldg(in + j[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < MP_UNROLL; ++u) {
+      const float w = WEIGHTED ? v[u].w : 1.f;
+      s[0] = fmaf(w, v[u].x, s[0]);
+      s[1] = fmaf(w, v[u].y, s[1]);
+      s[2] = fmaf(w, v[u].z, s[2]);
+    }
   }
   const unsigned gm = group_mask();
 #pragma unroll
@@ -573,17 +584,24 @@ __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __res
 }
 
 // Horner step of the adjoint: out = C_kᵀ u + Aᵀ g (g.w = 1/deg); out.w = 1/deg_i
-// for the next step
+// for the next step.  FCG (the last step, out = v = NᵀN y): also block partials
+// of Σ D^{-1/2}(y + v)·q_old, flexible CG's β term of the smoother, into
+// t1part[block] (fixed order).
+template <bool FCG>
 __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __restrict__ nb_ptr,
                                                      const int* __restrict__ nbr, const float* __restrict__ invdeg,
                                                      const float4* __restrict__ g, const float4* __restrict__ u,
-                                                     const float* __restrict__ poly, int k, float4* __restrict__ out) {
+                                                     const float* __restrict__ poly, int k, float4* __restrict__ out,
+                                                     const float4* __restrict__ y, const float* __restrict__ dinvf,
+                                                     const float* __restrict__ qold, double* __restrict__ t1part) {
   __shared__ float C[9];
+  __shared__ double sh[32];
   if (threadIdx.x < 9) C[threadIdx.x] = poly[9 * k + threadIdx.x];
   __syncthreads();
   const int gl = threadIdx.x & (MP_GL - 1);
   const int64_t g0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / MP_GL;
   const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
+  float2 t1 = make_float2(0.f, 0.f);
   for (int64_t i = g0; i < N; i += gs) {
     float s[3];
     group_neighbour_sum<true>(nb_ptr, nbr, g, i, gl, s);
@@ -592,6 +610,17 @@ __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __res
     const float uv[3] = {u4.x, u4.y, u4.z};
     mat3_acc(C, true, uv, s);
     out[i] = make_float4(s[0], s[1], s[2], __ldg(invdeg + i));
+    if (FCG) {
+      const float4 y4 = y[i];
+      const float yv[3] = {y4.x, y4.y, y4.z};
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        t1 = df_add(t1, df_two_prod(sqrtf(dinvf[3 * i + c]) * (yv[c] + s[c]), qold[3 * i + c]));
+    }
+  }
+  if (FCG) {
+    const double b = block_sum_df(t1, sh);
+    if (threadIdx.x == 0) t1part[blockIdx.x] = b;
   }
 }
 
@@ -864,7 +893,7 @@ int mpnn_ensure_infer(Ctx* c) {
   return 0;
 }
 
-void enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v) {
+int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf, const float* qold, double* t1part) {
   const float* P = c->mp->poly;
   const unsigned g = grid_for(c->N * MP_GL, 256);
   float4 *a1 = c->mi + c->N, *a2 = c->mi + 2 * c->N, *u = c->mi + 3 * c->N, *h = c->mi + 4 * c->N,
@@ -875,10 +904,18 @@ void enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v) {
                                                   c->mask, a2, nullptr);
   k_mp_poly_fwd<true><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, a2, y, a1, P, c->mask, u, h);
   // h = C3ᵀu;  g2 = C2ᵀu + Aᵀh;  h = C1ᵀu + Aᵀg2;  v = C0ᵀu + Aᵀh
-  k_mp_poly_adj<<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 2, g2);
-  k_mp_poly_adj<<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, g2, u, P, 1, h);
-  k_mp_poly_adj<<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 0, v);
+  k_mp_poly_adj<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 2, g2, nullptr, nullptr,
+                                                  nullptr, nullptr);
+  k_mp_poly_adj<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, g2, u, P, 1, h, nullptr, nullptr,
+                                                  nullptr, nullptr);
+  if (t1part)
+    k_mp_poly_adj<true><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 0, v, y, dinvf, qold,
+                                                   t1part);
+  else
+    k_mp_poly_adj<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 0, v, nullptr,
+                                                    nullptr, nullptr, nullptr);
   c->launches += 6;
+  return (int)g;
 }
 
 // forward, loss and gradient for B pairs (y, sq [B][N][3], den [B]); the

@@ -362,7 +362,7 @@ void enqueue_axpy(Ctx* c, int64_t n, double a, const double* x, double* y) {
 // r) the explicit orthogonalisation against the previous direction keeps the
 // recursion consistent; the learned preconditioner is symmetric positive
 // definite, for which FCG is PCG.  part regions: [0,G) tile p·q, [3G,4G)
-// boundary p·q, [G,2G) z·q then r·r, [2G,3G) p·r.
+// boundary p·q, [G,2G) r·r, [2G,3G) p·r, and the β terms of JFEM_PART_*.
 // ---------------------------------------------------------------------------
 // y = mask ⊙ D^{-1/2} r (FP32), the network input, one float4 per node
 __global__ void __launch_bounds__(256) k_fcg_input(int64_t N, const float2* __restrict__ r,
@@ -381,69 +381,72 @@ __global__ void __launch_bounds__(256) k_fcg_input(int64_t N, const float2* __re
   }
 }
 
-// z = D^{-1/2}(y + NᵀN y) (NN; y, v = NᵀN y given) or z = D⁻¹r (Jacobi), plus
-// the coarse correction P Ec when COARSE (two-level); z·q_old partials → the
-// last block forms β = z·q_old / p_old·q_old (0 on restart)
-template <bool NN, bool COARSE>
-__global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_z(int64_t n, const float4* __restrict__ y,
-                                                            const float4* __restrict__ v,
-                                                            const float2* __restrict__ r,
-                                                            const float* __restrict__ dinv,
-                                                            const uint8_t* __restrict__ mask,
-                                                            const float* __restrict__ qold,
-                                                            const int* __restrict__ node_agg,
-                                                            const float4* __restrict__ d32,
-                                                            const float* __restrict__ Ec,
-                                                            SolverScalars* __restrict__ sc, float* __restrict__ z,
-                                                            double* __restrict__ part) {
+// β = z·q_old / p_old·q_old (0 on restart) from its two parts, formed before z
+// exists: Σ S(r)·q_old (the smoother's part; partials from the update kernel for
+// Jacobi, from the network's last pass otherwise) and Ec·Pᵀq_old (the coarse
+// part; partials from the coarse solve), each summed in a fixed order.
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_beta(SolverScalars* __restrict__ sc,
+                                                               const double* __restrict__ t1, int n1,
+                                                               const double* __restrict__ t2, int n2) {
   __shared__ double sh[32];
   if (sc->done[0]) return;
-  float2 dot = make_float2(0.f, 0.f);
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = q / 3;
-    const int cc = (int)(q % 3);
-    const bool fr = !((mask[i] >> cc) & 1);
-    float zq;
-    if (NN) {
-      const float* yf = reinterpret_cast<const float*>(y);
-      const float* vf = reinterpret_cast<const float*>(v);
-      zq = sqrtf(dinv[q]) * (yf[4 * i + cc] + vf[4 * i + cc]);
-    } else {
-      const float2 rq = r[q];
-      zq = dinv[q] * (rq.x + rq.y);
-    }
-    if (COARSE) zq += coarse_prolong(node_agg, d32, Ec, i, cc);
-    zq = fr ? zq : 0.f;
-    z[q] = zq;
-    dot = df_add(dot, df_two_prod(zq, qold[q]));
-  }
-  const double b = block_sum_df(dot, sh);
-  if (threadIdx.x == 0) part[G_ + blockIdx.x] = b;
-  if (arrive_last(&sc->arrive[2])) {
-    const double zq = reduce_partials_cg(part + G_, G_, sh);
-    if (threadIdx.x == 0) {
-      const double beta = sc->restart ? 0.0 : zq / sc->pAp;
-      sc->beta = beta;
-      sc->beta_df = df_from_double(beta);
-      sc->restart = 0;
-      sc->arrive[2] = 0;
-    }
+  const double a = reduce_partials_cg(t1, n1, sh);
+  const double b = t2 ? reduce_partials_cg(t2, n2, sh) : 0.0;
+  if (threadIdx.x == 0) {
+    const double beta = sc->restart ? 0.0 : (a + b) / sc->pAp;
+    sc->beta = beta;
+    sc->beta_df = df_from_double(beta);
+    sc->restart = 0;
   }
 }
 
-__global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_p(int64_t n, const float* __restrict__ z,
-                                                            float2* __restrict__ p, const float2* __restrict__ r,
-                                                            SolverScalars* __restrict__ sc, double* __restrict__ part) {
+// p = z − βp with z formed on the fly, node by node: z = D^{-1/2}(y + NᵀN y)
+// (NN; y, v = NᵀN y given) or D⁻¹r (Jacobi), plus the coarse correction P Ec
+// when COARSE, zero on prescribed DOFs (D⁻¹ is zero there).  p·r partials →
+// the last block leaves p·r for α.
+template <bool NN, bool COARSE>
+__global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_zp(int64_t N, const float4* __restrict__ y,
+                                                             const float4* __restrict__ v,
+                                                             const float* __restrict__ dinv,
+                                                             const uint8_t* __restrict__ mask,
+                                                             const int* __restrict__ node_agg,
+                                                             const float4* __restrict__ d32,
+                                                             const float* __restrict__ Ec, float2* __restrict__ p,
+                                                             const float2* __restrict__ r,
+                                                             SolverScalars* __restrict__ sc, double* __restrict__ part) {
   __shared__ double sh[32];
   if (sc->done[0]) return;
   const float2 nb = df_neg(sc->beta_df);
   const bool keep = sc->beta != 0.0;
   float2 dot = make_float2(0.f, 0.f);
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    float2 pi = make_float2(z[i], 0.f);
-    if (keep) pi = df_add(pi, df_mul(nb, p[i]));
-    p[i] = pi;
-    dot = df_add(dot, df_mul(pi, r[i]));
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    float zc[3];
+    if (NN) {
+      const float4 y4 = y[i], v4 = v[i];
+      zc[0] = sqrtf(dinv[3 * i]) * (y4.x + v4.x);
+      zc[1] = sqrtf(dinv[3 * i + 1]) * (y4.y + v4.y);
+      zc[2] = sqrtf(dinv[3 * i + 2]) * (y4.z + v4.z);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float2 rq = r[3 * i + c];
+        zc[c] = dinv[3 * i + c] * (rq.x + rq.y);
+      }
+    }
+    if (COARSE) {
+      const uint8_t m = mask[i];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        if (!((m >> c) & 1)) zc[c] += coarse_prolong(node_agg, d32, Ec, i, c);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int64_t q = 3 * i + c;
+      float2 pi = make_float2(zc[c], 0.f);
+      if (keep) pi = df_add(pi, df_mul(nb, p[q]));
+      p[q] = pi;
+      dot = df_add(dot, df_mul(pi, r[q]));
+    }
   }
   const double b = block_sum_df(dot, sh);
   if (threadIdx.x == 0) part[2 * G_ + blockIdx.x] = b;
@@ -456,23 +459,32 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_p(int64_t n, const flo
   }
 }
 
+// x += αp, r −= αq; r·r partials → the last block updates the scalars and the
+// stop flag.  T1 (Jacobi smoother): also Σ D⁻¹r·q partials for the next β.
+template <bool T1>
 __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_update(int64_t n, SolverScalars* __restrict__ sc,
                                                                  float2* __restrict__ x, float2* __restrict__ r,
                                                                  const float2* __restrict__ p,
                                                                  const float* __restrict__ q,
+                                                                 const float* __restrict__ dinv,
                                                                  double* __restrict__ part) {
   __shared__ double sh[32];
   if (sc->done[0]) return;
   const float2 a = sc->alpha_df, na = df_neg(a);
-  float2 rr = make_float2(0.f, 0.f);
+  float2 rr = make_float2(0.f, 0.f), t1 = make_float2(0.f, 0.f);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     x[i] = df_add(x[i], df_mul(a, p[i]));
-    const float2 ri = df_add(r[i], df_mul_f(na, q[i]));
+    const float qi = q[i];
+    const float2 ri = df_add(r[i], df_mul_f(na, qi));
     r[i] = ri;
     rr = df_add(rr, df_mul(ri, ri));
+    if (T1) t1 = df_add(t1, df_two_prod(dinv[i] * (ri.x + ri.y), qi));
   }
-  const double rrb = block_sum_df(rr, sh);
-  if (threadIdx.x == 0) part[G_ + blockIdx.x] = rrb;
+  const double2 bs = block_sum2_df(rr, t1, sh);
+  if (threadIdx.x == 0) {
+    part[G_ + blockIdx.x] = bs.x;
+    if (T1) part[JFEM_PART_T1 + blockIdx.x] = bs.y;
+  }
   if (arrive_last(&sc->arrive[1])) {
     const double rr_new = reduce_partials_cg(part + G_, G_, sh);
     if (threadIdx.x == 0) {
@@ -486,17 +498,24 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_update(int64_t n, Solv
   }
 }
 
-// r·r → part[G..2G) for a (re)start
+// r·r → part[G..2G) for a (re)start, and Σ D⁻¹r·q_old partials (the Jacobi β term
+// for a kept direction)
 __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_norms(int64_t n, const float2* __restrict__ r,
+                                                                const float* __restrict__ dinv,
+                                                                const float* __restrict__ qold,
                                                                 double* __restrict__ part) {
   __shared__ double sh[32];
-  float2 rr = make_float2(0.f, 0.f);
+  float2 rr = make_float2(0.f, 0.f), t1 = make_float2(0.f, 0.f);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 ri = r[i];
     rr = df_add(rr, df_mul(ri, ri));
+    t1 = df_add(t1, df_two_prod(dinv[i] * (ri.x + ri.y), qold[i]));
   }
-  const double rrb = block_sum_df(rr, sh);
-  if (threadIdx.x == 0) part[G_ + blockIdx.x] = rrb;
+  const double2 bs = block_sum2_df(rr, t1, sh);
+  if (threadIdx.x == 0) {
+    part[G_ + blockIdx.x] = bs.x;
+    part[JFEM_PART_T1 + blockIdx.x] = bs.y;
+  }
 }
 
 __global__ void k_fcg_reset(SolverScalars* __restrict__ sc, const double* __restrict__ part, int set_bb, double tol,
@@ -552,37 +571,47 @@ static int true_residual(Ctx* c, const double* f, const double* xv, double* r, d
   return read_norms(c, rr_out, drift2);
 }
 
+// One flexible-CG iteration: [coarse: restriction of r and q_old, coarse solve]
+// [network: input, 6 neighbour passes] β; p = z − βp (z formed in place);
+// q = K p (tiled apply, α); x, r update.
 static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
   const int64_t n = 3 * c->N;
-  if (coarse) enqueue_coarse_restrict_solve(c, c->rd, &c->sc->done[0]);
+  double* t2 = coarse ? c->part + JFEM_PART_T2 : nullptr;
+  if (coarse) enqueue_coarse_restrict_solve(c, c->rd, &c->sc->done[0], c->Apf, t2);
+  const int n2 = coarse ? coarse_gemv_blocks(c) : 0;
   const int* na = coarse ? c->node_agg : nullptr;
   const float4* d32 = coarse ? c->node_d32 : nullptr;
   const float* Ec = coarse ? c->Ec : nullptr;
+  float4* y = c->mi;
+  float4* v = c->mi ? c->mi + 6 * c->N : nullptr;
   if (nn) {
-    float4* y = c->mi;
-    float4* v = c->mi + 6 * c->N;
     k_fcg_input<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, y);
-    enqueue_mpnn_spd(c, y, v);
+    const int n1 = enqueue_mpnn_spd(c, y, v, c->dinvf, c->Apf, c->part + JFEM_PART_T1N);
+    k_fcg_beta<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part + JFEM_PART_T1N, n1, t2, n2);
     if (coarse)
-      k_fcg_z<true, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, y, v, c->rd, c->dinvf, c->mask, c->Apf, na, d32,
-                                                                  Ec, c->sc, c->zf, c->part);
+      k_fcg_zp<true, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, y, v, c->dinvf, c->mask, na, d32, Ec, c->p2,
+                                                                   c->rd, c->sc, c->part);
     else
-      k_fcg_z<true, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, y, v, c->rd, c->dinvf, c->mask, c->Apf, na,
-                                                                   d32, Ec, c->sc, c->zf, c->part);
-    c->launches += 2;
+      k_fcg_zp<true, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, y, v, c->dinvf, c->mask, na, d32, Ec, c->p2,
+                                                                    c->rd, c->sc, c->part);
   } else {
+    k_fcg_beta<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part + JFEM_PART_T1, G_, t2, n2);
     if (coarse)
-      k_fcg_z<false, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, nullptr, nullptr, c->rd, c->dinvf, c->mask,
-                                                                   c->Apf, na, d32, Ec, c->sc, c->zf, c->part);
+      k_fcg_zp<false, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, nullptr, nullptr, c->dinvf, c->mask, na, d32,
+                                                                    Ec, c->p2, c->rd, c->sc, c->part);
     else
-      k_fcg_z<false, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, nullptr, nullptr, c->rd, c->dinvf, c->mask,
-                                                                    c->Apf, na, d32, Ec, c->sc, c->zf, c->part);
-    c->launches += 1;
+      k_fcg_zp<false, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, nullptr, nullptr, c->dinvf, c->mask, na,
+                                                                     d32, Ec, c->p2, c->rd, c->sc, c->part);
   }
-  k_fcg_p<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->zf, c->p2, c->rd, c->sc, c->part);
+  c->launches += nn ? 3 : 2;
   enqueue_apply_tiled(c, c->p2, c->Apf, true, c->part, &c->sc->done[0], c->sc);
-  k_fcg_update<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->xd, c->rd, c->p2, c->Apf, c->part);
-  c->launches += 2;
+  if (nn)
+    k_fcg_update<false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->xd, c->rd, c->p2, c->Apf, c->dinvf,
+                                                                c->part);
+  else
+    k_fcg_update<true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->xd, c->rd, c->p2, c->Apf, c->dinvf,
+                                                               c->part);
+  c->launches += 1;
 }
 
 static void enqueue_iteration(Ctx* c, bool fp32, int slot) {
@@ -813,7 +842,6 @@ static int fcg(Ctx* c, const double* f, bool nn, bool coarse, double tol, int ma
   if (nn && (rc = mpnn_refresh_poly(c))) return rc;
   if (coarse && (rc = coarse_prepare(c))) return rc;
   const auto kind_of = [&]() { return (nn ? 3 : 2) + (coarse ? 2 : 0); };
-  if (!c->zf && (rc = dalloc(c, &c->zf, (size_t)n))) return rc;
   if (x_zero) {
     k_residual<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, f, 1.0, nullptr, c->mask, c->r, 0, c->part);
     c->launches += 1;
@@ -826,7 +854,7 @@ static int fcg(Ctx* c, const double* f, bool nn, bool coarse, double tol, int ma
   cudaMemsetAsync(c->xd, 0, n * sizeof(float2), c->stream);
   cudaMemsetAsync(c->Apf, 0, n * sizeof(float), c->stream);
   k_df_from_double<<<gv, 256, 0, c->stream>>>(n, c->r, c->rd);
-  k_fcg_norms<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->rd, c->part);
+  k_fcg_norms<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->rd, c->dinvf, c->Apf, c->part);
   k_fcg_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 1, tol, max_iter, 1, 1);
   c->launches += 4;
   if ((rc = read_scalars(c))) return rc;
@@ -904,7 +932,7 @@ static int fcg(Ctx* c, const double* f, bool nn, bool coarse, double tol, int ma
       rec_best_it = iters;
       const int restart = (!finite || switch_jacobi || !(drift2 < 0.01 * rr_t)) ? 1 : 0;
       k_df_from_double<<<gv, 256, 0, c->stream>>>(n, c->r, c->rd);
-      k_fcg_norms<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->rd, c->part);
+      k_fcg_norms<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->rd, c->dinvf, c->Apf, c->part);
       k_fcg_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 0, tol, max_iter, 0, restart);
       c->launches += 3;
       if ((rc = read_scalars(c))) return rc;

@@ -197,7 +197,9 @@ def test_newton_neo_hookean_cube_16_against_oracle(jfem, orc, gpu_ctx_factory):
     u within 1e-8."""
     w = jfem.workloads.cube_compression(n=16, steps=10, top_uz=-0.1)
     d = np.load(GOLDEN / "hex8_neohookean_16.npz")
-    assert np.array_equal(d["E"], w.E)
+    # the fixture's E (np.exp may differ in the last bit between host architectures)
+    assert np.abs(d["E"] - w.E).max() <= 1e-14 * np.abs(w.E).max()
+    w.E = d["E"]
     with gpu_ctx_factory(w) as ctx:
         u, st, rc = ctx.solve(method=2, precision=1, tol=1e-10, newton_tol=1e-10, max_newton=30,
                               max_cg_per_newton=20000, n_load_steps=10, max_iter=200000)
