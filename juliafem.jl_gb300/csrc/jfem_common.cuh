@@ -28,11 +28,11 @@
 // Reduction partials (doubles) of the solvers: [0, 4G) the PCG/FCG dot products;
 // then the flexible-CG β terms: Σ D⁻¹r·q_old per reduction block, Σ
 // D^{-1/2}(y + v)·q_old per block of the network's last neighbour pass (its grid
-// is capped at 152·64 = 9,728 blocks), and Ec·Pᵀq_old per coarse-solve block
+// is capped at JFEM_RED_BLOCKS), and Ec·Pᵀq_old per coarse-solve block
 // (≤ 4,096 rows / 8 per block).
 #define JFEM_PART_T1 (4 * JFEM_RED_BLOCKS)
 #define JFEM_PART_T1N (5 * JFEM_RED_BLOCKS)
-#define JFEM_PART_T2 (5 * JFEM_RED_BLOCKS + 10240)
+#define JFEM_PART_T2 (6 * JFEM_RED_BLOCKS)
 #define JFEM_PART_SIZE (JFEM_PART_T2 + 512)
 #define JFEM_TILE 256             // elements per tile of the shared-memory apply
 #define JFEM_TILE_CTAS 3          // resident CTAs per SM the small-strain tile kernel is compiled for

@@ -895,7 +895,9 @@ int mpnn_ensure_infer(Ctx* c) {
 
 int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf, const float* qold, double* t1part) {
   const float* P = c->mp->poly;
-  const unsigned g = grid_for(c->N * MP_GL, 256);
+  // a resident grid (8 CTAs of 256 per SM) striding over the nodes; its block
+  // partials are what flexible CG's β sums
+  const unsigned g = grid_for(c->N * MP_GL, 256, JFEM_RED_BLOCKS);
   float4 *a1 = c->mi + c->N, *a2 = c->mi + 2 * c->N, *u = c->mi + 3 * c->N, *h = c->mi + 4 * c->N,
          *g2 = c->mi + 5 * c->N;
   k_mp_poly_fwd<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, y, nullptr, nullptr, P, c->mask,
