@@ -654,19 +654,27 @@ def run_gpu(args):
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                 "gpu_launches": int(launches),
                 "clocks": clk}
+        def leg(key, fn):
+            """An extra leg after the timed region; a failure is recorded in the
+            line (with its message) instead of losing the headline."""
+            try:
+                line[key] = fn()
+            except Exception as e:   # noqa: BLE001
+                line[key] = {"error": f"{type(e).__name__}: {e}"}
+
         if ws == 1 and not args.no_newton:
-            line["newton"] = newton_leg(jfem, args, local)
+            leg("newton", lambda: newton_leg(jfem, args, local))
         if ws == 1 and not args.no_batch:
-            line["batched"] = batch_leg(jfem, args, local)
+            leg("batched", lambda: batch_leg(jfem, args, local))
         if ws == 1 and not args.no_learned:
-            line["learned_preconditioner_family"] = family_eval(jfem, args, local, W)
+            leg("learned_preconditioner_family", lambda: family_eval(jfem, args, local, W))
         if ws == 1 and not args.no_oracle_full:
-            line["oracle_full"] = oracle_full_leg(jfem, w, u_headline, local)
+            leg("oracle_full", lambda: oracle_full_leg(jfem, w, u_headline, local))
         if ws == 1 and not args.no_cpu_baseline:
             cb = cpu_sample(jfem, args.size, args.cpu_sample_div, args.cpu_sample_iters)
             line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "assembly_s", "pcg_s",
                                                        "scipy_pcg_s")}
-            if "oracle_full" in line:   # the same run measured in full, and the sample's extrapolation error
+            if "measured_full_s" in line.get("oracle_full", {}):   # the same run measured in full
                 full = line["oracle_full"]["measured_full_s"]
                 line["cpu_baseline"]["measured_full_s"] = full
                 line["cpu_baseline"]["extrapolation_error"] = (cb["value"] - full) / full

@@ -286,19 +286,14 @@ __global__ void __launch_bounds__(256) k_gj_update(double* __restrict__ A, int l
 // ---------------------------------------------------------------------------
 // per-iteration kernels
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double warp_sum_d(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
 
 // Restriction Pᵀ r: for aggregate a, Σ_{i ∈ a} φ_k(d_i) · r_i — force (k < 3) and
 // moment (k ≥ 3) resultants of r about the centroid (r is zero on prescribed
 // DOFs) — and, when qold is given, the same for flexible CG's previous q (FP32).
 // Each aggregate's node list is cut into chunks of at most CR_CHUNK nodes, one
-// CTA per chunk (FP32 per thread, FP64 across the CTA, fixed order); the chunk
-// partials go to cpart[chunk][12] (r: 0..5, q_old: 6..11) and the coarse solve
-// sums them.
+// CTA per chunk (FP32 per thread and warp, FP64 across warps, fixed order); the
+// chunk partials go to cpart[chunk][12] (r: 0..5, q_old: 6..11) and the coarse
+// solve sums them.
 #define CR_CHUNK 1024
 __device__ __forceinline__ void add_resultants(float s[6], float4 d, float fx, float fy, float fz) {
   s[0] += fx;
@@ -350,11 +345,15 @@ __global__ void __launch_bounds__(256) k_coarse_restrict(int n_chunks, const int
     add_resultants(s, dv[u], rv[u][0].x + rv[u][0].y, rv[u][1].x + rv[u][1].y, rv[u][2].x + rv[u][2].y);
     if (qold) add_resultants(s + 6, dv[u], qv[u][0], qv[u][1], qv[u][2]);
   }
+  // FP32 warp trees (GB300's FP64 pipe would make a 32-lane FP64 tree the
+  // kernel's bottleneck), FP64 across the block's warps
 #pragma unroll
   for (int k = 0; k < 12; ++k) {
     if (k < nk) {   // nk is the same for the whole block
-      const double v = warp_sum_d((double)s[k]);
-      if (lane == 0) sh[wid][k] = v;
+      float v = s[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) sh[wid][k] = (double)v;
     }
   }
   __syncthreads();
@@ -401,6 +400,7 @@ __global__ void __launch_bounds__(256) k_coarse_gemv(int nc, int ld, const float
     const float4* a = reinterpret_cast<const float4*>(Ainv + (int64_t)row * ld);
     const float4* x = reinterpret_cast<const float4*>(R);
     float s = 0.f;
+#pragma unroll 4
     for (int j = lane; j < ld / 4; j += 32) {
       const float4 av = a[j], xv = x[j];
       s = fmaf(av.x, xv.x, s);
