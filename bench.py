@@ -67,6 +67,9 @@ def parse():
     p.add_argument("--no-newton", action="store_true", help="skip the Newton–Krylov leg")
     p.add_argument("--newton-n", type=int, default=128, help="Hex8 cells per side of the Newton cube")
     p.add_argument("--batch-count", type=int, default=256)
+    p.add_argument("--profile-solve", choices=["learned", "two_level", "jacobi"], default=None,
+                   help="profiling aid: one solve of the workload between cudaProfilerStart/Stop "
+                        "(after two warm solves; the network gets seeded random weights), no JSON line")
     return p.parse_args()
 
 
@@ -686,10 +689,41 @@ def run_gpu(args):
     return 0
 
 
+def profile_solve(args):
+    """One solve of the workload between cudaProfilerStart and cudaProfilerStop,
+    for `ncu --profile-from-start off`: the launch list and the kernel captures
+    in profiles/ come from this."""
+    import torch
+    import jfem_loader
+    jfem = jfem_loader.load_package()
+    from jfem_gb300 import build as _b
+    _b.build()
+    abi = jfem._abi
+    method = {"learned": abi.FCG_LEARNED, "two_level": abi.FCG_TWO_LEVEL, "jacobi": abi.PCG_JACOBI}[args.profile_solve]
+    w = jfem.workloads.cfg_tet10_cantilever(*args.size)
+    with setup_ctx(jfem, w, 0) as ctx:
+        ctx.set_coarse_space(-1)
+        ctx.mpnn_init(3)
+        o = jfem.default_opts(method=method, precision=abi.MIXED, tol=TOL, max_iter=500000)
+        ctx.solve(o)
+        ctx.solve(o)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        _, st, rc = ctx.solve(o)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        info = ctx.coarse_info() if method != abi.PCG_JACOBI else None
+    print(f"{args.profile_solve}: {st.cg_iterations} iterations, {st.refinements} refinements, status {rc}, "
+          f"{st.solve_time_s:.4f} s, coarse (aggregates, dofs, elements, set-up ms) {info}", flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_solve:
+        return profile_solve(args)
     return run_gpu(args)
 
 

@@ -22,7 +22,9 @@
 // offsets X_i − c_a, and the list of elements whose A_c contribution is not
 // zero — an element whose nodes all lie in one aggregate with no prescribed DOF
 // moves rigidly under every mode of that aggregate, so K_e P_e = 0 there.
-// Per geometry generation (material, coordinates) on the device, FP64:
+// Per geometry generation (material, coordinates) on the device, in
+// double-float (48-bit, on the FP32 pipe — GB300's FP64 pipe is far slower; the
+// physical gradients come from the FP64 geometry records):
 //   k_coarse_elem    one warp per listed element: the strain of each mode at
 //                    each integration point and the 6×6 blocks
 //                    Σ_q w_q (λ tr ε_a tr ε_b + 2μ ε_a : ε_b) for every pair
@@ -43,22 +45,29 @@
 #include <vector>
 
 #include "jfem_common.cuh"
+#include "jfem_df.cuh"
 
 namespace jfem {
 
 #define CG_MAXN 10   // node slots per element in celem_aggs (Tet10 has the most nodes)
 
 // ---------------------------------------------------------------------------
-// A_c contributions (FP64)
+// A_c contributions (double-float on the FP32 pipe: GB300's FP64 pipe runs at a
+// small fraction of its FP32 rate; the physical gradients start from the FP64
+// geometry records and every product after them is double-float, 48-bit)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void mode_vector(int k, double dx, double dy, double dz, double v[3]) {
+__device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ float2 df_zero() { return make_float2(0.f, 0.f); }
+
+// component c of mode k at offset d (translations, then e_x × d, e_y × d, e_z × d)
+__device__ __forceinline__ float2 mode_component(int k, int c, const float2 d[3]) {
   switch (k) {
-    case 0: v[0] = 1.0; v[1] = 0.0; v[2] = 0.0; break;
-    case 1: v[0] = 0.0; v[1] = 1.0; v[2] = 0.0; break;
-    case 2: v[0] = 0.0; v[1] = 0.0; v[2] = 1.0; break;
-    case 3: v[0] = 0.0; v[1] = -dz; v[2] = dy; break;    // e_x × d
-    case 4: v[0] = dz; v[1] = 0.0; v[2] = -dx; break;    // e_y × d
-    default: v[0] = -dy; v[1] = dx; v[2] = 0.0; break;   // e_z × d
+    case 0: return make_float2(c == 0 ? 1.f : 0.f, 0.f);
+    case 1: return make_float2(c == 1 ? 1.f : 0.f, 0.f);
+    case 2: return make_float2(c == 2 ? 1.f : 0.f, 0.f);
+    case 3: return c == 0 ? df_zero() : c == 1 ? df_neg(d[2]) : d[1];
+    case 4: return c == 0 ? d[2] : c == 1 ? df_zero() : df_neg(d[0]);
+    default: return c == 0 ? df_neg(d[1]) : c == 1 ? d[0] : df_zero();
   }
 }
 
@@ -68,16 +77,16 @@ __global__ void __launch_bounds__(64) k_coarse_elem(int64_t n_celem, const int* 
                                                     const int64_t* __restrict__ celem_off, int64_t E,
                                                     const int* __restrict__ conn, const uint8_t* __restrict__ mask,
                                                     const int* __restrict__ node_agg,
-                                                    const double* __restrict__ node_d,
+                                                    const float2* __restrict__ node_d,
                                                     const double* __restrict__ geo, int affine,
-                                                    double* __restrict__ contrib) {
+                                                    float2* __restrict__ contrib) {
   constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ, NC = 6 * NN;
-  __shared__ double s_d[2][NN][3];
+  __shared__ float2 s_d[2][NN][3];
   __shared__ int s_al[2][NN];
   __shared__ unsigned s_m[2][NN];
-  __shared__ double s_gN[2][NQ][NN][3];
-  __shared__ double s_S[2][NQ][NC][6];
-  __shared__ double s_lw[2][NQ], s_mw[2][NQ];
+  __shared__ float2 s_gN[2][NQ][NN][3];
+  __shared__ float2 s_S[2][NQ][NC][6];
+  __shared__ float2 s_lw[2][NQ], s_mw[2][NQ];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int64_t k = (int64_t)blockIdx.x * 2 + w; k < n_celem; k += (int64_t)gridDim.x * 2) {
     const int64_t e = celem[k];
@@ -94,7 +103,8 @@ __global__ void __launch_bounds__(64) k_coarse_elem(int64_t n_celem, const int* 
 #pragma unroll
       for (int b = 0; b < 3; ++b) s_d[w][lane][b] = node_d[3 * (int64_t)n + b];
     }
-    // physical gradients ∇N_i(q) = J⁻ᵀ dN_i(q) and the weights w_q λ detJ, w_q μ detJ
+    // physical gradients ∇N_i(q) = J⁻ᵀ dN_i(q) (FP64 from the records, then rounded
+    // to double-float) and the weights w_q λ detJ, w_q μ detJ
     for (int t = lane; t < NQ * NN; t += 32) {
       const int q = t / NN, i = t % NN;
       const int64_t base = affine ? 0 : 10 * q;
@@ -103,122 +113,141 @@ __global__ void __launch_bounds__(64) k_coarse_elem(int64_t n_celem, const int* 
         double s = 0.0;
 #pragma unroll
         for (int a = 0; a < 3; ++a) s += geo[(base + 3 * d + a) * E + e] * dshape(ET, q, i, a);
-        s_gN[w][q][i][d] = s;
+        s_gN[w][q][i][d] = df_from_double(s);
       }
     }
     if (lane < NQ) {
       const int q = lane;
       const double wq = qp_weight(ET, q);
+      double lw, mw;
       if (affine) {
-        s_lw[w][q] = wq * geo[9 * E + e];
-        s_mw[w][q] = wq * geo[10 * E + e];
+        lw = wq * geo[9 * E + e];
+        mw = wq * geo[10 * E + e];
       } else {
         const double det = geo[(int64_t)(10 * q + 9) * E + e];
-        s_lw[w][q] = wq * det * geo[(int64_t)(10 * NQ) * E + e];
-        s_mw[w][q] = wq * det * geo[(int64_t)(10 * NQ + 1) * E + e];
+        lw = wq * det * geo[(int64_t)(10 * NQ) * E + e];
+        mw = wq * det * geo[(int64_t)(10 * NQ + 1) * E + e];
       }
+      s_lw[w][q] = df_from_double(lw);
+      s_mw[w][q] = df_from_double(2.0 * mw);   // 2μ, the factor of ε:ε
     }
     __syncwarp();
     // strain (xx, yy, zz, xy, yz, xz) of every mode column (aggregate α, mode k) at every q
     const int ncol = 6 * A;
     for (int t = lane; t < NQ * ncol; t += 32) {
       const int q = t / ncol, col = t % ncol, alpha = col / 6, km = col % 6;
-      double G[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+      float2 G[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) G[c][d] = df_zero();
       for (int i = 0; i < NN; ++i) {
         if (s_al[w][i] != alpha) continue;
-        double v[3];
-        mode_vector(km, s_d[w][i][0], s_d[w][i][1], s_d[w][i][2], v);
         const unsigned m = s_m[w][i];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          const double vc = ((m >> c) & 1u) ? 0.0 : v[c];
+          if ((m >> c) & 1u) continue;
+          const float2 vc = mode_component(km, c, s_d[w][i]);
+          if (km < 3) {   // a translation: vc is 0 or 1
+            if (vc.x != 0.f)
 #pragma unroll
-          for (int d = 0; d < 3; ++d) G[c][d] += vc * s_gN[w][q][i][d];
+              for (int d = 0; d < 3; ++d) G[c][d] = df_add(G[c][d], s_gN[w][q][i][d]);
+          } else {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) G[c][d] = df_add(G[c][d], df_mul(vc, s_gN[w][q][i][d]));
+          }
         }
       }
-      double* S = s_S[w][q][col];
+      float2* S = s_S[w][q][col];
+      const float2 half = make_float2(0.5f, 0.f);
       S[0] = G[0][0];
       S[1] = G[1][1];
       S[2] = G[2][2];
-      S[3] = 0.5 * (G[0][1] + G[1][0]);
-      S[4] = 0.5 * (G[1][2] + G[2][1]);
-      S[5] = 0.5 * (G[0][2] + G[2][0]);
+      S[3] = df_mul(half, df_add(G[0][1], G[1][0]));
+      S[4] = df_mul(half, df_add(G[1][2], G[2][1]));
+      S[5] = df_mul(half, df_add(G[0][2], G[2][0]));
     }
     __syncwarp();
-    // blocks (α, β): entry (k, l) = Σ_q λ_q tr ε_αk tr ε_βl + 2 μ_q ε_αk : ε_βl.  The expression
-    // is symmetric in its two operands, so block (β, α) is exactly the transpose of (α, β).
+    // blocks (α, β): entry (k, l) = Σ_q λ_q tr ε_αk tr ε_βl + 2μ_q ε_αk : ε_βl, formed once
+    // per unordered column pair and written to both (α, β)[k][l] and (β, α)[l][k], so
+    // the assembled A_c is exactly symmetric
     const int64_t off = celem_off[k];
     for (int t = lane; t < ncol * ncol; t += 32) {
       const int ca = t / ncol, cb = t % ncol;
-      double s = 0.0;
+      if (cb < ca) continue;
+      float2 s = df_zero();
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
-        const double* a = s_S[w][q][ca];
-        const double* b = s_S[w][q][cb];
-        const double tra = a[0] + a[1] + a[2], trb = b[0] + b[1] + b[2];
-        const double dd = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
-        const double od = a[3] * b[3] + a[4] * b[4] + a[5] * b[5];
-        s += s_lw[w][q] * (tra * trb) + 2.0 * s_mw[w][q] * (dd + 2.0 * od);
+        const float2* a = s_S[w][q][ca];
+        const float2* b = s_S[w][q][cb];
+        const float2 tra = df_add(df_add(a[0], a[1]), a[2]), trb = df_add(df_add(b[0], b[1]), b[2]);
+        const float2 dd = df_add(df_add(df_mul(a[0], b[0]), df_mul(a[1], b[1])), df_mul(a[2], b[2]));
+        const float2 od = df_add(df_add(df_mul(a[3], b[3]), df_mul(a[4], b[4])), df_mul(a[5], b[5]));
+        s = df_add(s, df_mul(s_lw[w][q], df_mul(tra, trb)));
+        s = df_add(s, df_mul(s_mw[w][q], df_add(dd, df_add(od, od))));
       }
       const int alpha = ca / 6, beta = cb / 6;
       contrib[(off + alpha * A + beta) * 36 + 6 * (ca % 6) + (cb % 6)] = s;
+      if (ca != cb) contrib[(off + beta * A + alpha) * 36 + 6 * (cb % 6) + (ca % 6)] = s;
     }
     __syncwarp();
   }
 }
 
-// A_c block (a, b) = Σ of its element blocks, ascending element order
+// A_c block (a, b) = Σ of its element blocks, ascending element order (double-float)
 __global__ void k_coarse_reduce(int64_t n_cblk, const int* __restrict__ cblk_ab, const int* __restrict__ cblk_ptr,
-                                const int64_t* __restrict__ cblk_src, const double* __restrict__ contrib, int ld,
-                                double* __restrict__ Ac) {
+                                const int64_t* __restrict__ cblk_src, const float2* __restrict__ contrib, int ld,
+                                float2* __restrict__ Ac) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n_cblk * 36;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = t / 36;
     const int ent = (int)(t % 36);
-    double s = 0.0;
-    for (int p = cblk_ptr[b]; p < cblk_ptr[b + 1]; ++p) s += contrib[cblk_src[p] * 36 + ent];
+    float2 s = df_zero();
+    for (int p = cblk_ptr[b]; p < cblk_ptr[b + 1]; ++p) s = df_add(s, contrib[cblk_src[p] * 36 + ent]);
     const int ra = cblk_ab[2 * b], cb = cblk_ab[2 * b + 1];
     Ac[(int64_t)(6 * ra + ent / 6) * ld + 6 * cb + ent % 6] = s;
   }
 }
 
-__global__ void k_diag_copy(int n, int ld, const double* __restrict__ A, double* __restrict__ d) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) d[i] = A[(int64_t)i * ld + i];
+__global__ void k_diag_copy(int n, int ld, const float2* __restrict__ A, double* __restrict__ d) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    d[i] = df_to_double(A[(int64_t)i * ld + i]);
 }
 
-__global__ void k_round_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+__global__ void k_round_f32(int64_t n, const float2* __restrict__ a, float* __restrict__ b) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
+    b[i] = __fadd_rn(a[i].x, a[i].y);
 }
 
 // ---------------------------------------------------------------------------
-// blocked Gauss–Jordan inversion (FP64, in place; A symmetric positive definite)
-// Per pivot block K with P = A_KK⁻¹:  A_IJ −= A_IK P A_KJ,  A_KJ ← P A_KJ,
-// A_IK ← −A_IK P,  A_KK ← P  (I, J ≠ K).  After the last block A holds A⁻¹.
+// blocked Gauss–Jordan inversion (double-float, in place; A symmetric positive
+// definite).  Per pivot block K with P = A_KK⁻¹:  A_IJ −= A_IK P A_KJ,
+// A_KJ ← P A_KJ,  A_IK ← −A_IK P,  A_KK ← P  (I, J ≠ K).  After the last block A
+// holds A⁻¹.  Each pivot's reciprocal is formed in FP64 by one thread.
 // ---------------------------------------------------------------------------
 #define GJ_B 32
 
-__global__ void __launch_bounds__(1024) k_gj_pivot(const double* __restrict__ A, int ld, int K0,
-                                                   const double* __restrict__ diag0, double* __restrict__ P) {
-  __shared__ double B[GJ_B][GJ_B + 1];
-  __shared__ double prow[GJ_B], pcol[GJ_B];
-  __shared__ double pinv;
+__global__ void __launch_bounds__(1024) k_gj_pivot(const float2* __restrict__ A, int ld, int K0,
+                                                   const double* __restrict__ diag0, float2* __restrict__ P) {
+  __shared__ float2 B[GJ_B][GJ_B + 1];
+  __shared__ float2 prow[GJ_B], pcol[GJ_B];
+  __shared__ float2 pinv;
   const int i = threadIdx.y, j = threadIdx.x;
   B[i][j] = A[(int64_t)(K0 + i) * ld + K0 + j];
   __syncthreads();
   for (int k = 0; k < GJ_B; ++k) {
     if (i == 0 && j == 0) {
-      const double piv = B[k][k], d0 = diag0[K0 + k];
-      pinv = (d0 > 0.0 && piv > 1e-12 * d0) ? 1.0 / piv : 0.0;   // else: drop this mode
+      const double piv = df_to_double(B[k][k]), d0 = diag0[K0 + k];
+      pinv = (d0 > 0.0 && piv > 1e-12 * d0) ? df_from_double(1.0 / piv) : df_zero();   // else: drop this mode
     }
     if (i == 0) prow[j] = B[k][j];
     if (j == 0) pcol[i] = B[i][k];
     __syncthreads();
-    const double p = pinv;
-    double v = B[i][j];
-    if (i != k && j != k) v -= pcol[i] * prow[j] * p;
-    else if (i == k && j != k) v = prow[j] * p;
-    else if (i != k) v = -pcol[i] * p;
+    const float2 p = pinv;
+    float2 v = B[i][j];
+    if (i != k && j != k) v = df_sub(v, df_mul(df_mul(pcol[i], prow[j]), p));
+    else if (i == k && j != k) v = df_mul(prow[j], p);
+    else if (i != k) v = df_neg(df_mul(pcol[i], p));
     else v = p;
     B[i][j] = v;
     __syncthreads();
@@ -227,10 +256,10 @@ __global__ void __launch_bounds__(1024) k_gj_pivot(const double* __restrict__ A,
 }
 
 // row panel Brow[:, J] = P A_KJ and a copy of the old column panel Ccol[J, :] = A_JK
-__global__ void __launch_bounds__(256) k_gj_panel(const double* __restrict__ A, int ld, int Kb,
-                                                  const double* __restrict__ P, double* __restrict__ Brow,
-                                                  double* __restrict__ Ccol) {
-  __shared__ double sP[GJ_B][GJ_B + 1], sA[GJ_B][GJ_B + 1];
+__global__ void __launch_bounds__(256) k_gj_panel(const float2* __restrict__ A, int ld, int Kb,
+                                                  const float2* __restrict__ P, float2* __restrict__ Brow,
+                                                  float2* __restrict__ Ccol) {
+  __shared__ float2 sP[GJ_B][GJ_B + 1], sA[GJ_B][GJ_B + 1];
   const int J = blockIdx.x;
   if (J == Kb) return;
   const int K0 = Kb * GJ_B, J0 = J * GJ_B;
@@ -243,18 +272,18 @@ __global__ void __launch_bounds__(256) k_gj_panel(const double* __restrict__ A, 
   __syncthreads();
   for (int t = threadIdx.x; t < GJ_B * GJ_B; t += blockDim.x) {
     const int r = t / GJ_B, q = t % GJ_B;
-    double s = 0.0;
+    float2 s = df_zero();
 #pragma unroll 8
-    for (int k = 0; k < GJ_B; ++k) s += sP[r][k] * sA[k][q];
+    for (int k = 0; k < GJ_B; ++k) s = df_add(s, df_mul(sP[r][k], sA[k][q]));
     Brow[(int64_t)r * ld + J0 + q] = s;
   }
 }
 
 // every block of A; each CTA writes only its own block and reads only the panels
-__global__ void __launch_bounds__(256) k_gj_update(double* __restrict__ A, int ld, int Kb,
-                                                   const double* __restrict__ P, const double* __restrict__ Brow,
-                                                   const double* __restrict__ Ccol) {
-  __shared__ double sC[GJ_B][GJ_B + 1], sB[GJ_B][GJ_B + 1];
+__global__ void __launch_bounds__(256) k_gj_update(float2* __restrict__ A, int ld, int Kb,
+                                                   const float2* __restrict__ P, const float2* __restrict__ Brow,
+                                                   const float2* __restrict__ Ccol) {
+  __shared__ float2 sC[GJ_B][GJ_B + 1], sB[GJ_B][GJ_B + 1];
   const int I = blockIdx.y, J = blockIdx.x;
   const int I0 = I * GJ_B, J0 = J * GJ_B;
   if (I == Kb && J == Kb) {
@@ -275,11 +304,11 @@ __global__ void __launch_bounds__(256) k_gj_update(double* __restrict__ A, int l
   __syncthreads();
   for (int t = threadIdx.x; t < GJ_B * GJ_B; t += blockDim.x) {
     const int r = t / GJ_B, q = t % GJ_B;
-    double s = 0.0;
+    float2 s = df_zero();
 #pragma unroll 8
-    for (int k = 0; k < GJ_B; ++k) s += sC[r][k] * sB[k][q];
-    double* a = A + (int64_t)(I0 + r) * ld + J0 + q;
-    *a = (J == Kb) ? -s : *a - s;
+    for (int k = 0; k < GJ_B; ++k) s = df_add(s, df_mul(sC[r][k], sB[k][q]));
+    float2* a = A + (int64_t)(I0 + r) * ld + J0 + q;
+    *a = (J == Kb) ? df_neg(s) : df_sub(*a, s);
   }
 }
 
@@ -534,13 +563,16 @@ static int coarse_build(Ctx* c, int target_nc) {
     const double cnt = (double)(agg_ptr[(size_t)a + 1] - agg_ptr[(size_t)a]);
     for (int d = 0; d < 3; ++d) cen[3 * (size_t)a + d] = s[d] / cnt;
   }
-  std::vector<double> d64((size_t)(3 * N));
+  std::vector<float2> ddf((size_t)(3 * N));
   std::vector<float4> d32((size_t)N);
   for (int64_t i = 0; i < N; ++i) {
     const int a = node_agg[(size_t)i];
-    for (int d = 0; d < 3; ++d) d64[3 * (size_t)i + d] = X[3 * (size_t)i + d] - cen[3 * (size_t)a + d];
-    d32[(size_t)i] = make_float4((float)d64[3 * (size_t)i], (float)d64[3 * (size_t)i + 1],
-                                 (float)d64[3 * (size_t)i + 2], 0.f);
+    double dv[3];
+    for (int d = 0; d < 3; ++d) {
+      dv[d] = X[3 * (size_t)i + d] - cen[3 * (size_t)a + d];
+      ddf[3 * (size_t)i + d] = df_from_double(dv[d]);
+    }
+    d32[(size_t)i] = make_float4((float)dv[0], (float)dv[1], (float)dv[2], 0.f);
   }
   // elements with a nonzero contribution, their aggregates and contribution blocks
   std::vector<int> celem, celem_aggs;
@@ -603,7 +635,7 @@ static int coarse_build(Ctx* c, int target_nc) {
     c->pcg_graph = nullptr;
     c->pcg_graph_key = -1;
   }
-  void* old[] = {c->agg_ptr, c->agg_nodes, c->node_agg, c->node_d32, c->node_d64, c->celem, c->celem_aggs,
+  void* old[] = {c->agg_ptr, c->agg_nodes, c->node_agg, c->node_d32, c->node_ddf, c->celem, c->celem_aggs,
                  c->celem_off, c->contrib, c->cblk_ab, c->cblk_ptr, c->cblk_src, c->Ac, c->Ac_diag, c->gj_buf,
                  c->Ainv32, c->Ec, c->chunk_begin, c->agg_chunk_ptr, c->cpart};
   for (void* p : old) dfree(c, p);
@@ -617,7 +649,7 @@ static int coarse_build(Ctx* c, int target_nc) {
   c->n_chunks = n_chunks;
   if ((rc = dalloc(c, &c->agg_ptr, (size_t)nagg + 1)) || (rc = dalloc(c, &c->agg_nodes, (size_t)N)) ||
       (rc = dalloc(c, &c->node_agg, (size_t)N)) || (rc = dalloc(c, &c->node_d32, (size_t)N)) ||
-      (rc = dalloc(c, &c->node_d64, (size_t)(3 * N))) || (rc = dalloc(c, &c->celem, (size_t)n_celem)) ||
+      (rc = dalloc(c, &c->node_ddf, (size_t)(3 * N))) || (rc = dalloc(c, &c->celem, (size_t)n_celem)) ||
       (rc = dalloc(c, &c->celem_aggs, (size_t)n_celem * CG_MAXN)) ||
       (rc = dalloc(c, &c->celem_off, (size_t)n_celem)) || (rc = dalloc(c, &c->contrib, (size_t)n_contrib * 36)) ||
       (rc = dalloc(c, &c->cblk_ab, (size_t)(2 * n_cblk))) || (rc = dalloc(c, &c->cblk_ptr, (size_t)n_cblk + 1)) ||
@@ -635,7 +667,7 @@ static int coarse_build(Ctx* c, int target_nc) {
   up(c->agg_nodes, agg_nodes.data(), agg_nodes.size() * sizeof(int));
   up(c->node_agg, node_agg.data(), node_agg.size() * sizeof(int));
   up(c->node_d32, d32.data(), d32.size() * sizeof(float4));
-  up(c->node_d64, d64.data(), d64.size() * sizeof(double));
+  up(c->node_ddf, ddf.data(), ddf.size() * sizeof(float2));
   up(c->celem, celem.data(), celem.size() * sizeof(int));
   up(c->celem_aggs, celem_aggs.data(), celem_aggs.size() * sizeof(int));
   up(c->celem_off, celem_off.data(), celem_off.size() * sizeof(int64_t));
@@ -659,7 +691,7 @@ template <int ET>
 static void launch_coarse_elem(Ctx* c) {
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((c->n_celem + 1) / 2, 152LL * 64));
   k_coarse_elem<ET><<<g, 64, 0, c->stream>>>(c->n_celem, c->celem, c->celem_aggs, c->celem_off, c->E, c->conn,
-                                             c->mask, c->node_agg, c->node_d64, c->geo64, c->geo_affine ? 1 : 0,
+                                             c->mask, c->node_agg, c->node_ddf, c->geo64, c->geo_affine ? 1 : 0,
                                              c->contrib);
 }
 
@@ -673,7 +705,7 @@ static int coarse_assemble(Ctx* c) {
     }
     c->launches += 1;
   }
-  cudaMemsetAsync(c->Ac, 0, (size_t)c->nc_pad * c->nc_pad * sizeof(double), c->stream);
+  cudaMemsetAsync(c->Ac, 0, (size_t)c->nc_pad * c->nc_pad * sizeof(float2), c->stream);
   if (c->n_cblk > 0) {
     k_coarse_reduce<<<grid_for(c->n_cblk * 36, 256), 256, 0, c->stream>>>(c->n_cblk, c->cblk_ab, c->cblk_ptr,
                                                                           c->cblk_src, c->contrib, c->nc_pad, c->Ac);
@@ -692,9 +724,9 @@ static int coarse_values(Ctx* c) {
   const int n = c->nc_pad, nbk = n / GJ_B;
   k_diag_copy<<<grid_for(n, 256), 256, 0, c->stream>>>(n, n, c->Ac, c->Ac_diag);
   c->launches += 1;
-  double* P = c->gj_buf;
-  double* Brow = P + GJ_B * GJ_B;
-  double* Ccol = Brow + (size_t)GJ_B * n;
+  float2* P = c->gj_buf;
+  float2* Brow = P + GJ_B * GJ_B;
+  float2* Ccol = Brow + (size_t)GJ_B * n;
   for (int kb = 0; kb < nbk; ++kb) {
     k_gj_pivot<<<1, dim3(GJ_B, GJ_B), 0, c->stream>>>(c->Ac, n, kb * GJ_B, c->Ac_diag, P);
     k_gj_panel<<<nbk, 256, 0, c->stream>>>(c->Ac, n, kb, P, Brow, Ccol);
@@ -754,13 +786,18 @@ int coarse_matrix(Ctx* c, double* Ac_h, int* node_agg_h) {
   int rc = coarse_prepare(c);
   if (rc) return rc;
   if (node_agg_h) cudaMemcpyAsync(node_agg_h, c->node_agg, c->N * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  std::vector<float2> tmp;
   if (Ac_h) {
     coarse_assemble(c);   // overwrites the inverse: recomputed by the next coarse_prepare
     c->coarse_geo_gen = 0;
-    cudaMemcpy2DAsync(Ac_h, (size_t)c->nc * sizeof(double), c->Ac, (size_t)c->nc_pad * sizeof(double),
-                      (size_t)c->nc * sizeof(double), (size_t)c->nc, cudaMemcpyDeviceToHost, c->stream);
+    tmp.resize((size_t)c->nc * c->nc);
+    cudaMemcpy2DAsync(tmp.data(), (size_t)c->nc * sizeof(float2), c->Ac, (size_t)c->nc_pad * sizeof(float2),
+                      (size_t)c->nc * sizeof(float2), (size_t)c->nc, cudaMemcpyDeviceToHost, c->stream);
   }
-  return sync_and_check(c, "coarse matrix download");
+  const int rc2 = sync_and_check(c, "coarse matrix download");
+  if (rc2) return rc2;
+  for (size_t k = 0; k < tmp.size(); ++k) Ac_h[k] = df_to_double(tmp[k]);
+  return 0;
 }
 
 int coarse_precondition(Ctx* c, const double* r_h, double* z_h) {

@@ -406,20 +406,20 @@ struct Ctx {
   int* agg_nodes = nullptr;     // [N]
   int* node_agg = nullptr;      // [N] aggregate of each node
   float4* node_d32 = nullptr;   // [N] X_i − centroid of its aggregate (FP32; w unused)
-  double* node_d64 = nullptr;   // [N][3] the same in FP64 (coarse matrix)
+  float2* node_ddf = nullptr;   // [N][3] the same in double-float (coarse matrix)
   int64_t n_celem = 0;          // elements whose A_c contribution is not zero
   int* celem = nullptr;         // [n_celem] element ids, ascending
   int* celem_aggs = nullptr;    // [n_celem][10] distinct aggregates of the element, ascending, −1 padded
   int64_t* celem_off = nullptr; // [n_celem] first contribution block of the element (A_e² blocks)
   int64_t n_contrib = 0;
-  double* contrib = nullptr;    // [n_contrib][36] 6×6 element blocks of A_c (FP64)
+  float2* contrib = nullptr;    // [n_contrib][36] 6×6 element blocks of A_c (double-float)
   int64_t n_cblk = 0;           // nonzero 6×6 blocks of A_c
   int* cblk_ab = nullptr;       // [n_cblk][2] (row aggregate, column aggregate)
   int* cblk_ptr = nullptr;      // [n_cblk+1] into cblk_src
   int64_t* cblk_src = nullptr;  // contribution blocks of each A_c block, ascending element
-  double* Ac = nullptr;         // [nc_pad][nc_pad] A_c, inverted in place (FP64)
+  float2* Ac = nullptr;         // [nc_pad][nc_pad] A_c, inverted in place (double-float)
   double* Ac_diag = nullptr;    // [nc_pad] diagonal of A_c before the inversion
-  double* gj_buf = nullptr;     // Gauss–Jordan panels: P (32×32), row panel, old column panel
+  float2* gj_buf = nullptr;     // Gauss–Jordan panels: P (32×32), row panel, old column panel
   float* Ainv32 = nullptr;      // [nc_pad][nc_pad] A_c⁻¹ rounded to FP32 (the per-iteration coarse solve)
   int n_chunks = 0;             // restriction chunks (≤ 1,024 nodes of one aggregate each)
   int* chunk_begin = nullptr;   // [n_chunks+1] into agg_nodes

@@ -1,5 +1,5 @@
 """Two-level preconditioner (jfem_coarse.cu) through the C ABI against the
-numpy/scipy restatement in oracle/coarse_oracle.py: the aggregation, the FP64
+numpy/scipy restatement in oracle/coarse_oracle.py: the aggregation, the double-float
 coarse matrix A_c = Pᵀ K P (≤ 1e-12 relative; K from the oracle's FP64
 assembly), the preconditioner z = D⁻¹r + P A_c⁻¹ Pᵀ r applied by the solver's
 kernels (FP32 coarse solve), and flexible CG with it: the displacement of the
