@@ -15,6 +15,7 @@
 // sparse() sums the COO duplicates — with no atomics, and element matrices are
 // never written to HBM.
 #include "jfem_common.cuh"
+#include "jfem_df.cuh"
 
 namespace jfem {
 
@@ -34,16 +35,16 @@ struct QD {
   static constexpr int SIZE = P + 9;
 };
 
-// Integration-point record of the isotropic small-strain scatter: the factors
-// every lane of a block column would otherwise recompute.
+// Integration-point record of the isotropic small-strain scatter, in
+// double-float pairs (the scatter runs on the FP32 pipe; GB300's FP64 pipe is a
+// small fraction of it): the physical gradients and the point's weights.
 template <int ET>
 struct QDI {
   static constexpr int NN = Elem<ET>::NN;
-  static constexpr int G = 0;                 // ∇N         [NN][3]
-  static constexpr int SL = 3 * NN;           // w·λ·∇N     [NN][3]
-  static constexpr int SM = 6 * NN;           // w·μ·∇N     [NN][3]
-  static constexpr int GR = 9 * NN;           // w·μ·∇N_a·∇N_b [NN][NN]
-  static constexpr int W = GR + NN * NN;      // w·detJ
+  static constexpr int G = 0;                 // ∇N   [NN][3]
+  static constexpr int WL = 3 * NN;           // w·λ
+  static constexpr int WM = WL + 1;           // w·μ
+  static constexpr int W = WM + 1;            // w·detJ
   static constexpr int P = W + 1;             // σ [3][3] (P = σ for small strain)
   static constexpr int SIZE = P + 9;
 };
@@ -169,27 +170,20 @@ __global__ void __launch_bounds__(128) k_qpoint64(int64_t E, const int* __restri
     const int rc = material64(model, finite != 0, lam_e[e], mu_e[e], gu, F, S6, D);
     if (rc) raise_error(err, rc);
     if constexpr (ISO) {
+      float2* o2 = reinterpret_cast<float2*>(qd) + t * RSIZE;
       const double w = qp_weight(ET, q) * det;
-      const double wl = w * lam_e[e], wm = w * mu_e[e];
 #pragma unroll
       for (int i = 0; i < NN; ++i)
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          out[LI::G + 3 * i + a] = g[i][a];
-          out[LI::SL + 3 * i + a] = wl * g[i][a];
-          out[LI::SM + 3 * i + a] = wm * g[i][a];
-        }
-#pragma unroll
-      for (int a = 0; a < NN; ++a)
-#pragma unroll
-        for (int b = 0; b < NN; ++b)
-          out[LI::GR + NN * a + b] = wm * (g[a][0] * g[b][0] + g[a][1] * g[b][1] + g[a][2] * g[b][2]);
-      out[LI::W] = w;
+        for (int a = 0; a < 3; ++a) o2[LI::G + 3 * i + a] = df_from_double(g[i][a]);
+      o2[LI::WL] = df_from_double(w * lam_e[e]);
+      o2[LI::WM] = df_from_double(w * mu_e[e]);
+      o2[LI::W] = df_from_double(w);
       const int vi[6] = {0, 1, 2, 0, 1, 0}, vj[6] = {0, 1, 2, 1, 2, 2};   // Voigt order (c_VI, c_VJ)
 #pragma unroll
       for (int I = 0; I < 6; ++I) {
-        out[LI::P + 3 * vi[I] + vj[I]] = S6[I];
-        out[LI::P + 3 * vj[I] + vi[I]] = S6[I];
+        o2[LI::P + 3 * vi[I] + vj[I]] = df_from_double(S6[I]);
+        o2[LI::P + 3 * vj[I] + vi[I]] = df_from_double(S6[I]);
       }
       continue;
     }
@@ -227,9 +221,10 @@ __device__ __forceinline__ void bl_column(const double F[9], const double g[3], 
 // ISO (small strain, Hooke; QDI records): the block is formed from its closed
 // form
 //   (B_bᵢ)ᵀ 𝔻 B_aₖ = λ ∇N_b,i ∇N_a,k + μ ∇N_a,i ∇N_b,k + μ δ_ik ∇N_a·∇N_b
-// with w·λ·∇N, w·μ·∇N and w·μ·∇N_a·∇N_b precomputed per integration point:
-// 7 FP64 operations per lane and point instead of the ≈105 of the general
-// BL(F)ᵀ 𝔻 BL(F) product; equal to it up to rounding.
+// in double-float on the FP32 pipe (products ≤ 5u², sums ≤ 3u², u = 2⁻²⁴:
+// ≈ 1e-14 relative to the entry's terms) with a double-float accumulator, then
+// rounded to FP64 once per entry; the general path (finite strain, geometric
+// stiffness) forms BL(F)ᵀ 𝔻 BL(F) in FP64.
 template <int ET, bool ISO>
 __global__ void k_scatter64(int64_t N, int64_t E, const int* __restrict__ conn,
                             const int* __restrict__ adj_ptr, const unsigned* __restrict__ adj,
@@ -244,40 +239,61 @@ __global__ void k_scatter64(int64_t N, int64_t E, const int* __restrict__ conn,
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   double* acc = smem + (size_t)wib * 9 * dmax;
+  float2* acc2 = reinterpret_cast<float2*>(acc);   // ISO: the same bytes as double-float pairs
   const int b = lane / 3, i = lane - 3 * (lane / 3);
   const bool active = lane < 3 * NN;
   for (int64_t J = (int64_t)blockIdx.x * wpb + wib; J < N; J += (int64_t)gridDim.x * wpb) {
     const int d = nb_ptr[J + 1] - nb_ptr[J];
-    for (int k = lane; k < 9 * d; k += 32) acc[k] = 0.0;
+    if constexpr (ISO) {
+      for (int k = lane; k < 9 * d; k += 32) acc2[k] = make_float2(0.f, 0.f);
+    } else {
+      for (int k = lane; k < 9 * d; k += 32) acc[k] = 0.0;
+    }
     __syncwarp();
     double fa = 0.0;
+    float2 fa2 = make_float2(0.f, 0.f);
     for (int t = adj_ptr[J]; t < adj_ptr[J + 1]; ++t) {
       const unsigned pk = adj[t];
       const int64_t e = pk >> 4;
       const int a = (int)(pk & 15u);
-      double K0 = 0.0, K1 = 0.0, K2 = 0.0;
       if constexpr (ISO) {
-        double Kc = 0.0;   // the μ δ_ik ∇N_a·∇N_b term, added to component i below
+        float2 K0 = make_float2(0.f, 0.f), K1 = K0, K2 = K0, Kc = K0;   // Kc: the μ δ_ik ∇N_a·∇N_b term
+        const float2* recs = reinterpret_cast<const float2*>(qd) + e * NQ * LI::SIZE;
+#pragma unroll
         for (int q = 0; q < NQ; ++q) {
-          const double* rec = qd + (e * NQ + q) * LI::SIZE;
-          const double ga0 = rec[LI::G + 3 * a], ga1 = rec[LI::G + 3 * a + 1], ga2 = rec[LI::G + 3 * a + 2];
+          const float2* rec = recs + q * LI::SIZE;
+          const float2 ga0 = rec[LI::G + 3 * a], ga1 = rec[LI::G + 3 * a + 1], ga2 = rec[LI::G + 3 * a + 2];
           if (active) {
-            const double gb0 = rec[LI::G + 3 * b], gb1 = rec[LI::G + 3 * b + 1], gb2 = rec[LI::G + 3 * b + 2];
-            const double A = rec[LI::SL + 3 * b + i], B = rec[LI::SM + 3 * a + i];
-            K0 += A * ga0 + B * gb0;
-            K1 += A * ga1 + B * gb1;
-            K2 += A * ga2 + B * gb2;
-            Kc += rec[LI::GR + NN * a + b];
+            const float2 gb0 = rec[LI::G + 3 * b], gb1 = rec[LI::G + 3 * b + 1], gb2 = rec[LI::G + 3 * b + 2];
+            const float2 wm = rec[LI::WM];
+            const float2 A = df_mul(rec[LI::WL], i == 0 ? gb0 : i == 1 ? gb1 : gb2);   // w λ ∇N_b,i
+            const float2 B = df_mul(wm, i == 0 ? ga0 : i == 1 ? ga1 : ga2);             // w μ ∇N_a,i
+            K0 = df_add(K0, df_add(df_mul(A, ga0), df_mul(B, gb0)));
+            K1 = df_add(K1, df_add(df_mul(A, ga1), df_mul(B, gb1)));
+            K2 = df_add(K2, df_add(df_mul(A, ga2), df_mul(B, gb2)));
+            const float2 dot = df_add(df_add(df_mul(ga0, gb0), df_mul(ga1, gb1)), df_mul(ga2, gb2));
+            Kc = df_add(Kc, df_mul(wm, dot));
           }
-          if (lane < 3) {
-            const double* P = rec + LI::P;
-            fa += rec[LI::W] * (P[3 * lane] * ga0 + P[3 * lane + 1] * ga1 + P[3 * lane + 2] * ga2);
+          if (fint && lane < 3) {
+            const float2* P = rec + LI::P + 3 * lane;
+            const float2 pg = df_add(df_add(df_mul(P[0], ga0), df_mul(P[1], ga1)), df_mul(P[2], ga2));
+            fa2 = df_add(fa2, df_mul(rec[LI::W], pg));
           }
         }
-        if (i == 0) K0 += Kc;
-        else if (i == 1) K1 += Kc;
-        else K2 += Kc;
+        if (active) {
+          if (i == 0) K0 = df_add(K0, Kc);
+          else if (i == 1) K1 = df_add(K1, Kc);
+          else K2 = df_add(K2, Kc);
+          const int s = slot[(int64_t)t * NN + b];
+          float2* a0 = acc2 + 3 * s + i;
+          a0[0] = df_add(a0[0], K0);
+          a0[3 * d] = df_add(a0[3 * d], K1);
+          a0[6 * d] = df_add(a0[6 * d], K2);
+        }
+        __syncwarp();
+        continue;
       } else {
+      double K0 = 0.0, K1 = 0.0, K2 = 0.0;
       for (int q = 0; q < NQ; ++q) {
         const double* rec = qd + (e * NQ + q) * L::SIZE;
         const double w = rec[L::W];
@@ -324,7 +340,6 @@ __global__ void k_scatter64(int64_t N, int64_t E, const int* __restrict__ conn,
           fa += w * (P[3 * lane] * ga[0] + P[3 * lane + 1] * ga[1] + P[3 * lane + 2] * ga[2]);
         }
       }
-      }   // general path
       if (active) {
         const int s = slot[(int64_t)t * NN + b];
         acc[0 * 3 * d + 3 * s + i] += K0;
@@ -332,12 +347,17 @@ __global__ void k_scatter64(int64_t N, int64_t E, const int* __restrict__ conn,
         acc[2 * 3 * d + 3 * s + i] += K2;
       }
       __syncwarp();
+      }   // general path
     }
     if (nzval) {
       double* out = nzval + 9 * (int64_t)nb_ptr[J];
-      for (int k = lane; k < 9 * d; k += 32) out[k] = acc[k];
+      if constexpr (ISO) {
+        for (int k = lane; k < 9 * d; k += 32) out[k] = df_to_double(acc2[k]);
+      } else {
+        for (int k = lane; k < 9 * d; k += 32) out[k] = acc[k];
+      }
     }
-    if (fint && lane < 3) fint[3 * J + lane] = fa;
+    if (fint && lane < 3) fint[3 * J + lane] = ISO ? df_to_double(fa2) : fa;
     __syncwarp();
   }
 }
@@ -481,7 +501,7 @@ static bool iso_assembly(const Ctx* c) { return !c->finite && !c->geom && c->mod
 
 template <int ET>
 static size_t qpoint_bytes(const Ctx* c) {
-  return (size_t)c->E * Elem<ET>::NQ * (iso_assembly(c) ? QDI<ET>::SIZE : QD<ET>::SIZE) * sizeof(double);
+  return (size_t)c->E * Elem<ET>::NQ * (iso_assembly(c) ? QDI<ET>::SIZE : QD<ET>::SIZE) * sizeof(double);   // float2 pairs: 8 B too
 }
 
 // The two assembly launches: integration-point records → qd, then the
