@@ -27,12 +27,9 @@ namespace jfem {
 void launch_apply_tet4(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in, const int* stop);
 void launch_apply_tet10(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in, const int* stop);
 void launch_apply_hex8(Ctx* c, bool fp32, int mode, const double* v, const float2* v2, bool mask_in, const int* stop);
-void launch_tile_tet4(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop,
-                      SolverScalars* sc);
-void launch_tile_tet10(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop,
-                      SolverScalars* sc);
-void launch_tile_hex8(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop,
-                      SolverScalars* sc);
+void launch_tile_tet4(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop);
+void launch_tile_tet10(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop);
+void launch_tile_hex8(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop);
 void nh_state_tet4(Ctx* c);
 void nh_state_tet10(Ctx* c);
 void nh_state_hex8(Ctx* c);
@@ -207,22 +204,29 @@ __global__ void k_split(int64_t n, const double* __restrict__ v, float2* __restr
 }
 
 // Boundary nodes of the tiled apply: sum the tile partials in ascending tile
-// order into y (FP32), masked.  Launched with G = JFEM_RED_BLOCKS blocks.  Each
-// thread takes BND_ROUNDS nodes (k, k + stride, …) and issues their loads in
-// two waves (node and run offsets; then the first BND_UNROLL partials of each
-// run and the mask byte), so a thread waits for about two memory latencies;
-// runs longer than BND_UNROLL (nodes shared by more tiles) finish in a loop.
-// The solvers do not launch it: their vector updates form the same sums, in
-// the same order, where they read q (tile_q in jfem_common.cuh).
+// order into y (FP32); optional v·y partials (double-float products, v the
+// split input) into part[3G + blockIdx.x].  With sc (mixed PCG), the last block
+// to finish forms p·Ap = Σ part[0..G) + Σ part[3G..4G) in FP64, in index order,
+// and α = r·z / p·Ap for the update kernel.  Launched with G = JFEM_RED_BLOCKS
+// blocks.  Each thread takes BND_ROUNDS nodes (k, k + stride, …) and issues
+// their loads in two waves (node and run offsets; then the first BND_UNROLL
+// partials of each run, the mask byte and v), so a thread waits for about two
+// memory latencies; runs longer than BND_UNROLL (nodes shared by more tiles)
+// finish in a loop.
 constexpr int BND_ROUNDS = 1;
 constexpr int BND_UNROLL = 4;
+
 __global__ void __launch_bounds__(JFEM_RED_THREADS, 4) k_tile_boundary(int64_t nb, const int* __restrict__ bnodes,
                                                                     const int* __restrict__ bptr,
                                                                     const float4* __restrict__ bpart,
                                                                     const uint8_t* __restrict__ mask, int masked,
-                                                                    float* __restrict__ y,
+                                                                    const float2* __restrict__ vdot,
+                                                                    float* __restrict__ y, double* __restrict__ part,
+                                                                    SolverScalars* __restrict__ sc,
                                                                     const int* __restrict__ stop) {
+  __shared__ double sh[32];
   if (stop && *stop) return;
+  float2 dot = make_float2(0.f, 0.f);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k0 < nb; k0 += BND_ROUNDS * stride) {
     int g[BND_ROUNDS], i0[BND_ROUNDS], i1[BND_ROUNDS];
@@ -239,6 +243,7 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS, 4) k_tile_boundary(int64_t n
     }
     float4 q[BND_ROUNDS][BND_UNROLL];
     unsigned m[BND_ROUNDS];
+    float2 vv[BND_ROUNDS][3];
 #pragma unroll
     for (int r = 0; r < BND_ROUNDS; ++r) {   // wave 2
       const int64_t k = k0 + r * stride;
@@ -246,6 +251,10 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS, 4) k_tile_boundary(int64_t n
       for (int u = 0; u < BND_UNROLL; ++u)
         q[r][u] = i0[r] + u < i1[r] ? __ldcs(bpart + i0[r] + u) : make_float4(0.f, 0.f, 0.f, 0.f);   // read once
       m[r] = (k < nb && masked) ? (unsigned)__ldg(mask + g[r]) : 0u;
+      if (part && k < nb) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vv[r][c] = __ldg(vdot + 3 * (int64_t)g[r] + c);
+      }
     }
 #pragma unroll
     for (int r = 0; r < BND_ROUNDS; ++r) {
@@ -271,6 +280,26 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS, 4) k_tile_boundary(int64_t n
       y[3 * gg] = s0;
       y[3 * gg + 1] = s1;
       y[3 * gg + 2] = s2;
+      if (part) {
+        dot = df_add(dot, df_mul_f(vv[r][0], s0));
+        dot = df_add(dot, df_mul_f(vv[r][1], s1));
+        dot = df_add(dot, df_mul_f(vv[r][2], s2));
+      }
+    }
+  }
+  if (part) {
+    const double b = block_sum_df(dot, sh);
+    if (threadIdx.x == 0) part[3 * JFEM_RED_BLOCKS + blockIdx.x] = b;
+    if (sc && arrive_last(&sc->arrive[0])) {
+      const double2 ab = reduce_partials2_cg(part, part + 3 * JFEM_RED_BLOCKS, JFEM_RED_BLOCKS, sh);
+      const double pAp = ab.x + ab.y;
+      if (threadIdx.x == 0) {
+        const double a = sc->rz[0] / pAp;
+        sc->pAp = pAp;
+        sc->alpha = a;
+        sc->alpha_df = df_from_double(a);
+        sc->arrive[0] = 0;
+      }
     }
   }
 }
@@ -411,35 +440,28 @@ int nh_state_prepare(Ctx* c) {
   return 0;
 }
 
-static void launch_tiles(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop,
-                         SolverScalars* sc = nullptr) {
+static void launch_tiles(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
   switch (c->et) {
-    case JFEM_TET4: launch_tile_tet4(c, v2, y, masked, part, stop, sc); break;
-    case JFEM_TET10: launch_tile_tet10(c, v2, y, masked, part, stop, sc); break;
-    default: launch_tile_hex8(c, v2, y, masked, part, stop, sc); break;
+    case JFEM_TET4: launch_tile_tet4(c, v2, y, masked, part, stop); break;
+    case JFEM_TET10: launch_tile_tet10(c, v2, y, masked, part, stop); break;
+    default: launch_tile_hex8(c, v2, y, masked, part, stop); break;
   }
 }
 
-static void launch_tile_boundary(Ctx* c, float* y, bool masked, const int* stop) {
-  k_tile_boundary<<<JFEM_RED_BLOCKS, JFEM_RED_THREADS, 0, c->stream>>>(c->n_bnodes, c->bnodes, c->bptr, c->bpart,
-                                                                        c->mask, masked ? 1 : 0, y, stop);
+static void launch_tile_boundary(Ctx* c, const float2* vdot, float* y, bool masked, double* part, const int* stop,
+                                 SolverScalars* sc = nullptr) {
+  k_tile_boundary<<<JFEM_RED_BLOCKS, JFEM_RED_THREADS, 0, c->stream>>>(
+      c->n_bnodes, c->bnodes, c->bptr, c->bpart, c->mask, masked ? 1 : 0, vdot, y, part, sc, stop);
   c->launches += 1;
 }
 
 // Tiled FP32 apply of the split input v2: tile pass + boundary pass, y FP32;
-// v·Kv partials (element quadratic forms) into part[0..G).  With sc: the tile
-// pass also forms α (see k_tile_apply).
+// v·y partials (double-float products) into part[0..G) and part[3G..4G).
+// With sc (mixed PCG): the boundary pass also forms α (see k_tile_boundary).
 void enqueue_apply_tiled(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop,
                          SolverScalars* sc) {
-  launch_tiles(c, v2, y, masked, part, stop, sc);
-  launch_tile_boundary(c, y, masked, stop);
-}
-
-// Tile pass only (masked), v·Kv partials into part[0..G) and α into sc: y holds
-// the interior nodes; the shared nodes' sums are left in bpart for the caller's
-// vector update (tile_q).
-void enqueue_tiles_fused(Ctx* c, const float2* v2, float* y, double* part, const int* stop, SolverScalars* sc) {
-  launch_tiles(c, v2, y, true, part, stop, sc);
+  launch_tiles(c, v2, y, masked, part, stop);
+  launch_tile_boundary(c, v2, y, masked, part, stop, sc);
 }
 
 void enqueue_apply(Ctx* c, const double* v, double* y, bool fp32, bool masked, bool mask_in, double* part,
@@ -520,7 +542,7 @@ int time_apply(Ctx* c, bool fp32, bool masked, int reps, double* ms_elem, double
     if (fp32 && apply_is_tiled(c)) {
       launch_tiles(c, c->p2, c->Apf, masked, c->part, nullptr);
       cudaEventRecord(e1, c->stream);
-      launch_tile_boundary(c, c->Apf, masked, nullptr);
+      launch_tile_boundary(c, c->p2, c->Apf, masked, c->part, nullptr);
     } else {
       launch_elements(c, fp32, 0, c->tmp, fp32 ? c->p2 : nullptr, masked, nullptr);
       cudaEventRecord(e1, c->stream);

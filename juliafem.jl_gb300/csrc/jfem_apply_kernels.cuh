@@ -223,9 +223,6 @@ struct GeoRegs {
 //   dv[i] = v_i − v_0, du[i] = u_i − u_0 (i ≥ 1; index 0 unused).
 //   geo: record source (GeoGlobal / GeoRegs), record k = geo(k).
 //   MODE 0: y = K v (linear) / K_T(u) v (finite); MODE 1: y = f_int(u).
-//   en (MODE 0, optional): the element's quadratic form vᵀK_e v = Σ_q w_q ∇v : P(∇v),
-//   formed from the gradients of the differences dv, so a rigid translation in v
-//   (large next to the deformation as CG converges) never enters the sum.
 // Returns false when the material state is invalid (det C ≤ 0).
 // ---------------------------------------------------------------------------
 struct NoState {
@@ -234,8 +231,7 @@ struct NoState {
 
 template <int ET, typename R, bool AFFINE, int KIN, bool GEOM, int MODE, class GEO, class ST = NoState>
 __device__ __forceinline__ bool element_op(const R (&dv)[Elem<ET>::NN][3], const R (&du)[Elem<ET>::NN][3],
-                                           const GEO& geo, R (&y)[Elem<ET>::NN][3], const ST& st = ST(),
-                                           R* en = nullptr) {
+                                           const GEO& geo, R (&y)[Elem<ET>::NN][3], const ST& st = ST()) {
   constexpr int NN = Elem<ET>::NN, NQ = Elem<ET>::NQ;
   constexpr bool NEED_U = kin_needs_u(KIN);
   constexpr bool NEED_V = (MODE == 0);
@@ -310,14 +306,6 @@ __device__ __forceinline__ bool element_op(const R (&dv)[Elem<ET>::NN][3], const
     }
     // Q[c][a] = w·detJ Σ_d P[c][d] J⁻¹[d][a]   (affine records carry detJ inside λ, μ)
     const R wq = (R)qp_weight(ET, q) * det;
-    if (MODE == 0 && en) {
-      R e = R(0);
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) e += gv[c][d] * P[c][d];
-      *en += wq * e;
-    }
     R Q[3][3];
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -425,12 +413,9 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
 //   wave 2   per node (depends on wave 1): mask byte, v (hi, lo) and u
 // The node gather then loads one output word per node (tout: the global node
 // when interior, −1 − slot when shared), sums its element slots from shared
-// memory and writes y (interior) or bpart[slot] (shared).  Optional v·Kv: the
-// element quadratic forms (element_op's energy, FP32 per element, accumulated
-// in double-float per thread) summed per block into part[blockIdx.x]; with sc
-// the last block to finish sums the partials in index order (FP64) and forms
-// α = (r·z or p·r, sc->rz) / v·Kv for the vector update — so no node sum is
-// needed before α, and the boundary sums can be formed by the update itself.
+// memory and writes y (interior) or bpart[slot] (shared).  Optional v·y
+// partial over interior nodes (double-float, v = hi + lo as staged) into
+// part[blockIdx.x] (FP64).
 // ---------------------------------------------------------------------------
 __host__ __device__ constexpr int tile_sptr_len(int Lmax) { return (Lmax + 8) & ~7; }
 
@@ -466,8 +451,7 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
     const uint16_t* __restrict__ tadj, const int* __restrict__ tout,
     const float2* __restrict__ v2, const double* __restrict__ u,
     const uint8_t* __restrict__ mask, int masked, int Lmax, float* __restrict__ y, float4* __restrict__ bpart,
-    double* __restrict__ part, const float* __restrict__ nhs, int* err, const int* __restrict__ stop,
-    SolverScalars* __restrict__ sc) {
+    double* __restrict__ part, const float* __restrict__ nhs, int* err, const int* __restrict__ stop) {
   constexpr int NN = Elem<ET>::NN;
   constexpr int T = JFEM_TILE;
   constexpr int NADJ = T * NN;   // adjacency entries per tile; NADJ·2 bytes is a multiple of 16
@@ -601,19 +585,15 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
         }
       }
       float yl[NN][3];
-      float en = 0.f;
-      float* enp = part ? &en : nullptr;
       if constexpr (KIN == KIN_NHC) {   // point state cached in tile order: [16·n_q][Epad]
         const GeoGlobal<float> st{nhs + e, Epad};
-        if constexpr (AFFINE)
-          ok &= element_op<ET, float, true, KIN, GEOM, 0>(dv, du, GeoRegs<float>{rec}, yl, st, enp);
-        else ok &= element_op<ET, float, false, KIN, GEOM, 0>(dv, du, GeoGlobal<float>{geo + e, Epad}, yl, st, enp);
+        if constexpr (AFFINE) ok &= element_op<ET, float, true, KIN, GEOM, 0>(dv, du, GeoRegs<float>{rec}, yl, st);
+        else ok &= element_op<ET, float, false, KIN, GEOM, 0>(dv, du, GeoGlobal<float>{geo + e, Epad}, yl, st);
       } else if constexpr (AFFINE) {
-        ok &= element_op<ET, float, true, KIN, GEOM, 0>(dv, du, GeoRegs<float>{rec}, yl, NoState(), enp);
+        ok &= element_op<ET, float, true, KIN, GEOM, 0>(dv, du, GeoRegs<float>{rec}, yl);
       } else {
-        ok &= element_op<ET, float, false, KIN, GEOM, 0>(dv, du, GeoGlobal<float>{geo + e, Epad}, yl, NoState(), enp);
+        ok &= element_op<ET, float, false, KIN, GEOM, 0>(dv, du, GeoGlobal<float>{geo + e, Epad}, yl);
       }
-      if (part) dot = df_add(dot, make_float2(en, 0.f));
 #pragma unroll
       for (int a = 0; a < NN; ++a) {
         yxy[a * T + tid] = make_float2(yl[a][0], yl[a][1]);
@@ -648,6 +628,11 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
           y[3 * g] = s0;
           y[3 * g + 1] = s1;
           y[3 * g + 2] = s2;
+          if (part) {   // v·y in double-float from the staged (masked) v
+            dot = df_add(dot, df_mul_f(vs[3 * j], s0));
+            dot = df_add(dot, df_mul_f(vs[3 * j + 1], s1));
+            dot = df_add(dot, df_mul_f(vs[3 * j + 2], s2));
+          }
         } else {   // shared node: partial sum; the boundary pass applies the mask
           bpart[-1 - o] = make_float4(s0, s1, s2, 0.f);
         }
@@ -665,16 +650,6 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
   if (part) {
     const double b = block_sum_df(dot, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = b;
-    if (sc && arrive_last(&sc->arrive[0])) {
-      const double pAp = reduce_partials_cg(part, (int)gridDim.x, sh);
-      if (threadIdx.x == 0) {
-        const double a = sc->rz[0] / pAp;
-        sc->pAp = pAp;
-        sc->alpha = a;
-        sc->alpha_df = df_from_double(a);
-        sc->arrive[0] = 0;
-      }
-    }
   }
 }
 
@@ -712,8 +687,7 @@ static void dispatch_kin(Ctx* c, const R* geo, const double* v, const float2* v2
 }
 
 template <int ET, bool AFFINE, int KIN, bool GEOM>
-static void launch_tile_k(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop,
-                          SolverScalars* sc) {
+static void launch_tile_k(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
   constexpr int NN = Elem<ET>::NN;
   const size_t sm = tile_smem_bytes<NN, kin_needs_u(KIN), AFFINE>(c->tile_Lmax);
   auto kern = k_tile_apply<ET, AFFINE, KIN, GEOM>;
@@ -721,42 +695,41 @@ static void launch_tile_k(Ctx* c, const float2* v2, float* y, bool masked, doubl
   const unsigned g = JFEM_RED_BLOCKS;   // CTAs take tiles b, b + g, …
   kern<<<g, JFEM_TILE, sm, c->stream>>>(
       c->ntiles, c->E, c->Epad, c->tnode_ptr, c->tnodes, c->tconn, c->geoT32, c->tadj_ptr, c->tadj, c->tout,
-      v2, c->u_state, c->mask, masked ? 1 : 0, c->tile_Lmax, y, c->bpart, part, c->nhstate, c->d_err, stop, sc);
+      v2, c->u_state, c->mask, masked ? 1 : 0, c->tile_Lmax, y, c->bpart, part, c->nhstate, c->d_err, stop);
   c->launches += 1;
 }
 
 // Tiled FP32 element + in-tile gather launch (the boundary sum is a separate kernel).
 template <int ET>
-void launch_tile_et(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop,
-                    SolverScalars* sc) {
+void launch_tile_et(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
   int kin = !c->finite ? KIN_SMALL : (c->model == JFEM_NEO_HOOKEAN ? KIN_NH : KIN_SVK);
   if (kin == KIN_NH && nh_cache_ready(c)) {
     if (c->geo_affine) {
-      if (c->geom) launch_tile_k<ET, true, KIN_NHC, true>(c, v2, y, masked, part, stop, sc);
-      else launch_tile_k<ET, true, KIN_NHC, false>(c, v2, y, masked, part, stop, sc);
+      if (c->geom) launch_tile_k<ET, true, KIN_NHC, true>(c, v2, y, masked, part, stop);
+      else launch_tile_k<ET, true, KIN_NHC, false>(c, v2, y, masked, part, stop);
     } else {
-      if (c->geom) launch_tile_k<ET, false, KIN_NHC, true>(c, v2, y, masked, part, stop, sc);
-      else launch_tile_k<ET, false, KIN_NHC, false>(c, v2, y, masked, part, stop, sc);
+      if (c->geom) launch_tile_k<ET, false, KIN_NHC, true>(c, v2, y, masked, part, stop);
+      else launch_tile_k<ET, false, KIN_NHC, false>(c, v2, y, masked, part, stop);
     }
     return;
   }
   if (c->geo_affine) {
-    if (kin == KIN_SMALL) launch_tile_k<ET, true, KIN_SMALL, false>(c, v2, y, masked, part, stop, sc);
+    if (kin == KIN_SMALL) launch_tile_k<ET, true, KIN_SMALL, false>(c, v2, y, masked, part, stop);
     else if (kin == KIN_SVK) {
-      if (c->geom) launch_tile_k<ET, true, KIN_SVK, true>(c, v2, y, masked, part, stop, sc);
-      else launch_tile_k<ET, true, KIN_SVK, false>(c, v2, y, masked, part, stop, sc);
+      if (c->geom) launch_tile_k<ET, true, KIN_SVK, true>(c, v2, y, masked, part, stop);
+      else launch_tile_k<ET, true, KIN_SVK, false>(c, v2, y, masked, part, stop);
     } else {
-      if (c->geom) launch_tile_k<ET, true, KIN_NH, true>(c, v2, y, masked, part, stop, sc);
-      else launch_tile_k<ET, true, KIN_NH, false>(c, v2, y, masked, part, stop, sc);
+      if (c->geom) launch_tile_k<ET, true, KIN_NH, true>(c, v2, y, masked, part, stop);
+      else launch_tile_k<ET, true, KIN_NH, false>(c, v2, y, masked, part, stop);
     }
   } else {
-    if (kin == KIN_SMALL) launch_tile_k<ET, false, KIN_SMALL, false>(c, v2, y, masked, part, stop, sc);
+    if (kin == KIN_SMALL) launch_tile_k<ET, false, KIN_SMALL, false>(c, v2, y, masked, part, stop);
     else if (kin == KIN_SVK) {
-      if (c->geom) launch_tile_k<ET, false, KIN_SVK, true>(c, v2, y, masked, part, stop, sc);
-      else launch_tile_k<ET, false, KIN_SVK, false>(c, v2, y, masked, part, stop, sc);
+      if (c->geom) launch_tile_k<ET, false, KIN_SVK, true>(c, v2, y, masked, part, stop);
+      else launch_tile_k<ET, false, KIN_SVK, false>(c, v2, y, masked, part, stop);
     } else {
-      if (c->geom) launch_tile_k<ET, false, KIN_NH, true>(c, v2, y, masked, part, stop, sc);
-      else launch_tile_k<ET, false, KIN_NH, false>(c, v2, y, masked, part, stop, sc);
+      if (c->geom) launch_tile_k<ET, false, KIN_NH, true>(c, v2, y, masked, part, stop);
+      else launch_tile_k<ET, false, KIN_NH, false>(c, v2, y, masked, part, stop);
     }
   }
 }

@@ -12,9 +12,8 @@ void launch_apply_tet10(Ctx* c, bool fp32, int mode, const double* v, const floa
   if (fp32) launch_apply_tet10_f32(c, v, v2, mask_in, stop);
   else launch_apply_tet10_f64(c, mode, v, mask_in, stop);
 }
-void launch_tile_tet10(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop,
-                       SolverScalars* sc) {
-  launch_tile_et<JFEM_TET10>(c, v2, y, masked, part, stop, sc);
+void launch_tile_tet10(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop) {
+  launch_tile_et<JFEM_TET10>(c, v2, y, masked, part, stop);
 }
 void nh_state_tet10(Ctx* c) { nh_state_et<JFEM_TET10>(c); }
 }  // namespace jfem

@@ -221,10 +221,11 @@ __device__ __forceinline__ void bl_column(const double F[9], const double g[3], 
 // ISO (small strain, Hooke; QDI records): the block is formed from its closed
 // form
 //   (B_bᵢ)ᵀ 𝔻 B_aₖ = λ ∇N_b,i ∇N_a,k + μ ∇N_a,i ∇N_b,k + μ δ_ik ∇N_a·∇N_b
-// in double-float on the FP32 pipe (products ≤ 5u², sums ≤ 3u², u = 2⁻²⁴:
-// ≈ 1e-14 relative to the entry's terms) with a double-float accumulator, then
-// rounded to FP64 once per entry; the general path (finite strain, geometric
-// stiffness) forms BL(F)ᵀ 𝔻 BL(F) in FP64.
+// in double-float on the FP32 pipe (products within 5u² relative, sums within
+// ≈ 2u² of their terms' magnitudes, u = 2⁻²⁴: ≈ 1e-14 of the entry's terms, far
+// inside the 1e-12 of max |K| that the entries are held to) with a double-float
+// accumulator, then rounded to FP64 once per entry; the general path (finite
+// strain, geometric stiffness) forms BL(F)ᵀ 𝔻 BL(F) in FP64.
 template <int ET, bool ISO>
 __global__ void k_scatter64(int64_t N, int64_t E, const int* __restrict__ conn,
                             const int* __restrict__ adj_ptr, const unsigned* __restrict__ adj,
@@ -268,27 +269,27 @@ __global__ void k_scatter64(int64_t N, int64_t E, const int* __restrict__ conn,
             const float2 wm = rec[LI::WM];
             const float2 A = df_mul(rec[LI::WL], i == 0 ? gb0 : i == 1 ? gb1 : gb2);   // w λ ∇N_b,i
             const float2 B = df_mul(wm, i == 0 ? ga0 : i == 1 ? ga1 : ga2);             // w μ ∇N_a,i
-            K0 = df_add(K0, df_add(df_mul(A, ga0), df_mul(B, gb0)));
-            K1 = df_add(K1, df_add(df_mul(A, ga1), df_mul(B, gb1)));
-            K2 = df_add(K2, df_add(df_mul(A, ga2), df_mul(B, gb2)));
-            const float2 dot = df_add(df_add(df_mul(ga0, gb0), df_mul(ga1, gb1)), df_mul(ga2, gb2));
-            Kc = df_add(Kc, df_mul(wm, dot));
+            K0 = df_add_abs(K0, df_add_abs(df_mul(A, ga0), df_mul(B, gb0)));
+            K1 = df_add_abs(K1, df_add_abs(df_mul(A, ga1), df_mul(B, gb1)));
+            K2 = df_add_abs(K2, df_add_abs(df_mul(A, ga2), df_mul(B, gb2)));
+            const float2 dot = df_add_abs(df_add_abs(df_mul(ga0, gb0), df_mul(ga1, gb1)), df_mul(ga2, gb2));
+            Kc = df_add_abs(Kc, df_mul(wm, dot));
           }
           if (fint && lane < 3) {
             const float2* P = rec + LI::P + 3 * lane;
-            const float2 pg = df_add(df_add(df_mul(P[0], ga0), df_mul(P[1], ga1)), df_mul(P[2], ga2));
-            fa2 = df_add(fa2, df_mul(rec[LI::W], pg));
+            const float2 pg = df_add_abs(df_add_abs(df_mul(P[0], ga0), df_mul(P[1], ga1)), df_mul(P[2], ga2));
+            fa2 = df_add_abs(fa2, df_mul(rec[LI::W], pg));
           }
         }
         if (active) {
-          if (i == 0) K0 = df_add(K0, Kc);
-          else if (i == 1) K1 = df_add(K1, Kc);
-          else K2 = df_add(K2, Kc);
+          if (i == 0) K0 = df_add_abs(K0, Kc);
+          else if (i == 1) K1 = df_add_abs(K1, Kc);
+          else K2 = df_add_abs(K2, Kc);
           const int s = slot[(int64_t)t * NN + b];
           float2* a0 = acc2 + 3 * s + i;
-          a0[0] = df_add(a0[0], K0);
-          a0[3 * d] = df_add(a0[3 * d], K1);
-          a0[6 * d] = df_add(a0[6 * d], K2);
+          a0[0] = df_add_abs(a0[0], K0);
+          a0[3 * d] = df_add_abs(a0[3 * d], K1);
+          a0[6 * d] = df_add_abs(a0[6 * d], K2);
         }
         __syncwarp();
         continue;

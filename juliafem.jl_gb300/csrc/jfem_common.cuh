@@ -217,26 +217,6 @@ __device__ __forceinline__ float coarse_prolong(const int* __restrict__ node_agg
   return c == 0 ? e[0] + e[4] * d.z - e[5] * d.y : c == 1 ? e[1] + e[5] * d.x - e[3] * d.z : e[2] + e[3] * d.y - e[4] * d.x;
 }
 
-// q (= K p from the fused tile pass) at DOF k = 3 j + c: y when node j lies in
-// one tile only; otherwise the tile partials of j summed in ascending tile order
-// (the boundary pass's order and bits), zero on a prescribed DOF.
-__device__ __forceinline__ float tile_q(int64_t k, const float* __restrict__ y, const int* __restrict__ bidx,
-                                        const int* __restrict__ bptr, const float4* __restrict__ bpart,
-                                        const uint8_t* __restrict__ mask, bool* shared) {
-  const int64_t j = k / 3;
-  const int c = (int)(k - 3 * j);
-  const int b = __ldg(bidx + j);
-  *shared = b >= 0;
-  if (b < 0) return y[k];
-  const int i0 = __ldg(bptr + b), i1 = __ldg(bptr + b + 1);
-  float s = 0.f;
-  for (int i = i0; i < i1; ++i) {
-    const float4 t = __ldg(bpart + i);
-    s += c == 0 ? t.x : c == 1 ? t.y : t.z;
-  }
-  return ((__ldg(mask + j) >> c) & 1) ? 0.f : s;
-}
-
 // ---------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------
@@ -366,7 +346,6 @@ struct Ctx {
   int* tout = nullptr;          // per tile node: its global node when interior, −1 − (bpart position) when shared
   int* bnodes = nullptr;        // nodes shared by several tiles
   int* bptr = nullptr;          // [n_bnodes+1] runs of bpart per shared node
-  int* bidx = nullptr;          // [N] index of the node in bnodes, −1 when in one tile only
   float4* bpart = nullptr;      // [n_bslots] tile partial sums (x, y, z, unused), grouped by node, ascending tile
   float* geoT32 = nullptr;      // geometry records in tile order
   float* nhstate = nullptr;     // [16·n_q][Epad] Neo-Hookean point state at u_state (F, C⁻¹ sym, μ − λ ln J), tile order
@@ -412,6 +391,19 @@ struct Ctx {
   int64_t m_actB = 0, m_gpart_cap = 0;
   float4* mi = nullptr;       // network inference vectors, 7 × [N] float4: y, A y, A² y, u, h, g, v
   float* invdeg = nullptr;    // 1 / (neighbours of each node), the mean-aggregation weights
+  // The network's inference graph in a sweep order (nodes sorted along the
+  // mesh's longest axis, then the others): neighbour offsets j − i as int16 in
+  // rows padded to multiples of 4 entries (0 = padding).  mpg_mode 0: not
+  // built; 1: this graph; 2: an offset exceeded int16, the mesh-order int32
+  // graph (nb_ptr, nbr) is used instead.
+  int mpg_mode = 0;
+  int* mpg_n2o = nullptr;     // [N] sweep position → mesh node
+  int* mpg_o2n = nullptr;     // [N] mesh node → sweep position
+  int2* mpg_row = nullptr;    // [N] entry range of each row (start a multiple of 4)
+  int16_t* mpg_idx = nullptr;
+  float* mpg_invdeg = nullptr;   // [N] sweep order
+  uint8_t* mpg_mask = nullptr;   // [N] sweep order, of mask generation mpg_mask_gen
+  int mpg_mask_gen = -1;
 
   // two-level preconditioner: Galerkin coarse space of rigid-body modes on node
   // aggregates (jfem_coarse.cu).  Structure per (mesh, Dirichlet mask); values
@@ -505,7 +497,6 @@ inline bool nh_cache_ready(const Ctx* c) { return c->nhstate && c->nhstate_versi
 int nh_state_prepare(Ctx* c);
 void enqueue_apply_tiled(Ctx* c, const float2* v2, float* y, bool masked, double* part, const int* stop,
                          SolverScalars* sc = nullptr);
-void enqueue_tiles_fused(Ctx* c, const float2* v2, float* y, double* part, const int* stop, SolverScalars* sc);
 void enqueue_internal_force(Ctx* c, double* f);
 int apply_device(Ctx* c, const double* v, double* y, bool fp32, bool masked, double* partial_pAp);
 void prepare_geo_tet4_affine(int64_t E, const int* conn, const double* X, const double* lam, const double* mu,
@@ -525,6 +516,9 @@ int mpnn_precondition(Ctx* c, const double* r, double* z);
 int mpnn_ensure_act(Ctx* c, int64_t B);
 int mpnn_refresh_poly(Ctx* c);
 int mpnn_ensure_infer(Ctx* c);                             // the float4 inference vectors
+int mpnn_graph_prepare(Ctx* c);                            // the inference graph (after mpnn_refresh_poly)
+// position of mesh node i in the inference vectors
+__device__ __forceinline__ int64_t mp_pos(const int* __restrict__ o2n, int64_t i) { return o2n ? __ldg(o2n + i) : i; }
 // v = NᵀN y for one sample (y, v: [N] float4).  With t1part, the last pass also
 // leaves block partials of Σ D^{-1/2}(y + v)·q_old (flexible CG's β) and
 // returns the number of blocks.

@@ -173,27 +173,19 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_precond(int64_t n, const d
 // ---------------------------------------------------------------------------
 // mixed solver (double-float vectors)
 // ---------------------------------------------------------------------------
-// x += αp, r −= α Ap (Ap from the fused tile pass: tile_q), r·z and r·r partials;
-// the last block forms β and the stop flag.
 __global__ void __launch_bounds__(JFEM_RED_THREADS) k_dfcg_update1(int64_t n, SolverScalars* __restrict__ sc,
                                                                    float2* __restrict__ x, float2* __restrict__ r,
                                                                    const float2* __restrict__ p,
                                                                    const float* __restrict__ Ap,
                                                                    const float* __restrict__ dinv,
-                                                                   const int* __restrict__ bidx,
-                                                                   const int* __restrict__ bptr,
-                                                                   const float4* __restrict__ bpart,
-                                                                   const uint8_t* __restrict__ mask,
                                                                    double* __restrict__ part) {
   __shared__ double sh[32];
   if (sc->done[0]) return;
   const float2 a = sc->alpha_df, na = df_neg(a);
   float2 rz = make_float2(0.f, 0.f), rr = make_float2(0.f, 0.f);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    bool sh_node;
-    const float q = tile_q(i, Ap, bidx, bptr, bpart, mask, &sh_node);
     x[i] = df_add(x[i], df_mul(a, p[i]));
-    const float2 ri = df_add(r[i], df_mul_f(na, q));
+    const float2 ri = df_add(r[i], df_mul_f(na, Ap[i]));
     r[i] = ri;
     rz = df_add(rz, df_mul(ri, df_mul_f(ri, dinv[i])));
     rr = df_add(rr, df_mul(ri, ri));
@@ -369,14 +361,14 @@ void enqueue_axpy(Ctx* c, int64_t n, double a, const double* x, double* y) {
 // With a fixed SPD preconditioner this is PCG; with the network (nonlinear in
 // r) the explicit orthogonalisation against the previous direction keeps the
 // recursion consistent; the learned preconditioner is symmetric positive
-// definite, for which FCG is PCG.  part regions: [0,G) p·q (element quadratic
-// forms from the tile pass), [G,2G) r·r, [2G,3G) p·r, and the β terms of
-// JFEM_PART_*.
+// definite, for which FCG is PCG.  part regions: [0,G) tile p·q, [3G,4G)
+// boundary p·q, [G,2G) r·r, [2G,3G) p·r, and the β terms of JFEM_PART_*.
 // ---------------------------------------------------------------------------
 // y = mask ⊙ D^{-1/2} r (FP32), the network input, one float4 per node
 __global__ void __launch_bounds__(256) k_fcg_input(int64_t N, const float2* __restrict__ r,
                                                    const float* __restrict__ dinv, const uint8_t* __restrict__ mask,
-                                                   const SolverScalars* __restrict__ sc, float4* __restrict__ y) {
+                                                   const int* __restrict__ o2n, const SolverScalars* __restrict__ sc,
+                                                   float4* __restrict__ y) {
   if (sc->done[0]) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     const uint8_t m = mask[i];
@@ -386,7 +378,7 @@ __global__ void __launch_bounds__(256) k_fcg_input(int64_t N, const float2* __re
       const float2 rq = r[3 * i + c];
       v[c] = ((m >> c) & 1) ? 0.f : sqrtf(dinv[3 * i + c]) * (rq.x + rq.y);
     }
-    y[i] = make_float4(v[0], v[1], v[2], 0.f);
+    y[mp_pos(o2n, i)] = make_float4(v[0], v[1], v[2], 0.f);
   }
 }
 
@@ -421,7 +413,7 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_zp(int64_t N, const fl
                                                              const int* __restrict__ node_agg,
                                                              const float4* __restrict__ d32,
                                                              const float* __restrict__ Ec, float2* __restrict__ p,
-                                                             const float2* __restrict__ r,
+                                                             const float2* __restrict__ r, const int* __restrict__ o2n,
                                                              SolverScalars* __restrict__ sc, double* __restrict__ part) {
   __shared__ double sh[32];
   if (sc->done[0]) return;
@@ -431,7 +423,8 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_zp(int64_t N, const fl
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     float zc[3];
     if (NN) {
-      const float4 y4 = y[i], v4 = v[i];
+      const int64_t pi = mp_pos(o2n, i);
+      const float4 y4 = y[pi], v4 = v[pi];
       zc[0] = sqrtf(dinv[3 * i]) * (y4.x + v4.x);
       zc[1] = sqrtf(dinv[3 * i + 1]) * (y4.y + v4.y);
       zc[2] = sqrtf(dinv[3 * i + 2]) * (y4.z + v4.z);
@@ -470,28 +463,20 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_zp(int64_t N, const fl
 
 // x += αp, r −= αq; r·r partials → the last block updates the scalars and the
 // stop flag.  T1 (Jacobi smoother): also Σ D⁻¹r·q partials for the next β.
-// q = K p from the fused tile pass (tile_q; the shared nodes' sums are written
-// back into q, which the next iteration reads as q_old).
 template <bool T1>
 __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_update(int64_t n, SolverScalars* __restrict__ sc,
                                                                  float2* __restrict__ x, float2* __restrict__ r,
                                                                  const float2* __restrict__ p,
-                                                                 float* __restrict__ q,
+                                                                 const float* __restrict__ q,
                                                                  const float* __restrict__ dinv,
-                                                                 const int* __restrict__ bidx,
-                                                                 const int* __restrict__ bptr,
-                                                                 const float4* __restrict__ bpart,
-                                                                 const uint8_t* __restrict__ mask,
                                                                  double* __restrict__ part) {
   __shared__ double sh[32];
   if (sc->done[0]) return;
   const float2 a = sc->alpha_df, na = df_neg(a);
   float2 rr = make_float2(0.f, 0.f), t1 = make_float2(0.f, 0.f);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    bool sh_node;
-    const float qi = tile_q(i, q, bidx, bptr, bpart, mask, &sh_node);
-    if (sh_node) q[i] = qi;
     x[i] = df_add(x[i], df_mul(a, p[i]));
+    const float qi = q[i];
     const float2 ri = df_add(r[i], df_mul_f(na, qi));
     r[i] = ri;
     rr = df_add(rr, df_mul(ri, ri));
@@ -602,41 +587,41 @@ static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
   float4* y = c->mi;
   float4* v = c->mi ? c->mi + 6 * c->N : nullptr;
   if (nn) {
-    k_fcg_input<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, y);
+    k_fcg_input<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->mpg_o2n, c->sc, y);
     const int n1 = enqueue_mpnn_spd(c, y, v, c->dinvf, c->Apf, c->part + JFEM_PART_T1N);
     k_fcg_beta<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part + JFEM_PART_T1N, n1, t2, n2);
     if (coarse)
       k_fcg_zp<true, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, y, v, c->dinvf, c->mask, na, d32, Ec, c->p2,
-                                                                   c->rd, c->sc, c->part);
+                                                                   c->rd, c->mpg_o2n, c->sc, c->part);
     else
       k_fcg_zp<true, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, y, v, c->dinvf, c->mask, na, d32, Ec, c->p2,
-                                                                    c->rd, c->sc, c->part);
+                                                                    c->rd, c->mpg_o2n, c->sc, c->part);
   } else {
     k_fcg_beta<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part + JFEM_PART_T1, G_, t2, n2);
     if (coarse)
       k_fcg_zp<false, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, nullptr, nullptr, c->dinvf, c->mask, na, d32,
-                                                                    Ec, c->p2, c->rd, c->sc, c->part);
+                                                                    Ec, c->p2, c->rd, c->mpg_o2n, c->sc, c->part);
     else
       k_fcg_zp<false, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, nullptr, nullptr, c->dinvf, c->mask, na,
-                                                                     d32, Ec, c->p2, c->rd, c->sc, c->part);
+                                                                     d32, Ec, c->p2, c->rd, c->mpg_o2n, c->sc, c->part);
   }
   c->launches += nn ? 3 : 2;
-  enqueue_tiles_fused(c, c->p2, c->Apf, c->part, &c->sc->done[0], c->sc);
+  enqueue_apply_tiled(c, c->p2, c->Apf, true, c->part, &c->sc->done[0], c->sc);
   if (nn)
     k_fcg_update<false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->xd, c->rd, c->p2, c->Apf, c->dinvf,
-                                                                c->bidx, c->bptr, c->bpart, c->mask, c->part);
+                                                                c->part);
   else
     k_fcg_update<true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->xd, c->rd, c->p2, c->Apf, c->dinvf,
-                                                               c->bidx, c->bptr, c->bpart, c->mask, c->part);
+                                                               c->part);
   c->launches += 1;
 }
 
 static void enqueue_iteration(Ctx* c, bool fp32, int slot) {
   const int64_t n = 3 * c->N;
   if (fp32) {   // mixed: double-float vectors, tiled FP32 apply
-    enqueue_tiles_fused(c, c->p2, c->Apf, c->part, &c->sc->done[0], c->sc);
+    enqueue_apply_tiled(c, c->p2, c->Apf, true, c->part, &c->sc->done[0], c->sc);
     k_dfcg_update1<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->xd, c->rd, c->p2, c->Apf, c->dinvf,
-                                                          c->bidx, c->bptr, c->bpart, c->mask, c->part);
+                                                          c->part);
     k_dfcg_update2<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->p2, c->rd, c->dinvf);
     c->launches += 2;
     return;
@@ -857,6 +842,7 @@ static int fcg(Ctx* c, const double* f, bool nn, bool coarse, double tol, int ma
   if (nn && (!c->mp || !c->mp->ready)) return set_err(c, JFEM_ERR_INVALID, "no network weights (jfem_mpnn_init)");
   if (nn && (rc = mpnn_ensure_infer(c))) return rc;
   if (nn && (rc = mpnn_refresh_poly(c))) return rc;
+  if (nn && (rc = mpnn_graph_prepare(c))) return rc;
   if (coarse && (rc = coarse_prepare(c))) return rc;
   const auto kind_of = [&]() { return (nn ? 3 : 2) + (coarse ? 2 : 0); };
   if (x_zero) {

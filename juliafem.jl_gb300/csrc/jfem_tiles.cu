@@ -243,7 +243,6 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   if ((rc = up(&c->tout, tout))) return rc;
   if ((rc = up(&c->bnodes, bnodes))) return rc;
   if ((rc = up(&c->bptr, bptr))) return rc;
-  if ((rc = up(&c->bidx, bidx))) return rc;
   if ((rc = dalloc(c, &c->bpart, std::max<int64_t>(nslots, 1)))) return rc;
   c->ntiles = ntiles;
   c->Epad = Epad;
