@@ -627,32 +627,34 @@ __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __res
 
 // ---------------------------------------------------------------------------
 // the same passes on the sweep-ordered int16 graph (mpg_mode 1).  A group of 8
-// lanes takes two rows per round (i and i + gs), so each round overlaps the
-// row-pointer, offset and gather latencies of two nodes; within a row every
+// lanes takes MP_NODES rows per round (i, i + gs, …), so each round overlaps the
+// row-pointer, offset and gather latencies of those nodes; within a row every
 // lane loads 4 consecutive offsets with one 8-byte load (rows start at
 // multiples of 4 entries) and gathers their vectors.  Per-lane sums in entry
 // order, then the fixed xor-shuffle tree: the bits do not depend on scheduling.
 // ---------------------------------------------------------------------------
+#define MP_NODES 2   // rows per lane group and round of the sweep-ordered passes
 template <bool WEIGHTED>
 __device__ __forceinline__ void group_sum16(const int2* __restrict__ row, const int16_t* __restrict__ idx,
-                                            const float4* __restrict__ in, const int64_t (&i)[2],
-                                            const bool (&val)[2], int g, float (&s)[2][3]) {
-  int2 rp[2];
+                                            const float4* __restrict__ in, const int64_t (&i)[MP_NODES],
+                                            const bool (&val)[MP_NODES], int g, float (&s)[MP_NODES][3]) {
+  int2 rp[MP_NODES];
+  int len = 0;
 #pragma unroll
-  for (int n = 0; n < 2; ++n) {
+  for (int n = 0; n < MP_NODES; ++n) {
     s[n][0] = s[n][1] = s[n][2] = 0.f;
     rp[n] = val[n] ? __ldg(row + i[n]) : make_int2(0, 0);
+    len = max(len, rp[n].y - rp[n].x);
   }
-  const int len = max(rp[0].y - rp[0].x, rp[1].y - rp[1].x);
   const int2* idx8 = reinterpret_cast<const int2*>(idx);
   for (int off = 4 * g; off < len; off += 4 * MP_GL) {
-    int2 raw[2];
+    int2 raw[MP_NODES];
 #pragma unroll
-    for (int n = 0; n < 2; ++n)
+    for (int n = 0; n < MP_NODES; ++n)
       raw[n] = rp[n].x + off < rp[n].y ? __ldg(idx8 + ((rp[n].x + off) >> 2)) : make_int2(0, 0);
-    float4 v[2][4];
+    float4 v[MP_NODES][4];
 #pragma unroll
-    for (int n = 0; n < 2; ++n)
+    for (int n = 0; n < MP_NODES; ++n)
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const unsigned w = (unsigned)(u < 2 ? raw[n].x : raw[n].y);
@@ -660,7 +662,7 @@ __device__ __forceinline__ void group_sum16(const int2* __restrict__ row, const 
         v[n][u] = d != 0 ? __ldg(in + i[n] + d) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
-    for (int n = 0; n < 2; ++n)
+    for (int n = 0; n < MP_NODES; ++n)
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const float wgt = WEIGHTED ? v[n][u].w : 1.f;
@@ -671,7 +673,7 @@ __device__ __forceinline__ void group_sum16(const int2* __restrict__ row, const 
   }
   const unsigned gm = group_mask();
 #pragma unroll
-  for (int n = 0; n < 2; ++n)
+  for (int n = 0; n < MP_NODES; ++n)
 #pragma unroll
     for (int o = MP_GL / 2; o > 0; o >>= 1) {
       s[n][0] += __shfl_xor_sync(gm, s[n][0], o, MP_GL);
@@ -682,7 +684,7 @@ __device__ __forceinline__ void group_sum16(const int2* __restrict__ row, const 
 
 // k_mp_poly_fwd on the sweep-ordered graph (vectors, invdeg and mask in sweep order)
 template <bool LAST>
-__global__ void __launch_bounds__(256, LAST ? 3 : 1) k_mp_fwd16(int64_t N, const int2* __restrict__ row,
+__global__ void __launch_bounds__(256, LAST ? 3 : (MP_NODES == 1 ? 8 : 1)) k_mp_fwd16(int64_t N, const int2* __restrict__ row,
                                                   const int16_t* __restrict__ idx, const float* __restrict__ invdeg,
                                                   const float4* __restrict__ in, const float4* __restrict__ y,
                                                   const float4* __restrict__ a1, const float* __restrict__ poly,
@@ -694,14 +696,19 @@ __global__ void __launch_bounds__(256, LAST ? 3 : 1) k_mp_fwd16(int64_t N, const
   const int g = threadIdx.x & (MP_GL - 1);
   const int64_t g0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / MP_GL;
   const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
-  for (int64_t i0 = g0; i0 < N; i0 += 2 * gs) {
-    const int64_t ii[2] = {i0, i0 + gs};
-    const bool val[2] = {true, i0 + gs < N};
-    float s[2][3];
+  for (int64_t i0 = g0; i0 < N; i0 += MP_NODES * gs) {
+    int64_t ii[MP_NODES];
+    bool val[MP_NODES];
+#pragma unroll
+    for (int n = 0; n < MP_NODES; ++n) {
+      ii[n] = i0 + n * gs;
+      val[n] = ii[n] < N;
+    }
+    float s[MP_NODES][3];
     group_sum16<false>(row, idx, in, ii, val, g, s);
     if (g != 0) continue;
 #pragma unroll
-    for (int n = 0; n < 2; ++n) {
+    for (int n = 0; n < MP_NODES; ++n) {
       if (!val[n]) continue;
       const int64_t i = ii[n];
       const float id = __ldg(invdeg + i);
@@ -733,7 +740,7 @@ __global__ void __launch_bounds__(256, LAST ? 3 : 1) k_mp_fwd16(int64_t N, const
 // k_mp_poly_adj on the sweep-ordered graph; FCG: q_old and D⁻¹ are read at the
 // mesh node n2o[i]
 template <bool FCG>
-__global__ void __launch_bounds__(256, FCG ? 5 : 6) k_mp_adj16(int64_t N, const int2* __restrict__ row,
+__global__ void __launch_bounds__(256, FCG ? 5 : (MP_NODES == 1 ? 8 : 6)) k_mp_adj16(int64_t N, const int2* __restrict__ row,
                                                   const int16_t* __restrict__ idx, const float* __restrict__ invdeg,
                                                   const float4* __restrict__ g, const float4* __restrict__ u,
                                                   const float* __restrict__ poly, int k, float4* __restrict__ out,
@@ -748,14 +755,19 @@ __global__ void __launch_bounds__(256, FCG ? 5 : 6) k_mp_adj16(int64_t N, const 
   const int64_t g0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / MP_GL;
   const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
   float2 t1 = make_float2(0.f, 0.f);
-  for (int64_t i0 = g0; i0 < N; i0 += 2 * gs) {
-    const int64_t ii[2] = {i0, i0 + gs};
-    const bool val[2] = {true, i0 + gs < N};
-    float s[2][3];
+  for (int64_t i0 = g0; i0 < N; i0 += MP_NODES * gs) {
+    int64_t ii[MP_NODES];
+    bool val[MP_NODES];
+#pragma unroll
+    for (int n = 0; n < MP_NODES; ++n) {
+      ii[n] = i0 + n * gs;
+      val[n] = ii[n] < N;
+    }
+    float s[MP_NODES][3];
     group_sum16<true>(row, idx, g, ii, val, gl, s);
     if (gl != 0) continue;
 #pragma unroll
-    for (int n = 0; n < 2; ++n) {
+    for (int n = 0; n < MP_NODES; ++n) {
       if (!val[n]) continue;
       const int64_t i = ii[n];
       const float4 u4 = u[i];
