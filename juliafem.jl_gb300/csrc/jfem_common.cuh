@@ -391,19 +391,6 @@ struct Ctx {
   int64_t m_actB = 0, m_gpart_cap = 0;
   float4* mi = nullptr;       // network inference vectors, 7 × [N] float4: y, A y, A² y, u, h, g, v
   float* invdeg = nullptr;    // 1 / (neighbours of each node), the mean-aggregation weights
-  // The network's inference graph in a sweep order (nodes sorted along the
-  // mesh's longest axis, then the others): neighbour offsets j − i as int16 in
-  // rows padded to multiples of 4 entries (0 = padding).  mpg_mode 0: not
-  // built; 1: this graph; 2: an offset exceeded int16, the mesh-order int32
-  // graph (nb_ptr, nbr) is used instead.
-  int mpg_mode = 0;
-  int* mpg_n2o = nullptr;     // [N] sweep position → mesh node
-  int* mpg_o2n = nullptr;     // [N] mesh node → sweep position
-  int2* mpg_row = nullptr;    // [N] entry range of each row (start a multiple of 4)
-  int16_t* mpg_idx = nullptr;
-  float* mpg_invdeg = nullptr;   // [N] sweep order
-  uint8_t* mpg_mask = nullptr;   // [N] sweep order, of mask generation mpg_mask_gen
-  int mpg_mask_gen = -1;
 
   // two-level preconditioner: Galerkin coarse space of rigid-body modes on node
   // aggregates (jfem_coarse.cu).  Structure per (mesh, Dirichlet mask); values
@@ -516,9 +503,6 @@ int mpnn_precondition(Ctx* c, const double* r, double* z);
 int mpnn_ensure_act(Ctx* c, int64_t B);
 int mpnn_refresh_poly(Ctx* c);
 int mpnn_ensure_infer(Ctx* c);                             // the float4 inference vectors
-int mpnn_graph_prepare(Ctx* c);                            // the inference graph (after mpnn_refresh_poly)
-// position of mesh node i in the inference vectors
-__device__ __forceinline__ int64_t mp_pos(const int* __restrict__ o2n, int64_t i) { return o2n ? __ldg(o2n + i) : i; }
 // v = NᵀN y for one sample (y, v: [N] float4).  With t1part, the last pass also
 // leaves block partials of Σ D^{-1/2}(y + v)·q_old (flexible CG's β) and
 // returns the number of blocks.

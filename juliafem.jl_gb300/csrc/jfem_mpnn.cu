@@ -455,24 +455,23 @@ __global__ void k_mp_sub(int64_t n, const double* __restrict__ a, const double* 
 
 // y = mask ⊙ D^{-1/2} r (FP64 r, for the host-facing preconditioner), one float4 per node
 __global__ void k_mp_input_d(int64_t N, const double* __restrict__ r, const double* __restrict__ dinv,
-                             const uint8_t* __restrict__ mask, const int* __restrict__ o2n, float4* __restrict__ y) {
+                             const uint8_t* __restrict__ mask, float4* __restrict__ y) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     float v[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) v[c] = dof_free(mask, i, c) ? (float)(sqrt(dinv[3 * i + c]) * r[3 * i + c]) : 0.f;
-    y[mp_pos(o2n, i)] = make_float4(v[0], v[1], v[2], 0.f);
+    y[i] = make_float4(v[0], v[1], v[2], 0.f);
   }
 }
 
 // z = D^{-1/2} (y + v) (FP64 out)
 __global__ void k_mp_precond_out(int64_t N, const float4* __restrict__ y, const float4* __restrict__ v,
                                  const double* __restrict__ dinv, const uint8_t* __restrict__ mask,
-                                 const int* __restrict__ o2n, double* __restrict__ z) {
+                                 double* __restrict__ z) {
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * N; q += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = q / 3;
     const int c = (int)(q % 3);
-    const int64_t pi = mp_pos(o2n, i);
-    const float yq = reinterpret_cast<const float*>(y)[4 * pi + c], vq = reinterpret_cast<const float*>(v)[4 * pi + c];
+    const float yq = reinterpret_cast<const float*>(y)[4 * i + c], vq = reinterpret_cast<const float*>(v)[4 * i + c];
     z[q] = dof_free(mask, i, c) ? sqrt(dinv[q]) * ((double)yq + (double)vq) : 0.0;
   }
 }
@@ -623,215 +622,6 @@ __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __res
     const double b = block_sum_df(t1, sh);
     if (threadIdx.x == 0) t1part[blockIdx.x] = b;
   }
-}
-
-// ---------------------------------------------------------------------------
-// the same passes on the sweep-ordered int16 graph (mpg_mode 1).  A group of 8
-// lanes takes MP_NODES rows per round (i, i + gs, …), so each round overlaps the
-// row-pointer, offset and gather latencies of those nodes; within a row every
-// lane loads 4 consecutive offsets with one 8-byte load (rows start at
-// multiples of 4 entries) and gathers their vectors.  Per-lane sums in entry
-// order, then the fixed xor-shuffle tree: the bits do not depend on scheduling.
-// ---------------------------------------------------------------------------
-#define MP_NODES 2   // rows per lane group and round of the sweep-ordered passes
-template <bool WEIGHTED>
-__device__ __forceinline__ void group_sum16(const int2* __restrict__ row, const int16_t* __restrict__ idx,
-                                            const float4* __restrict__ in, const int64_t (&i)[MP_NODES],
-                                            const bool (&val)[MP_NODES], int g, float (&s)[MP_NODES][3]) {
-  int2 rp[MP_NODES];
-  int len = 0;
-#pragma unroll
-  for (int n = 0; n < MP_NODES; ++n) {
-    s[n][0] = s[n][1] = s[n][2] = 0.f;
-    rp[n] = val[n] ? __ldg(row + i[n]) : make_int2(0, 0);
-    len = max(len, rp[n].y - rp[n].x);
-  }
-  const int2* idx8 = reinterpret_cast<const int2*>(idx);
-  for (int off = 4 * g; off < len; off += 4 * MP_GL) {
-    int2 raw[MP_NODES];
-#pragma unroll
-    for (int n = 0; n < MP_NODES; ++n)
-      raw[n] = rp[n].x + off < rp[n].y ? __ldg(idx8 + ((rp[n].x + off) >> 2)) : make_int2(0, 0);
-    float4 v[MP_NODES][4];
-#pragma unroll
-    for (int n = 0; n < MP_NODES; ++n)
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const unsigned w = (unsigned)(u < 2 ? raw[n].x : raw[n].y);
-        const int d = (int)(int16_t)(w >> (16 * (u & 1)));
-        v[n][u] = d != 0 ? __ldg(in + i[n] + d) : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-#pragma unroll
-    for (int n = 0; n < MP_NODES; ++n)
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const float wgt = WEIGHTED ? v[n][u].w : 1.f;
-        s[n][0] = fmaf(wgt, v[n][u].x, s[n][0]);
-        s[n][1] = fmaf(wgt, v[n][u].y, s[n][1]);
-        s[n][2] = fmaf(wgt, v[n][u].z, s[n][2]);
-      }
-  }
-  const unsigned gm = group_mask();
-#pragma unroll
-  for (int n = 0; n < MP_NODES; ++n)
-#pragma unroll
-    for (int o = MP_GL / 2; o > 0; o >>= 1) {
-      s[n][0] += __shfl_xor_sync(gm, s[n][0], o, MP_GL);
-      s[n][1] += __shfl_xor_sync(gm, s[n][1], o, MP_GL);
-      s[n][2] += __shfl_xor_sync(gm, s[n][2], o, MP_GL);
-    }
-}
-
-// k_mp_poly_fwd on the sweep-ordered graph (vectors, invdeg and mask in sweep order)
-template <bool LAST>
-__global__ void __launch_bounds__(256, LAST ? 3 : (MP_NODES == 1 ? 8 : 1)) k_mp_fwd16(int64_t N, const int2* __restrict__ row,
-                                                  const int16_t* __restrict__ idx, const float* __restrict__ invdeg,
-                                                  const float4* __restrict__ in, const float4* __restrict__ y,
-                                                  const float4* __restrict__ a1, const float* __restrict__ poly,
-                                                  const uint8_t* __restrict__ mask, float4* __restrict__ out,
-                                                  float4* __restrict__ h) {
-  __shared__ float C[36];
-  if (threadIdx.x < 36) C[threadIdx.x] = poly[threadIdx.x];
-  __syncthreads();
-  const int g = threadIdx.x & (MP_GL - 1);
-  const int64_t g0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / MP_GL;
-  const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
-  for (int64_t i0 = g0; i0 < N; i0 += MP_NODES * gs) {
-    int64_t ii[MP_NODES];
-    bool val[MP_NODES];
-#pragma unroll
-    for (int n = 0; n < MP_NODES; ++n) {
-      ii[n] = i0 + n * gs;
-      val[n] = ii[n] < N;
-    }
-    float s[MP_NODES][3];
-    group_sum16<false>(row, idx, in, ii, val, g, s);
-    if (g != 0) continue;
-#pragma unroll
-    for (int n = 0; n < MP_NODES; ++n) {
-      if (!val[n]) continue;
-      const int64_t i = ii[n];
-      const float id = __ldg(invdeg + i);
-      float a[3] = {s[n][0] * id, s[n][1] * id, s[n][2] * id};
-      if (!LAST) {
-        out[i] = make_float4(a[0], a[1], a[2], 0.f);
-      } else {
-        const float4 y4 = y[i], a14 = a1[i], a24 = in[i];
-        const float yv[3] = {y4.x, y4.y, y4.z};
-        const float a1v[3] = {a14.x, a14.y, a14.z};
-        const float a2v[3] = {a24.x, a24.y, a24.z};
-        float u[3] = {0.f, 0.f, 0.f};
-        mat3_acc(C, false, yv, u);
-        mat3_acc(C + 9, false, a1v, u);
-        mat3_acc(C + 18, false, a2v, u);
-        mat3_acc(C + 27, false, a, u);
-        const uint8_t m = mask[i];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) u[k] = ((m >> k) & 1) ? 0.f : u[k];
-        float hv[3] = {0.f, 0.f, 0.f};
-        mat3_acc(C + 27, true, u, hv);
-        out[i] = make_float4(u[0], u[1], u[2], 0.f);
-        h[i] = make_float4(hv[0], hv[1], hv[2], id);
-      }
-    }
-  }
-}
-
-// k_mp_poly_adj on the sweep-ordered graph; FCG: q_old and D⁻¹ are read at the
-// mesh node n2o[i]
-template <bool FCG>
-__global__ void __launch_bounds__(256, FCG ? 5 : (MP_NODES == 1 ? 8 : 6)) k_mp_adj16(int64_t N, const int2* __restrict__ row,
-                                                  const int16_t* __restrict__ idx, const float* __restrict__ invdeg,
-                                                  const float4* __restrict__ g, const float4* __restrict__ u,
-                                                  const float* __restrict__ poly, int k, float4* __restrict__ out,
-                                                  const float4* __restrict__ y, const int* __restrict__ n2o,
-                                                  const float* __restrict__ dinvf, const float* __restrict__ qold,
-                                                  double* __restrict__ t1part) {
-  __shared__ float C[9];
-  __shared__ double sh[32];
-  if (threadIdx.x < 9) C[threadIdx.x] = poly[9 * k + threadIdx.x];
-  __syncthreads();
-  const int gl = threadIdx.x & (MP_GL - 1);
-  const int64_t g0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / MP_GL;
-  const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
-  float2 t1 = make_float2(0.f, 0.f);
-  for (int64_t i0 = g0; i0 < N; i0 += MP_NODES * gs) {
-    int64_t ii[MP_NODES];
-    bool val[MP_NODES];
-#pragma unroll
-    for (int n = 0; n < MP_NODES; ++n) {
-      ii[n] = i0 + n * gs;
-      val[n] = ii[n] < N;
-    }
-    float s[MP_NODES][3];
-    group_sum16<true>(row, idx, g, ii, val, gl, s);
-    if (gl != 0) continue;
-#pragma unroll
-    for (int n = 0; n < MP_NODES; ++n) {
-      if (!val[n]) continue;
-      const int64_t i = ii[n];
-      const float4 u4 = u[i];
-      const float uv[3] = {u4.x, u4.y, u4.z};
-      mat3_acc(C, true, uv, s[n]);
-      out[i] = make_float4(s[n][0], s[n][1], s[n][2], __ldg(invdeg + i));
-      if (FCG) {
-        const float4 y4 = y[i];
-        const float yv[3] = {y4.x, y4.y, y4.z};
-        const int64_t o = __ldg(n2o + i);
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-          t1 = df_add(t1, df_two_prod(sqrtf(dinvf[3 * o + c]) * (yv[c] + s[n][c]), qold[3 * o + c]));
-      }
-    }
-  }
-  if (FCG) {
-    const double b = block_sum_df(t1, sh);
-    if (threadIdx.x == 0) t1part[blockIdx.x] = b;
-  }
-}
-
-// sweep-order graph: padded row lengths (new order) and the largest offset
-__global__ void k_mpg_count(int64_t N, const int* __restrict__ n2o, const int* __restrict__ o2n,
-                            const int* __restrict__ nb_ptr, const int* __restrict__ nbr, int* __restrict__ len,
-                            int* __restrict__ maxoff) {
-  int mx = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-    const int o = n2o[i];
-    const int j0 = nb_ptr[o], j1 = nb_ptr[o + 1];
-    for (int k = j0; k < j1; ++k) {
-      const int d = o2n[nbr[k]] - (int)i;
-      mx = max(mx, d < 0 ? -d : d);
-    }
-    const int deg = j1 - j0 - 1;   // the row holds the node itself
-    len[i] = (deg + 3) & ~3;
-  }
-  mx = __reduce_max_sync(0xffffffffu, mx);
-  if ((threadIdx.x & 31) == 0) atomicMax(maxoff, mx);
-}
-
-__global__ void k_mpg_fill(int64_t N, const int* __restrict__ n2o, const int* __restrict__ o2n,
-                           const int* __restrict__ nb_ptr, const int* __restrict__ nbr,
-                           const int* __restrict__ start, const int* __restrict__ len, const float* __restrict__ invdeg,
-                           int2* __restrict__ row, int16_t* __restrict__ idx, float* __restrict__ invdeg_p) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-    const int o = n2o[i];
-    const int s0 = start[i], l = len[i];
-    int p = s0;
-    for (int k = nb_ptr[o]; k < nb_ptr[o + 1]; ++k) {
-      const int j = nbr[k];
-      if (j == o) continue;
-      idx[p++] = (int16_t)(o2n[j] - (int)i);
-    }
-    while (p < s0 + l) idx[p++] = 0;
-    row[i] = make_int2(s0, s0 + l);
-    invdeg_p[i] = invdeg[o];
-  }
-}
-
-__global__ void k_mpg_mask(int64_t N, const int* __restrict__ n2o, const uint8_t* __restrict__ mask,
-                           uint8_t* __restrict__ mask_p) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
-    mask_p[i] = mask[n2o[i]];
 }
 
 // ---------------------------------------------------------------------------
@@ -1103,81 +893,6 @@ int mpnn_ensure_infer(Ctx* c) {
   return 0;
 }
 
-// The sweep order: nodes sorted by their coordinates quantised to 21 bits,
-// the longest bounding-box axis most significant (ties keep the mesh order).
-// On a mesh whose elements span a few node layers along that axis, neighbours
-// are a few layers apart, which int16 offsets hold up to ±32767.
-int mpnn_graph_prepare(Ctx* c) {
-  const int64_t N = c->N;
-  if (c->mpg_mode == 0) {
-    std::vector<double> X((size_t)(3 * N));
-    cudaMemcpyAsync(X.data(), c->X64, X.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
-    int rc = sync_and_check(c, "coordinates for the sweep order");
-    if (rc) return rc;
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int64_t i = 0; i < N; ++i)
-      for (int d = 0; d < 3; ++d) {
-        lo[d] = std::min(lo[d], X[3 * (size_t)i + d]);
-        hi[d] = std::max(hi[d], X[3 * (size_t)i + d]);
-      }
-    int ax[3] = {0, 1, 2};
-    std::stable_sort(ax, ax + 3, [&](int a, int b) { return hi[a] - lo[a] > hi[b] - lo[b]; });
-    std::vector<std::pair<uint64_t, int>> key((size_t)N);
-    for (int64_t i = 0; i < N; ++i) {
-      uint64_t k = 0;
-      for (int r = 0; r < 3; ++r) {
-        const int d = ax[r];
-        const double ext = hi[d] - lo[d];
-        const double q = ext > 0.0 ? (X[3 * (size_t)i + d] - lo[d]) / ext * 2097151.0 : 0.0;
-        k = (k << 21) | (uint64_t)std::max(0.0, std::min(2097151.0, q));
-      }
-      key[(size_t)i] = {k, (int)i};
-    }
-    std::sort(key.begin(), key.end());
-    std::vector<int> n2o((size_t)N), o2n((size_t)N);
-    for (int64_t i = 0; i < N; ++i) {
-      n2o[(size_t)i] = key[(size_t)i].second;
-      o2n[(size_t)key[(size_t)i].second] = (int)i;
-    }
-    int *d_len = nullptr, *d_start = nullptr, *d_max = nullptr;
-    if ((rc = dalloc(c, &c->mpg_n2o, (size_t)N)) || (rc = dalloc(c, &c->mpg_o2n, (size_t)N)) ||
-        (rc = dalloc(c, &d_len, (size_t)N + 1)) || (rc = dalloc(c, &d_start, (size_t)N + 1)) ||
-        (rc = dalloc(c, &d_max, 1)))
-      return rc;
-    cudaMemcpyAsync(c->mpg_n2o, n2o.data(), N * sizeof(int), cudaMemcpyHostToDevice, c->stream);
-    cudaMemcpyAsync(c->mpg_o2n, o2n.data(), N * sizeof(int), cudaMemcpyHostToDevice, c->stream);
-    cudaMemsetAsync(d_max, 0, sizeof(int), c->stream);
-    cudaMemsetAsync(d_len + N, 0, sizeof(int), c->stream);
-    k_mpg_count<<<grid_for(N, 256), 256, 0, c->stream>>>(N, c->mpg_n2o, c->mpg_o2n, c->nb_ptr, c->nbr, d_len, d_max);
-    int64_t total = 0;
-    if ((rc = exclusive_scan_i32(c, d_len, d_start, N + 1, &total))) return rc;
-    int h_max = 0;
-    cudaMemcpyAsync(&h_max, d_max, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
-    if ((rc = sync_and_check(c, "sweep-order graph size"))) return rc;
-    c->launches += 1;
-    if (h_max > 32767) {
-      c->mpg_mode = 2;   // keep the mesh-order graph
-      c->mpg_o2n = nullptr;
-      c->mpg_n2o = nullptr;
-      return 0;
-    }
-    if ((rc = dalloc(c, &c->mpg_row, (size_t)N)) || (rc = dalloc(c, &c->mpg_idx, (size_t)std::max<int64_t>(total, 4))) ||
-        (rc = dalloc(c, &c->mpg_invdeg, (size_t)N)) || (rc = dalloc(c, &c->mpg_mask, (size_t)N)))
-      return rc;
-    k_mpg_fill<<<grid_for(N, 256), 256, 0, c->stream>>>(N, c->mpg_n2o, c->mpg_o2n, c->nb_ptr, c->nbr, d_start, d_len,
-                                                        c->invdeg, c->mpg_row, c->mpg_idx, c->mpg_invdeg);
-    c->launches += 1;
-    c->mpg_mode = 1;
-    c->mpg_mask_gen = -1;
-  }
-  if (c->mpg_mode == 1 && c->mpg_mask_gen != c->mask_gen) {
-    k_mpg_mask<<<grid_for(N, 256), 256, 0, c->stream>>>(N, c->mpg_n2o, c->mask, c->mpg_mask);
-    c->launches += 1;
-    c->mpg_mask_gen = c->mask_gen;
-  }
-  return sync_and_check(c, "inference graph");
-}
-
 int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf, const float* qold, double* t1part) {
   const float* P = c->mp->poly;
   // a resident grid (8 CTAs of 256 per SM) striding over the nodes; its block
@@ -1185,25 +900,6 @@ int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf, con
   const unsigned g = grid_for(c->N * MP_GL, 256, JFEM_RED_BLOCKS);
   float4 *a1 = c->mi + c->N, *a2 = c->mi + 2 * c->N, *u = c->mi + 3 * c->N, *h = c->mi + 4 * c->N,
          *g2 = c->mi + 5 * c->N;
-  if (c->mpg_mode == 1) {
-    const int2* R = c->mpg_row;
-    const int16_t* I = c->mpg_idx;
-    const float* D = c->mpg_invdeg;
-    k_mp_fwd16<false><<<g, 256, 0, c->stream>>>(c->N, R, I, D, y, nullptr, nullptr, P, c->mpg_mask, a1, nullptr);
-    k_mp_fwd16<false><<<g, 256, 0, c->stream>>>(c->N, R, I, D, a1, nullptr, nullptr, P, c->mpg_mask, a2, nullptr);
-    k_mp_fwd16<true><<<g, 256, 0, c->stream>>>(c->N, R, I, D, a2, y, a1, P, c->mpg_mask, u, h);
-    k_mp_adj16<false><<<g, 256, 0, c->stream>>>(c->N, R, I, D, h, u, P, 2, g2, nullptr, nullptr, nullptr, nullptr,
-                                                nullptr);
-    k_mp_adj16<false><<<g, 256, 0, c->stream>>>(c->N, R, I, D, g2, u, P, 1, h, nullptr, nullptr, nullptr, nullptr,
-                                                nullptr);
-    if (t1part)
-      k_mp_adj16<true><<<g, 256, 0, c->stream>>>(c->N, R, I, D, h, u, P, 0, v, y, c->mpg_n2o, dinvf, qold, t1part);
-    else
-      k_mp_adj16<false><<<g, 256, 0, c->stream>>>(c->N, R, I, D, h, u, P, 0, v, nullptr, nullptr, nullptr, nullptr,
-                                                  nullptr);
-    c->launches += 6;
-    return (int)g;
-  }
   k_mp_poly_fwd<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, y, nullptr, nullptr, P, c->mask,
                                                   a1, nullptr);
   k_mp_poly_fwd<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, a1, nullptr, nullptr, P,
@@ -1469,14 +1165,13 @@ int mpnn_precondition(Ctx* c, const double* r_h, double* z_h) {
   if ((rc = jacobi_diag_device(c, c->dinv))) return rc;
   if ((rc = mpnn_ensure_infer(c))) return rc;
   if ((rc = mpnn_refresh_poly(c))) return rc;
-  if ((rc = mpnn_graph_prepare(c))) return rc;
   const int64_t n3 = 3 * c->N;
   float4* y = c->mi;
   float4* v = c->mi + 6 * c->N;
   cudaMemcpyAsync(c->tmp, r_h, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
-  k_mp_input_d<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->tmp, c->dinv, c->mask, c->mpg_o2n, y);
+  k_mp_input_d<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->tmp, c->dinv, c->mask, y);
   enqueue_mpnn_spd(c, y, v);
-  k_mp_precond_out<<<grid_for(n3, 256), 256, 0, c->stream>>>(c->N, y, v, c->dinv, c->mask, c->mpg_o2n, c->tmp2);
+  k_mp_precond_out<<<grid_for(n3, 256), 256, 0, c->stream>>>(c->N, y, v, c->dinv, c->mask, c->tmp2);
   c->launches += 2;
   cudaMemcpyAsync(z_h, c->tmp2, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
   return sync_and_check(c, "preconditioner");

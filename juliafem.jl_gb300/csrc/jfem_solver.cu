@@ -367,8 +367,7 @@ void enqueue_axpy(Ctx* c, int64_t n, double a, const double* x, double* y) {
 // y = mask ⊙ D^{-1/2} r (FP32), the network input, one float4 per node
 __global__ void __launch_bounds__(256) k_fcg_input(int64_t N, const float2* __restrict__ r,
                                                    const float* __restrict__ dinv, const uint8_t* __restrict__ mask,
-                                                   const int* __restrict__ o2n, const SolverScalars* __restrict__ sc,
-                                                   float4* __restrict__ y) {
+                                                   const SolverScalars* __restrict__ sc, float4* __restrict__ y) {
   if (sc->done[0]) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     const uint8_t m = mask[i];
@@ -378,7 +377,7 @@ __global__ void __launch_bounds__(256) k_fcg_input(int64_t N, const float2* __re
       const float2 rq = r[3 * i + c];
       v[c] = ((m >> c) & 1) ? 0.f : sqrtf(dinv[3 * i + c]) * (rq.x + rq.y);
     }
-    y[mp_pos(o2n, i)] = make_float4(v[0], v[1], v[2], 0.f);
+    y[i] = make_float4(v[0], v[1], v[2], 0.f);
   }
 }
 
@@ -413,7 +412,7 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_zp(int64_t N, const fl
                                                              const int* __restrict__ node_agg,
                                                              const float4* __restrict__ d32,
                                                              const float* __restrict__ Ec, float2* __restrict__ p,
-                                                             const float2* __restrict__ r, const int* __restrict__ o2n,
+                                                             const float2* __restrict__ r,
                                                              SolverScalars* __restrict__ sc, double* __restrict__ part) {
   __shared__ double sh[32];
   if (sc->done[0]) return;
@@ -423,8 +422,7 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_zp(int64_t N, const fl
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     float zc[3];
     if (NN) {
-      const int64_t pi = mp_pos(o2n, i);
-      const float4 y4 = y[pi], v4 = v[pi];
+      const float4 y4 = y[i], v4 = v[i];
       zc[0] = sqrtf(dinv[3 * i]) * (y4.x + v4.x);
       zc[1] = sqrtf(dinv[3 * i + 1]) * (y4.y + v4.y);
       zc[2] = sqrtf(dinv[3 * i + 2]) * (y4.z + v4.z);
@@ -587,23 +585,23 @@ static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
   float4* y = c->mi;
   float4* v = c->mi ? c->mi + 6 * c->N : nullptr;
   if (nn) {
-    k_fcg_input<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->mpg_o2n, c->sc, y);
+    k_fcg_input<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, y);
     const int n1 = enqueue_mpnn_spd(c, y, v, c->dinvf, c->Apf, c->part + JFEM_PART_T1N);
     k_fcg_beta<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part + JFEM_PART_T1N, n1, t2, n2);
     if (coarse)
       k_fcg_zp<true, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, y, v, c->dinvf, c->mask, na, d32, Ec, c->p2,
-                                                                   c->rd, c->mpg_o2n, c->sc, c->part);
+                                                                   c->rd, c->sc, c->part);
     else
       k_fcg_zp<true, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, y, v, c->dinvf, c->mask, na, d32, Ec, c->p2,
-                                                                    c->rd, c->mpg_o2n, c->sc, c->part);
+                                                                    c->rd, c->sc, c->part);
   } else {
     k_fcg_beta<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part + JFEM_PART_T1, G_, t2, n2);
     if (coarse)
       k_fcg_zp<false, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, nullptr, nullptr, c->dinvf, c->mask, na, d32,
-                                                                    Ec, c->p2, c->rd, c->mpg_o2n, c->sc, c->part);
+                                                                    Ec, c->p2, c->rd, c->sc, c->part);
     else
       k_fcg_zp<false, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, nullptr, nullptr, c->dinvf, c->mask, na,
-                                                                     d32, Ec, c->p2, c->rd, c->mpg_o2n, c->sc, c->part);
+                                                                     d32, Ec, c->p2, c->rd, c->sc, c->part);
   }
   c->launches += nn ? 3 : 2;
   enqueue_apply_tiled(c, c->p2, c->Apf, true, c->part, &c->sc->done[0], c->sc);
@@ -842,7 +840,6 @@ static int fcg(Ctx* c, const double* f, bool nn, bool coarse, double tol, int ma
   if (nn && (!c->mp || !c->mp->ready)) return set_err(c, JFEM_ERR_INVALID, "no network weights (jfem_mpnn_init)");
   if (nn && (rc = mpnn_ensure_infer(c))) return rc;
   if (nn && (rc = mpnn_refresh_poly(c))) return rc;
-  if (nn && (rc = mpnn_graph_prepare(c))) return rc;
   if (coarse && (rc = coarse_prepare(c))) return rc;
   const auto kind_of = [&]() { return (nn ? 3 : 2) + (coarse ? 2 : 0); };
   if (x_zero) {
