@@ -281,9 +281,8 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS, 4) k_tile_boundary(int64_t n
       y[3 * gg + 1] = s1;
       y[3 * gg + 2] = s2;
       if (part) {
-        dot = df_add(dot, df_mul_f(vv[r][0], s0));
-        dot = df_add(dot, df_mul_f(vv[r][1], s1));
-        dot = df_add(dot, df_mul_f(vv[r][2], s2));
+        dot = df_add_abs(dot, df_add_abs(df_dot_term(vv[r][0], s0),
+                                         df_add_abs(df_dot_term(vv[r][1], s1), df_dot_term(vv[r][2], s2))));
       }
     }
   }

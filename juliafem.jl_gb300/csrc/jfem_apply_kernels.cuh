@@ -629,9 +629,8 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
           y[3 * g + 1] = s1;
           y[3 * g + 2] = s2;
           if (part) {   // v·y in double-float from the staged (masked) v
-            dot = df_add(dot, df_mul_f(vs[3 * j], s0));
-            dot = df_add(dot, df_mul_f(vs[3 * j + 1], s1));
-            dot = df_add(dot, df_mul_f(vs[3 * j + 2], s2));
+            dot = df_add_abs(dot, df_add_abs(df_dot_term(vs[3 * j], s0),
+                                             df_add_abs(df_dot_term(vs[3 * j + 1], s1), df_dot_term(vs[3 * j + 2], s2))));
           }
         } else {   // shared node: partial sum; the boundary pass applies the mask
           bpart[-1 - o] = make_float4(s0, s1, s2, 0.f);

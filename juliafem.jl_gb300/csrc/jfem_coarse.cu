@@ -36,9 +36,10 @@
 //                    its original diagonal drops that mode);
 // the inverse is rounded to FP32 for the per-iteration coarse solve.
 // Per CG iteration: k_coarse_restrict (one CTA per chunk of an aggregate's
-// nodes: partial force and moment resultants of r about c_a), k_coarse_gemv
-// (each block sums the chunk partials into shared memory, then Ec = A_c⁻¹ Pᵀ r
-// one warp per row); the prolongation P Ec is fused into the kernel that forms z.
+// nodes: partial force and moment resultants of r about c_a; the aggregate's
+// last chunk to finish sums its chunks in chunk order into Pᵀ r), k_coarse_gemv
+// (Ec = A_c⁻¹ Pᵀ r, one warp per row); the prolongation P Ec is fused into the
+// kernel that forms z.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -338,8 +339,12 @@ __global__ void __launch_bounds__(256) k_coarse_restrict(int n_chunks, const int
                                                          const float4* __restrict__ d32,
                                                          const float2* __restrict__ r,
                                                          const float* __restrict__ qold, const int* __restrict__ stop,
-                                                         float* __restrict__ cpart) {
-  __shared__ double sh[8][12];
+                                                         const int* __restrict__ chunk_agg,
+                                                         const int* __restrict__ agg_chunk_ptr,
+                                                         unsigned* __restrict__ agg_cnt, int ld,
+                                                         float* __restrict__ cpart, float* __restrict__ RQ) {
+  __shared__ float sh[8][12];
+  __shared__ int last;
   if (stop && *stop) return;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int ch = blockIdx.x;
@@ -374,53 +379,64 @@ __global__ void __launch_bounds__(256) k_coarse_restrict(int n_chunks, const int
     add_resultants(s, dv[u], rv[u][0].x + rv[u][0].y, rv[u][1].x + rv[u][1].y, rv[u][2].x + rv[u][2].y);
     if (qold) add_resultants(s + 6, dv[u], qv[u][0], qv[u][1], qv[u][2]);
   }
-  // FP32 warp trees (GB300's FP64 pipe would make a 32-lane FP64 tree the
-  // kernel's bottleneck), FP64 across the block's warps
+  // FP32 warp trees, then the block's warps in order (FP32: the coarse level
+  // is an FP32 preconditioner component; GB300's FP64 pipe would be the
+  // kernel's bottleneck)
 #pragma unroll
   for (int k = 0; k < 12; ++k) {
     if (k < nk) {   // nk is the same for the whole block
       float v = s[k];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) sh[wid][k] = (double)v;
+      if (lane == 0) sh[wid][k] = v;
     }
   }
   __syncthreads();
   if (threadIdx.x < nk) {
-    double v = 0.0;
+    float v = 0.f;
     for (int q = 0; q < nw; ++q) v += sh[q][threadIdx.x];
-    cpart[12 * ch + threadIdx.x] = (float)v;
+    cpart[12 * ch + threadIdx.x] = v;
+    __threadfence();
   }
+  __syncthreads();
+  // the aggregate's last chunk to finish sums its chunks' partials in chunk
+  // order into Pᵀr (RQ[0..ld)) and Pᵀq_old (RQ[ld..2ld)); nothing waits
+  const int a = chunk_agg[ch];
+  const int c0 = agg_chunk_ptr[a], c1 = agg_chunk_ptr[a + 1];
+  if (threadIdx.x == 0) last = atomicAdd(agg_cnt + a, 1u) == (unsigned)(c1 - c0 - 1) ? 1 : 0;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x < nk) {
+    float v = 0.f;
+    for (int q = c0; q < c1; ++q) v += __ldcg(cpart + 12 * q + threadIdx.x);
+    const int k = threadIdx.x % 6, half = threadIdx.x / 6;
+    RQ[half * ld + 6 * a + k] = v;
+  }
+  if (threadIdx.x == 0) agg_cnt[a] = 0;
 }
 
-// Ec = A_c⁻¹ Pᵀ r.  Every block first sums the chunk partials of each aggregate
-// (chunks of an aggregate are contiguous; fixed order) into shared memory —
-// Pᵀ r, and Pᵀ q_old when t2part is given — then one warp per row forms the
-// row's dot product from contiguous float4 loads of A_c⁻¹ (FP32, fixed lane
-// order and shuffle tree).  With t2part, also the products Ec_row·(Pᵀq_old)_row,
-// summed over the block's rows in warp order, into t2part[block].
+// Ec = A_c⁻¹ Pᵀ r, one warp per row: Pᵀr (and Pᵀq_old with t2part) staged in
+// shared memory from the restriction's per-aggregate sums, then each lane
+// issues its contiguous float4 loads of the row of A_c⁻¹ (FP32) in batches of
+// CG_GEMV_BATCH before it adds (fixed lane order and shuffle tree).  With
+// t2part, also the products Ec_row·(Pᵀq_old)_row, summed over the block's rows
+// in warp order, into t2part[block]; with sc, β (fcg_beta_last_block).
 #define CG_GEMV_MAX JFEM_COARSE_MAX_DOFS
-__global__ void __launch_bounds__(256) k_coarse_gemv(int nc, int ld, const float* __restrict__ Ainv, int nagg,
-                                                     const int* __restrict__ agg_chunk_ptr,
-                                                     const float* __restrict__ cpart, const int* __restrict__ stop,
-                                                     float* __restrict__ Ec, double* __restrict__ t2part) {
+#define CG_GEMV_BATCH 12
+__global__ void __launch_bounds__(256) k_coarse_gemv(int nc, int ld, const float* __restrict__ Ainv,
+                                                     const float* __restrict__ RQ, const int* __restrict__ stop,
+                                                     float* __restrict__ Ec, double* __restrict__ t2part,
+                                                     SolverScalars* __restrict__ sc, const double* __restrict__ t1,
+                                                     int n1) {
   __shared__ __align__(16) float R[CG_GEMV_MAX];
   __shared__ float Q[CG_GEMV_MAX];
-  __shared__ double sh[8];
+  __shared__ double sh[32];
   if (stop && *stop) return;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int t = threadIdx.x; t < ld; t += blockDim.x) {
-    float sr = 0.f, sq = 0.f;
-    if (t < 6 * nagg) {
-      const int ag = t / 6, k = t % 6;
-#pragma unroll 4
-      for (int ch = agg_chunk_ptr[ag]; ch < agg_chunk_ptr[ag + 1]; ++ch) {
-        sr += cpart[12 * ch + k];
-        if (t2part) sq += cpart[12 * ch + 6 + k];
-      }
-    }
-    R[t] = sr;
-    Q[t] = sq;
+    R[t] = __ldcg(RQ + t);
+    Q[t] = t2part ? __ldcg(RQ + ld + t) : 0.f;
   }
   __syncthreads();
   const int row = blockIdx.x * (blockDim.x >> 5) + wid;
@@ -428,14 +444,24 @@ __global__ void __launch_bounds__(256) k_coarse_gemv(int nc, int ld, const float
   if (row < nc) {
     const float4* a = reinterpret_cast<const float4*>(Ainv + (int64_t)row * ld);
     const float4* x = reinterpret_cast<const float4*>(R);
+    const int n4 = ld / 4;
     float s = 0.f;
-#pragma unroll 4
-    for (int j = lane; j < ld / 4; j += 32) {
-      const float4 av = a[j], xv = x[j];
-      s = fmaf(av.x, xv.x, s);
-      s = fmaf(av.y, xv.y, s);
-      s = fmaf(av.z, xv.z, s);
-      s = fmaf(av.w, xv.w, s);
+    for (int j0 = lane; j0 < n4; j0 += 32 * CG_GEMV_BATCH) {
+      float4 av[CG_GEMV_BATCH];
+#pragma unroll
+      for (int b = 0; b < CG_GEMV_BATCH; ++b) {
+        const int j = j0 + 32 * b;
+        av[b] = j < n4 ? __ldg(a + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int b = 0; b < CG_GEMV_BATCH; ++b) {
+        const int j = j0 + 32 * b;
+        const float4 xv = j < n4 ? x[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        s = fmaf(av[b].x, xv.x, s);
+        s = fmaf(av[b].y, xv.y, s);
+        s = fmaf(av[b].z, xv.z, s);
+        s = fmaf(av[b].w, xv.w, s);
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -449,6 +475,12 @@ __global__ void __launch_bounds__(256) k_coarse_gemv(int nc, int ld, const float
     double t = 0.0;
     for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sh[q];
     t2part[blockIdx.x] = t;
+  }
+  // with sc: the last block forms flexible CG's β from the smoother's t1
+  // partials (written by an earlier launch) and this launch's t2 partials
+  if (sc && arrive_last(&sc->arrive[2])) {
+    fcg_beta_last_block(sc, t1, n1, t2part, (int)gridDim.x, sh);
+    if (threadIdx.x == 0) sc->arrive[2] = 0;
   }
 }
 
@@ -548,9 +580,12 @@ static int coarse_build(Ctx* c, int target_nc) {
     for (int64_t i = 0; i < N; ++i) agg_nodes[(size_t)cur[(size_t)node_agg[(size_t)i]]++] = (int)i;
   }
   // restriction chunks: each aggregate's node list cut into pieces of ≤ CR_CHUNK
-  std::vector<int> chunk_begin, agg_chunk_ptr(1, 0);
+  std::vector<int> chunk_begin, agg_chunk_ptr(1, 0), chunk_agg;
   for (int a = 0; a < nagg; ++a) {
-    for (int t = agg_ptr[(size_t)a]; t < agg_ptr[(size_t)a + 1]; t += CR_CHUNK) chunk_begin.push_back(t);
+    for (int t = agg_ptr[(size_t)a]; t < agg_ptr[(size_t)a + 1]; t += CR_CHUNK) {
+      chunk_begin.push_back(t);
+      chunk_agg.push_back(a);
+    }
     agg_chunk_ptr.push_back((int)chunk_begin.size());
   }
   const int n_chunks = (int)chunk_begin.size();
@@ -637,7 +672,7 @@ static int coarse_build(Ctx* c, int target_nc) {
   }
   void* old[] = {c->agg_ptr, c->agg_nodes, c->node_agg, c->node_d32, c->node_ddf, c->celem, c->celem_aggs,
                  c->celem_off, c->contrib, c->cblk_ab, c->cblk_ptr, c->cblk_src, c->Ac, c->Ac_diag, c->gj_buf,
-                 c->Ainv32, c->Ec, c->chunk_begin, c->agg_chunk_ptr, c->cpart};
+                 c->Ainv32, c->Ec, c->chunk_begin, c->agg_chunk_ptr, c->cpart, c->chunk_agg, c->agg_cnt, c->RQ};
   for (void* p : old) dfree(c, p);
   c->nagg = nagg;
   c->nc = nc;
@@ -656,7 +691,8 @@ static int coarse_build(Ctx* c, int target_nc) {
       (rc = dalloc(c, &c->cblk_src, cblk_src.size())) || (rc = dalloc(c, &c->Ac, (size_t)nc_pad * nc_pad)) ||
       (rc = dalloc(c, &c->Ac_diag, (size_t)nc_pad)) || (rc = dalloc(c, &c->chunk_begin, (size_t)n_chunks + 1)) ||
       (rc = dalloc(c, &c->agg_chunk_ptr, (size_t)nagg + 1)) ||
-      (rc = dalloc(c, &c->cpart, (size_t)12 * n_chunks)) ||
+      (rc = dalloc(c, &c->cpart, (size_t)12 * n_chunks)) || (rc = dalloc(c, &c->chunk_agg, (size_t)n_chunks)) ||
+      (rc = dalloc(c, &c->agg_cnt, (size_t)nagg)) || (rc = dalloc(c, &c->RQ, (size_t)2 * nc_pad)) ||
       (rc = dalloc(c, &c->gj_buf, (size_t)GJ_B * GJ_B + 2 * (size_t)GJ_B * nc_pad)) ||
       (rc = dalloc(c, &c->Ainv32, (size_t)nc_pad * nc_pad)) || (rc = dalloc(c, &c->Ec, (size_t)nc_pad)))
     return rc;
@@ -676,6 +712,9 @@ static int coarse_build(Ctx* c, int target_nc) {
   up(c->cblk_src, cblk_src.data(), cblk_src.size() * sizeof(int64_t));
   up(c->chunk_begin, chunk_begin.data(), chunk_begin.size() * sizeof(int));
   up(c->agg_chunk_ptr, agg_chunk_ptr.data(), agg_chunk_ptr.size() * sizeof(int));
+  up(c->chunk_agg, chunk_agg.data(), chunk_agg.size() * sizeof(int));
+  cudaMemsetAsync(c->agg_cnt, 0, (size_t)nagg * sizeof(unsigned), c->stream);
+  cudaMemsetAsync(c->RQ, 0, (size_t)2 * nc_pad * sizeof(float), c->stream);
   cudaMemsetAsync(c->Ec, 0, (size_t)nc_pad * sizeof(float), c->stream);
   if ((rc = sync_and_check(c, "coarse set-up upload"))) return rc;
   c->coarse_mask_gen = c->mask_gen;
@@ -764,11 +803,13 @@ int coarse_prepare(Ctx* c) {
 
 int coarse_gemv_blocks(const Ctx* c) { return (c->nc + 7) / 8; }
 
-void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop, const float* qold, double* t2part) {
+void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop, const float* qold, double* t2part,
+                                   SolverScalars* sc, const double* t1, int n1) {
   k_coarse_restrict<<<c->n_chunks, 256, 0, c->stream>>>(c->n_chunks, c->chunk_begin, c->agg_nodes, c->node_d32, r,
-                                                        t2part ? qold : nullptr, stop, c->cpart);
-  k_coarse_gemv<<<coarse_gemv_blocks(c), 256, 0, c->stream>>>(c->nc, c->nc_pad, c->Ainv32, c->nagg, c->agg_chunk_ptr,
-                                                              c->cpart, stop, c->Ec, t2part);
+                                                        t2part ? qold : nullptr, stop, c->chunk_agg,
+                                                        c->agg_chunk_ptr, c->agg_cnt, c->nc_pad, c->cpart, c->RQ);
+  k_coarse_gemv<<<coarse_gemv_blocks(c), 256, 0, c->stream>>>(c->nc, c->nc_pad, c->Ainv32, c->RQ, stop, c->Ec,
+                                                              t2part, sc, t1, n1);
   c->launches += 2;
 }
 

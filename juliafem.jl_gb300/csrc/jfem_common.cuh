@@ -209,12 +209,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
 // Prolongation of the two-level preconditioner at DOF (i, c): (P Ec)_ic =
 // t_a + (ω_a × d_i)_c with (t_a, ω_a) = Ec[6a .. 6a+5], a the aggregate of node
 // i and d_i = X_i − c_a (jfem_coarse.cu).  The caller applies the Dirichlet mask.
+__device__ __forceinline__ float coarse_prolong_v(const float* e, float4 d, int c) {
+  return c == 0 ? e[0] + e[4] * d.z - e[5] * d.y : c == 1 ? e[1] + e[5] * d.x - e[3] * d.z : e[2] + e[3] * d.y - e[4] * d.x;
+}
 __device__ __forceinline__ float coarse_prolong(const int* __restrict__ node_agg, const float4* __restrict__ d32,
                                                 const float* __restrict__ Ec, int64_t i, int c) {
-  const int a = node_agg[i];
-  const float4 d = d32[i];
-  const float* e = Ec + 6 * a;
-  return c == 0 ? e[0] + e[4] * d.z - e[5] * d.y : c == 1 ? e[1] + e[5] * d.x - e[3] * d.z : e[2] + e[3] * d.y - e[4] * d.x;
+  return coarse_prolong_v(Ec + 6 * node_agg[i], d32[i], c);
 }
 
 // ---------------------------------------------------------------------------
@@ -425,6 +425,9 @@ struct Ctx {
   int* chunk_begin = nullptr;   // [n_chunks+1] into agg_nodes
   int* agg_chunk_ptr = nullptr; // [nagg+1] the chunks of each aggregate (contiguous)
   float* cpart = nullptr;       // [n_chunks][12] chunk partials of Pᵀ r and Pᵀ q_old
+  int* chunk_agg = nullptr;     // [n_chunks] aggregate of each restriction chunk
+  unsigned* agg_cnt = nullptr;  // [nagg] chunks of the aggregate finished in this restriction (back to 0)
+  float* RQ = nullptr;          // [2][nc_pad] Pᵀr, Pᵀq_old (zero beyond nc)
   float* Ec = nullptr;          // [nc_pad] coarse correction A_c⁻¹ Pᵀ r
   double coarse_setup_ms = 0.0; // last coarse value setup (CUDA events)
 
@@ -507,7 +510,7 @@ int mpnn_ensure_infer(Ctx* c);                             // the float4 inferen
 // leaves block partials of Σ D^{-1/2}(y + v)·q_old (flexible CG's β) and
 // returns the number of blocks.
 int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf = nullptr, const float* qold = nullptr,
-                     double* t1part = nullptr);
+                     double* t1part = nullptr, SolverScalars* sc = nullptr, const double* t2 = nullptr, int n2 = 0);
 // jfem_coarse.cu
 int coarse_prepare(Ctx* c);   // structure and values for the current mesh, mask and geometry
 int coarse_info(Ctx* c, int* n_agg, int* n_coarse, int64_t* n_elem_listed, double* setup_ms);
@@ -515,7 +518,8 @@ int coarse_matrix(Ctx* c, double* Ac_h, int* node_agg_h);
 int coarse_precondition(Ctx* c, const double* r_h, double* z_h);
 // Ec = A_c⁻¹ Pᵀ r; with qold, also the block partials of Ec·Pᵀ q_old into t2part
 void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop, const float* qold = nullptr,
-                                   double* t2part = nullptr);
+                                   double* t2part = nullptr, SolverScalars* sc = nullptr, const double* t1 = nullptr,
+                                   int n1 = 0);
 int coarse_gemv_blocks(const Ctx* c);
 // jfem_recovery.cu
 int recover_field(Ctx* c, const double* u_h, int field, double tol, int max_iter, double* nodal_h, int* iters_out);
@@ -524,6 +528,28 @@ int pcg_fp64_snapshots(Ctx* c, const double* f, double tol, int max_iter, double
                        int* n_snaps, int* snap_iters, int* iters_out, double* relres_out);
 void enqueue_axpy(Ctx* c, int64_t n, double a, const double* x, double* y);
 int solve_device(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stats* st);
+
+}  // namespace jfem
+
+#include "jfem_df.cuh"
+
+namespace jfem {
+
+// Flexible CG's β = (Σ t1 + Σ t2) / p·q_old (0 on restart), each partial list
+// summed in index order (FP64) as k_fcg_beta sums them — run by the last block
+// of the launch that writes the final partials (after arrive_last), so β needs
+// no launch of its own.  sh: ≥ 32 doubles of shared memory.
+__device__ __forceinline__ void fcg_beta_last_block(SolverScalars* sc, const double* t1, int n1, const double* t2,
+                                                    int n2, double* sh) {
+  const double a = reduce_partials_cg(t1, n1, sh);
+  const double b = t2 ? reduce_partials_cg(t2, n2, sh) : 0.0;
+  if (threadIdx.x == 0) {
+    const double beta = sc->restart ? 0.0 : (a + b) / sc->pAp;
+    sc->beta = beta;
+    sc->beta_df = df_from_double(beta);
+    sc->restart = 0;
+  }
+}
 
 }  // namespace jfem
 

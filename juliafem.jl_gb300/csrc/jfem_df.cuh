@@ -51,10 +51,19 @@ __device__ __forceinline__ float2 df_add(float2 x, float2 y) {
 // parts added in FP32, one Fast2Sum.  Its error is bounded in absolute terms,
 // ≈ 2u²(|x| + |y|), not relative to the result (no bound under cancellation):
 // for sums judged against the size of their terms, e.g. matrix entries
-// compared relative to max |K|.  11 operations against 20 for df_add.
+// compared relative to max |K|, and the dot products of the solvers, whose
+// per-thread sums of a few terms then meet FP64 block sums (error ≈ 2u² of the
+// summed magnitudes per term, FP64-class).  11 operations against 20 for df_add.
 __device__ __forceinline__ float2 df_add_abs(float2 x, float2 y) {
   const float2 s = df_two_sum(x.x, y.x);
   return df_fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(x.y, y.y)));
+}
+
+// x·y for a dot-product sum: hi·y exactly (TwoProd) plus lo·y in FP32, left
+// unnormalised (the next df_add_abs renormalises); 3 operations.
+__device__ __forceinline__ float2 df_dot_term(float2 x, float y) {
+  const float2 p = df_two_prod(x.x, y);
+  return make_float2(p.x, __fmaf_rn(x.y, y, p.y));
 }
 
 __device__ __forceinline__ float2 df_mul_f(float2 x, float y) {

@@ -586,14 +586,16 @@ __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __res
 // Horner step of the adjoint: out = C_kᵀ u + Aᵀ g (g.w = 1/deg); out.w = 1/deg_i
 // for the next step.  FCG (the last step, out = v = NᵀN y): also block partials
 // of Σ D^{-1/2}(y + v)·q_old, flexible CG's β term of the smoother, into
-// t1part[block] (fixed order).
+// t1part[block] (fixed order), and with sc flexible CG's β in the last block.
 template <bool FCG>
 __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __restrict__ nb_ptr,
                                                      const int* __restrict__ nbr, const float* __restrict__ invdeg,
                                                      const float4* __restrict__ g, const float4* __restrict__ u,
                                                      const float* __restrict__ poly, int k, float4* __restrict__ out,
                                                      const float4* __restrict__ y, const float* __restrict__ dinvf,
-                                                     const float* __restrict__ qold, double* __restrict__ t1part) {
+                                                     const float* __restrict__ qold, double* __restrict__ t1part,
+                                                     SolverScalars* __restrict__ sc, const double* __restrict__ t2,
+                                                     int n2) {
   __shared__ float C[9];
   __shared__ double sh[32];
   if (threadIdx.x < 9) C[threadIdx.x] = poly[9 * k + threadIdx.x];
@@ -615,12 +617,18 @@ __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __res
       const float yv[3] = {y4.x, y4.y, y4.z};
 #pragma unroll
       for (int c = 0; c < 3; ++c)
-        t1 = df_add(t1, df_two_prod(sqrtf(dinvf[3 * i + c]) * (yv[c] + s[c]), qold[3 * i + c]));
+        t1 = df_add_abs(t1, df_two_prod(sqrtf(dinvf[3 * i + c]) * (yv[c] + s[c]), qold[3 * i + c]));
     }
   }
   if (FCG) {
     const double b = block_sum_df(t1, sh);
     if (threadIdx.x == 0) t1part[blockIdx.x] = b;
+    // with sc: the last block forms flexible CG's β (t2: the coarse level's
+    // partials from an earlier launch, or none)
+    if (sc && arrive_last(&sc->arrive[2])) {
+      fcg_beta_last_block(sc, t1part, (int)gridDim.x, t2, n2, sh);
+      if (threadIdx.x == 0) sc->arrive[2] = 0;
+    }
   }
 }
 
@@ -893,7 +901,8 @@ int mpnn_ensure_infer(Ctx* c) {
   return 0;
 }
 
-int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf, const float* qold, double* t1part) {
+int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf, const float* qold, double* t1part,
+                     SolverScalars* sc, const double* t2, int n2) {
   const float* P = c->mp->poly;
   // a resident grid (8 CTAs of 256 per SM) striding over the nodes; its block
   // partials are what flexible CG's β sums
@@ -907,15 +916,15 @@ int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf, con
   k_mp_poly_fwd<true><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, a2, y, a1, P, c->mask, u, h);
   // h = C3ᵀu;  g2 = C2ᵀu + Aᵀh;  h = C1ᵀu + Aᵀg2;  v = C0ᵀu + Aᵀh
   k_mp_poly_adj<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 2, g2, nullptr, nullptr,
-                                                  nullptr, nullptr);
+                                                  nullptr, nullptr, nullptr, nullptr, 0);
   k_mp_poly_adj<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, g2, u, P, 1, h, nullptr, nullptr,
-                                                  nullptr, nullptr);
+                                                  nullptr, nullptr, nullptr, nullptr, 0);
   if (t1part)
     k_mp_poly_adj<true><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 0, v, y, dinvf, qold,
-                                                   t1part);
+                                                   t1part, sc, t2, n2);
   else
     k_mp_poly_adj<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 0, v, nullptr,
-                                                    nullptr, nullptr, nullptr);
+                                                    nullptr, nullptr, nullptr, nullptr, nullptr, 0);
   c->launches += 6;
   return (int)g;
 }

@@ -187,8 +187,8 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_dfcg_update1(int64_t n, So
     x[i] = df_add(x[i], df_mul(a, p[i]));
     const float2 ri = df_add(r[i], df_mul_f(na, Ap[i]));
     r[i] = ri;
-    rz = df_add(rz, df_mul(ri, df_mul_f(ri, dinv[i])));
-    rr = df_add(rr, df_mul(ri, ri));
+    rz = df_add_abs(rz, df_mul(ri, df_mul_f(ri, dinv[i])));
+    rr = df_add_abs(rr, df_mul(ri, ri));
   }
   const double2 zr = block_sum2_df(rz, rr, sh);
   if (threadIdx.x == 0) {
@@ -233,8 +233,8 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_dfcg_precond(int64_t n, co
     const float2 ri = r[i];
     const float2 zi = df_mul_f(ri, dinv[i]);
     if (restart) p[i] = zi;
-    rz = df_add(rz, df_mul(ri, zi));
-    rr = df_add(rr, df_mul(ri, ri));
+    rz = df_add_abs(rz, df_mul(ri, zi));
+    rr = df_add_abs(rr, df_mul(ri, ri));
   }
   const double rzb = block_sum_df(rz, sh);
   const double rrb = block_sum_df(rr, sh);
@@ -405,7 +405,7 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_beta(SolverScalars* __
 // when COARSE, zero on prescribed DOFs (D⁻¹ is zero there).  p·r partials →
 // the last block leaves p·r for α.
 template <bool NN, bool COARSE>
-__global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_zp(int64_t N, const float4* __restrict__ y,
+__global__ void __launch_bounds__(JFEM_RED_THREADS, 4) k_fcg_zp(int64_t N, const float4* __restrict__ y,
                                                              const float4* __restrict__ v,
                                                              const float* __restrict__ dinv,
                                                              const uint8_t* __restrict__ mask,
@@ -419,33 +419,76 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_zp(int64_t N, const fl
   const float2 nb = df_neg(sc->beta_df);
   const bool keep = sc->beta != 0.0;
   float2 dot = make_float2(0.f, 0.f);
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-    float zc[3];
-    if (NN) {
-      const float4 y4 = y[i], v4 = v[i];
-      zc[0] = sqrtf(dinv[3 * i]) * (y4.x + v4.x);
-      zc[1] = sqrtf(dinv[3 * i + 1]) * (y4.y + v4.y);
-      zc[2] = sqrtf(dinv[3 * i + 2]) * (y4.z + v4.z);
-    } else {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // ND nodes per thread and round (two with the Jacobi smoother; the
+  // network's variant needs the registers for its own vectors): every load
+  // (and the coarse aggregate's Ec after its index) is issued before any
+  // arithmetic
+  constexpr int ND = NN ? 1 : 2;
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < N; i0 += ND * stride) {
+    int64_t ii[ND];
+    bool val[ND];
+#pragma unroll
+    for (int n = 0; n < ND; ++n) {
+      ii[n] = i0 + n * stride;
+      val[n] = ii[n] < N;
+    }
+    float2 rq[ND][3], po[ND][3];
+    float dv[ND][3];
+    float4 y4[ND], v4[ND], dd[ND];
+    int ag[ND];
+    uint8_t m[ND];
+#pragma unroll
+    for (int n = 0; n < ND; ++n) {
+      const int64_t i = val[n] ? ii[n] : i0;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const float2 rq = r[3 * i + c];
-        zc[c] = dinv[3 * i + c] * (rq.x + rq.y);
+        rq[n][c] = r[3 * i + c];
+        po[n][c] = keep ? p[3 * i + c] : make_float2(0.f, 0.f);
+        dv[n][c] = dinv[3 * i + c];
+      }
+      if (NN) {
+        y4[n] = y[i];
+        v4[n] = v[i];
+      }
+      if (COARSE) {
+        m[n] = mask[i];
+        ag[n] = node_agg[i];
+        dd[n] = d32[i];
       }
     }
+    float ec[ND][6];
     if (COARSE) {
-      const uint8_t m = mask[i];
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
-        if (!((m >> c) & 1)) zc[c] += coarse_prolong(node_agg, d32, Ec, i, c);
+      for (int n = 0; n < ND; ++n)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) ec[n][k] = Ec[6 * ag[n] + k];
     }
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const int64_t q = 3 * i + c;
-      float2 pi = make_float2(zc[c], 0.f);
-      if (keep) pi = df_add(pi, df_mul(nb, p[q]));
-      p[q] = pi;
-      dot = df_add(dot, df_mul(pi, r[q]));
+    for (int n = 0; n < ND; ++n) {
+      if (!val[n]) continue;
+      const int64_t i = ii[n];
+      float zc[3];
+      if (NN) {
+        zc[0] = sqrtf(dv[n][0]) * (y4[n].x + v4[n].x);
+        zc[1] = sqrtf(dv[n][1]) * (y4[n].y + v4[n].y);
+        zc[2] = sqrtf(dv[n][2]) * (y4[n].z + v4[n].z);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) zc[c] = dv[n][c] * (rq[n][c].x + rq[n][c].y);
+      }
+      if (COARSE) {   // P Ec at the node: e_a + θ_a × d
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          if (!((m[n] >> c) & 1)) zc[c] += coarse_prolong_v(ec[n], dd[n], c);
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float2 pi = make_float2(zc[c], 0.f);
+        if (keep) pi = df_add(pi, df_mul(nb, po[n][c]));
+        p[3 * i + c] = pi;
+        dot = df_add_abs(dot, df_mul(pi, rq[n][c]));
+      }
     }
   }
   const double b = block_sum_df(dot, sh);
@@ -477,8 +520,8 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_update(int64_t n, Solv
     const float qi = q[i];
     const float2 ri = df_add(r[i], df_mul_f(na, qi));
     r[i] = ri;
-    rr = df_add(rr, df_mul(ri, ri));
-    if (T1) t1 = df_add(t1, df_two_prod(dinv[i] * (ri.x + ri.y), qi));
+    rr = df_add_abs(rr, df_mul(ri, ri));
+    if (T1) t1 = df_add_abs(t1, df_two_prod(dinv[i] * (ri.x + ri.y), qi));
   }
   const double2 bs = block_sum2_df(rr, t1, sh);
   if (threadIdx.x == 0) {
@@ -508,8 +551,8 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_norms(int64_t n, const
   float2 rr = make_float2(0.f, 0.f), t1 = make_float2(0.f, 0.f);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 ri = r[i];
-    rr = df_add(rr, df_mul(ri, ri));
-    t1 = df_add(t1, df_two_prod(dinv[i] * (ri.x + ri.y), qold[i]));
+    rr = df_add_abs(rr, df_mul(ri, ri));
+    t1 = df_add_abs(t1, df_two_prod(dinv[i] * (ri.x + ri.y), qold[i]));
   }
   const double2 bs = block_sum2_df(rr, t1, sh);
   if (threadIdx.x == 0) {
@@ -577,7 +620,12 @@ static int true_residual(Ctx* c, const double* f, const double* xv, double* r, d
 static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
   const int64_t n = 3 * c->N;
   double* t2 = coarse ? c->part + JFEM_PART_T2 : nullptr;
-  if (coarse) enqueue_coarse_restrict_solve(c, c->rd, &c->sc->done[0], c->Apf, t2);
+  // β is formed by the last block of the launch that writes the last of its
+  // partials: the network's last pass (nn), else the coarse solve (coarse),
+  // else its own launch
+  if (coarse)
+    enqueue_coarse_restrict_solve(c, c->rd, &c->sc->done[0], c->Apf, t2, nn ? nullptr : c->sc,
+                                  c->part + JFEM_PART_T1, G_);
   const int n2 = coarse ? coarse_gemv_blocks(c) : 0;
   const int* na = coarse ? c->node_agg : nullptr;
   const float4* d32 = coarse ? c->node_d32 : nullptr;
@@ -586,8 +634,7 @@ static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
   float4* v = c->mi ? c->mi + 6 * c->N : nullptr;
   if (nn) {
     k_fcg_input<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, y);
-    const int n1 = enqueue_mpnn_spd(c, y, v, c->dinvf, c->Apf, c->part + JFEM_PART_T1N);
-    k_fcg_beta<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part + JFEM_PART_T1N, n1, t2, n2);
+    enqueue_mpnn_spd(c, y, v, c->dinvf, c->Apf, c->part + JFEM_PART_T1N, c->sc, t2, n2);
     if (coarse)
       k_fcg_zp<true, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, y, v, c->dinvf, c->mask, na, d32, Ec, c->p2,
                                                                    c->rd, c->sc, c->part);
@@ -595,7 +642,7 @@ static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
       k_fcg_zp<true, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, y, v, c->dinvf, c->mask, na, d32, Ec, c->p2,
                                                                     c->rd, c->sc, c->part);
   } else {
-    k_fcg_beta<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part + JFEM_PART_T1, G_, t2, n2);
+    if (!coarse) k_fcg_beta<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part + JFEM_PART_T1, G_, t2, n2);
     if (coarse)
       k_fcg_zp<false, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, nullptr, nullptr, c->dinvf, c->mask, na, d32,
                                                                     Ec, c->p2, c->rd, c->sc, c->part);
@@ -603,7 +650,7 @@ static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
       k_fcg_zp<false, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, nullptr, nullptr, c->dinvf, c->mask, na,
                                                                      d32, Ec, c->p2, c->rd, c->sc, c->part);
   }
-  c->launches += nn ? 3 : 2;
+  c->launches += nn ? 2 : (coarse ? 1 : 2);
   enqueue_apply_tiled(c, c->p2, c->Apf, true, c->part, &c->sc->done[0], c->sc);
   if (nn)
     k_fcg_update<false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->xd, c->rd, c->p2, c->Apf, c->dinvf,

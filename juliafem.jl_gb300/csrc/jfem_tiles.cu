@@ -116,7 +116,7 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   // Per tile (independent, built on host threads): its sorted unique nodes,
   // their adjacency offsets, and which of them other tiles share.
   struct TileNodes {
-    std::vector<int> loc;            // global nodes of the tile, ascending
+    std::vector<int> loc;            // global nodes of the tile (element slots descending, then ascending)
     std::vector<uint16_t> ptr;       // L + 1 offsets into the tile's adjacency block
     std::vector<uint8_t> shared;     // node also in another tile
     int nshared = 0;
@@ -134,6 +134,24 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
     std::sort(loc.begin(), loc.end());
     loc.erase(std::unique(loc.begin(), loc.end()), loc.end());
     const int L = (int)loc.size();
+    // local order: element slots per node descending (ties: ascending global
+    // node), so the 32 nodes a warp sums have similar loop lengths
+    std::vector<int> cnt((size_t)L, 0), order((size_t)L), newidx((size_t)L);
+    for (int k = 0; k < T; ++k) {
+      const int e = perm[(size_t)(t * T + k)];
+      if (e < 0) continue;
+      for (int a = 0; a < nn; ++a) {
+        const int g = (int)(conn_h[(int64_t)e * nn + a] - base);
+        cnt[(size_t)(std::lower_bound(loc.begin(), loc.end(), g) - loc.begin())]++;
+      }
+    }
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cnt[(size_t)x] > cnt[(size_t)y]; });
+    std::vector<int> sorted_loc(loc);
+    for (int j = 0; j < L; ++j) {
+      newidx[(size_t)order[(size_t)j]] = j;
+      loc[(size_t)j] = sorted_loc[(size_t)order[(size_t)j]];
+    }
     lcnt.assign((size_t)L + 1, 0);
     // local connectivity and counts
     for (int k = 0; k < T; ++k) {
@@ -141,7 +159,7 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
       if (e < 0) continue;
       for (int a = 0; a < nn; ++a) {
         const int g = (int)(conn_h[(int64_t)e * nn + a] - base);
-        const int li = (int)(std::lower_bound(loc.begin(), loc.end(), g) - loc.begin());
+        const int li = newidx[(size_t)(std::lower_bound(sorted_loc.begin(), sorted_loc.end(), g) - sorted_loc.begin())];
         tconn[(size_t)a * Epad + t * T + k] = (uint16_t)li;
         lcnt[(size_t)li + 1]++;
       }
