@@ -434,9 +434,22 @@ __global__ void __launch_bounds__(256) k_coarse_gemv(int nc, int ld, const float
   __shared__ double sh[32];
   if (stop && *stop) return;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int t = threadIdx.x; t < ld; t += blockDim.x) {
-    R[t] = __ldcg(RQ + t);
-    Q[t] = t2part ? __ldcg(RQ + ld + t) : 0.f;
+  for (int t0 = threadIdx.x; t0 < ld; t0 += 8 * blockDim.x) {   // ld ≤ 4096: at most two rounds
+    float a[8], b[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int t = t0 + u * blockDim.x;
+      a[u] = t < ld ? __ldcg(RQ + t) : 0.f;
+      b[u] = (t2part && t < ld) ? __ldcg(RQ + ld + t) : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int t = t0 + u * blockDim.x;
+      if (t < ld) {
+        R[t] = a[u];
+        Q[t] = b[u];
+      }
+    }
   }
   __syncthreads();
   const int row = blockIdx.x * (blockDim.x >> 5) + wid;
