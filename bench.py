@@ -590,12 +590,14 @@ def run_gpu(args):
     achieved = alg_bytes / t_apply / 1e9
     # FP64 apply for the residual path, for reference
     ms_el64, ms_ga64 = ctx.time_apply(reps=10, fp32=False, masked=True)
-    # FP64 assembly of K's values and f_int (integration points + CSC scatter).
-    # Algorithmic work per element: the element matrix streamed as values and
-    # destination indices, (3·n_en)²·(8 + 4) bytes, plus the CSC values written
-    # (8·nnz); FP64 flops n_q·(400 + 60·n_en(n_en+1)/2) (geometry, then the
-    # isotropic block contractions).  written_bytes: what the result needs
-    # (K, f_int) plus the element inputs.
+    # Assembly of K's values and f_int (integration points + CSC scatter):
+    # FP64 geometry per integration point, the isotropic block contractions in
+    # double-float (48-bit) on the FP32 pipe, FP64 entries.  Algorithmic work
+    # per element: the element matrix streamed as values and destination
+    # indices, (3·n_en)²·(8 + 4) bytes, plus the CSC values written (8·nnz);
+    # n_q·(400 + 60·n_en(n_en+1)/2) FP64-equivalent operations (geometry, then
+    # the block contractions).  written_bytes: what the result needs (K, f_int)
+    # plus the element inputs.
     ms_q, ms_s, nnz = ctx.time_assembly(reps=3)
     t_asm = (ms_q + ms_s) / 1e3
     nq = 4
@@ -605,8 +607,9 @@ def run_gpu(args):
     assembly = {"elements_per_s": m.n_elem / t_asm, "ms": {"qpoint": ms_q, "scatter": ms_s},
                 "nnz": int(nnz), "algorithmic_bytes": int(asm_bytes),
                 "achieved_gbs": asm_bytes / t_asm / 1e9, "frac": asm_bytes / t_asm / 1e9 / peak,
-                "written_bytes": int(written), "fp64_gflops": asm_flops / t_asm / 1e9,
-                "fp64_nominal_peak_gflops": 1250.0, "bound": "fp64 pipe", "precision": "FP64"}
+                "written_bytes": int(written), "fp64_equivalent_gflops": asm_flops / t_asm / 1e9,
+                "fp64_nominal_peak_gflops": 1250.0,
+                "precision": "FP64 geometry, double-float block products and sums, FP64 entries"}
 
     # end to end through the C ABI from pinned host buffers: a new context per
     # step (mesh, material, loads, network weights uploaded; coarse level built)

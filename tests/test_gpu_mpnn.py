@@ -102,8 +102,12 @@ def test_preconditioner_matches_oracle_and_is_spd(jfem, orc):
 def test_fcg_with_zero_network_is_jacobi_pcg(jfem):
     """With Nᵀ N = 0 the preconditioner is Jacobi and flexible CG is PCG in
     exact arithmetic; in finite precision the two β formulas (z·q_old / p·q vs
-    r·z ratios) give different iteration counts, the same solution."""
-    w = jfem.workloads.learned_family(1, seed_item=901)[0]
+    r·z ratios) give different iteration counts, the same solution.  The system
+    is homogeneous and small (a few hundred iterations): on the heterogeneous
+    40×4×4 family members (σ_log 0.5, ~3,000 Jacobi iterations) both counts move
+    by 15–30 % with the summation order alone — loss of orthogonality, not the
+    method — so they cannot test this identity."""
+    w = jfem.workloads.learned_family(1, seed_item=901, nx=12, ny=3, nz=3, L=4.0, sigma_log=0.0)[0]
     with jfem.Context(0) as ctx:
         _setup(ctx, w)
         ctx.set_coarse_space(0)                  # one-level: the learned method without a coarse space
