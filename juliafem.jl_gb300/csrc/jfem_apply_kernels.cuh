@@ -405,12 +405,16 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
 // The loads of one tile are issued in two waves, so a tile waits for about
 // three global-memory latencies instead of one per node round:
 //   header   n0, L                                   (tnode_ptr)
+//   (nodes are staged in ascending global order — tnodes, coalesced — into
+//    their local slots tloc; the local order, by element slots descending,
+//    gives the gather's warps nodes of similar loop length)
 //   wave 1   bulk async copies (cp.async.bulk, one mbarrier, issued by the
 //            lanes of warp 0): the adjacency block, the NN connectivity rows
 //            and the 11 affine record rows of the tile (all 16-byte aligned:
 //            rows of T elements of a tile-padded [k][Epad] array);
-//            per node: global index, adjacency end offset
-//   wave 2   per node (depends on wave 1): mask byte, v (hi, lo) and u
+//            per node: global index, local slot
+//   wave 2   per node (depends on wave 1): adjacency end offset, mask byte,
+//            v (hi, lo) and u
 // The node gather then loads one output word per node (tout: the global node
 // when interior, −1 − slot when shared), sums its element slots from shared
 // memory and writes y (interior) or bpart[slot] (shared).  Optional v·y
@@ -447,7 +451,7 @@ static_assert(JFEM_TILE * 10 < (1 << TILE_PTR_BITS), "tile adjacency offsets mus
 template <int ET, bool AFFINE, int KIN, bool GEOM>
 __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS : (KIN == KIN_NHC ? 2 : 1)) k_tile_apply(
     int64_t ntiles, int64_t E, int64_t Epad, const int* __restrict__ tnode_ptr, const int* __restrict__ tnodes,
-    const uint16_t* __restrict__ tconn, const float* __restrict__ geo, const uint16_t* __restrict__ tadj_ptr,
+    const uint16_t* __restrict__ tloc, const uint16_t* __restrict__ tconn, const float* __restrict__ geo, const uint16_t* __restrict__ tadj_ptr,
     const uint16_t* __restrict__ tadj, const int* __restrict__ tout,
     const float2* __restrict__ v2, const double* __restrict__ u,
     const uint8_t* __restrict__ mask, int masked, int Lmax, float* __restrict__ y, float4* __restrict__ bpart,
@@ -502,29 +506,31 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
     const int L = __ldg(tnode_ptr + t + 1) - n0;
     const int64_t e = t * T + tid;
     const bool valid = e < E;
-    {   // node staging, wave 1: global index and adjacency end offset per node
-      int gn[NR];
-      unsigned pe[NR];
+    {   // node staging in ascending global order (coalesced), each node written
+        // to its local slot jl (the gather order); wave 1: global index, slot
+      int gn[NR], jl[NR];
 #pragma unroll
       for (int r = 0; r < NR; ++r) {
-        const int j = tid + r * T;
+        const int k = tid + r * T;
         gn[r] = 0;
-        pe[r] = 0;
-        if (j < L) {
-          gn[r] = __ldg(tnodes + n0 + j);
-          pe[r] = __ldg(tadj_ptr + n0 + t + j + 1);
+        jl[r] = 0;
+        if (k < L) {
+          gn[r] = __ldg(tnodes + n0 + k);
+          jl[r] = __ldg(tloc + n0 + k);
         }
       }
-      // wave 2: mask, v (hi, lo), u
-      unsigned mk[NR];
+      // wave 2: adjacency end offset, mask, v (hi, lo), u
+      unsigned mk[NR], pe[NR];
       float2 h[NR][3];
       float uu[NR][3];
 #pragma unroll
       for (int r = 0; r < NR; ++r) {
-        const int j = tid + r * T;
+        const int k = tid + r * T;
         mk[r] = 0;
-        if (j < L) {
+        pe[r] = 0;
+        if (k < L) {
           const int64_t g = gn[r];
+          pe[r] = __ldg(tadj_ptr + n0 + t + jl[r] + 1);
           mk[r] = masked ? (unsigned)__ldg(mask + g) : 0u;
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
@@ -535,8 +541,9 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
       }
 #pragma unroll
       for (int r = 0; r < NR; ++r) {
-        const int j = tid + r * T;
-        if (j < L) {
+        const int k = tid + r * T;
+        if (k < L) {
+          const int j = jl[r];
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             vs[3 * j + c] = ((mk[r] >> c) & 1) ? make_float2(0.f, 0.f) : h[r][c];
@@ -546,8 +553,9 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
         }
       }
       if (tid == 0) sptr[0] = 0;
-      for (int j = tid + NR * T; j < L; j += T) {   // tiles with more nodes than the unrolled rounds
-        const int64_t g = __ldg(tnodes + n0 + j);
+      for (int k = tid + NR * T; k < L; k += T) {   // tiles with more nodes than the unrolled rounds
+        const int64_t g = __ldg(tnodes + n0 + k);
+        const int j = __ldg(tloc + n0 + k);
         const unsigned m = masked ? (unsigned)__ldg(mask + g) : 0u;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -693,7 +701,7 @@ static void launch_tile_k(Ctx* c, const float2* v2, float* y, bool masked, doubl
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   const unsigned g = JFEM_RED_BLOCKS;   // CTAs take tiles b, b + g, …
   kern<<<g, JFEM_TILE, sm, c->stream>>>(
-      c->ntiles, c->E, c->Epad, c->tnode_ptr, c->tnodes, c->tconn, c->geoT32, c->tadj_ptr, c->tadj, c->tout,
+      c->ntiles, c->E, c->Epad, c->tnode_ptr, c->tnodes, c->tloc, c->tconn, c->geoT32, c->tadj_ptr, c->tadj, c->tout,
       v2, c->u_state, c->mask, masked ? 1 : 0, c->tile_Lmax, y, c->bpart, part, c->nhstate, c->d_err, stop);
   c->launches += 1;
 }

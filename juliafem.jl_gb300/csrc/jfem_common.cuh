@@ -340,7 +340,8 @@ struct Ctx {
   int* tperm = nullptr;         // [Epad] tile position → element (−1 padding)
   uint16_t* tconn = nullptr;    // [n_en][Epad] tile-local node of each element node
   int* tnode_ptr = nullptr;     // [ntiles+1]
-  int* tnodes = nullptr;        // global node of each tile node
+  int* tnodes = nullptr;        // [Σ L] each tile's nodes in ascending global order (the staging order)
+  uint16_t* tloc = nullptr;     // [Σ L] local index (gather order: element slots descending) of each
   uint16_t* tadj_ptr = nullptr; // per tile: L+1 offsets into the tile's adjacency block
   uint16_t* tadj = nullptr;     // [ntiles][T·n_en] local node · T + local element (an element-vector slot)
   int* tout = nullptr;          // per tile node: its global node when interior, −1 − (bpart position) when shared

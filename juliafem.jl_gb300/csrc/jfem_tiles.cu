@@ -116,6 +116,8 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   // Per tile (independent, built on host threads): its sorted unique nodes,
   // their adjacency offsets, and which of them other tiles share.
   struct TileNodes {
+    std::vector<int> asc;            // global nodes of the tile, ascending (the staging order)
+    std::vector<uint16_t> asc_loc;   // local index of each of them
     std::vector<int> loc;            // global nodes of the tile (element slots descending, then ascending)
     std::vector<uint16_t> ptr;       // L + 1 offsets into the tile's adjacency block
     std::vector<uint8_t> shared;     // node also in another tile
@@ -152,6 +154,8 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
       newidx[(size_t)order[(size_t)j]] = j;
       loc[(size_t)j] = sorted_loc[(size_t)order[(size_t)j]];
     }
+    o.asc = sorted_loc;
+    o.asc_loc.assign(newidx.begin(), newidx.end());
     lcnt.assign((size_t)L + 1, 0);
     // local connectivity and counts
     for (int k = 0; k < T; ++k) {
@@ -207,6 +211,7 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   // the slots in tile order keeps tiles ascending within a node).
   std::vector<int> slot_node((size_t)nslots);
   std::vector<int> tnodes((size_t)total), tout((size_t)total);
+  std::vector<uint16_t> tloc((size_t)total);
   std::vector<uint16_t> tadj_ptr((size_t)(total + ntiles));
   parallel_tiles(ntiles, [&](int64_t t0, int64_t t1) {
     for (int64_t t = t0; t < t1; ++t) {
@@ -214,7 +219,8 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
       const int64_t n0 = tnode_ptr[(size_t)t];
       int64_t sl = slot_base[(size_t)t];
       for (size_t j = 0; j < o.loc.size(); ++j) {
-        tnodes[(size_t)(n0 + j)] = o.loc[j];
+        tnodes[(size_t)(n0 + j)] = o.asc[j];
+        tloc[(size_t)(n0 + j)] = o.asc_loc[j];
         if (o.shared[j]) slot_node[(size_t)sl++] = o.loc[j];
       }
       for (size_t j = 0; j < o.ptr.size(); ++j) tadj_ptr[(size_t)(n0 + t + j)] = o.ptr[j];
@@ -256,6 +262,7 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   if ((rc = up(&c->tconn, tconn))) return rc;
   if ((rc = up(&c->tnode_ptr, tnode_ptr))) return rc;
   if ((rc = up(&c->tnodes, tnodes))) return rc;
+  if ((rc = up(&c->tloc, tloc))) return rc;
   if ((rc = up(&c->tadj_ptr, tadj_ptr))) return rc;
   if ((rc = up(&c->tadj, tadj))) return rc;
   if ((rc = up(&c->tout, tout))) return rc;
