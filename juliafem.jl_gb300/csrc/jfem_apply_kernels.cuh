@@ -402,6 +402,7 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
 //                           Dirichlet mask (bits 13-15; entry j+1 is node j's)
 //   vs   [3·Lmax]    float2 (hi, lo) of the tile's nodes (masked DOFs zero)
 //   us   [3·Lmax]    f32    state u of the tile's nodes (finite strain only)
+//   stout [Lmax]     i32    output word of each local node (tout)
 // The loads of one tile are issued in two waves, so a tile waits for about
 // three global-memory latencies instead of one per node round:
 //   header   n0, L                                   (tnode_ptr)
@@ -415,8 +416,8 @@ __global__ void __launch_bounds__(128) k_apply_elem(int64_t E, const int* __rest
 //            per node: global index, local slot
 //   wave 2   per node (depends on wave 1): adjacency end offset, mask byte,
 //            v (hi, lo) and u
-// The node gather then loads one output word per node (tout: the global node
-// when interior, −1 − slot when shared), sums its element slots from shared
+// The node gather then reads each node's output word (tout, staged with the
+// node: the global node when interior, −1 − slot when shared), sums its element slots from shared
 // memory and writes y (interior) or bpart[slot] (shared).  Optional v·y
 // partial over interior nodes (double-float, v = hi + lo as staged) into
 // part[blockIdx.x] (FP64).
@@ -435,7 +436,7 @@ template <int NN, bool NEED_U, bool AFFINE>
 __host__ __device__ constexpr size_t tile_smem_bytes(int Lmax) {
   return tile_elem_region_bytes<NN, AFFINE>() + (size_t)JFEM_TILE * NN * sizeof(uint16_t) +
          (size_t)tile_sptr_len(Lmax) * sizeof(uint16_t) + (size_t)3 * Lmax * sizeof(float2) +
-         (NEED_U ? (size_t)3 * Lmax * sizeof(float) : 0);
+         (NEED_U ? (size_t)3 * Lmax * sizeof(float) : 0) + (size_t)Lmax * sizeof(int);
 }
 
 // node rounds per thread covered by the unrolled waves (tiles of JFEM_TILE
@@ -476,6 +477,7 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
   uint16_t* sptr = sadj + NADJ;
   float2* vs = reinterpret_cast<float2*>(sptr + tile_sptr_len(Lmax));
   float* us = reinterpret_cast<float*>(vs + 3 * Lmax);
+  int* stout = reinterpret_cast<int*>(us + (NEED_U ? 3 * Lmax : 0));   // output word per local node
   __shared__ double sh[32];
   __shared__ uint64_t tile_bar;
   if (stop && *stop) return;
@@ -519,8 +521,9 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
           jl[r] = __ldg(tloc + n0 + k);
         }
       }
-      // wave 2: adjacency end offset, mask, v (hi, lo), u
+      // wave 2: adjacency end offset, output word, mask, v (hi, lo), u
       unsigned mk[NR], pe[NR];
+      int ow[NR];
       float2 h[NR][3];
       float uu[NR][3];
 #pragma unroll
@@ -528,9 +531,11 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
         const int k = tid + r * T;
         mk[r] = 0;
         pe[r] = 0;
+        ow[r] = 0;
         if (k < L) {
           const int64_t g = gn[r];
           pe[r] = __ldg(tadj_ptr + n0 + t + jl[r] + 1);
+          ow[r] = __ldg(tout + n0 + jl[r]);
           mk[r] = masked ? (unsigned)__ldg(mask + g) : 0u;
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
@@ -550,6 +555,7 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
             if (NEED_U) us[3 * j + c] = uu[r][c];
           }
           sptr[j + 1] = (uint16_t)(pe[r] | (mk[r] << TILE_PTR_BITS));
+          stout[j] = ow[r];
         }
       }
       if (tid == 0) sptr[0] = 0;
@@ -564,6 +570,7 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
           if (NEED_U) us[3 * j + c] = (float)__ldg(u + 3 * g + c);
         }
         sptr[j + 1] = (uint16_t)(__ldg(tadj_ptr + n0 + t + j + 1) | (m << TILE_PTR_BITS));
+        stout[j] = __ldg(tout + n0 + j);
       }
     }
     const bool have_tile = mbar_wait_bounded(&tile_bar, phase, err);
@@ -609,18 +616,32 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
       }
     }
     __syncthreads();
-    {   // node gather
-      int on[NR];
-#pragma unroll
-      for (int r = 0; r < NR; ++r) {
-        const int j = tid + r * T;
-        on[r] = j < L ? __ldg(tout + n0 + j) : 0;
-      }
+    {   // node gather: four slots per step (their indices, then their element
+        // vectors, then the adds in slot order: the sum's order is unchanged)
       auto gather = [&](int j, int o) {
         const unsigned w1 = sptr[j + 1];
         const int k1 = (int)(w1 & PMASK);
         float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-        for (int k = (int)(sptr[j] & PMASK); k < k1; ++k) {
+        int k = (int)(sptr[j] & PMASK);
+        for (; k + 4 <= k1; k += 4) {
+          int sl[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) sl[u] = sadj[k + u];
+          float2 q[4];
+          float z[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            q[u] = yxy[sl[u]];
+            z[u] = yz[sl[u]];
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            s0 += q[u].x;
+            s1 += q[u].y;
+            s2 += z[u];
+          }
+        }
+        for (; k < k1; ++k) {
           const int sl = sadj[k];
           const float2 q = yxy[sl];
           s0 += q.x;
@@ -647,9 +668,9 @@ __global__ void __launch_bounds__(JFEM_TILE, KIN == KIN_SMALL ? JFEM_TILE_CTAS :
 #pragma unroll
       for (int r = 0; r < NR; ++r) {
         const int j = tid + r * T;
-        if (j < L) gather(j, on[r]);
+        if (j < L) gather(j, stout[j]);
       }
-      for (int j = tid + NR * T; j < L; j += T) gather(j, __ldg(tout + n0 + j));
+      for (int j = tid + NR * T; j < L; j += T) gather(j, stout[j]);
     }
     __syncthreads();
   }
