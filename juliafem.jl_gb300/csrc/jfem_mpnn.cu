@@ -507,6 +507,13 @@ __device__ __forceinline__ void mat3_acc(const float* __restrict__ C, bool trans
 __device__ __forceinline__ unsigned group_mask() { return 0xffu << (threadIdx.x & 24); }
 
 #define MP_UNROLL 4   // neighbours per lane and round: index loads, then gathers, then sums
+
+// float4 held by lane `src` of the 8-lane group, to every lane of the group
+__device__ __forceinline__ float4 group_bcast4(float4 v, int src) {
+  const unsigned gm = group_mask();
+  return make_float4(__shfl_sync(gm, v.x, src, MP_GL), __shfl_sync(gm, v.y, src, MP_GL),
+                     __shfl_sync(gm, v.z, src, MP_GL), __shfl_sync(gm, v.w, src, MP_GL));
+}
 template <bool WEIGHTED>
 __device__ __forceinline__ void group_neighbour_sum(const int* __restrict__ nb_ptr, const int* __restrict__ nbr,
                                                     const float4* __restrict__ in, int64_t i, int g, float s[3]) {
@@ -555,15 +562,29 @@ __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __res
   const int64_t g0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / MP_GL;
   const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
   for (int64_t i = g0; i < N; i += gs) {
+    // the epilogue's operands, one per lane, loaded before the neighbour sum so
+    // their latency overlaps it: lane 0 1/deg and the mask, lanes 1-3 y, A y, A² y
+    float4 pre = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (g == 0) pre = make_float4(__ldg(invdeg + i), LAST ? __int_as_float((int)mask[i]) : 0.f, 0.f, 0.f);
+    if (LAST) {
+      if (g == 1) pre = y[i];
+      else if (g == 2) pre = a1[i];
+      else if (g == 3) pre = in[i];
+    }
     float s[3];
     group_neighbour_sum<false>(nb_ptr, nbr, in, i, g, s);
+    float4 y4, a14, a24;
+    if (LAST) {
+      y4 = group_bcast4(pre, 1);
+      a14 = group_bcast4(pre, 2);
+      a24 = group_bcast4(pre, 3);
+    }
     if (g != 0) continue;
-    const float id = __ldg(invdeg + i);
+    const float id = pre.x;
     float a[3] = {s[0] * id, s[1] * id, s[2] * id};
     if (!LAST) {
       out[i] = make_float4(a[0], a[1], a[2], 0.f);
     } else {
-      const float4 y4 = y[i], a14 = a1[i], a24 = in[i];
       const float yv[3] = {y4.x, y4.y, y4.z};
       const float a1v[3] = {a14.x, a14.y, a14.z};
       const float a2v[3] = {a24.x, a24.y, a24.z};
@@ -572,7 +593,7 @@ __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __res
       mat3_acc(C + 9, false, a1v, u);
       mat3_acc(C + 18, false, a2v, u);
       mat3_acc(C + 27, false, a, u);
-      const uint8_t m = mask[i];
+      const unsigned m = (unsigned)__float_as_int(pre.y);
 #pragma unroll
       for (int k = 0; k < 3; ++k) u[k] = ((m >> k) & 1) ? 0.f : u[k];
       float hv[3] = {0.f, 0.f, 0.f};
@@ -605,19 +626,33 @@ __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __res
   const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
   float2 t1 = make_float2(0.f, 0.f);
   for (int64_t i = g0; i < N; i += gs) {
+    // epilogue operands, one per lane, loaded before the neighbour sum: lane 0
+    // u, lane 1 1/deg; FCG: lane 2 y, lane 3 D⁻¹, lane 4 q_old
+    float4 pre = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (gl == 0) pre = u[i];
+    else if (gl == 1) pre.x = __ldg(invdeg + i);
+    if (FCG) {
+      if (gl == 2) pre = y[i];
+      else if (gl == 3) pre = make_float4(dinvf[3 * i], dinvf[3 * i + 1], dinvf[3 * i + 2], 0.f);
+      else if (gl == 4) pre = make_float4(qold[3 * i], qold[3 * i + 1], qold[3 * i + 2], 0.f);
+    }
     float s[3];
     group_neighbour_sum<true>(nb_ptr, nbr, g, i, gl, s);
-    if (gl != 0) continue;
-    const float4 u4 = u[i];
-    const float uv[3] = {u4.x, u4.y, u4.z};
-    mat3_acc(C, true, uv, s);
-    out[i] = make_float4(s[0], s[1], s[2], __ldg(invdeg + i));
+    const float idg = __shfl_sync(group_mask(), pre.x, 1, MP_GL);
+    float4 y4, d4, q4;
     if (FCG) {
-      const float4 y4 = y[i];
-      const float yv[3] = {y4.x, y4.y, y4.z};
+      y4 = group_bcast4(pre, 2);
+      d4 = group_bcast4(pre, 3);
+      q4 = group_bcast4(pre, 4);
+    }
+    if (gl != 0) continue;
+    const float uv[3] = {pre.x, pre.y, pre.z};
+    mat3_acc(C, true, uv, s);
+    out[i] = make_float4(s[0], s[1], s[2], idg);
+    if (FCG) {
+      const float yv[3] = {y4.x, y4.y, y4.z}, dv[3] = {d4.x, d4.y, d4.z}, qv[3] = {q4.x, q4.y, q4.z};
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
-        t1 = df_add_abs(t1, df_two_prod(sqrtf(dinvf[3 * i + c]) * (yv[c] + s[c]), qold[3 * i + c]));
+      for (int c = 0; c < 3; ++c) t1 = df_add_abs(t1, df_two_prod(sqrtf(dv[c]) * (yv[c] + s[c]), qv[c]));
     }
   }
   if (FCG) {
