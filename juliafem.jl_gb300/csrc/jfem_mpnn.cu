@@ -626,33 +626,31 @@ __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __res
   const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
   float2 t1 = make_float2(0.f, 0.f);
   for (int64_t i = g0; i < N; i += gs) {
-    // epilogue operands, one per lane, loaded before the neighbour sum: lane 0
-    // u, lane 1 1/deg; FCG: lane 2 y, lane 3 D⁻¹, lane 4 q_old
-    float4 pre = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (gl == 0) pre = u[i];
-    else if (gl == 1) pre.x = __ldg(invdeg + i);
-    if (FCG) {
-      if (gl == 2) pre = y[i];
-      else if (gl == 3) pre = make_float4(dinvf[3 * i], dinvf[3 * i + 1], dinvf[3 * i + 2], 0.f);
-      else if (gl == 4) pre = make_float4(qold[3 * i], qold[3 * i + 1], qold[3 * i + 2], 0.f);
+    // epilogue operands loaded before the neighbour sum, so their latency
+    // overlaps it: lane 0 u and 1/deg (the output); FCG: lanes 2-4 u and, for
+    // component c = lane − 2, y_c, D⁻¹_c and q_old,c (each forms its own term of
+    // the β partial: every lane holds the neighbour sum after the xor tree)
+    const int cc = gl - 2;
+    const bool own = gl == 0 || (FCG && cc >= 0 && cc < 3);
+    float4 u4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float idg = 0.f, yc = 0.f, dc = 0.f, qc = 0.f;
+    if (own) u4 = u[i];
+    if (gl == 0) idg = __ldg(invdeg + i);
+    if (FCG && cc >= 0 && cc < 3) {
+      yc = reinterpret_cast<const float*>(y)[4 * i + cc];
+      dc = dinvf[3 * i + cc];
+      qc = qold[3 * i + cc];
     }
     float s[3];
     group_neighbour_sum<true>(nb_ptr, nbr, g, i, gl, s);
-    const float idg = __shfl_sync(group_mask(), pre.x, 1, MP_GL);
-    float4 y4, d4, q4;
-    if (FCG) {
-      y4 = group_bcast4(pre, 2);
-      d4 = group_bcast4(pre, 3);
-      q4 = group_bcast4(pre, 4);
-    }
-    if (gl != 0) continue;
-    const float uv[3] = {pre.x, pre.y, pre.z};
+    if (!own) continue;
+    const float uv[3] = {u4.x, u4.y, u4.z};
     mat3_acc(C, true, uv, s);
-    out[i] = make_float4(s[0], s[1], s[2], idg);
-    if (FCG) {
-      const float yv[3] = {y4.x, y4.y, y4.z}, dv[3] = {d4.x, d4.y, d4.z}, qv[3] = {q4.x, q4.y, q4.z};
-#pragma unroll
-      for (int c = 0; c < 3; ++c) t1 = df_add_abs(t1, df_two_prod(sqrtf(dv[c]) * (yv[c] + s[c]), qv[c]));
+    if (gl == 0) {
+      out[i] = make_float4(s[0], s[1], s[2], idg);
+    } else if (FCG) {
+      const float sc_ = cc == 0 ? s[0] : cc == 1 ? s[1] : s[2];
+      t1 = df_add_abs(t1, df_two_prod(sqrtf(dc) * (yc + sc_), qc));
     }
   }
   if (FCG) {
