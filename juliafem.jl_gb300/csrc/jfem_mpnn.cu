@@ -626,31 +626,27 @@ __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __res
   const int64_t gs = (int64_t)gridDim.x * blockDim.x / MP_GL;
   float2 t1 = make_float2(0.f, 0.f);
   for (int64_t i = g0; i < N; i += gs) {
-    // epilogue operands loaded before the neighbour sum, so their latency
-    // overlaps it: lane 0 u and 1/deg (the output); FCG: lanes 2-4 u and, for
-    // component c = lane − 2, y_c, D⁻¹_c and q_old,c (each forms its own term of
-    // the β partial: every lane holds the neighbour sum after the xor tree)
-    const int cc = gl - 2;
-    const bool own = gl == 0 || (FCG && cc >= 0 && cc < 3);
+    // lane 0 loads u and 1/deg before the neighbour sum (their latency overlaps
+    // it); the β term's operands follow the sum (loaded earlier, they queue in
+    // front of the neighbour gathers on the L1 this pass saturates)
     float4 u4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    float idg = 0.f, yc = 0.f, dc = 0.f, qc = 0.f;
-    if (own) u4 = u[i];
-    if (gl == 0) idg = __ldg(invdeg + i);
-    if (FCG && cc >= 0 && cc < 3) {
-      yc = reinterpret_cast<const float*>(y)[4 * i + cc];
-      dc = dinvf[3 * i + cc];
-      qc = qold[3 * i + cc];
+    float idg = 0.f;
+    if (gl == 0) {
+      u4 = u[i];
+      idg = __ldg(invdeg + i);
     }
     float s[3];
     group_neighbour_sum<true>(nb_ptr, nbr, g, i, gl, s);
-    if (!own) continue;
+    if (gl != 0) continue;
     const float uv[3] = {u4.x, u4.y, u4.z};
     mat3_acc(C, true, uv, s);
-    if (gl == 0) {
-      out[i] = make_float4(s[0], s[1], s[2], idg);
-    } else if (FCG) {
-      const float sc_ = cc == 0 ? s[0] : cc == 1 ? s[1] : s[2];
-      t1 = df_add_abs(t1, df_two_prod(sqrtf(dc) * (yc + sc_), qc));
+    out[i] = make_float4(s[0], s[1], s[2], idg);
+    if (FCG) {
+      const float4 y4 = y[i];
+      const float yv[3] = {y4.x, y4.y, y4.z};
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        t1 = df_add_abs(t1, df_two_prod(sqrtf(dinvf[3 * i + c]) * (yv[c] + s[c]), qold[3 * i + c]));
     }
   }
   if (FCG) {
