@@ -511,8 +511,7 @@ int mpnn_ensure_infer(Ctx* c);                             // the float4 inferen
 // leaves block partials of Σ D^{-1/2}(y + v)·q_old (flexible CG's β) and
 // returns the number of blocks.
 int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf = nullptr, const float* qold = nullptr,
-                     double* t1part = nullptr, SolverScalars* sc = nullptr, const double* t2 = nullptr, int n2 = 0,
-                     bool bf16 = false);
+                     double* t1part = nullptr, SolverScalars* sc = nullptr, const double* t2 = nullptr, int n2 = 0);
 // jfem_coarse.cu
 int coarse_prepare(Ctx* c);   // structure and values for the current mesh, mask and geometry
 int coarse_info(Ctx* c, int* n_agg, int* n_coarse, int64_t* n_elem_listed, double* setup_ms);

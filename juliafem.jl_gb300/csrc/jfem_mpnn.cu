@@ -508,43 +508,15 @@ __device__ __forceinline__ unsigned group_mask() { return 0xffu << (threadIdx.x 
 
 #define MP_UNROLL 4   // neighbours per lane and round: index loads, then gathers, then sums
 
-// Storage of the inference node vectors: FP32 float4, or four BF16 in 8 bytes
-// (the solver's intermediates A y, A² y and the Horner terms: half the bytes
-// of the neighbour gathers that bound these passes; arithmetic stays FP32).
-struct VecF {
-  using T = float4;
-  __device__ __forceinline__ static float4 ld(const T* p, int64_t i) { return __ldg(p + i); }
-  __device__ __forceinline__ static void st(T* p, int64_t i, float4 v) { p[i] = v; }
-};
-struct VecH {
-  using T = uint2;
-  __device__ __forceinline__ static float4 ld(const T* p, int64_t i) {
-    const uint2 r = __ldg(p + i);
-    __nv_bfloat162 a, b;
-    memcpy(&a, &r.x, 4);
-    memcpy(&b, &r.y, 4);
-    const float2 fa = __bfloat1622float2(a), fb = __bfloat1622float2(b);
-    return make_float4(fa.x, fa.y, fb.x, fb.y);
-  }
-  __device__ __forceinline__ static void st(T* p, int64_t i, float4 v) {
-    const __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y), b = __floats2bfloat162_rn(v.z, v.w);
-    uint2 r;
-    memcpy(&r.x, &a, 4);
-    memcpy(&r.y, &b, 4);
-    p[i] = r;
-  }
-};
-
 // float4 held by lane `src` of the 8-lane group, to every lane of the group
 __device__ __forceinline__ float4 group_bcast4(float4 v, int src) {
   const unsigned gm = group_mask();
   return make_float4(__shfl_sync(gm, v.x, src, MP_GL), __shfl_sync(gm, v.y, src, MP_GL),
                      __shfl_sync(gm, v.z, src, MP_GL), __shfl_sync(gm, v.w, src, MP_GL));
 }
-template <bool WEIGHTED, class VI>
+template <bool WEIGHTED>
 __device__ __forceinline__ void group_neighbour_sum(const int* __restrict__ nb_ptr, const int* __restrict__ nbr,
-                                                    const typename VI::T* __restrict__ in, int64_t i, int g,
-                                                    float s[3]) {
+                                                    const float4* __restrict__ in, int64_t i, int g, float s[3]) {
   s[0] = s[1] = s[2] = 0.f;
   const int j0 = __ldg(nb_ptr + i), j1 = __ldg(nb_ptr + i + 1);
   for (int base = j0 + g; base < j1; base += MP_GL * MP_UNROLL) {
@@ -556,7 +528,7 @@ __device__ __forceinline__ void group_neighbour_sum(const int* __restrict__ nb_p
     }
     float4 v[MP_UNROLL];
 #pragma unroll
-    for (int u = 0; u < MP_UNROLL; ++u) v[u] = j[u] != i ? VI::ld(in, j[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int u = 0; u < MP_UNROLL; ++u) v[u] = j[u] != i ? __ldg(in + j[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int u = 0; u < MP_UNROLL; ++u) {
       const float w = WEIGHTED ? v[u].w : 1.f;
@@ -576,16 +548,13 @@ __device__ __forceinline__ void group_neighbour_sum(const int* __restrict__ nb_p
 
 // a = A in (neighbour mean); LAST: also u = mask ⊙ Σ_k C_k A^k y (with y, a1 = A y,
 // in = A² y, a = A³ y) and h = C_3ᵀ u, the first Horner term of the adjoint
-// VI: storage of in (and a1); VO: of out (!LAST) and h (LAST); y and u FP32.
-template <bool LAST, class VI, class VO>
+template <bool LAST>
 __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __restrict__ nb_ptr,
                                                      const int* __restrict__ nbr, const float* __restrict__ invdeg,
-                                                     const typename VI::T* __restrict__ in,
-                                                     const float4* __restrict__ y,
-                                                     const typename VI::T* __restrict__ a1,
-                                                     const float* __restrict__ poly, const uint8_t* __restrict__ mask,
-                                                     typename VO::T* __restrict__ out, float4* __restrict__ u_out,
-                                                     typename VO::T* __restrict__ h) {
+                                                     const float4* __restrict__ in, const float4* __restrict__ y,
+                                                     const float4* __restrict__ a1, const float* __restrict__ poly,
+                                                     const uint8_t* __restrict__ mask, float4* __restrict__ out,
+                                                     float4* __restrict__ h) {
   __shared__ float C[36];
   if (threadIdx.x < 36) C[threadIdx.x] = poly[threadIdx.x];
   __syncthreads();
@@ -599,11 +568,11 @@ __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __res
     if (g == 0) pre = make_float4(__ldg(invdeg + i), LAST ? __int_as_float((int)mask[i]) : 0.f, 0.f, 0.f);
     if (LAST) {
       if (g == 1) pre = y[i];
-      else if (g == 2) pre = VI::ld(a1, i);
-      else if (g == 3) pre = VI::ld(in, i);
+      else if (g == 2) pre = a1[i];
+      else if (g == 3) pre = in[i];
     }
     float s[3];
-    group_neighbour_sum<false, VI>(nb_ptr, nbr, in, i, g, s);
+    group_neighbour_sum<false>(nb_ptr, nbr, in, i, g, s);
     float4 y4, a14, a24;
     if (LAST) {
       y4 = group_bcast4(pre, 1);
@@ -614,7 +583,7 @@ __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __res
     const float id = pre.x;
     float a[3] = {s[0] * id, s[1] * id, s[2] * id};
     if (!LAST) {
-      VO::st(out, i, make_float4(a[0], a[1], a[2], 0.f));
+      out[i] = make_float4(a[0], a[1], a[2], 0.f);
     } else {
       const float yv[3] = {y4.x, y4.y, y4.z};
       const float a1v[3] = {a14.x, a14.y, a14.z};
@@ -629,8 +598,8 @@ __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __res
       for (int k = 0; k < 3; ++k) u[k] = ((m >> k) & 1) ? 0.f : u[k];
       float hv[3] = {0.f, 0.f, 0.f};
       mat3_acc(C + 27, true, u, hv);
-      u_out[i] = make_float4(u[0], u[1], u[2], 0.f);
-      VO::st(h, i, make_float4(hv[0], hv[1], hv[2], id));
+      out[i] = make_float4(u[0], u[1], u[2], 0.f);
+      h[i] = make_float4(hv[0], hv[1], hv[2], id);
     }
   }
 }
@@ -639,12 +608,11 @@ __global__ void __launch_bounds__(256) k_mp_poly_fwd(int64_t N, const int* __res
 // for the next step.  FCG (the last step, out = v = NᵀN y): also block partials
 // of Σ D^{-1/2}(y + v)·q_old, flexible CG's β term of the smoother, into
 // t1part[block] (fixed order), and with sc flexible CG's β in the last block.
-template <bool FCG, class VI, class VO>
+template <bool FCG>
 __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __restrict__ nb_ptr,
                                                      const int* __restrict__ nbr, const float* __restrict__ invdeg,
-                                                     const typename VI::T* __restrict__ g,
-                                                     const float4* __restrict__ u, const float* __restrict__ poly,
-                                                     int k, typename VO::T* __restrict__ out,
+                                                     const float4* __restrict__ g, const float4* __restrict__ u,
+                                                     const float* __restrict__ poly, int k, float4* __restrict__ out,
                                                      const float4* __restrict__ y, const float* __restrict__ dinvf,
                                                      const float* __restrict__ qold, double* __restrict__ t1part,
                                                      SolverScalars* __restrict__ sc, const double* __restrict__ t2,
@@ -668,11 +636,11 @@ __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __res
       idg = __ldg(invdeg + i);
     }
     float s[3];
-    group_neighbour_sum<true, VI>(nb_ptr, nbr, g, i, gl, s);
+    group_neighbour_sum<true>(nb_ptr, nbr, g, i, gl, s);
     if (gl != 0) continue;
     const float uv[3] = {u4.x, u4.y, u4.z};
     mat3_acc(C, true, uv, s);
-    VO::st(out, i, make_float4(s[0], s[1], s[2], idg));
+    out[i] = make_float4(s[0], s[1], s[2], idg);
     if (FCG) {
       const float4 y4 = y[i];
       const float yv[3] = {y4.x, y4.y, y4.z};
@@ -962,46 +930,31 @@ int mpnn_ensure_infer(Ctx* c) {
   return 0;
 }
 
-// One application on the inference vectors; with VH the intermediates (A y,
-// A² y, h, g2) are stored as BF16 (the solver), otherwise FP32 (the host-facing
-// preconditioner, whose output the oracle checks).
-template <class VH>
-static void enqueue_mpnn_passes(Ctx* c, const unsigned g, const float4* y, float4* v, const float* dinvf,
-                                const float* qold, double* t1part, SolverScalars* sc, const double* t2, int n2) {
-  using T = typename VH::T;
-  const float* P = c->mp->poly;
-  T* a1 = reinterpret_cast<T*>(c->mi + c->N);
-  T* a2 = reinterpret_cast<T*>(c->mi + 2 * c->N);
-  float4* u = c->mi + 3 * c->N;
-  T* h = reinterpret_cast<T*>(c->mi + 4 * c->N);
-  T* g2 = reinterpret_cast<T*>(c->mi + 5 * c->N);
-  k_mp_poly_fwd<false, VecF, VH><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, y, nullptr, nullptr, P,
-                                                          c->mask, a1, nullptr, nullptr);
-  k_mp_poly_fwd<false, VH, VH><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, a1, nullptr, nullptr, P,
-                                                        c->mask, a2, nullptr, nullptr);
-  k_mp_poly_fwd<true, VH, VH><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, a2, y, a1, P, c->mask,
-                                                       nullptr, u, h);
-  // h = C3ᵀu;  g2 = C2ᵀu + Aᵀh;  h = C1ᵀu + Aᵀg2;  v = C0ᵀu + Aᵀh
-  k_mp_poly_adj<false, VH, VH><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 2, g2, nullptr,
-                                                        nullptr, nullptr, nullptr, nullptr, nullptr, 0);
-  k_mp_poly_adj<false, VH, VH><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, g2, u, P, 1, h, nullptr,
-                                                        nullptr, nullptr, nullptr, nullptr, nullptr, 0);
-  if (t1part)
-    k_mp_poly_adj<true, VH, VecF><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 0, v, y,
-                                                           dinvf, qold, t1part, sc, t2, n2);
-  else
-    k_mp_poly_adj<false, VH, VecF><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 0, v,
-                                                            nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0);
-  c->launches += 6;
-}
-
 int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf, const float* qold, double* t1part,
-                     SolverScalars* sc, const double* t2, int n2, bool bf16) {
+                     SolverScalars* sc, const double* t2, int n2) {
+  const float* P = c->mp->poly;
   // a resident grid (8 CTAs of 256 per SM) striding over the nodes; its block
   // partials are what flexible CG's β sums
   const unsigned g = grid_for(c->N * MP_GL, 256, JFEM_RED_BLOCKS);
-  if (bf16) enqueue_mpnn_passes<VecH>(c, g, y, v, dinvf, qold, t1part, sc, t2, n2);
-  else enqueue_mpnn_passes<VecF>(c, g, y, v, dinvf, qold, t1part, sc, t2, n2);
+  float4 *a1 = c->mi + c->N, *a2 = c->mi + 2 * c->N, *u = c->mi + 3 * c->N, *h = c->mi + 4 * c->N,
+         *g2 = c->mi + 5 * c->N;
+  k_mp_poly_fwd<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, y, nullptr, nullptr, P, c->mask,
+                                                  a1, nullptr);
+  k_mp_poly_fwd<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, a1, nullptr, nullptr, P,
+                                                  c->mask, a2, nullptr);
+  k_mp_poly_fwd<true><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, a2, y, a1, P, c->mask, u, h);
+  // h = C3ᵀu;  g2 = C2ᵀu + Aᵀh;  h = C1ᵀu + Aᵀg2;  v = C0ᵀu + Aᵀh
+  k_mp_poly_adj<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 2, g2, nullptr, nullptr,
+                                                  nullptr, nullptr, nullptr, nullptr, 0);
+  k_mp_poly_adj<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, g2, u, P, 1, h, nullptr, nullptr,
+                                                  nullptr, nullptr, nullptr, nullptr, 0);
+  if (t1part)
+    k_mp_poly_adj<true><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 0, v, y, dinvf, qold,
+                                                   t1part, sc, t2, n2);
+  else
+    k_mp_poly_adj<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 0, v, nullptr,
+                                                    nullptr, nullptr, nullptr, nullptr, nullptr, 0);
+  c->launches += 6;
   return (int)g;
 }
 

@@ -634,7 +634,7 @@ static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
   float4* v = c->mi ? c->mi + 6 * c->N : nullptr;
   if (nn) {
     k_fcg_input<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, y);
-    enqueue_mpnn_spd(c, y, v, c->dinvf, c->Apf, c->part + JFEM_PART_T1N, c->sc, t2, n2, true);
+    enqueue_mpnn_spd(c, y, v, c->dinvf, c->Apf, c->part + JFEM_PART_T1N, c->sc, t2, n2);
     if (coarse)
       k_fcg_zp<true, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, y, v, c->dinvf, c->mask, na, d32, Ec, c->p2,
                                                                    c->rd, c->sc, c->part);
