@@ -569,15 +569,17 @@ static int coarse_build(Ctx* c, int target_nc) {
   const int64_t ncell = (int64_t)nb[0] * nb[1] * nb[2];
   std::vector<int64_t> cell((size_t)N);
   std::vector<int> cell_id((size_t)ncell, -1);
-  for (int64_t i = 0; i < N; ++i) {
-    int64_t cidx = 0;
-    for (int d = 2; d >= 0; --d) {
-      const int64_t b = std::min<int64_t>(nb[d] - 1, (int64_t)std::floor((X[3 * i + d] - lo[d]) / ext[d] * nb[d]));
-      cidx = cidx * nb[d] + std::max<int64_t>(0, b);
+  host_parallel(N, [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; ++i) {
+      int64_t cidx = 0;
+      for (int d = 2; d >= 0; --d) {
+        const int64_t b = std::min<int64_t>(nb[d] - 1, (int64_t)std::floor((X[3 * i + d] - lo[d]) / ext[d] * nb[d]));
+        cidx = cidx * nb[d] + std::max<int64_t>(0, b);
+      }
+      cell[(size_t)i] = cidx;
     }
-    cell[(size_t)i] = cidx;
-    cell_id[(size_t)cidx] = 0;
-  }
+  });
+  for (int64_t i = 0; i < N; ++i) cell_id[(size_t)cell[(size_t)i]] = 0;
   int nagg = 0;
   for (int64_t k = 0; k < ncell; ++k)
     if (cell_id[(size_t)k] == 0) cell_id[(size_t)k] = nagg++;
@@ -604,46 +606,69 @@ static int coarse_build(Ctx* c, int target_nc) {
   const int n_chunks = (int)chunk_begin.size();
   chunk_begin.push_back((int)N);
   std::vector<double> cen((size_t)3 * nagg, 0.0);
-  for (int a = 0; a < nagg; ++a) {
-    double s[3] = {0, 0, 0};
-    for (int t = agg_ptr[(size_t)a]; t < agg_ptr[(size_t)a + 1]; ++t)
-      for (int d = 0; d < 3; ++d) s[d] += X[3 * (size_t)agg_nodes[(size_t)t] + d];
-    const double cnt = (double)(agg_ptr[(size_t)a + 1] - agg_ptr[(size_t)a]);
-    for (int d = 0; d < 3; ++d) cen[3 * (size_t)a + d] = s[d] / cnt;
-  }
+  host_parallel(nagg, [&](int64_t a0, int64_t a1) {
+    for (int64_t a = a0; a < a1; ++a) {
+      double s[3] = {0, 0, 0};
+      for (int t = agg_ptr[(size_t)a]; t < agg_ptr[(size_t)a + 1]; ++t)
+        for (int d = 0; d < 3; ++d) s[d] += X[3 * (size_t)agg_nodes[(size_t)t] + d];
+      const double cnt = (double)(agg_ptr[(size_t)a + 1] - agg_ptr[(size_t)a]);
+      for (int d = 0; d < 3; ++d) cen[3 * (size_t)a + d] = s[d] / cnt;
+    }
+  });
   std::vector<float2> ddf((size_t)(3 * N));
   std::vector<float4> d32((size_t)N);
-  for (int64_t i = 0; i < N; ++i) {
-    const int a = node_agg[(size_t)i];
-    double dv[3];
-    for (int d = 0; d < 3; ++d) {
-      dv[d] = X[3 * (size_t)i + d] - cen[3 * (size_t)a + d];
-      ddf[3 * (size_t)i + d] = df_from_double(dv[d]);
+  host_parallel(N, [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; ++i) {
+      const int a = node_agg[(size_t)i];
+      double dv[3];
+      for (int d = 0; d < 3; ++d) {
+        dv[d] = X[3 * (size_t)i + d] - cen[3 * (size_t)a + d];
+        ddf[3 * (size_t)i + d] = df_from_double(dv[d]);
+      }
+      d32[(size_t)i] = make_float4((float)dv[0], (float)dv[1], (float)dv[2], 0.f);
     }
-    d32[(size_t)i] = make_float4((float)dv[0], (float)dv[1], (float)dv[2], 0.f);
-  }
+  });
   // elements with a nonzero contribution, their aggregates and contribution blocks
+  // (per contiguous element range on host threads, concatenated in range order:
+  // the list is in ascending element order whatever the split)
   std::vector<int> celem, celem_aggs;
   std::vector<int64_t> celem_off;
   int64_t n_contrib = 0;
-  for (int64_t e = 0; e < E; ++e) {
-    int ag[CG_MAXN];
-    int A = 0;
-    bool masked = false;
-    for (int i = 0; i < nn; ++i) {
-      const int n = conn[(size_t)i * E + e];
-      masked = masked || mask[(size_t)n] != 0;
-      const int a = node_agg[(size_t)n];
-      bool seen = false;
-      for (int q = 0; q < A; ++q) seen = seen || ag[q] == a;
-      if (!seen) ag[A++] = a;
+  {
+    const int64_t nr = 16;
+    std::vector<std::vector<int>> r_elem((size_t)nr), r_aggs((size_t)nr);
+    host_parallel(nr, [&](int64_t r0, int64_t r1) {
+      for (int64_t r = r0; r < r1; ++r) {
+        for (int64_t e = E * r / nr; e < E * (r + 1) / nr; ++e) {
+          int ag[CG_MAXN];
+          int A = 0;
+          bool masked = false;
+          for (int i = 0; i < nn; ++i) {
+            const int n = conn[(size_t)i * E + e];
+            masked = masked || mask[(size_t)n] != 0;
+            const int a = node_agg[(size_t)n];
+            bool seen = false;
+            for (int q = 0; q < A; ++q) seen = seen || ag[q] == a;
+            if (!seen) ag[A++] = a;
+          }
+          if (A < 2 && !masked) continue;
+          std::sort(ag, ag + A);
+          r_elem[(size_t)r].push_back((int)e);
+          for (int q = 0; q < CG_MAXN; ++q) r_aggs[(size_t)r].push_back(q < A ? ag[q] : -1);
+        }
+      }
+    });
+    for (int64_t r = 0; r < nr; ++r) {
+      celem.insert(celem.end(), r_elem[(size_t)r].begin(), r_elem[(size_t)r].end());
+      celem_aggs.insert(celem_aggs.end(), r_aggs[(size_t)r].begin(), r_aggs[(size_t)r].end());
     }
-    if (A < 2 && !masked) continue;
-    std::sort(ag, ag + A);
-    celem.push_back((int)e);
-    for (int q = 0; q < CG_MAXN; ++q) celem_aggs.push_back(q < A ? ag[q] : -1);
-    celem_off.push_back(n_contrib);
-    n_contrib += (int64_t)A * A;
+    celem_off.resize(celem.size());
+    for (size_t k = 0; k < celem.size(); ++k) {
+      int A = 0;
+      while (A < CG_MAXN && celem_aggs[k * CG_MAXN + A] >= 0) ++A;
+      celem_off[k] = n_contrib;
+      n_contrib += (int64_t)A * A;
+    }
   }
   const int64_t n_celem = (int64_t)celem.size();
   if (n_contrib >= (1LL << 31)) return set_err(c, JFEM_ERR_TOO_LARGE, "coarse space: too many element blocks");

@@ -17,7 +17,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/jfem.h"
@@ -453,6 +455,23 @@ int dalloc(Ctx* c, T** p, size_t count) {
 }
 void dfree(Ctx* c, void* p);
 void free_mesh(Ctx* c);
+
+// Runs body(i0, i1) over contiguous ranges of [0, n) on up to 16 host threads
+// (at least 16 items each); callers make every range's work independent, so
+// results do not depend on the split.
+template <class F>
+void host_parallel(int64_t n, F body) {
+  const int64_t hw = std::max<int64_t>(1, std::min<int64_t>(16, (int64_t)std::thread::hardware_concurrency()));
+  const int64_t nt = std::min<int64_t>(hw, std::max<int64_t>(1, n / 16));
+  if (nt <= 1) {
+    body((int64_t)0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve((size_t)nt);
+  for (int64_t k = 0; k < nt; ++k) th.emplace_back(body, n * k / nt, n * (k + 1) / nt);
+  for (auto& x : th) x.join();
+}
 
 inline int grid_for(int64_t n, int threads, int64_t cap = 152LL * 64) {
   int64_t g = (n + threads - 1) / threads;

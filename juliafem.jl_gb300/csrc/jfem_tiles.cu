@@ -35,22 +35,6 @@ static inline uint64_t spread3(uint64_t v) {   // 21 bits → every third bit
   return v;
 }
 
-// Runs body(i0, i1) over contiguous ranges of [0, n) on up to 16 host threads;
-// every range's work is independent, so results do not depend on the split.
-template <class F>
-static void parallel_tiles(int64_t n, F body) {
-  const int64_t hw = std::max<int64_t>(1, std::min<int64_t>(16, std::thread::hardware_concurrency()));
-  const int64_t nt = std::min<int64_t>(hw, std::max<int64_t>(1, n / 16));
-  if (nt <= 1) {
-    body(0, n);
-    return;
-  }
-  std::vector<std::thread> th;
-  th.reserve((size_t)nt);
-  for (int64_t k = 0; k < nt; ++k) th.emplace_back(body, n * k / nt, n * (k + 1) / nt);
-  for (auto& x : th) x.join();
-}
-
 int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   const int64_t N = c->N, E = c->E;
   const int nn = c->nn;
@@ -66,7 +50,7 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   for (int d = 0; d < 3; ++d) span = std::max(span, hi[d] - lo[d]);
   if (!(span > 0.0)) span = 1.0;
   std::vector<std::pair<uint64_t, int64_t>> key((size_t)E);
-  parallel_tiles(E, [&](int64_t e0, int64_t e1) {
+  host_parallel(E, [&](int64_t e0, int64_t e1) {
     for (int64_t e = e0; e < e1; ++e) {
       double cen[3] = {0, 0, 0};
       for (int a = 0; a < nn; ++a)
@@ -124,47 +108,62 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
     int nshared = 0;
   };
   std::vector<TileNodes> tn((size_t)ntiles);
-  auto build_tile = [&](int64_t t, std::vector<int>& lcnt) {
+  // per-thread scratch, reused across the thread's tiles (no allocation per tile)
+  struct Scratch {
+    std::vector<int> lcnt, cnt, order, newidx;
+  };
+  auto build_tile = [&](int64_t t, Scratch& sc) {
     TileNodes& o = tn[(size_t)t];
-    std::vector<int>& loc = o.loc;
-    loc.clear();
+    std::vector<int>& asc = o.asc;   // the tile's global nodes, ascending
+    asc.clear();
+    asc.reserve((size_t)T * nn);
     for (int k = 0; k < T; ++k) {
       const int e = perm[(size_t)(t * T + k)];
       if (e < 0) continue;
-      for (int a = 0; a < nn; ++a) loc.push_back((int)(conn_h[(int64_t)e * nn + a] - base));
+      for (int a = 0; a < nn; ++a) asc.push_back((int)(conn_h[(int64_t)e * nn + a] - base));
     }
-    std::sort(loc.begin(), loc.end());
-    loc.erase(std::unique(loc.begin(), loc.end()), loc.end());
-    const int L = (int)loc.size();
-    // local order: element slots per node descending (ties: ascending global
-    // node), so the 32 nodes a warp sums have similar loop lengths
-    std::vector<int> cnt((size_t)L, 0), order((size_t)L), newidx((size_t)L);
+    std::sort(asc.begin(), asc.end());
+    asc.erase(std::unique(asc.begin(), asc.end()), asc.end());
+    const int L = (int)asc.size();
+    // ascending index of every (element, node) slot, found once; element
+    // slots per node
+    std::vector<int>& cnt = sc.cnt;
+    cnt.assign((size_t)L, 0);
     for (int k = 0; k < T; ++k) {
       const int e = perm[(size_t)(t * T + k)];
       if (e < 0) continue;
       for (int a = 0; a < nn; ++a) {
         const int g = (int)(conn_h[(int64_t)e * nn + a] - base);
-        cnt[(size_t)(std::lower_bound(loc.begin(), loc.end(), g) - loc.begin())]++;
+        const int ai = (int)(std::lower_bound(asc.begin(), asc.end(), g) - asc.begin());
+        tconn[(size_t)a * Epad + t * T + k] = (uint16_t)ai;
+        cnt[(size_t)ai]++;
       }
     }
+    // local order: element slots per node descending (ties: ascending global
+    // node), so the 32 nodes a warp sums have similar loop lengths
+    std::vector<int>& order = sc.order;
+    std::vector<int>& newidx = sc.newidx;
+    order.resize((size_t)L);
+    newidx.resize((size_t)L);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cnt[(size_t)x] > cnt[(size_t)y]; });
-    std::vector<int> sorted_loc(loc);
+    std::vector<int>& loc = o.loc;
+    loc.resize((size_t)L);
     for (int j = 0; j < L; ++j) {
       newidx[(size_t)order[(size_t)j]] = j;
-      loc[(size_t)j] = sorted_loc[(size_t)order[(size_t)j]];
+      loc[(size_t)j] = asc[(size_t)order[(size_t)j]];
     }
-    o.asc = sorted_loc;
     o.asc_loc.assign(newidx.begin(), newidx.end());
+    std::vector<int>& lcnt = sc.lcnt;
     lcnt.assign((size_t)L + 1, 0);
-    // local connectivity and counts
+    // local connectivity (ascending index → local index) and counts
     for (int k = 0; k < T; ++k) {
       const int e = perm[(size_t)(t * T + k)];
       if (e < 0) continue;
       for (int a = 0; a < nn; ++a) {
-        const int g = (int)(conn_h[(int64_t)e * nn + a] - base);
-        const int li = newidx[(size_t)(std::lower_bound(sorted_loc.begin(), sorted_loc.end(), g) - sorted_loc.begin())];
-        tconn[(size_t)a * Epad + t * T + k] = (uint16_t)li;
+        uint16_t& slot = tconn[(size_t)a * Epad + t * T + k];
+        const int li = newidx[slot];
+        slot = (uint16_t)li;
         lcnt[(size_t)li + 1]++;
       }
     }
@@ -188,9 +187,9 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
         ++o.nshared;
       }
   };
-  parallel_tiles(ntiles, [&](int64_t t0, int64_t t1) {
-    std::vector<int> lcnt;
-    for (int64_t t = t0; t < t1; ++t) build_tile(t, lcnt);
+  host_parallel(ntiles, [&](int64_t t0, int64_t t1) {
+    Scratch sc;
+    for (int64_t t = t0; t < t1; ++t) build_tile(t, sc);
   });
   // tile offsets (serial prefix sums in tile order)
   std::vector<int> tnode_ptr((size_t)ntiles + 1, 0);
@@ -213,7 +212,7 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   std::vector<int> tnodes((size_t)total), tout((size_t)total);
   std::vector<uint16_t> tloc((size_t)total);
   std::vector<uint16_t> tadj_ptr((size_t)(total + ntiles));
-  parallel_tiles(ntiles, [&](int64_t t0, int64_t t1) {
+  host_parallel(ntiles, [&](int64_t t0, int64_t t1) {
     for (int64_t t = t0; t < t1; ++t) {
       const TileNodes& o = tn[(size_t)t];
       const int64_t n0 = tnode_ptr[(size_t)t];
@@ -237,7 +236,7 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
     }
   std::vector<int> pos_of_slot((size_t)nslots, 0), fill(bptr.begin(), bptr.end() - 1);
   for (int64_t s2 = 0; s2 < nslots; ++s2) pos_of_slot[(size_t)s2] = fill[(size_t)bidx[(size_t)slot_node[(size_t)s2]]]++;
-  parallel_tiles(ntiles, [&](int64_t t0, int64_t t1) {
+  host_parallel(ntiles, [&](int64_t t0, int64_t t1) {
     for (int64_t t = t0; t < t1; ++t) {
       const TileNodes& o = tn[(size_t)t];
       const int64_t n0 = tnode_ptr[(size_t)t];
