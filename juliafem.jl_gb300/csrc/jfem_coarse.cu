@@ -629,44 +629,37 @@ static int coarse_build(Ctx* c, int target_nc) {
     }
   });
   // elements with a nonzero contribution, their aggregates and contribution blocks
-  // (per contiguous element range on host threads, concatenated in range order:
-  // the list is in ascending element order whatever the split)
+  // (each element's sorted aggregates on host threads into a scratch array,
+  // then compacted in ascending element order)
   std::vector<int> celem, celem_aggs;
   std::vector<int64_t> celem_off;
   int64_t n_contrib = 0;
   {
-    const int64_t nr = 16;
-    std::vector<std::vector<int>> r_elem((size_t)nr), r_aggs((size_t)nr);
-    host_parallel(nr, [&](int64_t r0, int64_t r1) {
-      for (int64_t r = r0; r < r1; ++r) {
-        for (int64_t e = E * r / nr; e < E * (r + 1) / nr; ++e) {
-          int ag[CG_MAXN];
-          int A = 0;
-          bool masked = false;
-          for (int i = 0; i < nn; ++i) {
-            const int n = conn[(size_t)i * E + e];
-            masked = masked || mask[(size_t)n] != 0;
-            const int a = node_agg[(size_t)n];
-            bool seen = false;
-            for (int q = 0; q < A; ++q) seen = seen || ag[q] == a;
-            if (!seen) ag[A++] = a;
-          }
-          if (A < 2 && !masked) continue;
-          std::sort(ag, ag + A);
-          r_elem[(size_t)r].push_back((int)e);
-          for (int q = 0; q < CG_MAXN; ++q) r_aggs[(size_t)r].push_back(q < A ? ag[q] : -1);
+    std::vector<int> eag((size_t)E * CG_MAXN);
+    std::vector<int8_t> eA((size_t)E);
+    host_parallel(E, [&](int64_t e0, int64_t e1) {
+      for (int64_t e = e0; e < e1; ++e) {
+        int* ag = &eag[(size_t)e * CG_MAXN];
+        int A = 0;
+        bool masked = false;
+        for (int i = 0; i < nn; ++i) {
+          const int n = conn[(size_t)i * E + e];
+          masked = masked || mask[(size_t)n] != 0;
+          const int a = node_agg[(size_t)n];
+          bool seen = false;
+          for (int q = 0; q < A; ++q) seen = seen || ag[q] == a;
+          if (!seen) ag[A++] = a;
         }
+        std::sort(ag, ag + A);
+        eA[(size_t)e] = (int8_t)((A < 2 && !masked) ? 0 : A);
       }
     });
-    for (int64_t r = 0; r < nr; ++r) {
-      celem.insert(celem.end(), r_elem[(size_t)r].begin(), r_elem[(size_t)r].end());
-      celem_aggs.insert(celem_aggs.end(), r_aggs[(size_t)r].begin(), r_aggs[(size_t)r].end());
-    }
-    celem_off.resize(celem.size());
-    for (size_t k = 0; k < celem.size(); ++k) {
-      int A = 0;
-      while (A < CG_MAXN && celem_aggs[k * CG_MAXN + A] >= 0) ++A;
-      celem_off[k] = n_contrib;
+    for (int64_t e = 0; e < E; ++e) {
+      const int A = eA[(size_t)e];
+      if (A == 0) continue;
+      celem.push_back((int)e);
+      for (int q = 0; q < CG_MAXN; ++q) celem_aggs.push_back(q < A ? eag[(size_t)e * CG_MAXN + q] : -1);
+      celem_off.push_back(n_contrib);
       n_contrib += (int64_t)A * A;
     }
   }
