@@ -254,7 +254,7 @@ int jfem_mpnn_precondition(jfem_ctx* ctx, const double* r, double* z);
  * (docs/src/book/design/gpu_solver_strategy_expert_validated.md:114-156) but
  * ships unpreconditioned CG.  Linear-elastic small strain only.
  * coarse_dofs: 0 = no coarse space (JFEM_FCG_LEARNED is then one-level),
- * < 0 = automatic (about one coarse DOF per 2,000 DOFs, within [192, 1152];
+ * < 0 = automatic (about one coarse DOF per 1,000 DOFs, within [192, 2304];
  * the default), > 0 = about that many, at most JFEM_COARSE_MAX_DOFS (the
  * binning never exceeds it).  Kept across jfem_set_mesh. */
 #define JFEM_COARSE_MAX_DOFS 4096

@@ -524,14 +524,15 @@ __global__ void k_to_df(int64_t n, const double* __restrict__ a, float2* __restr
 // ---------------------------------------------------------------------------
 // host: structure (aggregation, element lists, block pattern)
 // ---------------------------------------------------------------------------
-// Coarse DOFs when none are requested: about one per 2,000 fine DOFs, within
-// [192, 1152] — enough aggregates to carry the bending modes of slender parts
-// (on the 2M-DOF Tet10 cantilever: 1,404 coarse DOFs after rounding the bins,
-// about 290 iterations, against 392 with 552), few enough that the FP64
-// inversion stays a small share of a solve.
+// Coarse DOFs when none are requested: about one per 1,000 fine DOFs, within
+// [192, 2304] — enough aggregates to carry the bending modes of slender parts
+// (on the 2M-DOF Tet10 cantilever: 1,728 coarse DOFs after rounding the bins,
+// 261 two-level iterations, against 287 with 1,458, 392 with 552 and 207 with
+// 3,936), few enough that the set-up (the dense inverse is cubic in the coarse
+// size: 12 ms here, 69 ms at 3,936) stays a small share of a solve.
 static int auto_coarse_dofs(int64_t n_dofs) {
-  const int64_t v = n_dofs / 2000;
-  return (int)std::min<int64_t>(1152, std::max<int64_t>(192, v));
+  const int64_t v = n_dofs / 1000;
+  return (int)std::min<int64_t>(2304, std::max<int64_t>(192, v));
 }
 
 static int coarse_build(Ctx* c, int target_nc) {

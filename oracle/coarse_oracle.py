@@ -27,7 +27,7 @@ import scipy.sparse as sp
 
 
 def auto_coarse_dofs(n_dofs: int) -> int:
-    return int(min(1152, max(192, n_dofs // 2000)))
+    return int(min(2304, max(192, n_dofs // 1000)))
 
 
 def aggregates(X, target_nc: int):
