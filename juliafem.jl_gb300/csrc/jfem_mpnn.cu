@@ -504,7 +504,9 @@ __device__ __forceinline__ void mat3_acc(const float* __restrict__ C, bool trans
 // is uniform wherever the loop condition is.  Vectors are one float4 per node;
 // the inputs of the adjoint steps carry the neighbour weight 1/deg_j in .w.
 #define MP_GL 8
-__device__ __forceinline__ unsigned group_mask() { return 0xffu << (threadIdx.x & 24); }
+__device__ __forceinline__ unsigned group_mask() {
+  return ((1u << MP_GL) - 1u) << (threadIdx.x & (32 - MP_GL));
+}
 
 #define MP_UNROLL 4   // neighbours per lane and round: index loads, then gathers, then sums
 
