@@ -343,7 +343,7 @@ __device__ void batch_solve_instance(const BatchDev& a, Team<C>& tm, int inst, d
       const float2 al = df_from_double(alpha), nal = df_neg(al);
       float2 rzn = make_float2(0.f, 0.f), rrn = make_float2(0.f, 0.f);
       for (int64_t q = 3 * n0 + tm.tid(); q < 3 * n1; q += tm.nthr()) {
-        a.dx[q] = df_add(a.dx[q], df_mul(al, a.p[q]));
+        a.dx[q] = df_add_abs(a.dx[q], df_mul(al, a.p[q]));
         const float2 rq = df_add(a.r[q], df_mul_f(nal, a.Ap[q]));
         a.r[q] = rq;
         rzn = df_add(rzn, df_mul(rq, df_mul_f(rq, a.dinvf[q])));

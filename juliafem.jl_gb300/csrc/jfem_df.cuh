@@ -51,9 +51,12 @@ __device__ __forceinline__ float2 df_add(float2 x, float2 y) {
 // parts added in FP32, one Fast2Sum.  Its error is bounded in absolute terms,
 // ≈ 2u²(|x| + |y|), not relative to the result (no bound under cancellation):
 // for sums judged against the size of their terms, e.g. matrix entries
-// compared relative to max |K|, and the dot products of the solvers, whose
+// compared relative to max |K|, the dot products of the solvers, whose
 // per-thread sums of a few terms then meet FP64 block sums (error ≈ 2u² of the
-// summed magnitudes per term, FP64-class).  11 operations against 20 for df_add.
+// summed magnitudes per term, FP64-class), and the updates of the correction
+// δx and of the search direction p (errors ≈ 2u² of |δx| or |p|, where FP32
+// operators already perturb far more; the residual update r −= αq, which
+// cancels, keeps df_add).  11 operations against 20 for df_add.
 __device__ __forceinline__ float2 df_add_abs(float2 x, float2 y) {
   const float2 s = df_two_sum(x.x, y.x);
   return df_fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(x.y, y.y)));

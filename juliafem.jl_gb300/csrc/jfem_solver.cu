@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_dfcg_update1(int64_t n, So
   const float2 a = sc->alpha_df, na = df_neg(a);
   float2 rz = make_float2(0.f, 0.f), rr = make_float2(0.f, 0.f);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] = df_add(x[i], df_mul(a, p[i]));
+    x[i] = df_add_abs(x[i], df_mul(a, p[i]));
     const float2 ri = df_add(r[i], df_mul_f(na, Ap[i]));
     r[i] = ri;
     rz = df_add_abs(rz, df_mul(ri, df_mul_f(ri, dinv[i])));
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_dfcg_update2(int64_t n, co
   if (sc->done[0]) return;
   const float2 b = sc->beta_df;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = df_add(df_mul_f(r[i], dinv[i]), df_mul(b, p[i]));
+    p[i] = df_add_abs(df_mul_f(r[i], dinv[i]), df_mul(b, p[i]));
 }
 
 // r·z → part[G..2G), r·r → part[2G..3G) from the double-float r; p = D⁻¹r on restart
@@ -485,7 +485,7 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS, 4) k_fcg_zp(int64_t N, const
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         float2 pi = make_float2(zc[c], 0.f);
-        if (keep) pi = df_add(pi, df_mul(nb, po[n][c]));
+        if (keep) pi = df_add_abs(pi, df_mul(nb, po[n][c]));
         p[3 * i + c] = pi;
         dot = df_add_abs(dot, df_mul(pi, rq[n][c]));
       }
@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_update(int64_t n, Solv
   const float2 a = sc->alpha_df, na = df_neg(a);
   float2 rr = make_float2(0.f, 0.f), t1 = make_float2(0.f, 0.f);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] = df_add(x[i], df_mul(a, p[i]));
+    x[i] = df_add_abs(x[i], df_mul(a, p[i]));
     const float qi = q[i];
     const float2 ri = df_add(r[i], df_mul_f(na, qi));
     r[i] = ri;
