@@ -39,7 +39,6 @@ void dfree(Ctx* c, void* p) {
 
 void free_mesh(Ctx* c) {
   cudaStreamSynchronize(c->stream);
-  if (c->stream2) cudaStreamSynchronize(c->stream2);
   if (c->pcg_graph) {
     cudaGraphExecDestroy(c->pcg_graph);
     c->pcg_graph = nullptr;
@@ -48,14 +47,11 @@ void free_mesh(Ctx* c) {
   for (void* p : c->owned) cudaFree(p);
   c->owned.clear();
   Ctx fresh;
-  // keep device, streams, events, pinned mirrors, counters
+  // keep device, stream, events, pinned mirrors, counters
   fresh.device = c->device;
   fresh.stream = c->stream;
   fresh.ev0 = c->ev0;
   fresh.ev1 = c->ev1;
-  fresh.stream2 = c->stream2;
-  fresh.ev_fork = c->ev_fork;
-  fresh.ev_join = c->ev_join;
   fresh.sc_host = c->sc_host;
   fresh.norms_host = c->norms_host;
   fresh.mp = c->mp;
@@ -116,9 +112,6 @@ int jfem_create(jfem_ctx** out, int device_ordinal) {
   Ctx* c = &h->c;
   c->device = device_ordinal;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       cudaMallocHost(&c->sc_host, sizeof(jfem::SolverScalars)) != cudaSuccess ||
       cudaMallocHost(&c->norms_host, 2 * sizeof(double)) != cudaSuccess) {
@@ -148,9 +141,6 @@ int jfem_destroy(jfem_ctx* h) {
   if (c->norms_host) cudaFreeHost(c->norms_host);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
-  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
-  if (c->ev_join) cudaEventDestroy(c->ev_join);
-  if (c->stream2) cudaStreamDestroy(c->stream2);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete h;
   return JFEM_OK;

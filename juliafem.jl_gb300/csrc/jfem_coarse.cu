@@ -836,13 +836,12 @@ int coarse_prepare(Ctx* c) {
 int coarse_gemv_blocks(const Ctx* c) { return (c->nc + 7) / 8; }
 
 void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop, const float* qold, double* t2part,
-                                   SolverScalars* sc, const double* t1, int n1, cudaStream_t st) {
-  if (!st) st = c->stream;
-  k_coarse_restrict<<<c->n_chunks, 256, 0, st>>>(c->n_chunks, c->chunk_begin, c->agg_nodes, c->node_d32, r,
+                                   SolverScalars* sc, const double* t1, int n1) {
+  k_coarse_restrict<<<c->n_chunks, 256, 0, c->stream>>>(c->n_chunks, c->chunk_begin, c->agg_nodes, c->node_d32, r,
                                                         t2part ? qold : nullptr, stop, c->chunk_agg,
                                                         c->agg_chunk_ptr, c->agg_cnt, c->nc_pad, c->cpart, c->RQ);
-  k_coarse_gemv<<<coarse_gemv_blocks(c), 256, 0, st>>>(c->nc, c->nc_pad, c->Ainv32, c->RQ, stop, c->Ec, t2part,
-                                                       sc, t1, n1);
+  k_coarse_gemv<<<coarse_gemv_blocks(c), 256, 0, c->stream>>>(c->nc, c->nc_pad, c->Ainv32, c->RQ, stop, c->Ec,
+                                                              t2part, sc, t1, n1);
   c->launches += 2;
 }
 

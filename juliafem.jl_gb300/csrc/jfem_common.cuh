@@ -285,10 +285,6 @@ struct Ctx {
   int64_t launches = 0;
   double last_apply_ms = 0.0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  // second stream and fork/join events: the learned two-level iteration runs the
-  // coarse restriction and solve beside the network's passes
-  cudaStream_t stream2 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
   // mesh
   int et = 0, nn = 0;
@@ -534,8 +530,7 @@ int mpnn_ensure_infer(Ctx* c);                             // the float4 inferen
 // leaves block partials of Σ D^{-1/2}(y + v)·q_old (flexible CG's β) and
 // returns the number of blocks.
 int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf = nullptr, const float* qold = nullptr,
-                     double* t1part = nullptr, SolverScalars* sc = nullptr, const double* t2 = nullptr, int n2 = 0,
-                     cudaEvent_t wait_last = nullptr);
+                     double* t1part = nullptr, SolverScalars* sc = nullptr, const double* t2 = nullptr, int n2 = 0);
 // jfem_coarse.cu
 int coarse_prepare(Ctx* c);   // structure and values for the current mesh, mask and geometry
 int coarse_info(Ctx* c, int* n_agg, int* n_coarse, int64_t* n_elem_listed, double* setup_ms);
@@ -544,7 +539,7 @@ int coarse_precondition(Ctx* c, const double* r_h, double* z_h);
 // Ec = A_c⁻¹ Pᵀ r; with qold, also the block partials of Ec·Pᵀ q_old into t2part
 void enqueue_coarse_restrict_solve(Ctx* c, const float2* r, const int* stop, const float* qold = nullptr,
                                    double* t2part = nullptr, SolverScalars* sc = nullptr, const double* t1 = nullptr,
-                                   int n1 = 0, cudaStream_t st = nullptr);
+                                   int n1 = 0);
 int coarse_gemv_blocks(const Ctx* c);
 // jfem_recovery.cu
 int recover_field(Ctx* c, const double* u_h, int field, double tol, int max_iter, double* nodal_h, int* iters_out);

@@ -933,7 +933,7 @@ int mpnn_ensure_infer(Ctx* c) {
 }
 
 int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf, const float* qold, double* t1part,
-                     SolverScalars* sc, const double* t2, int n2, cudaEvent_t wait_last) {
+                     SolverScalars* sc, const double* t2, int n2) {
   const float* P = c->mp->poly;
   // a resident grid (8 CTAs of 256 per SM) striding over the nodes; its block
   // partials are what flexible CG's β sums
@@ -950,7 +950,6 @@ int enqueue_mpnn_spd(Ctx* c, const float4* y, float4* v, const float* dinvf, con
                                                   nullptr, nullptr, nullptr, nullptr, 0);
   k_mp_poly_adj<false><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, g2, u, P, 1, h, nullptr, nullptr,
                                                   nullptr, nullptr, nullptr, nullptr, 0);
-  if (wait_last) cudaStreamWaitEvent(c->stream, wait_last, 0);   // t2 comes from another stream
   if (t1part)
     k_mp_poly_adj<true><<<g, 256, 0, c->stream>>>(c->N, c->nb_ptr, c->nbr, c->invdeg, h, u, P, 0, v, y, dinvf, qold,
                                                    t1part, sc, t2, n2);

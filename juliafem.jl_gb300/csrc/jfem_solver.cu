@@ -622,20 +622,10 @@ static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
   double* t2 = coarse ? c->part + JFEM_PART_T2 : nullptr;
   // β is formed by the last block of the launch that writes the last of its
   // partials: the network's last pass (nn), else the coarse solve (coarse),
-  // else its own launch.  With the network, the coarse restriction and solve
-  // run on the second stream beside the network's passes (both only read r
-  // and q_old); the network's last pass, which sums the coarse partials into
-  // β, waits for them.
-  const bool branch = coarse && nn && c->stream2;
-  if (branch) {
-    cudaEventRecord(c->ev_fork, c->stream);
-    cudaStreamWaitEvent(c->stream2, c->ev_fork, 0);
-    enqueue_coarse_restrict_solve(c, c->rd, &c->sc->done[0], c->Apf, t2, nullptr, nullptr, 0, c->stream2);
-    cudaEventRecord(c->ev_join, c->stream2);
-  } else if (coarse) {
+  // else its own launch
+  if (coarse)
     enqueue_coarse_restrict_solve(c, c->rd, &c->sc->done[0], c->Apf, t2, nn ? nullptr : c->sc,
                                   c->part + JFEM_PART_T1, G_);
-  }
   const int n2 = coarse ? coarse_gemv_blocks(c) : 0;
   const int* na = coarse ? c->node_agg : nullptr;
   const float4* d32 = coarse ? c->node_d32 : nullptr;
@@ -644,8 +634,7 @@ static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
   float4* v = c->mi ? c->mi + 6 * c->N : nullptr;
   if (nn) {
     k_fcg_input<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, y);
-    enqueue_mpnn_spd(c, y, v, c->dinvf, c->Apf, c->part + JFEM_PART_T1N, c->sc, t2, n2,
-                     branch ? c->ev_join : nullptr);
+    enqueue_mpnn_spd(c, y, v, c->dinvf, c->Apf, c->part + JFEM_PART_T1N, c->sc, t2, n2);
     if (coarse)
       k_fcg_zp<true, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, y, v, c->dinvf, c->mask, na, d32, Ec, c->p2,
                                                                    c->rd, c->sc, c->part);
