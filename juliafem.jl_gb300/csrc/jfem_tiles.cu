@@ -109,24 +109,47 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   };
   std::vector<TileNodes> tn((size_t)ntiles);
   // per-thread scratch, reused across the thread's tiles (no allocation per tile)
+  // open-addressing table of a tile's nodes (power of two ≥ 2·T·n_en slots)
+  int HB = 1;
+  while (HB < 2 * T * nn) HB <<= 1;
   struct Scratch {
-    std::vector<int> lcnt, cnt, order, newidx;
+    std::vector<int> lcnt, cnt, order, newidx, hkey, hval;
+    std::vector<unsigned> used;   // table slots filled by the current tile
   };
   auto build_tile = [&](int64_t t, Scratch& sc) {
     TileNodes& o = tn[(size_t)t];
-    std::vector<int>& asc = o.asc;   // the tile's global nodes, ascending
+    std::vector<int>& hkey = sc.hkey;
+    std::vector<int>& hval = sc.hval;
+    if (hkey.size() != (size_t)HB) {
+      hkey.assign((size_t)HB, -1);
+      hval.assign((size_t)HB, 0);
+    }
+    auto slot_of = [&](int g) {
+      unsigned h = ((unsigned)g * 2654435761u) & (unsigned)(HB - 1);
+      while (hkey[h] != -1 && hkey[h] != g) h = (h + 1) & (unsigned)(HB - 1);
+      return h;
+    };
+    // the tile's distinct global nodes (hash table), then ascending
+    std::vector<int>& asc = o.asc;
     asc.clear();
-    asc.reserve((size_t)T * nn);
+    sc.used.clear();
     for (int k = 0; k < T; ++k) {
       const int e = perm[(size_t)(t * T + k)];
       if (e < 0) continue;
-      for (int a = 0; a < nn; ++a) asc.push_back((int)(conn_h[(int64_t)e * nn + a] - base));
+      for (int a = 0; a < nn; ++a) {
+        const int g = (int)(conn_h[(int64_t)e * nn + a] - base);
+        const unsigned h = slot_of(g);
+        if (hkey[h] == -1) {
+          hkey[h] = g;
+          sc.used.push_back(h);
+          asc.push_back(g);
+        }
+      }
     }
     std::sort(asc.begin(), asc.end());
-    asc.erase(std::unique(asc.begin(), asc.end()), asc.end());
     const int L = (int)asc.size();
-    // ascending index of every (element, node) slot, found once; element
-    // slots per node
+    for (int j = 0; j < L; ++j) hval[slot_of(asc[(size_t)j])] = j;
+    // ascending index of every (element, node) slot; element slots per node
     std::vector<int>& cnt = sc.cnt;
     cnt.assign((size_t)L, 0);
     for (int k = 0; k < T; ++k) {
@@ -134,11 +157,12 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
       if (e < 0) continue;
       for (int a = 0; a < nn; ++a) {
         const int g = (int)(conn_h[(int64_t)e * nn + a] - base);
-        const int ai = (int)(std::lower_bound(asc.begin(), asc.end(), g) - asc.begin());
+        const int ai = hval[slot_of(g)];
         tconn[(size_t)a * Epad + t * T + k] = (uint16_t)ai;
         cnt[(size_t)ai]++;
       }
     }
+    for (const unsigned h : sc.used) hkey[h] = -1;   // empty again for the thread's next tile
     // local order: element slots per node descending (ties: ascending global
     // node), so the 32 nodes a warp sums have similar loop lengths
     std::vector<int>& order = sc.order;
