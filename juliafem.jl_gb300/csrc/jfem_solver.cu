@@ -504,12 +504,16 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS, 4) k_fcg_zp(int64_t N, const
 
 // x += αp, r −= αq; r·r partials → the last block updates the scalars and the
 // stop flag.  T1 (Jacobi smoother): also Σ D⁻¹r·q partials for the next β.
+// ynext (the network): the next iteration's input D^{-1/2} r per node (float4
+// x, y, z; zero on prescribed DOFs, where D⁻¹ is zero), formed here while r is
+// in registers.
 template <bool T1>
 __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_update(int64_t n, SolverScalars* __restrict__ sc,
                                                                  float2* __restrict__ x, float2* __restrict__ r,
                                                                  const float2* __restrict__ p,
                                                                  const float* __restrict__ q,
                                                                  const float* __restrict__ dinv,
+                                                                 float* __restrict__ ynext,
                                                                  double* __restrict__ part) {
   __shared__ double sh[32];
   if (sc->done[0]) return;
@@ -522,6 +526,10 @@ __global__ void __launch_bounds__(JFEM_RED_THREADS) k_fcg_update(int64_t n, Solv
     r[i] = ri;
     rr = df_add_abs(rr, df_mul(ri, ri));
     if (T1) t1 = df_add_abs(t1, df_two_prod(dinv[i] * (ri.x + ri.y), qi));
+    if (ynext) {
+      const int64_t node = i / 3;
+      ynext[4 * node + (i - 3 * node)] = sqrtf(dinv[i]) * (ri.x + ri.y);
+    }
   }
   const double2 bs = block_sum2_df(rr, t1, sh);
   if (threadIdx.x == 0) {
@@ -633,7 +641,8 @@ static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
   float4* y = c->mi;
   float4* v = c->mi ? c->mi + 6 * c->N : nullptr;
   if (nn) {
-    k_fcg_input<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, y);
+    // y (the network's input) was formed by the previous update, or after the
+    // last (re)start
     enqueue_mpnn_spd(c, y, v, c->dinvf, c->Apf, c->part + JFEM_PART_T1N, c->sc, t2, n2);
     if (coarse)
       k_fcg_zp<true, true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, y, v, c->dinvf, c->mask, na, d32, Ec, c->p2,
@@ -650,14 +659,14 @@ static void enqueue_fcg_iteration(Ctx* c, bool nn, bool coarse) {
       k_fcg_zp<false, false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(c->N, nullptr, nullptr, c->dinvf, c->mask, na,
                                                                      d32, Ec, c->p2, c->rd, c->sc, c->part);
   }
-  c->launches += nn ? 2 : (coarse ? 1 : 2);
+  c->launches += nn ? 1 : (coarse ? 1 : 2);
   enqueue_apply_tiled(c, c->p2, c->Apf, true, c->part, &c->sc->done[0], c->sc);
   if (nn)
     k_fcg_update<false><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->xd, c->rd, c->p2, c->Apf, c->dinvf,
-                                                                c->part);
+                                                                reinterpret_cast<float*>(y), c->part);
   else
     k_fcg_update<true><<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->sc, c->xd, c->rd, c->p2, c->Apf, c->dinvf,
-                                                               c->part);
+                                                               nullptr, c->part);
   c->launches += 1;
 }
 
@@ -904,6 +913,10 @@ static int fcg(Ctx* c, const double* f, bool nn, bool coarse, double tol, int ma
   k_fcg_norms<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->rd, c->dinvf, c->Apf, c->part);
   k_fcg_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 1, tol, max_iter, 1, 1);
   c->launches += 4;
+  if (nn) {   // the network's first input; later ones come from the update kernel
+    k_fcg_input<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, c->mi);
+    c->launches += 1;
+  }
   if ((rc = read_scalars(c))) return rc;
   const double bb = c->sc_host->bb;
   *res = PcgResult();
@@ -982,6 +995,10 @@ static int fcg(Ctx* c, const double* f, bool nn, bool coarse, double tol, int ma
       k_fcg_norms<<<G_, JFEM_RED_THREADS, 0, c->stream>>>(n, c->rd, c->dinvf, c->Apf, c->part);
       k_fcg_reset<<<1, JFEM_RED_THREADS, 0, c->stream>>>(c->sc, c->part, 0, tol, max_iter, 0, restart);
       c->launches += 3;
+      if (nn) {   // the network's input from the refreshed residual
+        k_fcg_input<<<grid_for(c->N, 256), 256, 0, c->stream>>>(c->N, c->rd, c->dinvf, c->mask, c->sc, c->mi);
+        c->launches += 1;
+      }
       if ((rc = read_scalars(c))) return rc;
     }
     if (time_budget > 0.0 && now_s() - t_start > time_budget) {
