@@ -92,8 +92,10 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
   std::vector<int> perm((size_t)Epad, -1);
   for (int64_t k = 0; k < E; ++k) perm[(size_t)k] = (int)key[(size_t)k].second;
   // elements per global node
-  std::vector<int> cntg((size_t)N, 0);
-  for (int64_t t = 0; t < E * nn; ++t) cntg[(size_t)(conn_h[t] - base)]++;
+  std::vector<int> cntg((size_t)N, 0);   // elements per node (relaxed atomic counts: order-free)
+  host_parallel(E * nn, [&](int64_t t0, int64_t t1) {
+    for (int64_t t = t0; t < t1; ++t) __atomic_fetch_add(&cntg[(size_t)(conn_h[t] - base)], 1, __ATOMIC_RELAXED);
+  });
 
   std::vector<uint16_t> tconn((size_t)nn * Epad, 0);
   std::vector<uint16_t> tadj((size_t)ntiles * T * nn, 0);
@@ -249,8 +251,11 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
       for (size_t j = 0; j < o.ptr.size(); ++j) tadj_ptr[(size_t)(n0 + t + j)] = o.ptr[j];
     }
   });
-  std::vector<int> bcnt((size_t)N + 1, 0);
-  for (int64_t s2 = 0; s2 < nslots; ++s2) bcnt[(size_t)slot_node[(size_t)s2] + 1]++;
+  std::vector<int> bcnt((size_t)N + 1, 0);   // slots per node (relaxed atomic counts)
+  host_parallel(nslots, [&](int64_t s0, int64_t s1) {
+    for (int64_t s2 = s0; s2 < s1; ++s2)
+      __atomic_fetch_add(&bcnt[(size_t)slot_node[(size_t)s2] + 1], 1, __ATOMIC_RELAXED);
+  });
   std::vector<int> bnodes, bptr(1, 0), bidx((size_t)N, -1);
   for (int64_t g = 0; g < N; ++g)
     if (bcnt[(size_t)g + 1] > 0) {
