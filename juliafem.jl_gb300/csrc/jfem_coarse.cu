@@ -586,12 +586,10 @@ static int coarse_build(Ctx* c, int target_nc) {
     if (cell_id[(size_t)k] == 0) cell_id[(size_t)k] = nagg++;
   const int nc = 6 * nagg, nc_pad = (nc + GJ_B - 1) / GJ_B * GJ_B;
   std::vector<int> node_agg((size_t)N), agg_ptr((size_t)nagg + 1, 0), agg_nodes((size_t)N);
-  host_parallel(N, [&](int64_t i0, int64_t i1) {   // node counts per aggregate: relaxed atomics, order-free
-    for (int64_t i = i0; i < i1; ++i) {
-      node_agg[(size_t)i] = cell_id[(size_t)cell[(size_t)i]];
-      __atomic_fetch_add(&agg_ptr[(size_t)node_agg[(size_t)i] + 1], 1, __ATOMIC_RELAXED);
-    }
+  host_parallel(N, [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; ++i) node_agg[(size_t)i] = cell_id[(size_t)cell[(size_t)i]];
   });
+  for (int64_t i = 0; i < N; ++i) ++agg_ptr[(size_t)node_agg[(size_t)i] + 1];   // few counters: serial
   for (int a = 0; a < nagg; ++a) agg_ptr[(size_t)a + 1] += agg_ptr[(size_t)a];
   {
     std::vector<int> cur(agg_ptr.begin(), agg_ptr.end() - 1);
