@@ -1178,7 +1178,15 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
       cudaMemsetAsync(c->x, 0, n * sizeof(double), c->stream);
       if (fp32 && (rc = nh_state_prepare(c))) return rc;   // tangent point state at u for this Newton step
       PcgResult pr;
-      if ((rc = pcg(c, c->b, fp32, eta, o->max_cg_per_newton, o->time_budget_s, t0, false, true, &pr))) {
+      // With a coarse space (the default) the tangent system is solved by the
+      // two-level flexible CG: the tangent through the tiled apply, the
+      // linear-elastic coarse matrix PᵀKP as the coarse level (an SPD
+      // approximation of the tangent's; flexible CG needs no more).  Without
+      // one (jfem_set_coarse_space(ctx, 0)): Jacobi-PCG.
+      const bool two_level = fp32 && c->coarse_target != 0 && apply_is_tiled(c);
+      rc = two_level ? fcg(c, c->b, false, true, eta, o->max_cg_per_newton, o->time_budget_s, t0, true, &pr, 0.01)
+                     : pcg(c, c->b, fp32, eta, o->max_cg_per_newton, o->time_budget_s, t0, false, true, &pr);
+      if (rc) {
         if (rc == JFEM_ERR_TIMEOUT) newton_timeout_state(c, u_d, st, total_newton, total_cg + pr.iters, refin, last_rel, t0);
         return rc;
       }
