@@ -246,13 +246,17 @@ int jfem_mpnn_precondition(jfem_ctx* ctx, const double* r, double* z);
  * S the smoother (D⁻¹, or the learned network above), P the rigid-body modes
  * (3 translations, 3 rotations about the centroid) of node aggregates — the
  * nodes binned into a structured grid of equal boxes over the bounding box —
- * zero on prescribed DOFs.  A_c is assembled in FP64 on the device from the
- * elements that straddle aggregates or hold prescribed DOFs, inverted in FP64
- * (Gauss–Jordan, a pivot below 1e-12 of its diagonal drops that mode) and
- * applied in FP32.  No counterpart in the reference, whose GPU solver design
- * note recommends a multigrid-type coarse correction with point smoothers
+ * zero on prescribed DOFs.  A_c is assembled on the device (double-float, from
+ * the FP64 geometry records) from the elements that straddle aggregates or
+ * hold prescribed DOFs, inverted (Gauss–Jordan, a pivot below 1e-12 of its
+ * diagonal drops that mode) and applied in FP32.  No counterpart in the
+ * reference, whose GPU solver design note recommends a multigrid-type coarse
+ * correction with point smoothers
  * (docs/src/book/design/gpu_solver_strategy_expert_validated.md:114-156) but
- * ships unpreconditioned CG.  Linear-elastic small strain only.
+ * ships unpreconditioned CG.  A_c is the coarse projection of the small-strain
+ * stiffness; with finite strain it is the coarse level of the Newton tangent
+ * solves (JFEM_NEWTON solves each tangent system by this flexible CG whenever
+ * a coarse space is enabled, else by Jacobi-PCG).
  * coarse_dofs: 0 = no coarse space (JFEM_FCG_LEARNED is then one-level),
  * < 0 = automatic (about one coarse DOF per 1,000 DOFs, within [192, 2304];
  * the default), > 0 = about that many, at most JFEM_COARSE_MAX_DOFS (the

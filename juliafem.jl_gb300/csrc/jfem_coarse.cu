@@ -785,11 +785,13 @@ static int coarse_assemble(Ctx* c) {
   return 0;
 }
 
+// A_c is always the coarse projection of the small-strain stiffness (λ, μ of
+// the material records, reference configuration); for finite strain it is the
+// coarse level of the tangent systems' preconditioner, an SPD approximation of
+// the tangent's own coarse operator (flexible CG needs no more).
 static int coarse_values(Ctx* c) {
   int rc = geometry_prepare(c);
   if (rc) return rc;
-  if (c->model != JFEM_LINEAR_ELASTIC || c->finite)
-    return set_err(c, JFEM_ERR_INVALID, "the coarse space is built for the linear-elastic small-strain operator");
   cudaEventRecord(c->ev0, c->stream);
   coarse_assemble(c);
   const int n = c->nc_pad, nbk = n / GJ_B;
