@@ -886,8 +886,11 @@ static int pcg(Ctx* c, const double* f, bool fp32, double tol, int max_iter, dou
 // the recursive residual norm over `window` iterations — generous, since CG
 // residual norms are not monotone) the solve continues with Jacobi from the
 // best iterate (res->fallbacks = 1).
+// reliable = false (Newton's inner solves, whose caller judges every step by
+// its own FP64 residual): no FP64 true residual, neither on the way nor at
+// the end — the recursive residual decides, as in pcg without reliable updates.
 static int fcg(Ctx* c, const double* f, bool nn, bool coarse, double tol, int max_iter, double time_budget,
-               double t_start, bool x_zero, PcgResult* res, double drop, bool tol_abs = false) {
+               double t_start, bool x_zero, PcgResult* res, double drop, bool tol_abs = false, bool reliable = true) {
   int rc = 0;
   double rr0 = 0.0;
   const int64_t n = 3 * c->N;
@@ -946,7 +949,18 @@ static int fcg(Ctx* c, const double* f, bool nn, bool coarse, double tol, int ma
       rec_best_it = iters;
     }
     const bool stagnant = nn && iters - rec_best_it >= window;
-    const bool check = s.done[0] || bad || rr < ru * rr_true_last || stagnant;
+    if (!reliable && s.done[0] && !bad) {   // the recursive residual decides
+      k_df_absorb<<<gv, 256, 0, c->stream>>>(n, c->xd, c->x);
+      c->launches += 1;
+      if ((rc = sync_and_check(c, "flexible CG result"))) return rc;
+      res->iters = iters;
+      res->refinements = refinements;
+      res->fallbacks = fallbacks;
+      res->relres = std::sqrt(rr / bb);
+      res->status = rr <= goal ? (fallbacks ? JFEM_STALL : 0) : JFEM_NOT_CONVERGED;
+      return 0;
+    }
+    const bool check = s.done[0] || bad || (reliable && rr < ru * rr_true_last) || stagnant;
     if (check) {
       double rr_t = 0.0, drift2 = 0.0;
       k_df_absorb<<<gv, 256, 0, c->stream>>>(n, c->xd, c->x);
@@ -1184,7 +1198,8 @@ static int solve_newton(Ctx* c, const jfem_solve_opts* o, double* u_d, jfem_stat
       // approximation of the tangent's; flexible CG needs no more).  Without
       // one (jfem_set_coarse_space(ctx, 0)): Jacobi-PCG.
       const bool two_level = fp32 && c->coarse_target != 0 && apply_is_tiled(c);
-      rc = two_level ? fcg(c, c->b, false, true, eta, o->max_cg_per_newton, o->time_budget_s, t0, true, &pr, 0.01)
+      rc = two_level ? fcg(c, c->b, false, true, eta, o->max_cg_per_newton, o->time_budget_s, t0, true, &pr, 0.01,
+                           false, false)
                      : pcg(c, c->b, fp32, eta, o->max_cg_per_newton, o->time_budget_s, t0, false, true, &pr);
       if (rc) {
         if (rc == JFEM_ERR_TIMEOUT) newton_timeout_state(c, u_d, st, total_newton, total_cg + pr.iters, refin, last_rel, t0);
