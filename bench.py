@@ -354,8 +354,10 @@ def newton_leg(jfem, args, device):
     """Hex8 Neo-Hookean unit cube, n³ cells (128³: 2,097,152 elements,
     6,440,067 DOFs), 2×2×2 Gauss, per-element E = 210e3·exp(0.2 z) (seeded),
     ν = 0.3, bottom clamped, top u_z ramped to −0.1 over 10 load steps;
-    Newton–Krylov with the FP32 tiled tangent apply, double-float PCG vectors,
-    FP64 residuals and Eisenstat–Walker forcing, Newton tol 1e-8.  One timed
+    Newton–Krylov with the FP32 tiled tangent apply, each tangent system solved
+    by the two-level flexible CG (the default coarse space: the small-strain
+    coarse matrix, built inside the timed solve), double-float vectors, FP64
+    Newton residuals and Eisenstat–Walker forcing, Newton tol 1e-8.  One timed
     solve (CUDA events on the context stream) after the mesh is resident."""
     import torch
     w = jfem.workloads.cube_compression(n=args.newton_n, steps=10)
