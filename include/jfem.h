@@ -30,11 +30,17 @@ extern "C" {
 #define JFEM_STALL             2   /* learned preconditioner stalled; fell back to Jacobi */
 #define JFEM_ERR_INVALID      -1   /* bad argument / call order (error() in the reference) */
 #define JFEM_ERR_CUDA         -2
-#define JFEM_ERR_OOM          -3
+#define JFEM_ERR_OOM          -3   /* device or host memory (or host threads) exhausted */
 #define JFEM_ERR_NEG_JACOBIAN -4   /* detJ <= 0 in an element */
 #define JFEM_ERR_NAN          -5   /* NaN/Inf, or J <= 0 in the Neo-Hookean law */
 #define JFEM_ERR_TIMEOUT      -6   /* a bounded device loop ran out of its budget */
 #define JFEM_ERR_TOO_LARGE    -7   /* jfem_apply_noalloc: mesh needs more than its fixed scratch */
+
+/* Every entry point returns one of these codes; no C++ exception crosses this
+ * interface.  A jfem_set_mesh that fails after its argument checks leaves the
+ * context without a mesh (later calls answer JFEM_ERR_INVALID until a mesh is
+ * set); a failed jfem_set_traction / jfem_set_surface_load leaves it without a
+ * surface load; a failed jfem_batch_add leaves the batch as it was. */
 
 /* Size of the fixed device array jfem_apply_noalloc works in (every GPU that
  * loads the library holds it until the process exits). */

@@ -29,9 +29,9 @@ MPNN_WIDTH, MPNN_PARAMS = 32, 4384
 NEN = {TET4: 4, TET10: 10, HEX8: 8}
 NFN = {TRI3: 3, TRI6: 6, QUAD4: 4}
 
-_ERRNAMES = {ERR_INVALID: "invalid argument", ERR_CUDA: "CUDA error", ERR_OOM: "out of device memory",
+_ERRNAMES = {ERR_INVALID: "invalid argument", ERR_CUDA: "CUDA error", ERR_OOM: "out of memory",
              ERR_NEG_JACOBIAN: "non-positive Jacobian", ERR_NAN: "NaN / invalid material state",
-             ERR_TIMEOUT: "time budget exceeded"}
+             ERR_TIMEOUT: "time budget exceeded", ERR_TOO_LARGE: "mesh too large for the fixed scratch"}
 
 
 class JFEMError(RuntimeError):
@@ -481,5 +481,5 @@ def rcm(conn, n_nodes: int, start: int = 0, index_base: int = 0):
     rc = load().jfem_rcm(int(n_nodes), conn.shape[0], nen, _ptr(conn, _i64p), index_base, int(start),
                          _ptr(perm, _i64p), C.byref(b0), C.byref(b1))
     if rc != 0:
-        raise JFEMError(rc, "jfem_rcm: invalid arguments")
+        raise JFEMError(rc, "jfem_rcm")
     return perm, b0.value, b1.value

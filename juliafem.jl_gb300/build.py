@@ -34,7 +34,7 @@ def sources():
 def _stale(obj: Path, src: Path) -> bool:
     if not obj.exists():
         return True
-    deps = [src] + list(CSRC.glob("*.cuh")) + list((PKG.parent / "include").glob("*.h"))
+    deps = [src] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((PKG.parent / "include").glob("*.h"))
     return any(d.stat().st_mtime > obj.stat().st_mtime for d in deps)
 
 

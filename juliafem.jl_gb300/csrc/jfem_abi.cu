@@ -3,8 +3,10 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <utility>
 
 #include "jfem_common.cuh"
+#include "jfem_abi_guard.h"
 
 namespace jfem {
 
@@ -59,8 +61,8 @@ void free_mesh(Ctx* c) {
   fresh.geo_gen = c->geo_gen + 1;
   fresh.mask_gen = c->mask_gen + 1;
   fresh.launches = c->launches;
-  fresh.err = c->err;
-  *c = fresh;
+  fresh.err = std::move(c->err);
+  *c = std::move(fresh);   // moves only: nothing here allocates, so this cannot throw
 }
 
 }  // namespace jfem
@@ -101,6 +103,7 @@ void jfem_default_opts(jfem_solve_opts* o) {
 }
 
 int jfem_create(jfem_ctx** out, int device_ordinal) {
+  ABI_TRY
   if (!out) return JFEM_ERR_INVALID;
   *out = nullptr;
   int ndev = 0;
@@ -120,9 +123,11 @@ int jfem_create(jfem_ctx** out, int device_ordinal) {
   }
   *out = h;
   return JFEM_OK;
+  ABI_CATCH(nullptr)
 }
 
 int jfem_destroy(jfem_ctx* h) {
+  ABI_TRY
   if (!h) return JFEM_OK;
   cudaSetDevice(h->c.device);
   Ctx* c = &h->c;
@@ -144,6 +149,7 @@ int jfem_destroy(jfem_ctx* h) {
   if (c->stream) cudaStreamDestroy(c->stream);
   delete h;
   return JFEM_OK;
+  ABI_CATCH(nullptr)
 }
 
 const char* jfem_last_error(const jfem_ctx* h) { return h ? h->c.err.c_str() : "null context"; }
@@ -155,32 +161,39 @@ double jfem_last_apply_ms(const jfem_ctx* h) { return h ? h->c.last_apply_ms : 0
 void* jfem_stream(const jfem_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
 
 int jfem_time_apply(jfem_ctx* h, int flags, int reps, double* ms_element, double* ms_gather) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
   if (!ms_element || !ms_gather) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL output");
   return jfem::time_apply(c, (flags & JFEM_APPLY_FP32) != 0, (flags & JFEM_APPLY_MASKED) != 0, reps, ms_element,
                           ms_gather);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_time_assembly(jfem_ctx* h, int reps, double* ms_qpoint, double* ms_scatter, int64_t* nnz) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
   if (!ms_qpoint || !ms_scatter || !nnz) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL output");
   *nnz = 9 * c->n_blocks;
   return jfem::time_assembly(c, reps, ms_qpoint, ms_scatter);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_set_mesh(jfem_ctx* h, int elem_type, int64_t n_nodes, const double* X, int64_t n_elem, const int64_t* conn,
                   int index_base) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   c->err.clear();
   return jfem::mesh_setup(c, elem_type, n_nodes, X, n_elem, conn, index_base);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_set_material(jfem_ctx* h, int model, const double* E, const double* nu, int per_element) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0) return jfem::set_err(c, JFEM_ERR_INVALID, "jfem_set_mesh must come first");
@@ -209,18 +222,22 @@ int jfem_set_material(jfem_ctx* h, int model, const double* E, const double* nu,
   c->have_material = true;
   jfem::geometry_invalidate(c);
   return JFEM_OK;
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_set_formulation(jfem_ctx* h, int finite_strain, int geometric_stiffness) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   c->finite = finite_strain ? 1 : 0;
   c->geom = geometric_stiffness ? 1 : 0;
   ++c->state_version;
   return JFEM_OK;
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_set_dirichlet(jfem_ctx* h, int64_t n, const int64_t* dofs, const double* values, int index_base) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0) return jfem::set_err(c, JFEM_ERR_INVALID, "jfem_set_mesh must come first");
@@ -242,22 +259,28 @@ int jfem_set_dirichlet(jfem_ctx* h, int64_t n, const int64_t* dofs, const double
   c->n_fixed_nonzero = nz;
   ++c->mask_gen;
   return jfem::sync_and_check(c, "Dirichlet upload");
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_set_traction(jfem_ctx* h, int face_type, int64_t n_faces, const int64_t* face_conn, const double* t,
                       int index_base) {
+  ABI_TRY
   ENTER(h);
   if (n_faces > 0 && !t) return jfem::set_err(&h->c, JFEM_ERR_INVALID, "traction array is NULL");
   return jfem::faces_setup(&h->c, face_type, n_faces, face_conn, t, nullptr, index_base);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_set_surface_load(jfem_ctx* h, int face_type, int64_t n_faces, const int64_t* face_conn, const double* t,
                           const double* p, int index_base) {
+  ABI_TRY
   ENTER(h);
   return jfem::faces_setup(&h->c, face_type, n_faces, face_conn, t, p, index_base);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_set_state(jfem_ctx* h, const double* u) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0) return jfem::set_err(c, JFEM_ERR_INVALID, "jfem_set_mesh must come first");
@@ -270,10 +293,12 @@ int jfem_set_state(jfem_ctx* h, const double* u) {
   }
   ++c->state_version;
   return jfem::sync_and_check(c, "state upload");
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_assemble_csc(jfem_ctx* h, int index_base, int64_t* nnz_inout, int64_t* colptr, int64_t* rowval,
                       double* nzval, double* f) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0) return jfem::set_err(c, JFEM_ERR_INVALID, "jfem_set_mesh must come first");
@@ -324,17 +349,21 @@ int jfem_assemble_csc(jfem_ctx* h, int index_base, int64_t* nnz_inout, int64_t* 
   cudaFree(d_fint);
   cleanup();
   return rc;
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_apply_device(jfem_ctx* h, const double* v, double* y, int flags) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
   if (!v || !y) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL vector");
   return jfem::apply_device(c, v, y, (flags & JFEM_APPLY_FP32) != 0, (flags & JFEM_APPLY_MASKED) != 0, nullptr);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_apply(jfem_ctx* h, const double* v, double* y, int flags) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
@@ -346,9 +375,11 @@ int jfem_apply(jfem_ctx* h, const double* v, double* y, int flags) {
   if (rc) return rc;
   cudaMemcpyAsync(y, c->tmp2, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
   return jfem::sync_and_check(c, "apply download");
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_internal_force(jfem_ctx* h, double* f_int) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
@@ -357,9 +388,11 @@ int jfem_internal_force(jfem_ctx* h, double* f_int) {
   if (rc) return rc;
   cudaMemcpyAsync(f_int, c->tmp2, 3 * c->N * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
   return jfem::sync_and_check(c, "internal force download");
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_solve_device(jfem_ctx* h, const jfem_solve_opts* opts, double* u_device, jfem_stats* stats) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (!u_device) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL output");
@@ -367,9 +400,11 @@ int jfem_solve_device(jfem_ctx* h, const jfem_solve_opts* opts, double* u_device
   const int rc = jfem::solve_device(c, opts, u_device, stats);
   if (stats && rc < 0) stats->status = rc;
   return rc;
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_solve(jfem_ctx* h, const jfem_solve_opts* opts, double* u, jfem_stats* stats) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (!u) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL output");
@@ -388,10 +423,12 @@ int jfem_solve(jfem_ctx* h, const jfem_solve_opts* opts, double* u, jfem_stats* 
   if (rc == JFEM_ERR_TIMEOUT) jfem::set_err(c, JFEM_ERR_TIMEOUT, "solve exceeded its time budget");
   cudaFree(d_u);
   return rc;
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_recover_field(jfem_ctx* h, const double* u, int field, double tol, int max_iter, double* nodal,
                        int* iterations) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
@@ -400,89 +437,114 @@ int jfem_recover_field(jfem_ctx* h, const double* u, int field, double tol, int 
     return jfem::set_err(c, JFEM_ERR_INVALID, "field must be JFEM_FIELD_STRAIN or JFEM_FIELD_STRESS");
   if (!(tol > 0.0) || max_iter <= 0) return jfem::set_err(c, JFEM_ERR_INVALID, "tol and max_iter must be positive");
   return jfem::recover_field(c, u, field, tol, max_iter, nodal, iterations);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_set_coarse_space(jfem_ctx* h, int coarse_dofs) {
+  ABI_TRY
   ENTER(h);
   if (coarse_dofs > JFEM_COARSE_MAX_DOFS)
     return jfem::set_err(&h->c, JFEM_ERR_INVALID, "coarse_dofs above JFEM_COARSE_MAX_DOFS");
   h->c.coarse_target = coarse_dofs < 0 ? -1 : coarse_dofs;
   return JFEM_OK;
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_coarse_info(jfem_ctx* h, int* n_aggregates, int* n_coarse_dofs, int64_t* n_elements, double* setup_ms) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
   return jfem::coarse_info(c, n_aggregates, n_coarse_dofs, n_elements, setup_ms);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_coarse_matrix(jfem_ctx* h, double* Ac, int* node_aggregate) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
   return jfem::coarse_matrix(c, Ac, node_aggregate);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_coarse_precondition(jfem_ctx* h, const double* r, double* z) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
   if (!r || !z) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL array");
   return jfem::coarse_precondition(c, r, z);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_mpnn_init(jfem_ctx* h, uint64_t seed) {
+  ABI_TRY
   ENTER(h);
   return jfem::mpnn_init(&h->c, seed);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_mpnn_set_weights(jfem_ctx* h, const float* w) {
+  ABI_TRY
   ENTER(h);
   if (!w) return jfem::set_err(&h->c, JFEM_ERR_INVALID, "NULL weights");
   return jfem::mpnn_set_weights(&h->c, w);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_mpnn_get_weights(jfem_ctx* h, float* w) {
+  ABI_TRY
   ENTER(h);
   if (!w) return jfem::set_err(&h->c, JFEM_ERR_INVALID, "NULL weights");
   return jfem::mpnn_get_weights(&h->c, w);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_mpnn_collect(jfem_ctx* h, int max_pairs, double tol) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
   if (!(tol > 0.0)) return jfem::set_err(c, JFEM_ERR_INVALID, "tol must be positive");
   return jfem::mpnn_collect(c, max_pairs, tol);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_mpnn_clear(jfem_ctx* h) {
+  ABI_TRY
   ENTER(h);
   h->c.mp_pairs = 0;
   h->c.mp_coarse = -1;
   return JFEM_OK;
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_mpnn_train(jfem_ctx* h, int epochs, int batch, double lr, uint64_t seed, double* losses) {
+  ABI_TRY
   ENTER(h);
   return jfem::mpnn_train(&h->c, epochs, batch, lr, seed, losses);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_mpnn_loss_grad(jfem_ctx* h, const double* r, const double* e, double* loss, float* grad) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
   if (!r || !e || !loss || !grad) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL argument");
   return jfem::mpnn_loss_grad(c, r, e, loss, grad);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 int jfem_mpnn_precondition(jfem_ctx* h, const double* r, double* z) {
+  ABI_TRY
   ENTER(h);
   Ctx* c = &h->c;
   if (c->N == 0 || !c->have_material) return jfem::set_err(c, JFEM_ERR_INVALID, "mesh and material must be set");
   if (!r || !z) return jfem::set_err(c, JFEM_ERR_INVALID, "NULL vector");
   return jfem::mpnn_precondition(c, r, z);
+  ABI_CATCH(h ? &h->c.err : nullptr)
 }
 
 }  // extern "C"

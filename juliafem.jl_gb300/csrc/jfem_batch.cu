@@ -37,6 +37,7 @@
 #include <vector>
 
 #include "jfem_apply_kernels.cuh"
+#include "jfem_abi_guard.h"
 
 namespace jfem {
 
@@ -902,6 +903,7 @@ struct jfem_batch {
 extern "C" {
 
 int jfem_batch_create(jfem_batch** out, int device) {
+  ABI_TRY
   if (!out) return JFEM_ERR_INVALID;
   *out = nullptr;
   int ndev = 0;
@@ -924,9 +926,11 @@ int jfem_batch_create(jfem_batch** out, int device) {
   }
   *out = h;
   return JFEM_OK;
+  ABI_CATCH(nullptr)
 }
 
 int jfem_batch_destroy(jfem_batch* h) {
+  ABI_TRY
   if (!h) return JFEM_OK;
   cudaSetDevice(h->b.device);
   jfem::bfree_device(&h->b);
@@ -936,6 +940,7 @@ int jfem_batch_destroy(jfem_batch* h) {
   if (h->b.ev_join) cudaEventDestroy(h->b.ev_join);
   delete h;
   return JFEM_OK;
+  ABI_CATCH(nullptr)
 }
 
 const char* jfem_batch_last_error(const jfem_batch* h) { return h ? h->b.err.c_str() : "null batch"; }
@@ -943,6 +948,7 @@ const char* jfem_batch_last_error(const jfem_batch* h) { return h ? h->b.err.c_s
 int jfem_batch_add(jfem_batch* h, int64_t n_nodes, const double* X, int64_t n_elem, const int64_t* conn,
                    int index_base, double E, double nu, int64_t n_fixed, const int64_t* fixed_dofs,
                    int64_t n_faces, const int64_t* face_conn, const double* t) {
+  ABI_TRY
   if (!h) return JFEM_ERR_INVALID;
   BatchHost* b = &h->b;
   if (n_nodes <= 0 || n_elem <= 0 || !X || !conn) return jfem::bset_err(b, JFEM_ERR_INVALID, "empty instance");
@@ -974,42 +980,61 @@ int jfem_batch_add(jfem_batch* h, int64_t n_nodes, const double* X, int64_t n_el
     const int64_t v = face_conn[k] - index_base;
     if (v < 0 || v >= n_nodes) return jfem::bset_err(b, JFEM_ERR_INVALID, "face connectivity out of range");
   }
-  b->X.insert(b->X.end(), X, X + 3 * n_nodes);
-  for (int64_t k = 0; k < 4 * n_elem; ++k) b->conn.push_back((int)(N0 + conn[k] - index_base));
-  const double lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), mu = E / (2.0 * (1.0 + nu));
-  b->lam.insert(b->lam.end(), (size_t)n_elem, lam);
-  b->mu.insert(b->mu.end(), (size_t)n_elem, mu);
-  std::vector<uint8_t> mk((size_t)n_nodes, 0);
-  for (int64_t k = 0; k < n_fixed; ++k) {
-    const int64_t v = fixed_dofs[k] - index_base;
-    mk[(size_t)(v / 3)] |= (uint8_t)(1u << (v % 3));
-  }
-  b->mask.insert(b->mask.end(), mk.begin(), mk.end());
-  // consistent load of a constant traction on Tri3 faces: area/3 per node
-  // (src/problems_elasticity.jl:454-502 with the 1-point rule, exact here)
-  std::vector<double> f((size_t)3 * n_nodes, 0.0);
-  for (int64_t k = 0; k < n_faces; ++k) {
-    int64_t nd[3];
-    for (int i = 0; i < 3; ++i) nd[i] = face_conn[3 * k + i] - index_base;
-    double u[3], v[3];
-    for (int d = 0; d < 3; ++d) {
-      u[d] = X[3 * nd[1] + d] - X[3 * nd[0] + d];
-      v[d] = X[3 * nd[2] + d] - X[3 * nd[0] + d];
+  // The instance is appended to the batch's host arrays; if an append runs out
+  // of memory they are cut back to their previous lengths, so the batch never
+  // holds half an instance.
+  const size_t nX = b->X.size(), nconn = b->conn.size(), nlam = b->lam.size(), nmu = b->mu.size(),
+               nmask = b->mask.size(), nf = b->f.size(), nnode = b->node_off.size(), nelem = b->elem_off.size();
+  try {
+    b->X.insert(b->X.end(), X, X + 3 * n_nodes);
+    for (int64_t k = 0; k < 4 * n_elem; ++k) b->conn.push_back((int)(N0 + conn[k] - index_base));
+    const double lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), mu = E / (2.0 * (1.0 + nu));
+    b->lam.insert(b->lam.end(), (size_t)n_elem, lam);
+    b->mu.insert(b->mu.end(), (size_t)n_elem, mu);
+    std::vector<uint8_t> mk((size_t)n_nodes, 0);
+    for (int64_t k = 0; k < n_fixed; ++k) {
+      const int64_t v = fixed_dofs[k] - index_base;
+      mk[(size_t)(v / 3)] |= (uint8_t)(1u << (v % 3));
     }
-    const double cx = u[1] * v[2] - u[2] * v[1], cy = u[2] * v[0] - u[0] * v[2], cz = u[0] * v[1] - u[1] * v[0];
-    const double area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
-    for (int i = 0; i < 3; ++i)
-      for (int d = 0; d < 3; ++d) f[(size_t)(3 * nd[i] + d)] += area / 3.0 * t[3 * k + d];
+    b->mask.insert(b->mask.end(), mk.begin(), mk.end());
+    // consistent load of a constant traction on Tri3 faces: area/3 per node
+    // (src/problems_elasticity.jl:454-502 with the 1-point rule, exact here)
+    std::vector<double> f((size_t)3 * n_nodes, 0.0);
+    for (int64_t k = 0; k < n_faces; ++k) {
+      int64_t nd[3];
+      for (int i = 0; i < 3; ++i) nd[i] = face_conn[3 * k + i] - index_base;
+      double u[3], v[3];
+      for (int d = 0; d < 3; ++d) {
+        u[d] = X[3 * nd[1] + d] - X[3 * nd[0] + d];
+        v[d] = X[3 * nd[2] + d] - X[3 * nd[0] + d];
+      }
+      const double cx = u[1] * v[2] - u[2] * v[1], cy = u[2] * v[0] - u[0] * v[2], cz = u[0] * v[1] - u[1] * v[0];
+      const double area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+      for (int i = 0; i < 3; ++i)
+        for (int d = 0; d < 3; ++d) f[(size_t)(3 * nd[i] + d)] += area / 3.0 * t[3 * k + d];
+    }
+    b->f.insert(b->f.end(), f.begin(), f.end());
+    b->node_off.push_back(N0 + n_nodes);
+    b->elem_off.push_back(E0 + n_elem);
+  } catch (...) {
+    b->X.resize(nX);
+    b->conn.resize(nconn);
+    b->lam.resize(nlam);
+    b->mu.resize(nmu);
+    b->mask.resize(nmask);
+    b->f.resize(nf);
+    b->node_off.resize(nnode);
+    b->elem_off.resize(nelem);
+    throw;
   }
-  b->f.insert(b->f.end(), f.begin(), f.end());
-  b->node_off.push_back(N0 + n_nodes);
-  b->elem_off.push_back(E0 + n_elem);
   b->uploaded = false;
   return (int)(b->node_off.size() - 2);
+  ABI_CATCH(h ? &h->b.err : nullptr)
 }
 
 int jfem_batch_solve(jfem_batch* h, double tol, int max_iter, int block_size, double* u, int* iterations,
                      int* status, double* residual, double* latency_s, double* solve_s) {
+  ABI_TRY
   if (!h) return JFEM_ERR_INVALID;
   BatchHost* b = &h->b;
   if (cudaSetDevice(b->device) != cudaSuccess) return jfem::bset_err(b, JFEM_ERR_CUDA, "cudaSetDevice");
@@ -1058,6 +1083,7 @@ int jfem_batch_solve(jfem_batch* h, double tol, int max_iter, int block_size, do
     for (int k = 0; k < n; ++k) latency_s[k] = (double)tns[(size_t)k] * 1e-9;
   if (solve_s) *solve_s = ms * 1e-3;
   return JFEM_OK;
+  ABI_CATCH(h ? &h->b.err : nullptr)
 }
 
 int jfem_batch_tune_source(const jfem_batch* h) { return h ? h->b.tune_source : JFEM_ERR_INVALID; }
@@ -1071,6 +1097,7 @@ int jfem_batch_config(const jfem_batch* h, int* block_size, int* grid) {
 }
 
 int jfem_batch_set_config(jfem_batch* h, int block_size, int cluster_size, int n_clustered, int cluster_block) {
+  ABI_TRY
   if (!h) return JFEM_ERR_INVALID;
   BatchHost* b = &h->b;
   if (block_size == 0) {
@@ -1090,6 +1117,7 @@ int jfem_batch_set_config(jfem_batch* h, int block_size, int cluster_size, int n
   cf.bs_c = cluster_size > 1 ? cluster_block : 0;
   b->forced = cf;
   return JFEM_OK;
+  ABI_CATCH(h ? &h->b.err : nullptr)
 }
 
 int jfem_batch_cluster_config(const jfem_batch* h, int* cluster_size, int* n_clustered, int* cluster_block) {

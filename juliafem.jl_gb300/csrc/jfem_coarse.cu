@@ -702,10 +702,20 @@ static int coarse_build(Ctx* c, int target_nc) {
     c->pcg_graph = nullptr;
     c->pcg_graph_key = -1;
   }
-  void* old[] = {c->agg_ptr, c->agg_nodes, c->node_agg, c->node_d32, c->node_ddf, c->celem, c->celem_aggs,
-                 c->celem_off, c->contrib, c->cblk_ab, c->cblk_ptr, c->cblk_src, c->Ac, c->Ac_diag, c->gj_buf,
-                 c->Ainv32, c->Ec, c->chunk_begin, c->agg_chunk_ptr, c->cpart, c->chunk_agg, c->agg_cnt, c->RQ};
-  for (void* p : old) dfree(c, p);
+  // Until the last step below succeeds the context holds no coarse space
+  // (built target −1, released arrays null): a failure here makes the next
+  // coarse_prepare build it again instead of reading a partial set.
+  c->coarse_built_target = -1;
+  c->coarse_geo_gen = 0;
+  auto release = [&](auto*& p) {
+    dfree(c, p);
+    p = nullptr;
+  };
+  release(c->agg_ptr); release(c->agg_nodes); release(c->node_agg); release(c->node_d32); release(c->node_ddf);
+  release(c->celem); release(c->celem_aggs); release(c->celem_off); release(c->contrib); release(c->cblk_ab);
+  release(c->cblk_ptr); release(c->cblk_src); release(c->Ac); release(c->Ac_diag); release(c->gj_buf);
+  release(c->Ainv32); release(c->Ec); release(c->chunk_begin); release(c->agg_chunk_ptr); release(c->cpart);
+  release(c->chunk_agg); release(c->agg_cnt); release(c->RQ);
   c->nagg = nagg;
   c->nc = nc;
   c->nc_pad = nc_pad;

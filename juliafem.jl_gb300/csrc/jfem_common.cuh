@@ -18,6 +18,8 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <exception>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -445,6 +447,7 @@ template <typename T>
 int dalloc(Ctx* c, T** p, size_t count) {
   *p = nullptr;
   if (count == 0) count = 1;
+  c->owned.reserve(c->owned.size() + 1);   // may throw, before anything is allocated
   cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
   if (e != cudaSuccess) {
     *p = nullptr;
@@ -455,6 +458,37 @@ int dalloc(Ctx* c, T** p, size_t count) {
 }
 void dfree(Ctx* c, void* p);
 void free_mesh(Ctx* c);
+
+// Runs task(k) for k in [0, ntasks), each on its own host thread.  An exception
+// in a task is carried to the calling thread (the first one, after every thread
+// has been joined), and a thread that cannot be started runs its task on the
+// calling thread instead.
+template <class F>
+void host_tasks(int64_t ntasks, F task) {
+  std::exception_ptr first;
+  std::mutex mu;
+  auto run = [&](int64_t k) {
+    try {
+      task(k);
+    } catch (...) {
+      std::lock_guard<std::mutex> lk(mu);
+      if (!first) first = std::current_exception();
+    }
+  };
+  std::vector<std::thread> th;
+  th.reserve((size_t)ntasks);
+  for (int64_t k = 0; k < ntasks; ++k) {
+    bool started = false;
+    try {
+      th.emplace_back(run, k);
+      started = true;
+    } catch (...) {
+    }
+    if (!started) run(k);
+  }
+  for (auto& x : th) x.join();
+  if (first) std::rethrow_exception(first);
+}
 
 // Runs body(i0, i1) over contiguous ranges of [0, n) on up to 16 host threads
 // (at least 16 items each); callers make every range's work independent, so
@@ -467,10 +501,7 @@ void host_parallel(int64_t n, F body) {
     body((int64_t)0, n);
     return;
   }
-  std::vector<std::thread> th;
-  th.reserve((size_t)nt);
-  for (int64_t k = 0; k < nt; ++k) th.emplace_back(body, n * k / nt, n * (k + 1) / nt);
-  for (auto& x : th) x.join();
+  host_tasks(nt, [&](int64_t k) { body(n * k / nt, n * (k + 1) / nt); });
 }
 
 inline int grid_for(int64_t n, int threads, int64_t cap = 152LL * 64) {

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/jfem.h"
+#include "jfem_abi_guard.h"
 
 namespace jfem {
 
@@ -55,6 +56,7 @@ extern "C" {
 
 int jfem_rcm(int64_t n_nodes, int64_t n_elem, int nodes_per_elem, const int64_t* conn, int index_base,
              int64_t start, int64_t* perm, int64_t* bandwidth_before, int64_t* bandwidth_after) {
+  ABI_TRY
   if (n_nodes <= 0 || n_elem < 0 || nodes_per_elem <= 0 || !conn || !perm) return JFEM_ERR_INVALID;
   for (int64_t k = 0; k < n_elem * nodes_per_elem; ++k)
     if (conn[k] - index_base < 0 || conn[k] - index_base >= n_nodes) return JFEM_ERR_INVALID;
@@ -95,6 +97,7 @@ int jfem_rcm(int64_t n_nodes, int64_t n_elem, int nodes_per_elem, const int64_t*
   if (bandwidth_before) *bandwidth_before = jfem::graph_bandwidth(n_nodes, ptr, adj, nullptr);
   if (bandwidth_after) *bandwidth_after = jfem::graph_bandwidth(n_nodes, ptr, adj, newpos.data());
   return JFEM_OK;
+  ABI_CATCH(nullptr)
 }
 
 }  // extern "C"

@@ -298,6 +298,9 @@ static int build_adjacency(Ctx* c, const int* conn, int64_t M, int nper, int** p
   return rc;
 }
 
+static int mesh_build(Ctx* c, int et, int nn, int64_t N, const double* X, int64_t E, const int64_t* conn_h,
+                      int base);
+
 int mesh_setup(Ctx* c, int et, int64_t N, const double* X, int64_t E, const int64_t* conn_h, int base) {
   if (!(et == JFEM_TET4 || et == JFEM_TET10 || et == JFEM_HEX8))
     return set_err(c, JFEM_ERR_INVALID, "unsupported element type (4=Tet4, 10=Tet10, 8=Hex8)");
@@ -306,7 +309,23 @@ int mesh_setup(Ctx* c, int et, int64_t N, const double* X, int64_t E, const int6
   const int nn = et == JFEM_TET4 ? 4 : et == JFEM_TET10 ? 10 : 8;
   if (N > 0x7fffffffLL / 3 || E >= (1LL << 28) || E * nn > 0x7fffffffLL)
     return set_err(c, JFEM_ERR_INVALID, "mesh too large for 32-bit device indices");
+  // A failure past this point (a bad node number found on the device, device or
+  // host memory exhausted) leaves the context without a mesh, never with a
+  // partial one that later calls would read.
   free_mesh(c);
+  int rc = 0;
+  try {
+    rc = mesh_build(c, et, nn, N, X, E, conn_h, base);
+  } catch (...) {
+    free_mesh(c);
+    throw;
+  }
+  if (rc) free_mesh(c);
+  return rc;
+}
+
+static int mesh_build(Ctx* c, int et, int nn, int64_t N, const double* X, int64_t E, const int64_t* conn_h,
+                      int base) {
   c->et = et;
   c->nn = nn;
   c->N = N;
@@ -404,6 +423,9 @@ int mesh_setup(Ctx* c, int et, int64_t N, const double* X, int64_t E, const int6
 // ---------------------------------------------------------------------------
 // faces (surface traction table)
 // ---------------------------------------------------------------------------
+static void faces_clear(Ctx* c);
+static int faces_build(Ctx* c, int64_t F, const int64_t* fconn_h, const double* t_h, const double* p_h, int base);
+
 int faces_setup(Ctx* c, int ft, int64_t F, const int64_t* fconn_h, const double* t_h, const double* p_h,
                 int base) {
   if (c->N == 0) return set_err(c, JFEM_ERR_INVALID, "jfem_set_mesh must come first");
@@ -411,15 +433,35 @@ int faces_setup(Ctx* c, int ft, int64_t F, const int64_t* fconn_h, const double*
     return set_err(c, JFEM_ERR_INVALID, "unsupported face type (3=Tri3, 6=Tri6, 4=Quad4)");
   if (F < 0 || (F > 0 && (!fconn_h || (!t_h && !p_h)))) return set_err(c, JFEM_ERR_INVALID, "bad surface-load arrays");
   if (F >= (1LL << 28)) return set_err(c, JFEM_ERR_INVALID, "too many faces");
+  // The previous table is dropped first; a failure past this point leaves the
+  // context with no surface load rather than a table later calls would read
+  // half-built.
+  faces_clear(c);
+  c->ft = ft;
+  c->nfn = face_nodes(ft);
+  if (F == 0) return 0;
+  int rc = 0;
+  try {
+    rc = faces_build(c, F, fconn_h, t_h, p_h, base);
+  } catch (...) {
+    faces_clear(c);
+    throw;
+  }
+  if (rc) faces_clear(c);
+  return rc;
+}
+
+static void faces_clear(Ctx* c) {
   if (c->fconn) { dfree(c, c->fconn); c->fconn = nullptr; }
   if (c->ftrac) { dfree(c, c->ftrac); c->ftrac = nullptr; }
   if (c->fadj_ptr) { dfree(c, c->fadj_ptr); c->fadj_ptr = nullptr; }
   if (c->fadj) { dfree(c, c->fadj); c->fadj = nullptr; }
-  c->ft = ft;
-  c->nfn = face_nodes(ft);
-  c->F = F;
+  c->F = 0;
   c->f_ext_dirty = true;
-  if (F == 0) return 0;
+}
+
+static int faces_build(Ctx* c, int64_t F, const int64_t* fconn_h, const double* t_h, const double* p_h, int base) {
+  c->F = F;
   int rc = 0;
   if ((rc = dalloc(c, &c->fconn, F * c->nfn))) return rc;
   if ((rc = dalloc(c, &c->ftrac, 4 * F))) return rc;

@@ -23,6 +23,7 @@
 #include <mutex>
 
 #include "jfem_common.cuh"
+#include "jfem_abi_guard.h"
 
 namespace jfem {
 
@@ -253,6 +254,7 @@ int scratch_address(void** out) {
 extern "C" int jfem_apply_noalloc(int elem_type, int64_t n_nodes, const double* X, int64_t n_elem,
                                   const int64_t* conn, int index_base, const double* E, const double* nu,
                                   const double* v, double* y, void* stream) {
+  ABI_TRY
   using namespace jfem;
   if (!(elem_type == JFEM_TET4 || elem_type == JFEM_TET10 || elem_type == JFEM_HEX8)) return JFEM_ERR_INVALID;
   if (n_nodes <= 0 || n_elem <= 0 || !X || !conn || !E || !nu || !v || !y) return JFEM_ERR_INVALID;
@@ -305,4 +307,5 @@ extern "C" int jfem_apply_noalloc(int elem_type, int64_t n_nodes, const double* 
   const cudaError_t se = cudaStreamSynchronize(st);   // the work launched above has ended either way
   if (ce != cudaSuccess || se != cudaSuccess) return JFEM_ERR_CUDA;
   return h_err;
+  ABI_CATCH(nullptr)
 }

@@ -70,21 +70,15 @@ int tiles_build(Ctx* c, const double* X, const int64_t* conn_h, int base) {
     const int64_t nchunk = std::max<int64_t>(1, std::min<int64_t>(hw, E / 4096));
     std::vector<int64_t> cut((size_t)nchunk + 1);
     for (int64_t k = 0; k <= nchunk; ++k) cut[(size_t)k] = E * k / nchunk;
-    {
-      std::vector<std::thread> th;
-      for (int64_t k = 0; k < nchunk; ++k)
-        th.emplace_back([&key, &cut, k]() { std::sort(key.begin() + cut[(size_t)k], key.begin() + cut[(size_t)k + 1]); });
-      for (auto& x : th) x.join();
-    }
+    host_tasks(nchunk, [&](int64_t k) {
+      std::sort(key.begin() + cut[(size_t)k], key.begin() + cut[(size_t)k + 1]);
+    });
     for (int64_t w = 1; w < nchunk; w *= 2) {
-      std::vector<std::thread> th;
-      for (int64_t k = 0; k + w < nchunk; k += 2 * w) {
+      host_tasks((nchunk - w + 2 * w - 1) / (2 * w), [&](int64_t m) {
+        const int64_t k = 2 * w * m;
         const int64_t lo = cut[(size_t)k], mid = cut[(size_t)(k + w)], hi = cut[(size_t)std::min(k + 2 * w, nchunk)];
-        th.emplace_back([&key, lo, mid, hi]() {
-          std::inplace_merge(key.begin() + lo, key.begin() + mid, key.begin() + hi);
-        });
-      }
-      for (auto& x : th) x.join();
+        std::inplace_merge(key.begin() + lo, key.begin() + mid, key.begin() + hi);
+      });
     }
   }
   const int64_t ntiles = (E + T - 1) / T;

@@ -50,3 +50,24 @@ def test_no_device_fails_loudly(jfem):
     import pytest
     with pytest.raises(jfem.JFEMError):
         jfem.Context(0)
+
+
+def test_host_exception_does_not_cross_the_abi(jfem):
+    """A host allocation failure inside the library comes back as
+    JFEM_ERR_OOM, not as a C++ exception through the C interface (which would
+    end this process).  jfem_rcm runs on the host only: a node count of 10^15
+    makes its first per-node array (tens of PB) fail to allocate before
+    anything is written to perm."""
+    import ctypes as C
+    import numpy as np
+    conn = np.array([[0, 1, 2, 3]], np.int64)
+    perm = np.zeros(4, np.int64)
+    b0, b1 = C.c_int64(0), C.c_int64(0)
+    lib = jfem.load()
+    rc = lib.jfem_rcm(10 ** 15, 1, 4, conn.ctypes.data_as(C.POINTER(C.c_int64)), 0, 0,
+                      perm.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(b0), C.byref(b1))
+    assert rc == jfem._abi.ERR_OOM
+    assert not perm.any()
+    # the library still works afterwards
+    p, _, _ = jfem._abi.rcm(conn, 4, start=0)
+    assert sorted(p.tolist()) == [0, 1, 2, 3]

@@ -169,9 +169,22 @@ def test_tangent_apply_matches_assembled_tangent(jfem, orc, gpu_ctx_factory, mod
 def test_error_paths(jfem, gpu_ctx_factory):
     m = jfem.mesh.box_mesh(4, 2, 1, 1)
     with gpu_ctx_factory() as ctx:
+        ctx.set_mesh(4, m.X, m.conn)
         with pytest.raises(jfem.JFEMError) as e:
             ctx.set_mesh(4, m.X, m.conn + 100)
         assert e.value.code == jfem._abi.ERR_INVALID
+        with pytest.raises(jfem.JFEMError) as e:           # the failed call left no (partial) mesh
+            ctx.set_material(210e3, 0.3)
+        assert e.value.code == jfem._abi.ERR_INVALID and "set_mesh" in str(e.value)
+        ctx.set_mesh(4, m.X, m.conn)
+        ctx.set_material(210e3, 0.3)
+        ft, fc = m.face(0, 1)
+        ctx.set_traction(ft, fc, np.ones((fc.shape[0], 3)))
+        with pytest.raises(jfem.JFEMError) as e:           # a face node outside the mesh
+            ctx.set_traction(ft, fc + m.n_nodes, np.ones((fc.shape[0], 3)))
+        assert e.value.code == jfem._abi.ERR_INVALID
+        _, _, _, f = ctx.assemble_csc(0)                   # ...left no surface load: f = −f_int(0) = 0
+        assert not np.any(f)
         ctx.set_mesh(4, m.X, m.conn)
         with pytest.raises(jfem.JFEMError):
             ctx.apply(np.zeros(m.n_dofs))                  # material not set
