@@ -638,18 +638,33 @@ __global__ void __launch_bounds__(256) k_mp_poly_adj(int64_t N, const int* __res
       idg = __ldg(invdeg + i);
     }
     float s[3];
-    group_neighbour_sum<true>(nb_ptr, nbr, g, i, gl, s);
-    if (gl != 0) continue;
-    const float uv[3] = {u4.x, u4.y, u4.z};
-    mat3_acc(C, true, uv, s);
-    out[i] = make_float4(s[0], s[1], s[2], idg);
-    if (FCG) {
-      const float4 y4 = y[i];
-      const float yv[3] = {y4.x, y4.y, y4.z};
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-        t1 = df_add_abs(t1, df_two_prod(sqrtf(dinvf[3 * i + c]) * (yv[c] + s[c]), qold[3 * i + c]));
+    group_neighbour_sum<true>(nb_ptr, nbr, g, i, gl, s);   // every lane of the group holds the sum
+    if (!FCG) {
+      if (gl != 0) continue;
+      const float uv[3] = {u4.x, u4.y, u4.z};
+      mat3_acc(C, true, uv, s);
+      out[i] = make_float4(s[0], s[1], s[2], idg);
+      continue;
     }
+    // last step: out_c = s_c + (C_kᵀ u)_c and the β term's component c on lane c
+    // (lanes 0-2; lane 3 writes .w), the same fmaf order as a whole-vector
+    // product; on one lane the β term's loads and double-float sums made this
+    // pass 22 µs slower than a plain step on the 2M-DOF beam, on three 18 µs
+    const unsigned gm = group_mask();
+    const float u0 = __shfl_sync(gm, u4.x, 0, MP_GL), u1 = __shfl_sync(gm, u4.y, 0, MP_GL),
+                u2 = __shfl_sync(gm, u4.z, 0, MP_GL), id = __shfl_sync(gm, idg, 0, MP_GL);
+    if (gl > 3) continue;
+    const int c = gl < 3 ? gl : 0;
+    const float sc_ = gl == 0 ? s[0] : gl == 1 ? s[1] : s[2];
+    const float oc = fmaf(C[6 + c], u2, fmaf(C[3 + c], u1, fmaf(C[c], u0, sc_)));
+    float* outw = reinterpret_cast<float*>(out + i);
+    if (gl == 3) {
+      outw[3] = id;
+      continue;
+    }
+    outw[gl] = oc;
+    const float yc = reinterpret_cast<const float*>(y)[4 * i + gl];
+    t1 = df_add_abs(t1, df_two_prod(sqrtf(dinvf[3 * i + gl]) * (yc + oc), qold[3 * i + gl]));
   }
   if (FCG) {
     const double b = block_sum_df(t1, sh);
