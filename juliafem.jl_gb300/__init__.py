@@ -2,12 +2,13 @@
 
 The compute lives in libjfem_cuda.so (C ABI, include/jfem.h); this package is
 its Python binding (``_abi``), the reference-shaped host API (``problem``), the
-structured box mesher (``mesh``) and the Abaqus input reader (``abaqus``).
+structured box mesher (``mesh``), the Abaqus input reader (``abaqus``) and the
+weight and load-step checkpoint files (``checkpoint``).
 
 The directory name contains a dot, so it is loaded by path; ``load_package()``
 in __graft_entry__.py (and tests/conftest.py) registers it as ``jfem_gb300``.
 """
-from . import _abi, abaqus, mesh, workloads
+from . import _abi, abaqus, checkpoint, mesh, workloads
 from ._abi import Batch, Context, JFEMError, SolveOpts, Stats, default_opts, load
 from .problem import (CPU, GPU, Analysis, Auto, Dirichlet, DirichletBC, Elasticity, ElasticitySolution,
                       Element, Hex8, Linear, NeumannBC, Physics, Problem, Quad4, Tet4, Tet10, Tri3, Tri6,
