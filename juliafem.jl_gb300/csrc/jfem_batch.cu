@@ -38,6 +38,7 @@
 
 #include "jfem_apply_kernels.cuh"
 #include "jfem_abi_guard.h"
+#include "jfem_tune.h"
 
 namespace jfem {
 
@@ -725,15 +726,12 @@ static int sm_count(int device) {
 // ---------------------------------------------------------------------------
 // autotuner cache: the configuration chosen for a (GPU, element type, batch
 // shape) is kept for the process and, when JFEM_AUTOTUNE_CACHE names a file,
-// in that file (JSON object, one entry per line) for later processes.  The
+// in that file (JSON object, one entry per line) for later processes; entries
+// read back are launched only when tune_entry_valid accepts them.  The
 // batch shape is bucketed to powers of two: instance count, largest and mean
 // instance DOFs.  Entries hold the configuration in relative form (CTAs per SM,
 // fraction on clusters), re-derived for the batch at hand.
 // ---------------------------------------------------------------------------
-struct TuneEntry {
-  int bs, per_sm, cluster, bs_c, frac, per_sm_c;
-  double ms;
-};
 static std::mutex g_tune_mu;
 static std::map<std::string, TuneEntry> g_tune;
 static bool g_tune_loaded = false;
@@ -775,7 +773,8 @@ static void tune_cache_load_locked() {
     TuneEntry e;
     if (std::sscanf(line, " \"%511[^\"]\": {\"bs\": %d, \"per_sm\": %d, \"cluster\": %d, \"bs_c\": %d, "
                           "\"frac\": %d, \"per_sm_c\": %d, \"ms\": %lf}",
-                    key, &e.bs, &e.per_sm, &e.cluster, &e.bs_c, &e.frac, &e.per_sm_c, &e.ms) == 8)
+                    key, &e.bs, &e.per_sm, &e.cluster, &e.bs_c, &e.frac, &e.per_sm_c, &e.ms) == 8 &&
+        tune_entry_valid(e))
       g_tune[key] = e;
   }
   std::fclose(fp);

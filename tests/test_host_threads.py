@@ -1,9 +1,10 @@
-"""The library's host-side threading and exception barrier, compiled on their
-own (no GPU): host_parallel / host_tasks give split-independent results, carry
-an exception from a worker thread to the caller after every thread has been
-joined, and ABI_TRY / ABI_CATCH turn host exceptions into status codes.  These
-run in the mesh, tile and coarse-space builders, where a worker exception
-would otherwise end the process."""
+"""Host-side C++ pieces of the library, compiled on their own (no GPU): the
+threading helpers and the exception barrier — host_parallel / host_tasks give
+split-independent results and carry an exception from a worker thread to the
+caller after every thread has been joined, and ABI_TRY / ABI_CATCH turn host
+exceptions into status codes (they run in the mesh, tile and coarse-space
+builders, where a worker exception would otherwise end the process) — and the
+rule by which the batched solver accepts an autotuner cache entry."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -79,4 +80,49 @@ def test_host_threads_and_exception_barrier(tmp_path):
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", out.stdout + out.stderr
+
+
+TUNE_SOURCE = r"""
+#include "jfem_tune.h"
+#include <cstdio>
+#include <limits>
+
+int main() {
+  using jfem::TuneEntry;
+  // what the autotuner stores: single-CTA teams, or single-CTA plus clustered
+  const TuneEntry good[] = {{512, 1, 1, 0, 0, 1, 88.9}, {128, 4, 1, 0, 0, 1, 0.0}, {1024, 2, 1, 0, 0, 1, 5.0},
+                            {512, 1, 4, 256, 2, 1, 88.9}, {256, 2, 8, 512, 8, 2, 1.0}};
+  // anything else is not launched
+  const TuneEntry bad[] = {{96, 1, 1, 0, 0, 1, 1.0},    {512, 0, 1, 0, 0, 1, 1.0},   {1024, 4, 1, 0, 0, 1, 1.0},
+                           {512, 1, 3, 256, 2, 1, 1.0},  {512, 1, 16, 256, 2, 1, 1.0}, {512, 1, 4, 128, 2, 1, 1.0},
+                           {512, 1, 4, 256, 3, 1, 1.0},  {512, 1, 4, 256, 0, 1, 1.0},  {512, 1, 4, 256, 2, 4, 1.0},
+                           {512, 1, 1, 256, 0, 1, 1.0},  {512, 1, 1, 0, 2, 1, 1.0},    {512, 1, 1, 0, 0, 1, -1.0},
+                           {512, 1, 1, 0, 0, 1, std::numeric_limits<double>::quiet_NaN()}};
+  for (const TuneEntry& e : good)
+    if (!jfem::tune_entry_valid(e)) { std::printf("rejected bs %d\n", e.bs); return 1; }
+  int k = 0;
+  for (const TuneEntry& e : bad) {
+    if (jfem::tune_entry_valid(e)) { std::printf("accepted bad entry %d\n", k); return 1; }
+    ++k;
+  }
+  std::printf("ok\n");
+  return 0;
+}
+"""
+
+
+def test_autotuner_cache_entries_are_validated(tmp_path):
+    """The batched solver launches a cached autotuner entry only when it is one
+    of the configurations the autotuner can choose (csrc/jfem_tune.h)."""
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ unavailable")
+    src = tmp_path / "tune.cpp"
+    src.write_text(TUNE_SOURCE)
+    exe = tmp_path / "tune"
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", str(CSRC), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0 and out.stdout.strip() == "ok", out.stdout + out.stderr
