@@ -163,8 +163,9 @@ def newton_load_steps(ctx: _abi.Context, steps: int, fixed_dofs, fixed_values, s
     loads to s/steps of t and p, then runs JFEM_NEWTON with one load step from
     the context's current state — the same iteration jfem_solve runs for step
     s inside one call.  With ``checkpoint`` the state is written after every
-    step; ``resume=True`` starts from the state in that file (a fresh context
-    gets it through jfem_set_state).  ``stop_after`` ends the run after that
+    step; ``resume=True`` starts from the state in that file when it exists (a
+    fresh context gets it through jfem_set_state) and from step 1 when it does
+    not, so a job script can always pass it.  ``stop_after`` ends the run after that
     step (for a staged run).  Other keywords are jfem_solve_opts fields
     (precision, tol, newton_tol, max_newton, max_cg_per_newton, …).
 
@@ -177,9 +178,9 @@ def newton_load_steps(ctx: _abi.Context, steps: int, fixed_dofs, fixed_values, s
     dofs = np.ascontiguousarray(fixed_dofs, dtype=np.int64)
     vals = np.ascontiguousarray(np.broadcast_to(np.asarray(fixed_values, dtype=np.float64), dofs.shape))
     first = 1
-    if resume:
-        if checkpoint is None:
-            raise ValueError("resume needs a checkpoint file")
+    if resume and checkpoint is None:
+        raise ValueError("resume needs a checkpoint file")
+    if resume and Path(checkpoint).exists():
         u0, done, n_file = load_load_step(checkpoint)
         if n_file != steps:
             raise ValueError(f"checkpoint holds a run of {n_file} load steps, not {steps}")

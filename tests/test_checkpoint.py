@@ -135,7 +135,14 @@ def test_newton_driver_stages_and_resumes(ck, tmp_path):
     u5, info5 = ck.newton_load_steps(done, 4, [0, 1], [1.0, 1.0], checkpoint=p, resume=True, precision=0)
     assert info5["steps_done"] == 4 and np.allclose(u5, 1.0)
     assert not [c for c in done.calls if c[0] == "solve"]
+    new = _FakeContext(5)                                # resume without a file yet: from step 1
+    u6, info6 = ck.newton_load_steps(new, 2, [0], [1.0], checkpoint=tmp_path / "none.bin", resume=True,
+                                     precision=0)
+    assert [c for c in new.calls if c[0] == "solve"] == [("solve", 0.5), ("solve", 1.0)]
+    assert not [c for c in new.calls if c[0] == "state"] and ck.load_load_step(tmp_path / "none.bin")[1] == 2
     with pytest.raises(ValueError):
         ck.newton_load_steps(_FakeContext(5), 5, [0], [1.0], checkpoint=p, resume=True, precision=0)
+    with pytest.raises(ValueError):
+        ck.newton_load_steps(_FakeContext(5), 4, [0], [1.0], resume=True, precision=0)
     with pytest.raises(ValueError):
         ck.newton_load_steps(_FakeContext(6), 4, [0], [1.0], checkpoint=p, resume=True, precision=0)
